@@ -1,0 +1,250 @@
+"""Seeded synthetic structures and NNAP model files for the benchmark workloads.
+
+The reference repository ships no NNAP model files and no benchmark structures, so
+the workloads are generated here, deterministically from a seed:
+
+* ``fcc``             -- perturbed FCC lattice (single element).
+* ``random_liquid``   -- uniform random positions with a minimum pair separation,
+                         enforced by rejection (random sequential addition on a grid),
+                         in an orthogonal or LAMMPS-style triclinic periodic box.
+* ``write_model``     -- a model dict in the reference's JSON model format
+                         (``NNAP.java:129-307``, ``FeedForward.java:131-221``,
+                         ``SphericalChebyshev.java:60-103``, ``Chebyshev.java:33-69``)
+                         with feed-forward weights ~ N(0, 1/fan_in) and biases ~ N(0, 1/fan_in).
+
+Boxes are 3x3 row matrices ``[a; b; c]``.  ``box_kind`` 0 is orthogonal (diagonal only),
+1 is the LAMMPS lower-triangular form ``a=(lx,0,0), b=(xy,ly,0), c=(xz,yz,lz)``.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+BOX_ORTHO, BOX_LMP, BOX_PRISM = 0, 1, 2
+
+
+@dataclass
+class Structure:
+    x: np.ndarray        # (n, 3) float64 Cartesian positions
+    types: np.ndarray    # (n,) int32, 1-based species
+    box: np.ndarray      # (3, 3) float64 rows a, b, c
+    box_kind: int
+
+    @property
+    def natoms(self) -> int:
+        return len(self.types)
+
+
+def fcc(a: float, reps: int, sigma: float, seed: int) -> Structure:
+    """FCC lattice of ``reps^3`` cubic cells, Gaussian-perturbed by ``sigma``."""
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    g = np.stack(np.meshgrid(np.arange(reps), np.arange(reps), np.arange(reps), indexing="ij"), -1).reshape(-1, 3)
+    x = ((g[:, None, :] + base[None, :, :]).reshape(-1, 3)) * a
+    rng = np.random.default_rng(seed)
+    x = x + rng.normal(0.0, sigma, size=x.shape)
+    L = a * reps
+    return Structure(x, np.ones(len(x), dtype=np.int32), np.diag([L, L, L]), BOX_ORTHO)
+
+
+def _lmp_box(L: float, tilt: float) -> np.ndarray:
+    return np.array([[L, 0.0, 0.0], [tilt * L, L, 0.0], [tilt * L, tilt * L, L]])
+
+
+def _rsa_fractional(n: int, box: np.ndarray, rmin: float, rng: np.random.Generator, max_rounds: int = 4000):
+    """Random sequential addition of ``n`` points with pair distance >= rmin under PBC.
+
+    Works on a grid in fractional coordinates whose cells are small enough that no two
+    accepted points can share a cell; each round proposes a batch of candidates, drops
+    those closer than ``rmin`` to an accepted point or to an earlier candidate of the same
+    batch, and accepts the rest.
+    """
+    A = box
+    inv = np.linalg.inv(A)  # fractional = cart @ inv
+    vol = abs(np.linalg.det(A))
+    h = np.array([vol / np.linalg.norm(np.cross(A[1], A[2])), vol / np.linalg.norm(np.cross(A[2], A[0])),
+                  vol / np.linalg.norm(np.cross(A[0], A[1]))])
+    nc = np.maximum(1, np.floor(np.linalg.norm(A, axis=1) * math.sqrt(3.0) * 1.15 / rmin)).astype(np.int64)
+
+    def diag_ok(ncv):
+        cell = A / ncv[:, None]
+        diags = [cell[0] + cell[1] + cell[2], cell[0] + cell[1] - cell[2], cell[0] - cell[1] + cell[2],
+                 -cell[0] + cell[1] + cell[2]]
+        return max(np.linalg.norm(d) for d in diags) < rmin * 0.999
+
+    while not diag_ok(nc):
+        nc = nc + 1
+    R = np.ceil(rmin * nc / h).astype(np.int64)
+    offs = np.stack(np.meshgrid(*[np.arange(-r, r + 1) for r in R], indexing="ij"), -1).reshape(-1, 3)
+    grid = -np.ones(int(nc.prod()), dtype=np.int64)
+    pos = np.zeros((n, 3))
+    frac = np.zeros((n, 3))
+    count = 0
+    rmin2 = rmin * rmin
+
+    def cell_index(c):
+        return c[..., 0] + nc[0] * (c[..., 1] + nc[1] * c[..., 2])
+
+    for _ in range(max_rounds):
+        if count >= n:
+            break
+        need = n - count
+        B = int(min(max(2 * need, 64), 8192))
+        s = rng.random((B, 3))
+        c = np.minimum((s * nc).astype(np.int64), nc - 1)
+        q = c[:, None, :] + offs[None, :, :]                       # (B, M, 3) neighbour cells
+        img = np.floor_divide(q, nc)
+        qc = q - img * nc
+        occ = grid[cell_index(qc)]                                 # (B, M)
+        has = occ >= 0
+        ok = np.ones(B, dtype=bool)
+        if has.any():
+            bi, mi = np.nonzero(has)
+            other = frac[occ[bi, mi]] + img[bi, mi]
+            d = (other - s[bi]) @ A
+            close = (d * d).sum(-1) < rmin2
+            ok[bi[close]] = False
+        # conflicts inside the batch: keep the earliest candidate per cell, then test neighbours
+        cand = np.nonzero(ok)[0]
+        if cand.size:
+            cid = cell_index(c[cand])
+            first = np.full(grid.size, np.iinfo(np.int64).max)
+            np.minimum.at(first, cid, cand)
+            keep = first[cid] == cand
+            cand = cand[keep]
+            ok[:] = False
+            ok[cand] = True
+            tmp = -np.ones(grid.size, dtype=np.int64)
+            tmp[cell_index(c[cand])] = cand
+            occ2 = tmp[cell_index(qc[cand])]                       # (C, M)
+            earlier = (occ2 >= 0) & (occ2 < cand[:, None])
+            if earlier.any():
+                ci, mi = np.nonzero(earlier)
+                other = s[occ2[ci, mi]] + img[cand[ci], mi]
+                d = (other - s[cand[ci]]) @ A
+                close = (d * d).sum(-1) < rmin2
+                ok[cand[ci[close]]] = False
+        acc = np.nonzero(ok)[0][:need]
+        k = acc.size
+        frac[count:count + k] = s[acc]
+        grid[cell_index(c[acc])] = np.arange(count, count + k)
+        count += k
+    if count < n:
+        raise RuntimeError("random sequential addition stalled at %d of %d points" % (count, n))
+    pos = frac @ A
+    return pos
+
+
+def random_liquid(n: int, density: float, fractions: Sequence[float], rmin: float, seed: int,
+                  tilt: Optional[float] = None) -> Structure:
+    """Uniform random structure at number density ``density`` (1/A^3) with min separation."""
+    rng = np.random.default_rng(seed)
+    L = (n / density) ** (1.0 / 3.0)
+    if tilt is None:
+        box, kind = np.diag([L, L, L]), BOX_ORTHO
+    else:
+        box, kind = _lmp_box(L, tilt), BOX_LMP
+    x = _rsa_fractional(n, box, rmin, rng)
+    counts = [int(round(f * n)) for f in fractions]
+    counts[0] += n - sum(counts)
+    types = np.concatenate([np.full(c, t + 1, dtype=np.int32) for t, c in enumerate(counts)])
+    rng.shuffle(types)
+    return Structure(x, types, box, kind)
+
+
+def write_model(symbols: List[str], basis: dict, hidden: Sequence[int], seed: int,
+                norm_mu=None, norm_sigma=None, norm_mu_eng: float = 0.0, norm_sigma_eng: float = 1.0,
+                ref_eng=None) -> dict:
+    """Model dict in the reference's JSON format with random feed-forward weights."""
+    T = len(symbols)
+    D = descriptor_size(basis, T)
+    rng = np.random.default_rng(seed)
+    models = []
+    for t, sym in enumerate(symbols):
+        hw, hb = [], []
+        fan = D
+        for h in hidden:
+            hw.append(rng.normal(0.0, math.sqrt(1.0 / fan), size=(h, fan)).tolist())
+            hb.append(rng.normal(0.0, math.sqrt(1.0 / fan), size=h).tolist())
+            fan = h
+        ow = rng.normal(0.0, math.sqrt(1.0 / fan), size=fan).tolist()
+        ob = float(rng.normal(0.0, math.sqrt(1.0 / fan)))
+        m = {"symbol": sym, "basis": dict(basis),
+             "nn": {"type": "feed_forward", "input_dim": D, "hidden_dims": list(hidden),
+                    "hidden_weights": hw, "hidden_biases": hb, "output_weight": ow, "output_bias": ob}}
+        if norm_mu is not None:
+            m["norm_mu"] = list(map(float, norm_mu[t]))
+        if norm_sigma is not None:
+            m["norm_sigma"] = list(map(float, norm_sigma[t]))
+        if ref_eng is not None:
+            m["ref_eng"] = float(ref_eng[t])
+        models.append(m)
+    models[0]["norm_mu_eng"] = float(norm_mu_eng)
+    models[0]["norm_sigma_eng"] = float(norm_sigma_eng)
+    return {"version": 6, "units": "metal", "models": models}
+
+
+def descriptor_size(basis: dict, T: int) -> int:
+    """Descriptor length of a single (non-merged) basis dict without fuse/rfuse weights."""
+    nmax = int(basis.get("nmax", 5))
+    wt = basis.get("wtype", "default")
+    if wt == "default":
+        P = 2 * (nmax + 1) if T > 1 else nmax + 1
+    elif wt == "none":
+        P = nmax + 1
+    elif wt == "full":
+        P = T * (nmax + 1) if T > 1 else nmax + 1
+    elif wt == "exfull":
+        P = (T + 1) * (nmax + 1) if T > 1 else nmax + 1
+    else:
+        raise ValueError("descriptor_size only handles default/none/full/exfull")
+    if basis.get("type", "spherical_chebyshev") in ("chebyshev", "cheby"):
+        return P
+    return P * (int(basis.get("lmax", 6)) + 1)
+
+
+# ------------------------------------------------------------------ named workloads
+C1_BASIS = {"type": "chebyshev", "nmax": 10, "rcut": 6.0}
+C2_BASIS = {"type": "spherical_chebyshev", "nmax": 8, "lmax": 6, "rcut": 6.0, "wtype": "default"}
+C3_BASIS = {"type": "spherical_chebyshev", "nmax": 8, "lmax": 4, "rcut": 5.5, "wtype": "default"}
+
+
+def c1_structure(seed: int = 1) -> Structure:
+    """FCC a=3.61 A, 10x10x10 cells (4000 atoms), sigma=0.05 A."""
+    return fcc(3.61, 10, 0.05, seed)
+
+
+def c2_structure(n: int = 32000, seed: int = 2) -> Structure:
+    """Ternary liquid, density 0.060 /A^3, fractions 0.46/0.46/0.08, min separation 2.0 A."""
+    return random_liquid(n, 0.060, [0.46, 0.46, 0.08], 2.0, seed)
+
+
+def c3_structure(n: int = 1048576, seed: int = 3) -> Structure:
+    """Binary glass, density 0.058 /A^3, fractions 0.64/0.36, min separation 2.1 A, tilt 0.1."""
+    return random_liquid(n, 0.058, [0.64, 0.36], 2.1, seed, tilt=0.1)
+
+
+def c4_structures(count: int = 1024, seed: int = 4) -> List[Structure]:
+    """Mixed batch: n ~ log-uniform[32, 2048], half orthogonal / half triclinic (tilt 0.1),
+    density ~ U[0.055, 0.065], ternary species as the liquid workload, min separation 2.0 A."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(32), math.log(2048)))))
+        rho = float(rng.uniform(0.055, 0.065))
+        tilt = 0.1 if (k % 2 == 1) else None
+        out.append(random_liquid(n, rho, [0.46, 0.46, 0.08], 2.0, seed * 100003 + k, tilt=tilt))
+    return out
+
+
+def model_for(config: str, seed: int = 11, norm_mu=None, norm_sigma=None) -> dict:
+    """Model dict for the named workload; normalisation statistics may be supplied."""
+    if config == "c1":
+        return write_model(["Cu"], C1_BASIS, [32, 32], seed, norm_mu, norm_sigma, -3.5, 0.1)
+    if config in ("c2", "c4", "c5"):
+        return write_model(["A", "B", "C"], C2_BASIS, [64, 64], seed, norm_mu, norm_sigma, -3.0, 0.1)
+    if config == "c3":
+        return write_model(["A", "B"], C3_BASIS, [64, 64], seed, norm_mu, norm_sigma, -3.0, 0.1)
+    raise ValueError(config)
