@@ -1,0 +1,408 @@
+"""Benchmark: NNAP energy+force+virial evaluation, atom-evals/s, on one GB300 per rank.
+
+A step evaluates energies, forces and virials of one structure (or one batch of
+structures) of the chosen workload.  ``value`` is the device-resident throughput
+(inputs already in HBM, outputs left in HBM), timed per step with CUDA events on the
+caller's stream with an L2 flush (a 256 MiB write) between steps outside the events.
+``e2e`` is the same metric through the host-buffer C-ABI call ``nnap_compute`` with
+pinned host inputs and outputs: host->device copies of positions and species and the
+device->host read of energy, forces and virial are inside the timed region.
+
+Workloads (seeded synthetic inputs; the reference publishes none):
+  liquid32k   ternary liquid, 32000 atoms, spherical Chebyshev nmax 8 lmax 6 rc 6.0, 126->64->64->1
+  fcc4000     perturbed FCC Cu, 4000 atoms, radial Chebyshev nmax 10 rc 6.0, 11->32->32->1
+  glass1m     binary glass, 1048576 atoms, LAMMPS triclinic, nmax 8 lmax 4 rc 5.5, 90->64->64->1
+  batch1024   1024 structures, 32..2048 atoms log-uniform, half triclinic, liquid32k model
+
+``--impl reference`` times the reference's own per-atom C++ arithmetic (expanded from its
+headers, compiled -O3 -ffast-math into oracle/_ref) driven over the oracle's neighbour
+list on all host cores, or the oracle port when that build is absent; only rank 0 runs it.
+With torchrun and N > 1 every rank evaluates its own replica of the workload (the path
+has no collective); value = atoms of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from jse_gb300 import workloads as W  # noqa: E402
+
+METRIC = "NNAP E+F atom-evals/s"
+
+
+# ----------------------------------------------------------------------------- workloads
+def make_workload(name: str):
+    """Structures and a model-factory taking per-species normalisation statistics."""
+    if name == "liquid32k":
+        return [W.c2_structure()], "c2"
+    if name == "fcc4000":
+        return [W.c1_structure()], "c1"
+    if name == "glass1m":
+        return [W.c3_structure()], "c3"
+    if name == "batch1024":
+        return W.c4_structures(), "c4"
+    raise SystemExit("unknown workload " + name)
+
+
+def normalised_model(cfg: str, structures, precision: str):
+    """Model with norm_mu/norm_sigma set to descriptor statistics of the first structure,
+    computed with the GPU descriptors (as a trainer would set them)."""
+    from jse_gb300.nnap import NNAP
+    raw = W.model_for(cfg)
+    s = structures[0]
+    with NNAP(raw, precision="fp32") as p:
+        fp = p.calFp(s)
+    T = len(raw["models"])
+    mu, sg = [], []
+    for t in range(T):
+        D = raw["models"][t]["nn"]["input_dim"]
+        sel = fp[s.types == t + 1, :D]
+        if len(sel) == 0:
+            sel = fp[:, :D]
+        mu.append(sel.mean(0))
+        sg.append(sel.std(0) + 1e-3)
+    return W.model_for(cfg, norm_mu=mu, norm_sigma=sg)
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.flush()
+        self.out.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.read().splitlines():
+            f = [c.strip() for c in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.out.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- roofline
+def stage_costs(model: dict, mean_nei: float):
+    """Algorithmic HBM bytes and FP32 FLOPs per atom of each pipeline stage.
+
+    Bytes count every item once (positions, pair rows, descriptors, expansion
+    coefficients, gradients, outputs); FLOPs are the per-pair counts of the
+    descriptor mathematics: forward 6K + 3Nn + 8 + 2 P Nn + 2 P K, backward
+    4 P K + 2 P Nn + 14 K + 3 Nn, with K = (lmax+1)^2 (0 for a radial basis).
+    """
+    b = model["models"][0]["basis"]
+    T = len(model["models"])
+    nmax = int(b.get("nmax", 5))
+    N1 = nmax + 1
+    P = (2 * N1 if T > 1 else N1) if b.get("wtype", "default") == "default" else N1
+    sph = b.get("type", "spherical_chebyshev") not in ("chebyshev", "cheby")
+    L = int(b.get("lmax", 6)) if sph else -1
+    K = (L + 1) ** 2 if sph else 0
+    D = P * (L + 1) if sph else P
+    nn = mean_nei
+    H = model["models"][0]["nn"]["hidden_dims"]
+    pk = P * K * 4
+    stages = {
+        "neighbours": {"bytes": 24 + 4 + 24 + 16 + 4 + nn * (8 + 16 + 4) + 4, "flops": 0.0},
+        "descriptors_fwd": {"bytes": nn * 16 + 8 + D * 4 + pk, "flops": nn * (6 * K + 3 * N1 + 8 + 2 * P * N1 + 2 * P * K)},
+        "network": {"bytes": 2 * D * 4 + 8, "flops": 4.0 * (D * H[0] + sum(H[i] * H[i + 1] for i in range(len(H) - 1)) + H[-1])},
+        "descriptors_bwd": {"bytes": nn * 32 + 8 + D * 4 + pk, "flops": nn * (4 * P * K + 2 * P * N1 + 14 * K + 3 * N1)},
+        "scatter": {"bytes": nn * (16 + 4 + 16 + 16) + 4 + 24 + 72 + 8 + 72, "flops": 0.0},
+    }
+    return stages
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured", float(d.get("sm_max_mhz", 2070.0))
+    return 6800.0, "fallback", 2070.0
+
+
+def load_traffic():
+    """DRAM bytes per atom per stage from a committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+# ----------------------------------------------------------------------------- reference arm
+def cpu_reference(structures, model: dict, budget_s: float = 12.0, threads: int = 0):
+    """Time the reference's per-atom arithmetic (oracle/_ref, -O3 -ffast-math) or, when that
+    build is absent, the oracle port, on a bounded sample of atoms.  Returns (atoms/s, info)."""
+    from oracle import model as OM, native as ON
+    threads = threads or os.cpu_count() or 1
+    pm = OM.load(model)
+    s = structures[0]
+    xw = ON.wrap(s.x, s.box_kind, s.box)
+    nl_full = ON.neighbors(xw, s.box_kind, s.box, pm.rcut_max)
+    kind = "reference"
+    try:
+        ref = ON.RefLib(pm, fast=True)
+    except (FileNotFoundError, OSError, RuntimeError):
+        ref = None
+        kind = "port"
+    n = len(s.types)
+
+    def run(m):
+        # evaluate the first m atoms (full neighbour rows, scatter into full-size outputs)
+        t0 = time.perf_counter()
+        if ref is not None:
+            ref.compute(s.types, nl_full, nthreads=threads, n_eval=m)
+        else:
+            ON.compute(pm, s.x, s.types, s.box_kind, s.box, nl=nl_full, n_eval=m)
+        return time.perf_counter() - t0
+
+    m = min(n, 256)
+    dt = run(m)
+    while dt < 0.5 and m < n:
+        m = min(n, m * 4)
+        dt = run(m)
+    rate = m / dt
+    m_final = int(min(n, max(m, rate * budget_s)))
+    dt = run(m_final)
+    return m_final / dt, {"kind": kind, "cores": threads if ref is not None else 1,
+                          "sample": "%d of %d atoms of the first structure, full neighbour rows, %s" % (
+                              m_final, n, "reference per-atom C++ (-O3 -ffast-math), %d threads" % threads
+                              if ref is not None else "FP64 oracle port, 1 thread")}
+
+
+# ----------------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="liquid32k", choices=["liquid32k", "fcc4000", "glass1m", "batch1024"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    structures, cfg = make_workload(args.workload)
+    natoms_step = sum(s.natoms for s in structures)
+    config = {"workload": args.workload, "structures": len(structures), "atoms_per_step": natoms_step,
+              "precision": args.precision, "l2": "flushed between steps (256 MiB write)",
+              "parallelism": "replicas x%d" % world}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        model = W.model_for(cfg)
+        rates = []
+        info = None
+        for _ in range(args.warmup):
+            pass
+        for _ in range(args.steps):
+            r, info = cpu_reference(structures, model, budget_s=max(1.0, 20.0 / max(args.steps, 1)))
+            rates.append(r)
+        v = statistics.median(rates)
+        line = {"metric": METRIC, "value": v, "unit": "atom-evals/s", "n_gpus": 0, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": natoms_step / v * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                "config": config, "impl": "reference",
+                "cpu_baseline": dict(info, value=v, unit="atom-evals/s"),
+                "e2e": {"value": v, "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from jse_gb300.nnap import NNAP, WANT_ENERGY, WANT_FORCES, WANT_VIRIAL
+    torch.cuda.set_device(local)
+    model = normalised_model(cfg, structures, args.precision)
+    pot = NNAP(model, precision=args.precision, device=local)
+    dev = torch.device("cuda", local)
+    s = structures[0]
+    single = len(structures) == 1
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    if single:
+        n = s.natoms
+        x_d = torch.from_numpy(np.ascontiguousarray(s.x)).to(dev)
+        t_d = torch.from_numpy(np.ascontiguousarray(s.types)).to(dev)
+        e_d = torch.zeros(1, dtype=torch.float64, device=dev)
+        f_d = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+        v_d = torch.zeros(9, dtype=torch.float64, device=dev)
+        flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
+
+        def device_step():
+            st = torch.cuda.current_stream(dev).cuda_stream
+            pot.computeDevice(n, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
+                              f_d.data_ptr(), v_d.data_ptr(), 0, stream=st)
+    else:
+        def device_step():
+            pot.calEnergyForceVirialsBatch(structures)
+
+    pot.setProfiling(True)
+    for _ in range(args.warmup):
+        flush.zero_()
+        device_step()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.2)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    ms, stages, launches = [], np.zeros(5), 0
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        device_step()
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        stages += pot.stageTimes()
+        launches += pot.lastLaunchCount()
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t_wall
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    t_dev = sum(ms) / 1e3
+    if dist:
+        tt = torch.tensor([t_dev])
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt[0])
+    value = natoms_step * args.steps * world / t_dev
+    stages /= args.steps
+
+    # end to end through host buffers (pinned)
+    e2e = None
+    if single:
+        n = s.natoms
+        xh = torch.from_numpy(np.ascontiguousarray(s.x)).pin_memory().numpy()
+        th = torch.from_numpy(np.ascontiguousarray(s.types)).pin_memory().numpy()
+        fh = torch.zeros((n, 3), dtype=torch.float64).pin_memory().numpy()
+        eh = torch.zeros(1, dtype=torch.float64).pin_memory().numpy()
+        vh = torch.zeros(9, dtype=torch.float64).pin_memory().numpy()
+        from jse_gb300.nnap import _dptr, _iptr
+        box9 = np.ascontiguousarray(s.box, dtype=np.float64).reshape(9)
+        for _ in range(2):
+            pot._check(pot._L.nnap_compute(pot._handle(), n, _dptr(xh), _iptr(th), s.box_kind, _dptr(box9), flags,
+                                           _dptr(eh), None, _dptr(fh), _dptr(vh), None))
+        dts = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            pot._check(pot._L.nnap_compute(pot._handle(), n, _dptr(xh), _iptr(th), s.box_kind, _dptr(box9), flags,
+                                           _dptr(eh), None, _dptr(fh), _dptr(vh), None))
+            dts.append(time.perf_counter() - t0)
+        e2e = {"value": n * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": n * 24 + n * 4,
+               "d2h_bytes_per_step": 8 + n * 24 + 72}
+    else:
+        dts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            pot.calEnergyForceVirialsBatch(structures)
+            dts.append(time.perf_counter() - t0)
+        nat = natoms_step
+        e2e = {"value": nat * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": nat * 28,
+               "d2h_bytes_per_step": nat * 32 + len(structures) * 80}
+
+    # roofline of the dominant stage
+    peak, peak_kind, sm_max = load_peaks()
+    off, j, img = pot.neighborList(s)
+    mean_nei = float(len(j)) / max(1, s.natoms)
+    costs = stage_costs(model, mean_nei)
+    names = list(costs.keys())
+    dom = int(np.argmax(stages))
+    dname = names[dom]
+    t_dom = stages[dom] / 1e3
+    achieved = costs[dname]["bytes"] * natoms_step / t_dom / 1e9
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    traffic = load_traffic().get("%s/%s" % (args.workload, dname))
+    roof = {"bound": "hbm", "kernel_stage": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": traffic * natoms_step if traffic else None,
+            "fp32": {"achieved_tflops": costs[dname]["flops"] * natoms_step / t_dom / 1e12,
+                     "peak_tflops": fp32_peak, "peak_source": "nominal 152 SM x 128 lanes x 2 x max clock",
+                     "frac": costs[dname]["flops"] * natoms_step / t_dom / 1e12 / fp32_peak},
+            "stage_ms": dict(zip(names, [round(float(x), 5) for x in stages])),
+            "mean_neighbours": mean_nei}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            v_cpu, info = cpu_reference(structures, W.model_for(cfg), budget_s=10.0)
+            cpu = dict(info, value=v_cpu, unit="atom-evals/s")
+        except Exception as ex:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "atom-evals/s", "error": str(ex)[:200]}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16+f32",
+                "data": "synthetic (seeded)", "config": config, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+                "clocks": clk, "gpu_launches": launches, "wall_s_timed": wall}
+        print(json.dumps(line))
+    pot.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

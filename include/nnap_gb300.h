@@ -1,0 +1,144 @@
+/*
+ * nnap_gb300.h -- C ABI of the GB300-native NNAP energy/force/virial evaluator.
+ *
+ * The library replaces the per-structure evaluation path of jse's NNAP potential
+ * (jsex.nnap.NNAP).  It reads the same JSON model files and returns the same
+ * energies, forces and virials, computed on one GPU.  Plain pointers and sizes only;
+ * every call returns an nnap_status (0 = success) and never throws.
+ *
+ * Conventions (identical to the reference):
+ *   - species are 1-based integers indexing the model's "models" list;
+ *   - positions are Cartesian, in the frame whose origin is the box origin; they are
+ *     wrapped into the box in FP64 exactly as IBox.wrapPBC does (IBox.java:145-151);
+ *   - box is 9 doubles, rows a, b, c.  box_kind selects how it is read:
+ *       NNAP_BOX_ORTHO  diagonal only (jse.atom.Box / LmpBox),
+ *       NNAP_BOX_LMP    a=(lx,0,0) b=(xy,ly,0) c=(xz,yz,lz) (jse.lmp.LmpBoxPrism),
+ *       NNAP_BOX_PRISM  three general vectors (jse.atom.BoxPrism);
+ *   - neighbours are all periodic images j' with |x_j' - x_i|^2 < rcut^2 (strict, FP64),
+ *     including images of atom i itself (NeighborListGetter.java:1018-1050);
+ *   - forces F_i = -dE/dx_i; virials use the per-atom convention of
+ *     IPairPotential.calEnergyForceVirials (IPairPotential.java:811-1022): the pair term
+ *     dx_ij (x) g_ij is assigned to the neighbour j; components are ordered
+ *     xx, yy, zz, xy, xz, yz, yx, zx, zy; the total virial is their sum.
+ *
+ * Thread safety: one handle serves one host thread at a time (NNAP.java:38); distinct
+ * handles are independent.  Each handle owns one CUDA stream and grow-only device
+ * buffers; no allocation happens in steady-state calls once the buffers have grown.
+ */
+#ifndef NNAP_GB300_H
+#define NNAP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nnap_handle nnap_handle;
+
+/* Status codes.  Nonzero returns correspond to the reference's IllegalStateException /
+ * IllegalArgumentException / CudaException paths (NNAP.java:131-176, 507, 756;
+ * CudaCore.java:110). */
+typedef enum {
+    NNAP_OK = 0,
+    NNAP_ERR_BAD_MODEL = 1,    /* model text invalid or inconsistent                */
+    NNAP_ERR_BAD_TYPE = 2,     /* species outside 1..ntypes (NNAP.java:507)           */
+    NNAP_ERR_CAPACITY = 3,     /* internal capacity exceeded and could not grow       */
+    NNAP_ERR_CUDA = 4,         /* a CUDA runtime call failed; see nnap_last_error     */
+    NNAP_ERR_UNSUPPORTED = 5,  /* model shape without a compiled kernel               */
+    NNAP_ERR_ARG = 6,          /* invalid argument (null pointer, bad size, bad box)  */
+    NNAP_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up                  */
+    NNAP_ERR_DEAD = 8          /* handle already destroyed                            */
+} nnap_status;
+
+/* Precision modes.  NNAP_PREC_FP32 is the plain drop-in (FP32 descriptors and FP32
+ * network); NNAP_PREC_MIXED evaluates the network as BF16 tensor-core GEMMs with FP32
+ * accumulation and FP32 output layer.  Both use FP64 wrapping, FP64 displacements
+ * and FP64 energy/force/virial reductions. */
+typedef enum { NNAP_PREC_FP32 = 0, NNAP_PREC_MIXED = 1 } nnap_precision;
+
+typedef enum { NNAP_BOX_ORTHO = 0, NNAP_BOX_LMP = 1, NNAP_BOX_PRISM = 2 } nnap_box_kind;
+
+/* Output selection flags for the compute calls. */
+enum {
+    NNAP_WANT_ENERGY = 1,     /* total energy (1 double)                    */
+    NNAP_WANT_ENERGIES = 2,   /* per-atom energies (n doubles)              */
+    NNAP_WANT_FORCES = 4,     /* forces (3n doubles, xyz interleaved)       */
+    NNAP_WANT_VIRIAL = 8,     /* total virial (9 doubles)                   */
+    NNAP_WANT_VIRIALS = 16    /* per-atom virials (9n doubles)              */
+};
+
+/* Create a handle from model JSON text (the format read by NNAP(Map) /
+ * NNAP(String path), NNAP.java:402-426; YAML is not accepted).  device is the CUDA
+ * ordinal.  Replaces the NNAP constructor + JIT compile (NNAP.java:129-401, 446-470). */
+int nnap_create(const char* model_json, size_t len, int precision, int device, nnap_handle** out);
+/* Same, reading the JSON text from a file (NNAP(String), NNAP.java:407-411). */
+int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out);
+/* Release the handle and its device memory (NNAP.close, NNAP.java:472-486). */
+int nnap_destroy(nnap_handle* h);
+
+/* Model queries: NNAP.ntypes / rcutMax / symbol / units (NNAP.java:86-90, 489-491). */
+int nnap_ntypes(const nnap_handle* h, int* ntypes);
+int nnap_rcut_max(const nnap_handle* h, double* rcut);
+int nnap_symbol(const nnap_handle* h, int type, char* buf, size_t buflen);
+int nnap_descriptor_size(const nnap_handle* h, int type, int* size);
+/* Message of the last failing call on this handle (empty when none). */
+const char* nnap_last_error(const nnap_handle* h);
+
+/* Energy / forces / virials of one periodic structure, host buffers.
+ * Replaces IPairPotential.calEnergyForceVirials(APC, ...) for an NNAP
+ * (IPairPotential.java:811-1022 -> NNAP.calEnergyForceVirial, NNAP.java:553-594).
+ * x: 3n doubles; type: n ints (1-based); box: 9 doubles.  Outputs selected by flags;
+ * unselected output pointers may be NULL.  Synchronous. */
+int nnap_compute(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind, const double* box,
+                 int flags, double* energy, double* energies, double* forces, double* virial, double* virials);
+
+/* Same computation on device-resident buffers; x, type, and every output are device
+ * pointers, box stays a host array.  Work is ordered after `stream` (a cudaStream_t, may
+ * be NULL) and `stream` is made to wait for the results.  The call synchronises the
+ * handle's stream once, after the neighbour build, to validate the neighbour capacity
+ * and read the species ranges; the rest is queued and the call returns before it ends. */
+int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int* d_type, int box_kind,
+                        const double* box, int flags, double* d_energy, double* d_energies, double* d_forces,
+                        double* d_virial, double* d_virials, void* stream);
+
+/* Many independent structures in one launch sequence (the batched form; each structure
+ * gives the same result as nnap_compute on it alone, within floating-point rounding).
+ * natoms[s] atoms per structure; x/type are concatenated over structures; box_kind[s]
+ * and boxes[9*s] per structure.  energy[s] and virial[9*s] are per structure; energies,
+ * forces, virials are concatenated per atom.  Host buffers, synchronous. */
+int nnap_compute_batch(nnap_handle* h, int nstruct, const int* natoms, const double* x, const int* type,
+                       const int* box_kind, const double* boxes, int flags, double* energy, double* energies,
+                       double* forces, double* virial, double* virials);
+
+/* Descriptor vectors of every atom (NNAP.calFp, NNAP.java:596-632 -> jse_nnap_calFp,
+ * nnap_interface.cpp:11-25).  fp is n x stride doubles, stride >= the largest
+ * descriptor size; entries beyond an atom's own size are zero.  Host buffers. */
+int nnap_compute_fp(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind, const double* box,
+                    double* fp, int stride);
+
+/* Full neighbour list of one structure with the model's largest cutoff, for parity
+ * checks against NeighborListGetter (NeighborListGetter.java:1018-1050).  counts: n
+ * ints; if j is non-NULL, j/img (cap and 3*cap ints) receive, atom by atom, the
+ * neighbour index and its image (n_a, n_b, n_c) along a, b, c.  *total receives the
+ * number of pairs.  Host buffers. */
+int nnap_neighbor_list(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind,
+                       const double* box, int* counts, long long cap, int* j, int* img, long long* total);
+
+/* Number of this library's kernels launched by the last compute call on the handle. */
+int nnap_last_launch_count(const nnap_handle* h, int* count);
+
+/* Stage timing (no counterpart in the reference; used by the benchmark).  When on,
+ * compute calls record CUDA events on the handle's stream around five stages:
+ * [0] wrap, cells, neighbour rows, mirror index and species sort; [1] descriptors
+ * forward; [2] network; [3] descriptors backward; [4] force/virial gather and FP64
+ * reductions.  nnap_stage_times waits for the last call and returns milliseconds. */
+int nnap_set_profiling(nnap_handle* h, int on);
+int nnap_stage_times(nnap_handle* h, double* ms5);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NNAP_GB300_H */

@@ -1,0 +1,573 @@
+// Descriptor kernels (FP32): radial Chebyshev and spherical-Chebyshev power spectrum,
+// forward (descriptors) and backward (pair gradients from dE/dfp).
+//
+// Mathematics restated from the reference (see the oracle for an FP64 copy):
+//   x = 1 - 2r/rc, R_n = T_n(x), fc = (1 - (r/rc)^2)^4            nnap_util.hpp:226-271
+//   Rnp[p] = sum_n W[t_i][t_j][p][n] R_n  (internal fuse matrix)    nnap_util.hpp:273-280
+//   radial:     fp[p] = sum_j fc Rnp[p]                             basis_Chebyshev.hpp:82-133
+//   spherical:  A[p][lm] = sum_j fc Rnp[p] Y_lm,
+//               fp[p][l] = 4 pi/(2l+1) sum_m A[p][l,m]^2            basis_SphericalChebyshev.hpp:264-351
+//   backward:   g_j = -dE_i/d(x_j - x_i) through fc, R_n, theta, phi  basis_SphericalChebyshev.hpp:353-525
+// Real spherical harmonics use normalised associated Legendre functions with the
+// Condon-Shortley phase, Y_{l,m>0} = sqrt2 P_lm cos(m phi), Y_{l,-m} = sqrt2 P_lm sin(m phi)
+// (basis_SphericalUtil.hpp:12-101); dY/dtheta uses
+//   dP_lm/dtheta = 1/2 [sqrt((l-m)(l+m+1)) P_{l,m+1} - sqrt((l+m)(l-m+1)) P_{l,m-1}],
+// and the pole branch (dxy == 0) takes phi = 0 and drops the phi terms like
+// calYPthetaPphi (basis_SphericalUtil.hpp:160-181).
+//
+// Layout: one warp per atom slot (atoms are processed in species-sorted slot order);
+// forward lanes first evaluate one neighbour each into a shared-memory tile, then own
+// columns lm of the P x K accumulator A; backward lanes own one neighbour each and
+// stream G = dE/dA from shared memory.  The radial-fuse matrices of the basis live in
+// shared memory for the whole block.
+#include <math_constants.h>
+
+#include "common.cuh"
+#include "desc.cuh"
+
+namespace nnapgb {
+
+__constant__ float c_shA[91], c_shB[91], c_dup[91], c_ddn[91];
+__constant__ float c_diag[13], c_sub[13];
+
+cudaError_t upload_sh_constants() {
+    float A[91] = {0}, B[91] = {0}, up[91] = {0}, dn[91] = {0}, dg[13] = {0}, sb[13] = {0};
+    for (int l = 0; l <= 12; ++l)
+        for (int m = 0; m <= l; ++m) {
+            const int t = l * (l + 1) / 2 + m;
+            if (l >= m + 2) {
+                A[t] = (float)sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+                B[t] = (float)-sqrt(((double)(l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
+            }
+            up[t] = (float)sqrt((double)(l - m) * (l + m + 1));
+            dn[t] = (float)sqrt((double)(l + m) * (l - m + 1));
+        }
+    for (int m = 0; m <= 12; ++m) {
+        dg[m] = m ? (float)sqrt(1.0 + 0.5 / m) : 0.f;
+        sb[m] = (float)sqrt(2.0 * m + 3.0);
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(c_shA, A, sizeof(A))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_shB, B, sizeof(B))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_dup, up, sizeof(up))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_ddn, dn, sizeof(dn))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_diag, dg, sizeof(dg))) != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(c_sub, sb, sizeof(sb));
+}
+
+namespace {
+
+constexpr int kDescWarps = 4;
+constexpr float kPi4 = 12.566370614359172f;
+
+__host__ __device__ constexpr int tri(int l, int m) { return l * (l + 1) / 2 + m; }
+
+template <int N1>
+__device__ __forceinline__ void cheby_f(float x, float* T) {
+    T[0] = 1.f;
+    if (N1 > 1) T[1] = x;
+#pragma unroll
+    for (int n = 2; n < N1; ++n) T[n] = 2.f * x * T[n - 1] - T[n - 2];
+}
+// -(1/r) d/dr T_n(1 - 2r/rc) = (2/(r rc)) n U_{n-1}(x)
+template <int N1>
+__device__ __forceinline__ void cheby_grad_f(float x, float mul, float* G) {
+    G[0] = 0.f;
+    float um2 = 0.f, um1 = mul;
+#pragma unroll
+    for (int n = 1; n < N1; ++n) {
+        const float u = (n == 1) ? mul : ((n == 2) ? 2.f * mul * x : 2.f * x * um1 - um2);
+        if (n >= 2) { um2 = um1; um1 = u; }
+        G[n] = (float)n * u;
+    }
+}
+
+// Normalised associated Legendre functions P[tri(l,m)], Condon-Shortley phase included.
+template <int L>
+__device__ __forceinline__ void legendre_f(float ct, float st, float* P) {
+    P[0] = 0.28209479177387814f;
+#pragma unroll
+    for (int m = 1; m <= L; ++m) P[tri(m, m)] = -c_diag[m] * st * P[tri(m - 1, m - 1)];
+#pragma unroll
+    for (int m = 0; m < L; ++m) P[tri(m + 1, m)] = c_sub[m] * ct * P[tri(m, m)];
+#pragma unroll
+    for (int m = 0; m <= L; ++m)
+#pragma unroll
+        for (int l = m + 2; l <= L; ++l)
+            P[tri(l, m)] = c_shA[tri(l, m)] * (ct * P[tri(l - 1, m)] + c_shB[tri(l, m)] * P[tri(l - 2, m)]);
+}
+
+struct Angles {
+    float ct, st, cp, sp, dxy;
+    bool pole;
+};
+
+__device__ __forceinline__ Angles angles_f(float dx, float dy, float dz, float r) {
+    Angles a;
+    a.dxy = hypotf(dx, dy);
+    a.ct = dz / r;
+    a.st = a.dxy / r;
+    a.pole = a.dxy < 8.f * 1.17549435e-38f;  // numericEqual(dxy, 0) in single precision
+    if (a.pole) { a.cp = 1.f; a.sp = 0.f; } else { a.cp = dx / a.dxy; a.sp = dy / a.dxy; }
+    return a;
+}
+
+// Y (and optionally dY/dtheta) written to Y[lm*ys], Yt[lm*ys].
+template <int L, bool DTHETA>
+__device__ __forceinline__ void sph_harm(const Angles& an, float* Y, float* Yt, int ys) {
+    float P[tri(L, L) + 1];
+    legendre_f<L>(an.ct, an.st, P);
+    float cm[L + 1], sm[L + 1];
+    cm[0] = 1.f; sm[0] = 0.f;
+    if (L >= 1) { cm[1] = an.cp; sm[1] = an.sp; }
+#pragma unroll
+    for (int m = 2; m <= L; ++m) {
+        cm[m] = 2.f * an.cp * cm[m - 1] - cm[m - 2];
+        sm[m] = 2.f * an.cp * sm[m - 1] - sm[m - 2];
+    }
+    const float r2 = 1.41421356237309515f;
+#pragma unroll
+    for (int l = 0; l <= L; ++l) {
+        const int c0 = l * l + l;
+        Y[c0 * ys] = P[tri(l, 0)];
+#pragma unroll
+        for (int m = 1; m <= l; ++m) {
+            Y[(c0 + m) * ys] = r2 * P[tri(l, m)] * cm[m];
+            Y[(c0 - m) * ys] = r2 * P[tri(l, m)] * sm[m];
+        }
+        if (DTHETA) {
+#pragma unroll
+            for (int m = 0; m <= l; ++m) {
+                const float upv = (m + 1 <= l) ? c_dup[tri(l, m)] * P[tri(l, m + 1)] : 0.f;
+                const float pm1 = (m >= 1) ? P[tri(l, m - 1)] : (l >= 1 ? -P[tri(l, 1)] : 0.f);
+                const float dPt = 0.5f * (upv - c_ddn[tri(l, m)] * pm1);
+                if (m == 0) {
+                    Yt[c0 * ys] = dPt;
+                } else {
+                    Yt[(c0 + m) * ys] = r2 * dPt * cm[m];
+                    Yt[(c0 - m) * ys] = r2 * dPt * sm[m];
+                }
+            }
+        }
+    }
+}
+
+template <int NP, int N1>
+__device__ __forceinline__ void load_fuse(const float* __restrict__ Wg, float* sW, int count) {
+    for (int q = threadIdx.x; q < count; q += blockDim.x) sW[q] = Wg[q];
+}
+
+__device__ __forceinline__ int atom_of(const DescArgs& a, int warp) { return a.perm[a.s0 + warp]; }
+
+}  // namespace
+
+// =========================================================================== radial
+template <int NP, int N1>
+__global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
+    extern __shared__ float sW[];
+    load_fuse<NP, N1>(a.W, sW, a.T * a.T * NP * N1);
+    __syncthreads();
+    const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (a.s0 + w >= a.s1) return;
+    const int at = atom_of(a, w);
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut, irc = 1.f / a.rcut;
+    float acc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) acc[p] = 0.f;
+    for (int k = lane; k < cnt; k += 32) {
+        const float4 d = a.P.dx[(size_t)at * M + k];
+        const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+        if (r >= rc) continue;
+        const int tn = __float_as_int(d.w) - 1;
+        const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
+        float T[N1];
+        cheby_f<N1>(1.f - 2.f * u, T);
+        const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            float s = 0.f;
+#pragma unroll
+            for (int n = 0; n < N1; ++n) s += Wt[p * N1 + n] * T[n];
+            acc[p] += fc * s;
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[p] += __shfl_xor_sync(0xffffffffu, acc[p], o);
+    float* out = a.fp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+        if (lane == (p & 31)) out[p] = acc[p];
+}
+
+template <int NP, int N1>
+__global__ void __launch_bounds__(32 * kDescWarps) k_radial_bwd(DescArgs a) {
+    extern __shared__ float sW[];
+    load_fuse<NP, N1>(a.W, sW, a.T * a.T * NP * N1);
+    __syncthreads();
+    const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (a.s0 + w >= a.s1) return;
+    const int at = atom_of(a, w);
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut, irc = 1.f / a.rcut;
+    const float* gf = a.gfp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+    float gfp[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) gfp[p] = gf[p];
+    for (int k = lane; k < cnt; k += 32) {
+        const size_t e = (size_t)at * M + k;
+        const float4 d = a.P.dx[e];
+        const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+        float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r < rc) {
+            const int tn = __float_as_int(d.w) - 1;
+            const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
+            const float fcg = 8.f * fc1 * fc2 * irc * irc;
+            const float x = 1.f - 2.f * u;
+            float T[N1], TG[N1];
+            cheby_f<N1>(x, T);
+            cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+            const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+            float dfc = 0.f, drn = 0.f;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                float s = 0.f, sg = 0.f;
+#pragma unroll
+                for (int n = 0; n < N1; ++n) { s += Wt[p * N1 + n] * T[n]; sg += Wt[p * N1 + n] * TG[n]; }
+                dfc += gfp[p] * s;
+                drn += gfp[p] * sg;
+            }
+            const float gr = dfc * fcg + fc * drn;
+            g = make_float4(gr * d.x, gr * d.y, gr * d.z, 0.f);
+        }
+        if (a.accumulate) {
+            float4 o = a.P.g[e];
+            a.P.g[e] = make_float4(o.x + g.x, o.y + g.y, o.z + g.z, 0.f);
+        } else {
+            a.P.g[e] = g;
+        }
+    }
+}
+
+// =========================================================================== spherical
+template <int L, int NP>
+struct SphShape {
+    static constexpr int K = (L + 1) * (L + 1);
+    static constexpr int COLS = (K + 31) / 32;
+    static constexpr int KS = K | 1;                 // odd row stride: conflict-free lane writes
+    static constexpr int NPS = (NP + 3) & ~3;        // 16-byte rows for broadcast float4 reads
+    static constexpr int FWD_WARP_FLOATS =
+        (((32 * KS + 32 * NPS) > NP * K ? (32 * KS + 32 * NPS) : NP * K) + 3) & ~3;
+    static constexpr int BWD_WARP_FLOATS = K * NPS + 2 * K * 32;
+};
+
+template <int L, int NP, int N1>
+__global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
+    using S = SphShape<L, NP>;
+    extern __shared__ float smem[];
+    const int nW = a.T * a.T * NP * N1;
+    float* sW = smem;
+    load_fuse<NP, N1>(a.W, sW, nW);
+    __syncthreads();
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kDescWarps + wl;
+    if (a.s0 + w >= a.s1) return;
+    float* sY = smem + ((nW + 3) & ~3) + wl * S::FWD_WARP_FLOATS;  // [32][KS]
+    float* sC = sY + 32 * S::KS;                                       // [32][NPS]
+    const int at = atom_of(a, w);
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut, irc = 1.f / a.rcut;
+    float acc[NP][S::COLS];
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+        for (int c = 0; c < S::COLS; ++c) acc[p][c] = 0.f;
+    for (int base = 0; base < cnt; base += 32) {
+        const int k = base + lane;
+        float c[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) c[p] = 0.f;
+        float* y = sY + lane * S::KS;
+        bool valid = false;
+        if (k < cnt) {
+            const float4 d = a.P.dx[(size_t)at * M + k];
+            const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+            if (r < rc) {
+                valid = true;
+                const int tn = __float_as_int(d.w) - 1;
+                const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
+                float T[N1];
+                cheby_f<N1>(1.f - 2.f * u, T);
+                const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    float s = 0.f;
+#pragma unroll
+                    for (int n = 0; n < N1; ++n) s += Wt[p * N1 + n] * T[n];
+                    c[p] = fc * s;
+                }
+                const Angles an = angles_f(d.x, d.y, d.z, r);
+                sph_harm<L, false>(an, y, nullptr, 1);
+            }
+        }
+        if (!valid)
+#pragma unroll
+            for (int q = 0; q < S::K; ++q) y[q] = 0.f;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) sC[lane * S::NPS + p] = c[p];
+        __syncwarp();
+        const int nk = min(32, cnt - base);
+        for (int kk = 0; kk < nk; ++kk) {
+            float cv[S::NPS];
+            const float4* crow = reinterpret_cast<const float4*>(sC + kk * S::NPS);
+#pragma unroll
+            for (int q = 0; q < S::NPS / 4; ++q) {
+                const float4 v = crow[q];
+                cv[4 * q] = v.x; cv[4 * q + 1] = v.y; cv[4 * q + 2] = v.z; cv[4 * q + 3] = v.w;
+            }
+            const float* yrow = sY + kk * S::KS;
+#pragma unroll
+            for (int col = 0; col < S::COLS; ++col) {
+                const int lm = lane + 32 * col;
+                const float yv = lm < S::K ? yrow[lm] : 0.f;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) acc[p][col] += cv[p] * yv;
+            }
+        }
+        __syncwarp();
+    }
+    // A to global (backward input) and squared to shared memory for the power spectrum
+    float* Aout = a.A + (size_t)w * NP * S::K;
+    float* sA2 = sY;
+#pragma unroll
+    for (int col = 0; col < S::COLS; ++col) {
+        const int lm = lane + 32 * col;
+        if (lm < S::K)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                Aout[p * S::K + lm] = acc[p][col];
+                sA2[p * S::K + lm] = acc[p][col] * acc[p][col];
+            }
+    }
+    __syncwarp();
+    float* out = a.fp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+    for (int e = lane; e < NP * (L + 1); e += 32) {
+        const int p = e / (L + 1), l = e - p * (L + 1);
+        float s = 0.f;
+        for (int m = 0; m <= 2 * l; ++m) s += sA2[p * S::K + l * l + m];
+        out[e] = kPi4 / (float)(2 * l + 1) * s;
+    }
+}
+
+template <int L, int NP, int N1>
+__global__ void __launch_bounds__(32 * kDescWarps) k_sph_bwd(DescArgs a) {
+    using S = SphShape<L, NP>;
+    extern __shared__ float smem[];
+    const int nW = a.T * a.T * NP * N1;
+    float* sW = smem;
+    load_fuse<NP, N1>(a.W, sW, nW);
+    __syncthreads();
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kDescWarps + wl;
+    if (a.s0 + w >= a.s1) return;
+    float* sG = smem + ((nW + 3) & ~3) + wl * S::BWD_WARP_FLOATS;  // [K][NPS]
+    float* sY = sG + S::K * S::NPS;                                   // [K][32]
+    float* sYt = sY + S::K * 32;                                      // [K][32]
+    const int at = atom_of(a, w);
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut, irc = 1.f / a.rcut;
+    // G[p][lm] = 2 * 4pi/(2l+1) * dE/dfp[p][l] * A[p][lm], stored transposed
+    {
+        const float* Ain = a.A + (size_t)w * NP * S::K;
+        const float* gf = a.gfp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+        for (int lm = lane; lm < S::K; lm += 32) {
+            int l = 0;
+            while ((l + 1) * (l + 1) <= lm) ++l;
+            const float coef = 2.f * kPi4 / (float)(2 * l + 1);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) sG[lm * S::NPS + p] = coef * gf[p * (L + 1) + l] * Ain[p * S::K + lm];
+#pragma unroll
+            for (int p = NP; p < S::NPS; ++p) sG[lm * S::NPS + p] = 0.f;
+        }
+        __syncwarp();
+    }
+    for (int base = 0; base < cnt; base += 32) {
+        const int k = base + lane;
+        float c[NP], rnp[NP], rnpg[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) { c[p] = 0.f; rnp[p] = 0.f; rnpg[p] = 0.f; }
+        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        float r = 1.f, fc = 0.f, fcg = 0.f;
+        Angles an;
+        an.ct = an.st = an.sp = 0.f; an.cp = 1.f; an.dxy = 0.f; an.pole = true;
+        bool valid = false;
+        if (k < cnt) {
+            d = a.P.dx[(size_t)at * M + k];
+            r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+            valid = r < rc;
+        }
+        if (valid) {
+            const int tn = __float_as_int(d.w) - 1;
+            const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1;
+            fc = fc2 * fc2;
+            fcg = 8.f * fc1 * fc2 * irc * irc;
+            const float x = 1.f - 2.f * u;
+            float T[N1], TG[N1];
+            cheby_f<N1>(x, T);
+            cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+            const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                float s = 0.f, sg = 0.f;
+#pragma unroll
+                for (int n = 0; n < N1; ++n) { s += Wt[p * N1 + n] * T[n]; sg += Wt[p * N1 + n] * TG[n]; }
+                rnp[p] = s; rnpg[p] = sg; c[p] = fc * s;
+            }
+            an = angles_f(d.x, d.y, d.z, r);
+            sph_harm<L, true>(an, sY + lane, sYt + lane, 32);
+        } else {
+#pragma unroll
+            for (int q = 0; q < S::K; ++q) { sY[q * 32 + lane] = 0.f; sYt[q * 32 + lane] = 0.f; }
+        }
+        float dc[NP];
+#pragma unroll
+        for (int p = 0; p < NP; ++p) dc[p] = 0.f;
+        float gth = 0.f, gph = 0.f;
+#pragma unroll
+        for (int l = 0; l <= L; ++l) {
+            const int c0 = l * l + l;
+            {
+                const float4* gr = reinterpret_cast<const float4*>(sG + c0 * S::NPS);
+                float gv[S::NPS];
+#pragma unroll
+                for (int q = 0; q < S::NPS / 4; ++q) {
+                    const float4 v = gr[q];
+                    gv[4 * q] = v.x; gv[4 * q + 1] = v.y; gv[4 * q + 2] = v.z; gv[4 * q + 3] = v.w;
+                }
+                const float yv = sY[c0 * 32 + lane], ytv = sYt[c0 * 32 + lane];
+                float dY = 0.f;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) { dY += c[p] * gv[p]; dc[p] += gv[p] * yv; }
+                gth += dY * ytv;
+            }
+#pragma unroll
+            for (int m = 1; m <= l; ++m) {
+                const float4* gp4 = reinterpret_cast<const float4*>(sG + (c0 + m) * S::NPS);
+                const float4* gm4 = reinterpret_cast<const float4*>(sG + (c0 - m) * S::NPS);
+                float gp[S::NPS], gm[S::NPS];
+#pragma unroll
+                for (int q = 0; q < S::NPS / 4; ++q) {
+                    const float4 v = gp4[q], u = gm4[q];
+                    gp[4 * q] = v.x; gp[4 * q + 1] = v.y; gp[4 * q + 2] = v.z; gp[4 * q + 3] = v.w;
+                    gm[4 * q] = u.x; gm[4 * q + 1] = u.y; gm[4 * q + 2] = u.z; gm[4 * q + 3] = u.w;
+                }
+                const float yp = sY[(c0 + m) * 32 + lane], ym = sY[(c0 - m) * 32 + lane];
+                const float ytp = sYt[(c0 + m) * 32 + lane], ytm = sYt[(c0 - m) * 32 + lane];
+                float dYp = 0.f, dYm = 0.f;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    dYp += c[p] * gp[p];
+                    dYm += c[p] * gm[p];
+                    dc[p] += gp[p] * yp + gm[p] * ym;
+                }
+                gth += dYp * ytp + dYm * ytm;
+                gph += (float)m * (dYm * yp - dYp * ym);
+            }
+        }
+        if (k < cnt) {
+            const size_t e = (size_t)at * M + k;
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) {
+                float dfc = 0.f, drn = 0.f;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) { dfc += dc[p] * rnp[p]; drn += dc[p] * rnpg[p]; }
+                const float gr = dfc * fcg + fc * drn;
+                const float ir = 1.f / r;
+                const float tpx = -an.ct * an.cp * ir, tpy = -an.ct * an.sp * ir, tpz = an.st * ir;
+                const float ppx = an.pole ? 0.f : an.sp / an.dxy, ppy = an.pole ? 0.f : -an.cp / an.dxy;
+                g.x = gr * d.x + gth * tpx + gph * ppx;
+                g.y = gr * d.y + gth * tpy + gph * ppy;
+                g.z = gr * d.z + gth * tpz;
+            }
+            if (a.accumulate) {
+                if (valid) {
+                    const float4 o = a.P.g[e];
+                    a.P.g[e] = make_float4(o.x + g.x, o.y + g.y, o.z + g.z, 0.f);
+                }
+            } else {
+                a.P.g[e] = g;
+            }
+        }
+    }
+}
+
+// =========================================================================== dispatch
+namespace {
+
+template <int NP, int N1>
+cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
+    const int n = a.s1 - a.s0;
+    if (n <= 0) return cudaSuccess;
+    const int grid = (n + kDescWarps - 1) / kDescWarps;
+    const size_t sm = sizeof(float) * a.T * a.T * NP * N1;
+    if (fwd) k_radial_fwd<NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    else k_radial_bwd<NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L, int NP, int N1>
+cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
+    using S = SphShape<L, NP>;
+    const int n = a.s1 - a.s0;
+    if (n <= 0) return cudaSuccess;
+    const int grid = (n + kDescWarps - 1) / kDescWarps;
+    const size_t wbytes = sizeof(float) * (((size_t)a.T * a.T * NP * N1 + 3) & ~(size_t)3);
+    const size_t sm = wbytes + sizeof(float) * kDescWarps * (fwd ? S::FWD_WARP_FLOATS : S::BWD_WARP_FLOATS);
+    cudaError_t e;
+    if (fwd) {
+        e = cudaFuncSetAttribute(k_sph_fwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k_sph_fwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(k_sph_bwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        k_sph_bwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Compiled shapes.  Radial: (NP, N1).  Spherical: (L, NP, N1).
+#define NNAP_RADIAL_SHAPES(X) X(11, 11) X(12, 6) X(4, 4) X(8, 4) X(12, 4) X(18, 9)
+#define NNAP_SPH_SHAPES(X)                                                                    \
+    X(6, 18, 9) X(4, 18, 9) X(4, 5, 5) X(2, 4, 4) X(2, 8, 4) X(2, 12, 4) X(3, 5, 4) X(2, 16, 4) \
+    X(3, 10, 5) X(6, 9, 9) X(4, 9, 9) X(3, 8, 4) X(4, 10, 5)
+
+bool desc_supported(int kind, int lmax, int np, int n1) {
+#define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return true;
+#define S_CASE(L_, P_, N_) if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return true;
+    NNAP_RADIAL_SHAPES(R_CASE)
+    NNAP_SPH_SHAPES(S_CASE)
+#undef R_CASE
+#undef S_CASE
+    return false;
+}
+
+cudaError_t launch_descriptor(int kind, int lmax, int np, int n1, const DescArgs& a, bool fwd, cudaStream_t st) {
+#define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return launch_radial<P_, N_>(a, fwd, st);
+#define S_CASE(L_, P_, N_) if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return launch_sph<L_, P_, N_>(a, fwd, st);
+    NNAP_RADIAL_SHAPES(R_CASE)
+    NNAP_SPH_SHAPES(S_CASE)
+#undef R_CASE
+#undef S_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace nnapgb

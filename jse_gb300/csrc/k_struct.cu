@@ -1,0 +1,457 @@
+// Structure kernels: FP64 wrapping and cell binning, the full neighbour list,
+// the mirror index used by the atomic-free scatter, the species sort of atoms,
+// the force / per-atom virial gather and the per-structure FP64 reductions.
+//
+// Reference behaviour restated here:
+//   wrapping        IBox.wrapPBC / toDirect / toCartesian (IBox.java:145-222,
+//                   BoxPrism.java:162-175), including the snap of direct coordinates
+//                   within 1e-10 of an integer (MathEX.java:1213).  All FP64 operations
+//                   use explicit round-to-nearest intrinsics so that no multiply-add is
+//                   contracted and every rounding matches the reference's Java doubles.
+//   neighbours      NeighborListGetter.forEachNeighbor_ with check=true, half=false
+//                   (NeighborListGetter.java:1018-1050): all periodic images j' with
+//                   |(x_j + shift) - x_i|^2 < rcut^2 evaluated in FP64, images of i
+//                   itself included, (i, zero image) excluded (NeighborListGetter.java:119-173).
+//   scatter         NNAP.calEnergyForceVirial + IPairPotential accumulators
+//                   (NNAP.java:571-592, IPairPotential.java:919-1006): F_i -= g_ij,
+//                   F_j += g_ij, per-atom virial dx_ij (x) g_ij on j; computed here as a
+//                   gather over each atom's own row and the mirrored entries, without atomics.
+#include "common.cuh"
+
+namespace nnapgb {
+
+// ----------------------------------------------------------------- exact FP64 box math
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dd(double a, double b) { return __ddiv_rn(a, b); }
+
+__device__ __forceinline__ double snap_int(double v) {
+    double r = rint(v);
+    return fabs(ds(v, r)) < 1.0e-10 ? r : v;
+}
+
+__device__ void to_direct(const StructDev& S, double p[3]) {
+    const double x = p[0], y = p[1], z = p[2];
+    if (S.kind == 0) {
+        p[0] = dd(x, S.a[0]); p[1] = dd(y, S.b[1]); p[2] = dd(z, S.c[2]);
+    } else if (S.kind == 1) {
+        const double X = S.a[0], Y = S.b[1], Z = S.c[2], XY = S.b[0], XZ = S.c[0], YZ = S.c[1];
+        // x/X - XY*y/(X*Y) + (XY*YZ - XZ*Y)*z/(X*Y*Z)
+        p[0] = da(ds(dd(x, X), dd(dm(XY, y), dm(X, Y))), dd(dm(ds(dm(XY, YZ), dm(XZ, Y)), z), dm(dm(X, Y), Z)));
+        p[1] = ds(dd(y, Y), dd(dm(YZ, z), dm(Y, Z)));
+        p[2] = dd(z, Z);
+    } else {
+        p[0] = dd(da(da(dm(S.bc[0], x), dm(S.bc[1], y)), dm(S.bc[2], z)), S.vol);
+        p[1] = dd(da(da(dm(S.ca[0], x), dm(S.ca[1], y)), dm(S.ca[2], z)), S.vol);
+        p[2] = dd(da(da(dm(S.ab[0], x), dm(S.ab[1], y)), dm(S.ab[2], z)), S.vol);
+    }
+    p[0] = snap_int(p[0]); p[1] = snap_int(p[1]); p[2] = snap_int(p[2]);
+}
+
+__device__ void to_cartesian(const StructDev& S, double s[3]) {
+    const double u = s[0], v = s[1], w = s[2];
+    if (S.kind == 0) {
+        s[0] = dm(u, S.a[0]); s[1] = dm(v, S.b[1]); s[2] = dm(w, S.c[2]);
+    } else if (S.kind == 1) {
+        s[0] = da(da(dm(S.a[0], u), dm(S.b[0], v)), dm(S.c[0], w));
+        s[1] = da(dm(S.b[1], v), dm(S.c[1], w));
+        s[2] = dm(S.c[2], w);
+    } else {
+        s[0] = da(da(dm(S.a[0], u), dm(S.b[0], v)), dm(S.c[0], w));
+        s[1] = da(da(dm(S.a[1], u), dm(S.b[1], v)), dm(S.c[1], w));
+        s[2] = da(da(dm(S.a[2], u), dm(S.b[2], v)), dm(S.c[2], w));
+    }
+}
+
+// shift = (na*a + nb*b) + nc*c, component-wise, in this order.
+__device__ __forceinline__ void image_shift(const StructDev& S, int na, int nb, int nc, double sh[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) sh[d] = da(da(dm((double)na, S.a[d]), dm((double)nb, S.b[d])), dm((double)nc, S.c[d]));
+}
+
+// ----------------------------------------------------------------- wrap + cell binning
+// One thread per atom: wrap into the box, record the float copy used by the
+// candidate screen and the atom's cell, and count atoms per cell.
+__global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ x,
+                           const int* __restrict__ type, int n, int ntypes, double* __restrict__ xw,
+                           float4* __restrict__ xf, int* __restrict__ cell_of, int* __restrict__ cell_count,
+                           int* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const StructDev& st = S[sid[i]];
+    const int t = type[i];
+    if (t < 1 || t > ntypes) atomicOr(err, ERRBIT_BAD_TYPE);
+    double p[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+    to_direct(st, p);
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        if (p[d] < 0.0 || p[d] >= 1.0) p[d] = ds(p[d], floor(p[d]));
+    to_cartesian(st, p);
+    xw[3 * i] = p[0]; xw[3 * i + 1] = p[1]; xw[3 * i + 2] = p[2];
+    xf[i] = make_float4((float)p[0], (float)p[1], (float)p[2], __int_as_float(t));
+    double f[3] = {p[0], p[1], p[2]};
+    to_direct(st, f);
+    int c[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int ci = (int)floor(f[d] * (double)st.nc[d]);
+        c[d] = min(max(ci, 0), st.nc[d] - 1);
+    }
+    const int cid = st.c0 + c[0] + st.nc[0] * (c[1] + st.nc[1] * c[2]);
+    cell_of[i] = cid;
+    atomicAdd(&cell_count[cid], 1);
+}
+
+// Exclusive scan of n ints (one CTA of 1024 threads, sequential chunks); out has n+1 entries.
+__global__ void k_scan_excl(const int* __restrict__ in, int n, int* __restrict__ out) {
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += 1024) {
+        const int i = base + tid;
+        int v = i < n ? in[i] : 0;
+        int s = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += u;
+        }
+        if (lane == 31) warp_tot[w] = s;
+        __syncthreads();
+        if (w == 0) {
+            int t = warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += u;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        const int before = (w ? warp_tot[w - 1] : 0) + carry;
+        if (i < n) out[i] = before + s - v;
+        __syncthreads();
+        if (tid == 1023) carry = before + s;
+        __syncthreads();
+    }
+    if (tid == 0) out[n] = carry;
+}
+
+__global__ void k_fill_cells(const int* __restrict__ cell_of, int n, const int* __restrict__ cell_start,
+                             int* __restrict__ cell_fill, int* __restrict__ cell_atoms) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = cell_of[i];
+    cell_atoms[cell_start[c] + atomicAdd(&cell_fill[c], 1)] = i;
+}
+
+// Order each cell's atoms by index so that every neighbour row is deterministic.
+__global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int* __restrict__ cell_atoms) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const int b = cell_start[c], e = cell_start[c + 1];
+    for (int k = b + 1; k < e; ++k) {
+        const int v = cell_atoms[k];
+        int q = k - 1;
+        while (q >= b && cell_atoms[q] > v) { cell_atoms[q + 1] = cell_atoms[q]; --q; }
+        cell_atoms[q + 1] = v;
+    }
+}
+
+// ----------------------------------------------------------------- neighbour rows
+// One warp per atom.  Candidate cells are visited in a fixed order; within a batch
+// of 32 cells the candidates are spread over the lanes, screened in FP32 against
+// rc^2 plus a rounding margin, and confirmed with the exact FP64 test.  Accepted
+// pairs are compacted in candidate order with a ballot, so rows are deterministic.
+constexpr int kNbWarps = 4;
+
+__global__ void __launch_bounds__(32 * kNbWarps)
+k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ xw,
+            const float4* __restrict__ xf, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+            const int* __restrict__ cell_atoms, int n, PairBufs P, int* __restrict__ err, int* __restrict__ max_count) {
+    __shared__ int s_incl[kNbWarps][32], s_start[kNbWarps][32];
+    __shared__ uint32_t s_img[kNbWarps][32];
+    __shared__ double s_sh[kNbWarps][32][3];
+    __shared__ float s_fsh[kNbWarps][32][3];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kNbWarps + w;
+    if (i >= n) return;
+    const StructDev& st = S[sid[i]];
+    const int M = P.M;
+    const int cl = cell_of[i] - st.c0;
+    const int ci0 = cl % st.nc[0], ci1 = (cl / st.nc[0]) % st.nc[1], ci2 = cl / (st.nc[0] * st.nc[1]);
+    const int wa = 2 * st.R[0] + 1, wb = 2 * st.R[1] + 1;
+    const int noff = wa * wb * (2 * st.R[2] + 1);
+    const double xi = xw[3 * i], yi = xw[3 * i + 1], zi = xw[3 * i + 2];
+    const float4 fi = xf[i];
+    int cnt = 0;
+    for (int o0 = 0; o0 < noff; o0 += 32) {
+        const int o = o0 + lane;
+        int ccount = 0;
+        if (o < noff) {
+            const int oa = o % wa - st.R[0], ob = (o / wa) % wb - st.R[1], oc = o / (wa * wb) - st.R[2];
+            const int q0 = ci0 + oa, q1 = ci1 + ob, q2 = ci2 + oc;
+            const int na = (q0 >= 0) ? q0 / st.nc[0] : -((-q0 + st.nc[0] - 1) / st.nc[0]);
+            const int nb = (q1 >= 0) ? q1 / st.nc[1] : -((-q1 + st.nc[1] - 1) / st.nc[1]);
+            const int nc = (q2 >= 0) ? q2 / st.nc[2] : -((-q2 + st.nc[2] - 1) / st.nc[2]);
+            const int c0 = q0 - na * st.nc[0], c1 = q1 - nb * st.nc[1], c2 = q2 - nc * st.nc[2];
+            const int cid = st.c0 + c0 + st.nc[0] * (c1 + st.nc[1] * c2);
+            const int cs = cell_start[cid];
+            ccount = cell_start[cid + 1] - cs;
+            s_start[w][lane] = cs;
+            s_img[w][lane] = pack_img(na, nb, nc);
+            double sh[3];
+            image_shift(st, na, nb, nc, sh);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) { s_sh[w][lane][d] = sh[d]; s_fsh[w][lane][d] = (float)sh[d]; }
+        }
+        int incl = ccount;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += u;
+        }
+        s_incl[w][lane] = incl;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        for (int cb = 0; cb < total; cb += 32) {
+            const int cidx = cb + lane;
+            bool acc = false;
+            int j = 0, slot = 0;
+            double dxv = 0.0, dyv = 0.0, dzv = 0.0;
+            if (cidx < total) {
+                int lo = 0, hi = 31;  // first slot with incl > cidx
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_incl[w][mid] > cidx) hi = mid; else lo = mid + 1;
+                }
+                slot = lo;
+                const int before = slot ? s_incl[w][slot - 1] : 0;
+                j = cell_atoms[s_start[w][slot] + (cidx - before)];
+                const uint32_t img = s_img[w][slot];
+                if (!(j == i && img == pack_img(0, 0, 0))) {
+                    const float4 fj = xf[j];
+                    const float fx = (fj.x + s_fsh[w][slot][0]) - fi.x;
+                    const float fy = (fj.y + s_fsh[w][slot][1]) - fi.y;
+                    const float fz = (fj.z + s_fsh[w][slot][2]) - fi.z;
+                    if (fx * fx + fy * fy + fz * fz < st.rc2_hi) {
+                        dxv = ds(da(xw[3 * j], s_sh[w][slot][0]), xi);
+                        dyv = ds(da(xw[3 * j + 1], s_sh[w][slot][1]), yi);
+                        dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
+                        const double d2 = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv));
+                        acc = d2 < st.rc2;
+                    }
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, acc);
+            if (acc) {
+                const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                if (pos < M) {
+                    const size_t e = (size_t)i * M + pos;
+                    P.key[e] = pair_key(j, s_img[w][slot]);
+                    P.dx[e] = make_float4((float)dxv, (float)dyv, (float)dzv, xf[j].w);
+                }
+            }
+            cnt += __popc(m);
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        P.count[i] = cnt;
+        if (cnt > M) atomicOr(err, ERRBIT_CAPACITY);
+        atomicMax(max_count, cnt);
+    }
+}
+
+// Mirror index: for entry (i -> j, image n) the position of (j -> i, image -n) in j's row.
+__global__ void k_mirror(PairBufs P, int n, int* __restrict__ err) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int M = P.M;
+    const int i = (int)(t / M), k = (int)(t % M);
+    if (i >= n) return;
+    const int ci = min(P.count[i], M);
+    if (k >= ci) return;
+    const uint64_t key = P.key[(size_t)i * M + k];
+    const int j = (int)(key >> 32);
+    int na, nb, nc;
+    unpack_img((uint32_t)key, na, nb, nc);
+    const uint64_t want = pair_key(i, pack_img(-na, -nb, -nc));
+    const int cj = min(P.count[j], M);
+    const uint64_t* row = P.key + (size_t)j * M;
+    int found = -1;
+    for (int q = 0; q < cj; ++q)
+        if (row[q] == want) { found = q; break; }
+    if (found < 0) {
+        atomicOr(err, ERRBIT_NO_MIRROR);
+        P.rev[(size_t)i * M + k] = (int)((size_t)i * M + k);
+    } else {
+        P.rev[(size_t)i * M + k] = (int)((size_t)j * M + found);
+    }
+}
+
+// ----------------------------------------------------------------- species sort
+constexpr int kSortBlock = 256;
+
+__global__ void k_type_hist(const int* __restrict__ type, int n, int T, int* __restrict__ block_counts) {
+    __shared__ int h[kMaxTypes];
+    if (threadIdx.x < kMaxTypes) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * kSortBlock + threadIdx.x;
+    if (i < n) {
+        const int t = type[i] - 1;
+        if (t >= 0 && t < T) atomicAdd(&h[t], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < T) block_counts[blockIdx.x * T + threadIdx.x] = h[threadIdx.x];
+}
+
+// In place: block_counts -> exclusive offsets in (type, block) order; type_start[T+1].
+__global__ void k_type_offsets(int* __restrict__ block_counts, int nb, int T, int* __restrict__ type_start) {
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int t = 0; t < T; ++t) {
+        if (tid == 0) type_start[t] = carry;
+        __syncthreads();
+        for (int base = 0; base < nb; base += 1024) {
+            const int b = base + tid;
+            const int v = b < nb ? block_counts[b * T + t] : 0;
+            int s = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int u = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += u;
+            }
+            if (lane == 31) warp_tot[w] = s;
+            __syncthreads();
+            if (w == 0) {
+                int q = warp_tot[lane];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    int u = __shfl_up_sync(0xffffffffu, q, o);
+                    if (lane >= o) q += u;
+                }
+                warp_tot[lane] = q;
+            }
+            __syncthreads();
+            const int before = (w ? warp_tot[w - 1] : 0) + carry;
+            if (b < nb) block_counts[b * T + t] = before + s - v;
+            __syncthreads();
+            if (tid == 1023) carry = before + s;
+            __syncthreads();
+        }
+    }
+    if (tid == 0) type_start[T] = carry;
+}
+
+// Stable scatter: slot = offset(type, block) + rank of the atom among same-type atoms of its block.
+__global__ void k_type_scatter(const int* __restrict__ type, int n, int T, const int* __restrict__ block_offsets,
+                               int* __restrict__ perm) {
+    __shared__ int wc[kSortBlock / 32][kMaxTypes];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kSortBlock + threadIdx.x;
+    const int t = i < n ? type[i] - 1 : -1;
+    unsigned mine = 0;
+    for (int q = 0; q < T; ++q) {
+        const unsigned m = __ballot_sync(0xffffffffu, t == q);
+        if (lane == 0) wc[w][q] = __popc(m);
+        if (t == q) mine = m;
+    }
+    __syncthreads();
+    if (t < 0 || t >= T) return;
+    int rank = __popc(mine & ((1u << lane) - 1u));
+    for (int q = 0; q < w; ++q) rank += wc[q][t];
+    perm[block_offsets[blockIdx.x * T + t] + rank] = i;
+}
+
+// ----------------------------------------------------------------- gather
+// One warp per atom a: F_a = sum_k (g[mirror(a,k)] - g[a,k]);
+// W_a = sum_k dx[mirror(a,k)] (x) g[mirror(a,k)], accumulated in FP64.
+__global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double* __restrict__ virials) {
+    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (a >= n) return;
+    const int M = P.M;
+    const int cnt = min(P.count[a], M);
+    double f[3] = {0.0, 0.0, 0.0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = lane; k < cnt; k += 32) {
+        const size_t e = (size_t)a * M + k;
+        const float4 go = P.g[e];
+        const int r = P.rev[e];
+        const float4 gr = P.g[r];
+        const float4 dr = P.dx[r];
+        f[0] += (double)gr.x - (double)go.x;
+        f[1] += (double)gr.y - (double)go.y;
+        f[2] += (double)gr.z - (double)go.z;
+        const double x = dr.x, y = dr.y, z = dr.z, gx = gr.x, gy = gr.y, gz = gr.z;
+        v[0] += x * gx; v[1] += y * gy; v[2] += z * gz;
+        v[3] += x * gy; v[4] += x * gz; v[5] += y * gz;
+        v[6] += y * gx; v[7] += z * gx; v[8] += z * gy;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) f[d] += __shfl_xor_sync(0xffffffffu, f[d], o);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) v[d] += __shfl_xor_sync(0xffffffffu, v[d], o);
+    }
+    if (lane < 3) forces[3 * (size_t)a + lane] = lane == 0 ? f[0] : (lane == 1 ? f[1] : f[2]);
+    if (lane < 9) {
+        double out = v[0];
+#pragma unroll
+        for (int d = 1; d < 9; ++d) if (lane == d) out = v[d];
+        virials[9 * (size_t)a + lane] = out;
+    }
+}
+
+// ----------------------------------------------------------------- per-structure totals
+// chunk c covers atoms [cb[c], ce[c]); partial[c][0] = sum E, partial[c][1..9] = sum W.
+constexpr int kRedBlock = 256;
+
+__global__ void k_reduce_chunks(const int* __restrict__ cb, const int* __restrict__ ce,
+                                const double* __restrict__ e_atom, const double* __restrict__ virials,
+                                double* __restrict__ partial) {
+    __shared__ double sm[10][kRedBlock / 32];
+    const int c = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = cb[c] + threadIdx.x; a < ce[c]; a += kRedBlock) {
+        s[0] += e_atom[a];
+#pragma unroll
+        for (int d = 0; d < 9; ++d) s[1 + d] += virials[9 * (size_t)a + d];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int d = 0; d < 10; ++d) s[d] += __shfl_xor_sync(0xffffffffu, s[d], o);
+    if (lane == 0)
+#pragma unroll
+        for (int d = 0; d < 10; ++d) sm[d][w] = s[d];
+    __syncthreads();
+    if (threadIdx.x < 10) {
+        double t = 0.0;
+        for (int q = 0; q < kRedBlock / 32; ++q) t += sm[threadIdx.x][q];
+        partial[10 * (size_t)c + threadIdx.x] = t;
+    }
+}
+
+// structure s owns chunks [sc[s], sc[s+1]).
+__global__ void k_reduce_structs(const int* __restrict__ sc, int nstruct, const double* __restrict__ partial,
+                                 double* __restrict__ energy, double* __restrict__ virial) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nstruct) return;
+    double t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int c = sc[s]; c < sc[s + 1]; ++c)
+#pragma unroll
+        for (int d = 0; d < 10; ++d) t[d] += partial[10 * (size_t)c + d];
+    energy[s] = t[0];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) virial[9 * (size_t)s + d] = t[1 + d];
+}
+
+}  // namespace nnapgb

@@ -1,0 +1,46 @@
+// Host-side NNAP model: parsed from the reference's JSON model format and packed
+// into the per-species blocks the GPU kernels consume.
+#pragma once
+
+#include <string>
+#include <vector>
+
+namespace nnapgb {
+
+enum { KIND_RADIAL = 0, KIND_SPHERICAL = 1 };
+
+// One (possibly merged) sub-basis of a species.  W is the internal radial-fuse
+// matrix W[t_nei-1][np][n] (WTypeBasis.java:202-304); the descriptor entries of this
+// sub-basis start at fp_off within the species' descriptor.
+struct SubBasis {
+    int kind = KIND_SPHERICAL;
+    int nmax = 5, lmax = 0, np = 0;
+    int fp_off = 0, size = 0;
+    double rcut = 6.0;
+    std::vector<double> W;  // T * np * (nmax+1)
+};
+
+struct Species {
+    std::string symbol;
+    std::vector<SubBasis> subs;
+    int D = 0;                               // descriptor length
+    std::vector<int> hidden;                 // hidden widths
+    std::vector<std::vector<double>> Wh;     // per layer, row-major [out][in]
+    std::vector<std::vector<double>> bh;     // per layer
+    std::vector<double> wo;                  // output weights
+    double bo = 0.0;                         // output bias
+    std::vector<double> mu, sigma;           // descriptor normalisation
+    double mu_e = 0.0, sigma_e = 1.0;        // energy denormalisation (mu includes ref_eng)
+};
+
+struct Model {
+    std::vector<Species> sp;
+    std::string units;
+    double rcut_max = 0.0;
+    int ntypes() const { return (int)sp.size(); }
+};
+
+// Parse and pack; throws std::runtime_error with a message on invalid input.
+Model load_model(const char* text, size_t len);
+
+}  // namespace nnapgb

@@ -1,0 +1,25 @@
+// Tensor-core (tcgen05, BF16 operands, FP32 accumulation in TMEM) evaluation of the
+// per-species network and its input gradient: the mixed-precision path.
+#pragma once
+
+#include <string>
+
+#include "desc.cuh"
+#include "model.hpp"
+
+namespace nnapgb {
+
+struct NetTC {
+    bool ready = false;
+    int D = 0, Dp = 0, H1 = 0, H2 = 0;
+    void* blob = nullptr;     // device: packed operand images and FP32 vectors
+    size_t blob_bytes = 0;
+};
+
+// Pack a species' network for the tensor-core kernel; false (with a reason) when the
+// shape is outside what the kernel implements.
+bool net_tc_prepare(const Species& sp, NetTC& tc, std::string& why);
+void net_tc_release(NetTC& tc);
+cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, cudaStream_t st);
+
+}  // namespace nnapgb

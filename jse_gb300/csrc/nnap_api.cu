@@ -1,0 +1,850 @@
+// C ABI of the NNAP GB300 evaluator: handle lifetime, device buffers and the
+// evaluation pipeline (see include/nnap_gb300.h for the contract).
+//
+// Pipeline of one evaluation over a batch of structures (a single structure is a
+// batch of one):
+//   k_wrap_bin -> k_scan_excl -> k_fill_cells -> k_sort_cells -> k_neighbors
+//   -> species sort (k_type_hist, k_type_offsets, k_type_scatter)
+//   -> [one host synchronisation: neighbour capacity, species ranges, error bits]
+//   -> k_mirror -> descriptor forward (per run of species sharing a basis shape, per
+//   sub-basis) -> network per species -> descriptor backward -> k_gather
+//   -> k_reduce_chunks -> k_reduce_structs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/nnap_gb300.h"
+#include "common.cuh"
+#include "desc.cuh"
+#include "model.hpp"
+#include "net_tc.cuh"
+
+using namespace nnapgb;
+
+namespace nnapgb {
+// k_struct.cu
+__global__ void k_wrap_bin(const StructDev*, const int*, const double*, const int*, int, int, double*, float4*, int*,
+                           int*, int*);
+__global__ void k_scan_excl(const int*, int, int*);
+__global__ void k_fill_cells(const int*, int, const int*, int*, int*);
+__global__ void k_sort_cells(const int*, int, int*);
+__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const int*, const int*,
+                            const int*, int, PairBufs, int*, int*);
+__global__ void k_mirror(PairBufs, int, int*);
+__global__ void k_type_hist(const int*, int, int, int*);
+__global__ void k_type_offsets(int*, int, int, int*);
+__global__ void k_type_scatter(const int*, int, int, const int*, int*);
+__global__ void k_gather(PairBufs, int, double*, double*);
+__global__ void k_reduce_chunks(const int*, const int*, const double*, const double*, double*);
+__global__ void k_reduce_structs(const int*, int, const double*, double*, double*);
+}  // namespace nnapgb
+
+namespace {
+
+constexpr int kNbWarps = 4;       // must match k_struct.cu
+constexpr int kSortBlock = 256;   // must match k_struct.cu
+constexpr int kRedBlock = 256;    // must match k_struct.cu
+constexpr int kRedChunk = 4096;   // atoms per reduction chunk
+
+struct CudaFail : std::runtime_error {
+    cudaError_t code;
+    CudaFail(cudaError_t c, const char* what)
+        : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c) {}
+};
+struct ApiFail : std::runtime_error {
+    int status;
+    ApiFail(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define CK(call)                                            \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) throw CudaFail(e_, #call);   \
+    } while (0)
+
+// Grow-only device array.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    void ensure(size_t n) {
+        if (n <= cap) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n, 1);
+        CK(cudaMalloc(&p, want * sizeof(T)));
+        cap = want;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct SubShape {
+    int kind, lmax, np, n1;
+    double rcut;
+    bool operator==(const SubShape& o) const {
+        return kind == o.kind && lmax == o.lmax && np == o.np && n1 == o.n1 && rcut == o.rcut;
+    }
+};
+
+// Species t0..t1-1 sharing the sub-basis shapes (and descriptor length).
+struct Run {
+    int t0, t1;
+    std::vector<SubShape> subs;
+    std::vector<int> fp_off;
+    std::vector<DevBuf<float>> W;  // per sub: [T][T][NP][N1]
+};
+
+struct NetDev {
+    int D, nlayer;
+    int H[4];
+    DevBuf<float> w32;
+    double mu_e, sigma_e;
+    NetTC tc;  // tensor-core parameters (mixed precision)
+};
+
+}  // namespace
+
+struct nnap_handle {
+    Model model;
+    int precision = NNAP_PREC_FP32;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool dead = false;
+    int launches = 0;
+    int fp_stride = 0;
+    std::vector<Run> runs;
+    std::vector<NetDev> nets;
+    // work buffers
+    DevBuf<double> x, xw, e_atom, forces, virials, energy, virial, partial;
+    DevBuf<int> type, sid, cell_of, cell_count, cell_fill, cell_start, cell_atoms, perm, block_counts, type_start;
+    DevBuf<int> chunk_b, chunk_e, struct_chunks, status;
+    DevBuf<float4> xf;
+    DevBuf<StructDev> sdev;
+    DevBuf<uint64_t> pkey;
+    DevBuf<float4> pdx, pg;
+    DevBuf<int> prev, pcount;
+    DevBuf<float> fp, gfp, A;
+    int M = 0;
+    int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
+    bool profiling = false;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    void mark(int k) {
+        if (profiling) CK(cudaEventRecord(ev[k], stream));
+    }
+};
+
+namespace {
+
+int fail(nnap_handle* h, int status, const std::string& m) {
+    if (h) h->err = m;
+    return status;
+}
+
+template <class F>
+int guarded(nnap_handle* h, F&& f) {
+    if (!h) return NNAP_ERR_ARG;
+    if (h->dead) return fail(h, NNAP_ERR_DEAD, "this NNAP is dead");
+    h->err.clear();
+    try {
+        CK(cudaSetDevice(h->device));
+        return f();
+    } catch (const ApiFail& e) {
+        return fail(h, e.status, e.what());
+    } catch (const CudaFail& e) {
+        return fail(h, NNAP_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(h, NNAP_ERR_CAPACITY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(h, NNAP_ERR_ARG, e.what());
+    }
+}
+
+// ------------------------------------------------------------------ model upload
+void upload_model(nnap_handle* h) {
+    const Model& m = h->model;
+    const int T = m.ntypes();
+    if (T > kMaxTypes) throw ApiFail(NNAP_ERR_UNSUPPORTED, "more than 16 species");
+    int dmax = 0;
+    for (auto& sp : m.sp) dmax = std::max(dmax, sp.D);
+    h->fp_stride = (dmax + 3) & ~3;
+    // runs of consecutive species with identical sub-basis shapes
+    for (int t = 0; t < T;) {
+        Run r;
+        r.t0 = t;
+        for (auto& b : m.sp[t].subs) {
+            r.subs.push_back({b.kind, b.lmax, b.np, b.nmax + 1, b.rcut});
+            r.fp_off.push_back(b.fp_off);
+        }
+        int u = t + 1;
+        while (u < T) {
+            const auto& su = m.sp[u].subs;
+            bool same = su.size() == r.subs.size() && m.sp[u].D == m.sp[t].D;
+            for (size_t k = 0; same && k < su.size(); ++k)
+                same = r.subs[k] == SubShape{su[k].kind, su[k].lmax, su[k].np, su[k].nmax + 1, su[k].rcut};
+            if (!same) break;
+            ++u;
+        }
+        r.t1 = u;
+        for (size_t k = 0; k < r.subs.size(); ++k) {
+            const SubShape& s = r.subs[k];
+            if (!desc_supported(s.kind, s.lmax, s.np, s.n1)) {
+                char buf[160];
+                std::snprintf(buf, sizeof buf, "no compiled descriptor kernel for kind=%d lmax=%d np=%d nmax=%d",
+                              s.kind, s.lmax, s.np, s.n1 - 1);
+                throw ApiFail(NNAP_ERR_UNSUPPORTED, buf);
+            }
+            std::vector<float> W((size_t)T * T * s.np * s.n1, 0.f);
+            for (int tc = r.t0; tc < r.t1; ++tc) {
+                const std::vector<double>& src = m.sp[tc].subs[k].W;  // [tn][np][n1]
+                for (size_t q = 0; q < src.size(); ++q) W[(size_t)tc * T * s.np * s.n1 + q] = (float)src[q];
+            }
+            r.W.emplace_back();
+            r.W.back().ensure(W.size());
+            CK(cudaMemcpy(r.W.back().p, W.data(), W.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
+        h->runs.push_back(std::move(r));
+        t = u;
+    }
+    // networks
+    h->nets.resize(T);
+    for (int t = 0; t < T; ++t) {
+        const Species& sp = m.sp[t];
+        NetDev& nd = h->nets[t];
+        if (sp.hidden.size() > 4) throw ApiFail(NNAP_ERR_UNSUPPORTED, "more than 4 hidden layers");
+        nd.D = sp.D;
+        nd.nlayer = (int)sp.hidden.size();
+        for (int l = 0; l < nd.nlayer; ++l) {
+            nd.H[l] = sp.hidden[l];
+            if (sp.hidden[l] > 256) throw ApiFail(NNAP_ERR_UNSUPPORTED, "hidden width above 256");
+        }
+        nd.mu_e = sp.mu_e;
+        nd.sigma_e = sp.sigma_e;
+        std::vector<float> w;
+        for (int i = 0; i < sp.D; ++i) w.push_back((float)sp.mu[i]);
+        for (int i = 0; i < sp.D; ++i) w.push_back((float)(1.0 / sp.sigma[i]));
+        int in = sp.D;
+        for (int l = 0; l < nd.nlayer; ++l) {
+            const int H = sp.hidden[l];
+            for (int i = 0; i < in; ++i)
+                for (int o = 0; o < H; ++o) w.push_back((float)sp.Wh[l][(size_t)o * in + i]);
+            for (size_t q = 0; q < sp.Wh[l].size(); ++q) w.push_back((float)sp.Wh[l][q]);
+            for (int o = 0; o < H; ++o) w.push_back((float)sp.bh[l][o]);
+            in = H;
+        }
+        for (int o = 0; o < in; ++o) w.push_back((float)sp.wo[o]);
+        w.push_back((float)sp.bo);
+        nd.w32.ensure(w.size());
+        CK(cudaMemcpy(nd.w32.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+        if (h->precision == NNAP_PREC_MIXED) {
+            std::string why;
+            if (!net_tc_prepare(sp, nd.tc, why)) throw ApiFail(NNAP_ERR_UNSUPPORTED, why);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ structure setup (host)
+void cross3(const double* u, const double* v, double* r) {
+    r[0] = u[1] * v[2] - v[1] * u[2];
+    r[1] = u[2] * v[0] - v[2] * u[0];
+    r[2] = u[0] * v[1] - v[0] * u[1];
+}
+
+StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0) {
+    if (kind < 0 || kind > 2) throw ApiFail(NNAP_ERR_ARG, "box_kind must be 0, 1 or 2");
+    StructDev s;
+    std::memset(&s, 0, sizeof s);
+    s.kind = kind;
+    for (int d = 0; d < 3; ++d) { s.a[d] = box[d]; s.b[d] = box[3 + d]; s.c[d] = box[6 + d]; }
+    if (kind == 0) {
+        s.a[1] = s.a[2] = s.b[0] = s.b[2] = s.c[0] = s.c[1] = 0.0;
+    } else if (kind == 1) {
+        s.a[1] = s.a[2] = s.b[2] = 0.0;
+    }
+    cross3(s.b, s.c, s.bc);
+    cross3(s.c, s.a, s.ca);
+    cross3(s.a, s.b, s.ab);
+    s.vol = (s.a[1] * s.b[2] - s.b[1] * s.a[2]) * s.c[0] + (s.a[2] * s.b[0] - s.b[2] * s.a[0]) * s.c[1] +
+            (s.a[0] * s.b[1] - s.b[0] * s.a[1]) * s.c[2];
+    if (!(s.vol > 0.0) || !std::isfinite(s.vol)) throw ApiFail(NNAP_ERR_ARG, "box must be right-handed with positive volume");
+    auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+    const double h[3] = {s.vol / nrm(s.bc), s.vol / nrm(s.ca), s.vol / nrm(s.ab)};
+    double ext = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        s.nc[d] = std::max(1, (int)std::floor(h[d] / rc));
+        s.nc[d] = std::min(s.nc[d], 1024);
+        s.R[d] = (int)std::floor(rc * s.nc[d] / h[d] + 1e-6) + 1;
+        if (s.R[d] > 64) throw ApiFail(NNAP_ERR_ARG, "box too thin for the cutoff");
+        ext += std::fabs(s.a[d]) + std::fabs(s.b[d]) + std::fabs(s.c[d]);
+    }
+    for (int d = 0; d < 3; ++d) { s.fa[d] = (float)s.a[d]; s.fb[d] = (float)s.b[d]; s.fc[d] = (float)s.c[d]; }
+    s.rc2 = rc * rc;
+    const int Rm = std::max(s.R[0], std::max(s.R[1], s.R[2]));
+    const double eps = 16.0 * (ext * (2 + Rm)) * std::ldexp(1.0, -24);
+    const double margin = 2.0 * std::sqrt(3.0) * rc * eps + 3.0 * eps * eps + 16.0 * rc * rc * std::ldexp(1.0, -24);
+    s.rc2_hi = (float)(rc * rc + margin) * (1.0f + 1e-6f);
+    s.a0 = a0;
+    s.n = n;
+    s.c0 = c0;
+    return s;
+}
+
+// ------------------------------------------------------------------ pipeline
+struct Batch {
+    int nstruct = 0, natoms = 0, ncells = 0;
+    std::vector<StructDev> sd;
+    std::vector<int> sid, cb, ce, sc;
+};
+
+Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes) {
+    Batch B;
+    B.nstruct = nstruct;
+    const double rc = h->model.rcut_max;
+    int a0 = 0, c0 = 0;
+    B.sc.push_back(0);
+    for (int s = 0; s < nstruct; ++s) {
+        if (natoms[s] < 0) throw ApiFail(NNAP_ERR_ARG, "negative atom count");
+        StructDev d = make_struct(kinds[s], boxes + 9 * s, rc, a0, natoms[s], c0);
+        B.sd.push_back(d);
+        for (int k = 0; k < natoms[s]; ++k) B.sid.push_back(s);
+        for (int b = 0; b < natoms[s]; b += kRedChunk) {
+            B.cb.push_back(a0 + b);
+            B.ce.push_back(a0 + std::min(natoms[s], b + kRedChunk));
+        }
+        B.sc.push_back((int)B.cb.size());
+        c0 += d.nc[0] * d.nc[1] * d.nc[2];
+        a0 += natoms[s];
+    }
+    B.natoms = a0;
+    B.ncells = c0;
+    return B;
+}
+
+struct Outputs {
+    double *energy = nullptr, *energies = nullptr, *forces = nullptr, *virial = nullptr, *virials = nullptr;
+};
+
+void grow_pairs(nnap_handle* h, int n, int M) {
+    h->M = M;
+    const size_t np = (size_t)n * M;
+    h->pkey.ensure(np);
+    h->pdx.ensure(np);
+    h->pg.ensure(np);
+    h->prev.ensure(np);
+}
+
+PairBufs pair_bufs(nnap_handle* h) {
+    PairBufs P;
+    P.M = h->M;
+    P.key = h->pkey.p;
+    P.dx = h->pdx.p;
+    P.rev = h->prev.p;
+    P.g = h->pg.p;
+    P.count = h->pcount.p;
+    return P;
+}
+
+int initial_capacity(const Batch& B, double rc) {
+    double dens = 0.0;
+    for (auto& s : B.sd)
+        if (s.n > 0) dens = std::max(dens, s.n / s.vol);
+    const double mean = 4.18879020478639 * rc * rc * rc * dens;
+    int M = (int)std::ceil(1.3 * mean + 24.0);
+    return std::max(32, (M + 7) & ~7);
+}
+
+// Runs the structure part of the pipeline up to the species sort and validates it.
+// On return: pair rows, mirror index and species slot order are ready on the device,
+// and type_start is known on the host.
+void build_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, std::vector<int>& type_start,
+                     bool want_types) {
+    const int n = B.natoms;
+    const int T = h->model.ntypes();
+    cudaStream_t st = h->stream;
+    h->sdev.ensure(B.nstruct);
+    h->sid.ensure(n);
+    CK(cudaMemcpyAsync(h->sdev.p, B.sd.data(), sizeof(StructDev) * B.nstruct, cudaMemcpyHostToDevice, st));
+    if (n) CK(cudaMemcpyAsync(h->sid.p, B.sid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    h->xw.ensure(3 * (size_t)n);
+    h->xf.ensure(n);
+    h->cell_of.ensure(n);
+    h->cell_count.ensure(B.ncells);
+    h->cell_fill.ensure(B.ncells);
+    h->cell_start.ensure(B.ncells + 1);
+    h->cell_atoms.ensure(n);
+    h->pcount.ensure(n);
+    h->perm.ensure(n);
+    const int nb = (n + kSortBlock - 1) / kSortBlock;
+    h->block_counts.ensure((size_t)std::max(nb, 1) * T);
+    h->type_start.ensure(T + 1);
+    h->status.ensure(2);
+    if (h->M == 0 || (size_t)n * h->M > h->pkey.cap) grow_pairs(h, n, std::max(h->M, initial_capacity(B, h->model.rcut_max)));
+    CK(cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * B.ncells, st));
+    CK(cudaMemsetAsync(h->cell_fill.p, 0, sizeof(int) * B.ncells, st));
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
+    if (n > 0) {
+        k_wrap_bin<<<(n + 255) / 256, 256, 0, st>>>(h->sdev.p, h->sid.p, d_x, d_type, n, T, h->xw.p, h->xf.p,
+                                                    h->cell_of.p, h->cell_count.p, h->status.p);
+        ++h->launches;
+    }
+    k_scan_excl<<<1, 1024, 0, st>>>(h->cell_count.p, B.ncells, h->cell_start.p);
+    ++h->launches;
+    if (n > 0) {
+        k_fill_cells<<<(n + 255) / 256, 256, 0, st>>>(h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p);
+        k_sort_cells<<<(B.ncells + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
+        h->launches += 2;
+    }
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        CK(cudaMemsetAsync(h->status.p + 1, 0, sizeof(int), st));
+        if (n > 0) {
+            k_neighbors<<<(n + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
+                h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
+                pair_bufs(h), h->status.p, h->status.p + 1);
+            ++h->launches;
+        }
+        if (attempt == 0 && n > 0) {
+            k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
+            k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
+            k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
+            h->launches += 3;
+        }
+        CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+        if (attempt == 0) CK(cudaMemcpyAsync(h->h_status + 2, h->type_start.p, sizeof(int) * (T + 1),
+                                             cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        const int bits = h->h_status[0];
+        if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
+        if (attempt == 0) {
+            type_start.assign(h->h_status + 2, h->h_status + 3 + T);
+            if (n == 0) type_start.assign(T + 1, 0);
+        }
+        const int maxc = h->h_status[1];
+        if (maxc <= h->M) break;
+        if (attempt == 2) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour capacity could not be established");
+        grow_pairs(h, n, ((int)std::ceil(maxc * 1.15) + 8 + 7) & ~7);
+        CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st));
+    }
+    (void)want_types;
+    if (n > 0) {
+        const long long tot = (long long)n * h->M;
+        k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(pair_bufs(h), n, h->status.p);
+        ++h->launches;
+    }
+}
+
+void descriptors(nnap_handle* h, int n, const int* d_type, const std::vector<int>& ts, bool fwd) {
+    const int T = h->model.ntypes();
+    (void)T;
+    size_t a_off = 0;
+    for (auto& r : h->runs) {
+        const int s0 = ts[r.t0], s1 = ts[r.t1];
+        for (size_t k = 0; k < r.subs.size(); ++k) {
+            const SubShape& s = r.subs[k];
+            DescArgs a;
+            a.perm = h->perm.p;
+            a.s0 = s0;
+            a.s1 = s1;
+            a.type = d_type;
+            a.P = pair_bufs(h);
+            a.W = r.W[k].p;
+            a.T = h->model.ntypes();
+            a.rcut = (float)s.rcut;
+            a.fp = h->fp.p;
+            a.fp_stride = h->fp_stride;
+            a.fp_off = r.fp_off[k];
+            a.A = nullptr;
+            if (s.kind == KIND_SPHERICAL) {
+                a.A = h->A.p + a_off;
+                a_off += (size_t)(s1 - s0) * s.np * (s.lmax + 1) * (s.lmax + 1);
+            }
+            a.gfp = h->gfp.p;
+            a.accumulate = k > 0;
+            if (s1 > s0) {
+                CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, h->stream));
+                ++h->launches;
+            }
+        }
+    }
+    (void)n;
+}
+
+size_t a_arena_size(nnap_handle* h, const std::vector<int>& ts) {
+    size_t tot = 0;
+    for (auto& r : h->runs)
+        for (auto& s : r.subs)
+            if (s.kind == KIND_SPHERICAL) tot += (size_t)(ts[r.t1] - ts[r.t0]) * s.np * (s.lmax + 1) * (s.lmax + 1);
+    return tot;
+}
+
+void network(nnap_handle* h, const std::vector<int>& ts) {
+    for (int t = 0; t < h->model.ntypes(); ++t) {
+        const NetDev& nd = h->nets[t];
+        NetArgs a;
+        a.perm = h->perm.p;
+        a.s0 = ts[t];
+        a.s1 = ts[t + 1];
+        if (a.s1 <= a.s0) continue;
+        a.fp = h->fp.p;
+        a.fp_stride = h->fp_stride;
+        a.D = nd.D;
+        a.nlayer = nd.nlayer;
+        for (int l = 0; l < 4; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;
+        a.w = nd.w32.p;
+        a.mu_e = nd.mu_e;
+        a.sigma_e = nd.sigma_e;
+        a.e_atom = h->e_atom.p;
+        a.gfp = h->gfp.p;
+        if (h->precision == NNAP_PREC_MIXED) {
+            CK(launch_net_tc(a, nd.tc, h->stream));
+        } else {
+            CK(launch_net_fp32(a, h->stream));
+        }
+        ++h->launches;
+    }
+}
+
+// Full evaluation of a batch whose positions/types are already on the device.
+void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+    const int n = B.natoms;
+    cudaStream_t st = h->stream;
+    std::vector<int> ts;
+    h->mark(0);
+    build_neighbors(h, B, d_x, d_type, ts, true);
+    h->mark(1);
+    h->fp.ensure((size_t)std::max(n, 1) * h->fp_stride);
+    h->gfp.ensure((size_t)std::max(n, 1) * h->fp_stride);
+    h->A.ensure(std::max<size_t>(a_arena_size(h, ts), 1));
+    if (n > 0) CK(cudaMemsetAsync(h->fp.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
+    descriptors(h, n, d_type, ts, true);
+    h->mark(2);
+    if (fp_only) return;
+    h->e_atom.ensure(std::max(n, 1));
+    network(h, ts);
+    h->mark(3);
+    descriptors(h, n, d_type, ts, false);
+    h->mark(4);
+    h->forces.ensure(3 * (size_t)std::max(n, 1));
+    h->virials.ensure(9 * (size_t)std::max(n, 1));
+    if (n > 0) {
+        k_gather<<<(n * 32 + 255) / 256, 256, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
+        ++h->launches;
+    }
+    const int nchunks = (int)B.cb.size();
+    h->chunk_b.ensure(std::max(nchunks, 1));
+    h->chunk_e.ensure(std::max(nchunks, 1));
+    h->struct_chunks.ensure(B.nstruct + 1);
+    h->partial.ensure(10 * (size_t)std::max(nchunks, 1));
+    h->energy.ensure(std::max(B.nstruct, 1));
+    h->virial.ensure(9 * (size_t)std::max(B.nstruct, 1));
+    if (nchunks) {
+        CK(cudaMemcpyAsync(h->chunk_b.p, B.cb.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->chunk_e.p, B.ce.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+        k_reduce_chunks<<<nchunks, kRedBlock, 0, st>>>(h->chunk_b.p, h->chunk_e.p, h->e_atom.p, h->virials.p,
+                                                        h->partial.p);
+        ++h->launches;
+    }
+    CK(cudaMemcpyAsync(h->struct_chunks.p, B.sc.data(), sizeof(int) * (B.nstruct + 1), cudaMemcpyHostToDevice, st));
+    k_reduce_structs<<<(B.nstruct + 127) / 128, 128, 0, st>>>(h->struct_chunks.p, B.nstruct, h->partial.p,
+                                                               h->energy.p, h->virial.p);
+    ++h->launches;
+    h->mark(5);
+    CK(cudaGetLastError());
+}
+
+void check_after(nnap_handle* h) {
+    CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->h_status[0] & ERRBIT_NO_MIRROR) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
+    if (h->h_status[0] & ERRBIT_CAPACITY) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour capacity exceeded");
+}
+
+void copy_out(nnap_handle* h, const Batch& B, int flags, const Outputs& o, cudaMemcpyKind kind) {
+    cudaStream_t st = h->stream;
+    const size_t n = B.natoms;
+    if ((flags & NNAP_WANT_ENERGY) && o.energy)
+        CK(cudaMemcpyAsync(o.energy, h->energy.p, sizeof(double) * B.nstruct, kind, st));
+    if ((flags & NNAP_WANT_ENERGIES) && o.energies && n)
+        CK(cudaMemcpyAsync(o.energies, h->e_atom.p, sizeof(double) * n, kind, st));
+    if ((flags & NNAP_WANT_FORCES) && o.forces && n)
+        CK(cudaMemcpyAsync(o.forces, h->forces.p, sizeof(double) * 3 * n, kind, st));
+    if ((flags & NNAP_WANT_VIRIAL) && o.virial)
+        CK(cudaMemcpyAsync(o.virial, h->virial.p, sizeof(double) * 9 * B.nstruct, kind, st));
+    if ((flags & NNAP_WANT_VIRIALS) && o.virials && n)
+        CK(cudaMemcpyAsync(o.virials, h->virials.p, sizeof(double) * 9 * n, kind, st));
+}
+
+void check_outputs(int flags, const Outputs& o) {
+    if ((flags & NNAP_WANT_ENERGY) && !o.energy) throw ApiFail(NNAP_ERR_ARG, "energy output is NULL");
+    if ((flags & NNAP_WANT_ENERGIES) && !o.energies) throw ApiFail(NNAP_ERR_ARG, "energies output is NULL");
+    if ((flags & NNAP_WANT_FORCES) && !o.forces) throw ApiFail(NNAP_ERR_ARG, "forces output is NULL");
+    if ((flags & NNAP_WANT_VIRIAL) && !o.virial) throw ApiFail(NNAP_ERR_ARG, "virial output is NULL");
+    if ((flags & NNAP_WANT_VIRIALS) && !o.virials) throw ApiFail(NNAP_ERR_ARG, "virials output is NULL");
+}
+
+void upload_inputs(nnap_handle* h, int n, const double* x, const int* type) {
+    h->x.ensure(3 * (size_t)std::max(n, 1));
+    h->type.ensure(std::max(n, 1));
+    if (n) {
+        CK(cudaMemcpyAsync(h->x.p, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->type.p, type, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+    }
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+int nnap_create(const char* model_json, size_t len, int precision, int device, nnap_handle** out) {
+    if (!model_json || !out) return NNAP_ERR_ARG;
+    *out = nullptr;
+    if (precision != NNAP_PREC_FP32 && precision != NNAP_PREC_MIXED) return NNAP_ERR_ARG;
+    std::unique_ptr<nnap_handle> h(new (std::nothrow) nnap_handle());
+    if (!h) return NNAP_ERR_CAPACITY;
+    try {
+        h->model = load_model(model_json, len);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "nnap_create: %s\n", e.what());
+        return NNAP_ERR_BAD_MODEL;
+    }
+    h->precision = precision;
+    h->device = device;
+    try {
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        CK(cudaMallocHost(&h->h_status, sizeof(int) * (3 + kMaxTypes)));
+        CK(upload_sh_constants());
+        upload_model(h.get());
+    } catch (const ApiFail& e) {
+        std::fprintf(stderr, "nnap_create: %s\n", e.what());
+        nnap_destroy(h.release());
+        return e.status;
+    } catch (const CudaFail& e) {
+        std::fprintf(stderr, "nnap_create: %s\n", e.what());
+        nnap_destroy(h.release());
+        return NNAP_ERR_CUDA;
+    }
+    *out = h.release();
+    return NNAP_OK;
+}
+
+int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out) {
+    if (!path || !out) return NNAP_ERR_ARG;
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return NNAP_ERR_ARG;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string s = ss.str();
+    return nnap_create(s.data(), s.size(), precision, device, out);
+}
+
+int nnap_destroy(nnap_handle* h) {
+    if (!h) return NNAP_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->dead = true;
+    for (auto& r : h->runs)
+        for (auto& w : r.W) w.release();
+    for (auto& nd : h->nets) { nd.w32.release(); net_tc_release(nd.tc); }
+    h->x.release(); h->xw.release(); h->e_atom.release(); h->forces.release(); h->virials.release();
+    h->energy.release(); h->virial.release(); h->partial.release();
+    h->type.release(); h->sid.release(); h->cell_of.release(); h->cell_count.release(); h->cell_fill.release();
+    h->cell_start.release(); h->cell_atoms.release(); h->perm.release(); h->block_counts.release();
+    h->type_start.release(); h->chunk_b.release(); h->chunk_e.release(); h->struct_chunks.release();
+    h->status.release(); h->xf.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
+    h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release();
+    for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+    if (h->h_status) cudaFreeHost(h->h_status);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return NNAP_OK;
+}
+
+int nnap_ntypes(const nnap_handle* h, int* ntypes) {
+    if (!h || !ntypes) return NNAP_ERR_ARG;
+    *ntypes = h->model.ntypes();
+    return NNAP_OK;
+}
+
+int nnap_rcut_max(const nnap_handle* h, double* rcut) {
+    if (!h || !rcut) return NNAP_ERR_ARG;
+    *rcut = h->model.rcut_max;
+    return NNAP_OK;
+}
+
+int nnap_symbol(const nnap_handle* h, int type, char* buf, size_t buflen) {
+    if (!h || !buf || buflen == 0) return NNAP_ERR_ARG;
+    if (type < 1 || type > h->model.ntypes()) return NNAP_ERR_BAD_TYPE;
+    std::snprintf(buf, buflen, "%s", h->model.sp[type - 1].symbol.c_str());
+    return NNAP_OK;
+}
+
+int nnap_descriptor_size(const nnap_handle* h, int type, int* size) {
+    if (!h || !size) return NNAP_ERR_ARG;
+    if (type < 1 || type > h->model.ntypes()) return NNAP_ERR_BAD_TYPE;
+    *size = h->model.sp[type - 1].D;
+    return NNAP_OK;
+}
+
+const char* nnap_last_error(const nnap_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int nnap_last_launch_count(const nnap_handle* h, int* count) {
+    if (!h || !count) return NNAP_ERR_ARG;
+    *count = h->launches;
+    return NNAP_OK;
+}
+
+int nnap_set_profiling(nnap_handle* h, int on) {
+    return guarded(h, [&]() -> int {
+        for (auto& e : h->ev)
+            if (!e) CK(cudaEventCreate(&e));
+        h->profiling = on != 0;
+        return NNAP_OK;
+    });
+}
+
+int nnap_stage_times(nnap_handle* h, double* ms5) {
+    if (!ms5) return NNAP_ERR_ARG;
+    return guarded(h, [&]() -> int {
+        if (!h->ev[5]) throw ApiFail(NNAP_ERR_ARG, "profiling was never enabled");
+        CK(cudaEventSynchronize(h->ev[5]));
+        for (int k = 0; k < 5; ++k) {
+            float t = 0.f;
+            CK(cudaEventElapsedTime(&t, h->ev[k], h->ev[k + 1]));
+            ms5[k] = t;
+        }
+        return NNAP_OK;
+    });
+}
+
+int nnap_compute(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind, const double* box,
+                 int flags, double* energy, double* energies, double* forces, double* virial, double* virials) {
+    return nnap_compute_batch(h, 1, &natoms, x, type, &box_kind, box, flags, energy, energies, forces, virial,
+                              virials);
+}
+
+int nnap_compute_batch(nnap_handle* h, int nstruct, const int* natoms, const double* x, const int* type,
+                       const int* box_kind, const double* boxes, int flags, double* energy, double* energies,
+                       double* forces, double* virial, double* virials) {
+    return guarded(h, [&]() -> int {
+        if (nstruct < 1 || !natoms || !box_kind || !boxes) throw ApiFail(NNAP_ERR_ARG, "invalid batch description");
+        Outputs o{energy, energies, forces, virial, virials};
+        check_outputs(flags, o);
+        h->launches = 0;
+        Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
+        if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
+        upload_inputs(h, B.natoms, x, type);
+        evaluate(h, B, h->x.p, h->type.p, false);
+        copy_out(h, B, flags, o, cudaMemcpyDeviceToHost);
+        check_after(h);
+        return NNAP_OK;
+    });
+}
+
+int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int* d_type, int box_kind,
+                        const double* box, int flags, double* d_energy, double* d_energies, double* d_forces,
+                        double* d_virial, double* d_virials, void* stream) {
+    return guarded(h, [&]() -> int {
+        if (!box) throw ApiFail(NNAP_ERR_ARG, "box is NULL");
+        Outputs o{d_energy, d_energies, d_forces, d_virial, d_virials};
+        check_outputs(flags, o);
+        h->launches = 0;
+        Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
+        if (natoms && (!d_x || !d_type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
+        cudaStream_t user = (cudaStream_t)stream;
+        cudaEvent_t ev = nullptr;
+        if (user) {  // order the handle's stream after the caller's work
+            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CK(cudaEventRecord(ev, user));
+            CK(cudaStreamWaitEvent(h->stream, ev, 0));
+        }
+        evaluate(h, B, d_x, d_type, false);
+        copy_out(h, B, flags, o, cudaMemcpyDeviceToDevice);
+        if (user) {
+            CK(cudaEventRecord(ev, h->stream));
+            CK(cudaStreamWaitEvent(user, ev, 0));
+            CK(cudaEventDestroy(ev));
+        }
+        return NNAP_OK;
+    });
+}
+
+int nnap_compute_fp(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind, const double* box,
+                    double* fp, int stride) {
+    return guarded(h, [&]() -> int {
+        if (!box || !fp) throw ApiFail(NNAP_ERR_ARG, "NULL argument");
+        int dmax = 0;
+        for (auto& sp : h->model.sp) dmax = std::max(dmax, sp.D);
+        if (stride < dmax) throw ApiFail(NNAP_ERR_ARG, "stride smaller than the descriptor size");
+        h->launches = 0;
+        Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
+        if (natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
+        upload_inputs(h, natoms, x, type);
+        evaluate(h, B, h->x.p, h->type.p, true);
+        std::vector<float> f((size_t)natoms * h->fp_stride);
+        std::vector<int> perm(natoms);
+        if (natoms) {
+            CK(cudaMemcpyAsync(f.data(), h->fp.p, sizeof(float) * f.size(), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(perm.data(), h->perm.p, sizeof(int) * natoms, cudaMemcpyDeviceToHost, h->stream));
+        }
+        check_after(h);
+        for (int s = 0; s < natoms; ++s) {
+            const int a = perm[s];
+            const int D = h->model.sp[type[a] - 1].D;
+            for (int q = 0; q < stride; ++q) fp[(size_t)a * stride + q] = q < D ? f[(size_t)s * h->fp_stride + q] : 0.0;
+        }
+        return NNAP_OK;
+    });
+}
+
+int nnap_neighbor_list(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind, const double* box,
+                       int* counts, long long cap, int* j, int* img, long long* total) {
+    return guarded(h, [&]() -> int {
+        if (!box || !counts || !total) throw ApiFail(NNAP_ERR_ARG, "NULL argument");
+        h->launches = 0;
+        Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
+        if (natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
+        upload_inputs(h, natoms, x, type);
+        std::vector<int> ts;
+        build_neighbors(h, B, h->x.p, h->type.p, ts, false);
+        std::vector<int> cnt(natoms);
+        std::vector<uint64_t> keys((size_t)natoms * h->M);
+        if (natoms) {
+            CK(cudaMemcpyAsync(cnt.data(), h->pcount.p, sizeof(int) * natoms, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(keys.data(), h->pkey.p, sizeof(uint64_t) * keys.size(), cudaMemcpyDeviceToHost,
+                               h->stream));
+        }
+        check_after(h);
+        long long t = 0;
+        for (int i = 0; i < natoms; ++i) {
+            counts[i] = cnt[i];
+            for (int k = 0; k < cnt[i]; ++k, ++t) {
+                if (!j) continue;
+                if (t >= cap) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour output capacity too small");
+                const uint64_t key = keys[(size_t)i * h->M + k];
+                j[t] = (int)(key >> 32);
+                int na, nb, nc;
+                unpack_img((uint32_t)key, na, nb, nc);
+                img[3 * t] = na; img[3 * t + 1] = nb; img[3 * t + 2] = nc;
+            }
+        }
+        *total = t;
+        return NNAP_OK;
+    });
+}
+
+}  // extern "C"

@@ -145,6 +145,7 @@ def _load_sub(kind: str, T: int, m: dict) -> SubBasis:
         rfuse_w = _post_fuse_to_rfuse(pw, wtype, T, nmax, sn, fuse_w, fuse_size)
         wtype = WTYPE_RFUSE
         fuse_w = None
+        sn = size_n(WTYPE_RFUSE, T, nmax, 0)
     typed = wtype
     if T == 1 and wtype in (WTYPE_EXFULL, WTYPE_FULL, WTYPE_NONE, WTYPE_DEFAULT):
         typed = WTYPE_NONE

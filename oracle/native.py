@@ -119,8 +119,10 @@ def neighbors(xw, box_kind: int, box, rcut: float, brute: bool = False) -> Neigh
 
 
 def compute(model: PackedModel, x, types, box_kind: int, box, want_fp: bool = False, want_pair: bool = False,
-            nl: Optional[NeighborList] = None):
-    """Full structure evaluation: wrap -> neighbour list -> per-atom arithmetic -> scatter."""
+            nl: Optional[NeighborList] = None, n_eval: Optional[int] = None):
+    """Full structure evaluation: wrap -> neighbour list -> per-atom arithmetic -> scatter.
+
+    ``n_eval`` restricts the per-atom evaluation to the first ``n_eval`` atoms (timing samples)."""
     types = np.ascontiguousarray(types, dtype=np.int32)
     n = len(types)
     xw = wrap(x, box_kind, box)
@@ -134,7 +136,8 @@ def compute(model: PackedModel, x, types, box_kind: int, box, want_fp: bool = Fa
     fp = np.zeros((n, Dmax)) if want_fp else None
     pg = np.zeros((max(len(nl.j), 1), 3)) if want_pair else None
     code = lib().oracle_compute(model.ntypes, _p(spec, C.c_int), _p(rcuts, C.c_double), _p(params, C.c_double),
-                                n, _p(types, C.c_int), _p(nl.offsets, C.c_long), _p(nl.j, C.c_int),
+                                n, n if n_eval is None else int(n_eval), _p(types, C.c_int),
+                                _p(nl.offsets, C.c_long), _p(nl.j, C.c_int),
                                 _p(nl.dx, C.c_double), _p(e, C.c_double), _p(f, C.c_double), _p(v, C.c_double),
                                 _p(fp, C.c_double) if want_fp else None, Dmax,
                                 _p(pg, C.c_double) if want_pair else None)
@@ -186,14 +189,15 @@ class RefLib:
             per, const = max(per, p), max(const, c)
         self.cache_per, self.cache_const = per, const + 16
 
-    def compute(self, types, nl: NeighborList, nthreads: int = 1):
+    def compute(self, types, nl: NeighborList, nthreads: int = 1, n_eval: Optional[int] = None):
         types = np.ascontiguousarray(types, dtype=np.int32)
         n = len(types)
         e = np.zeros(n)
         f = np.zeros((n, 3))
         v = np.zeros((n, 9))
         dx = np.ascontiguousarray(nl.dx, dtype=np.float64)
-        code = self.lib.ref_compute(self.model.ntypes, self.hp, self.fpp, self.nnp, self.nrm, n, _p(types, C.c_int),
+        code = self.lib.ref_compute(self.model.ntypes, self.hp, self.fpp, self.nnp, self.nrm, n,
+                                    n if n_eval is None else int(n_eval), _p(types, C.c_int),
                                     _p(nl.offsets, C.c_long), _p(nl.j, C.c_int), _p(dx, C.c_double),
                                     C.c_long(self.cache_per), C.c_long(self.cache_const), nthreads,
                                     _p(e, C.c_double), _p(f, C.c_double), _p(v, C.c_double))

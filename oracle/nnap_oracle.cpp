@@ -578,8 +578,9 @@ long oracle_neighbors_brute(int n, const double* xw, int box_kind, const double*
 //   type[i] is 1-based; nei_off has n+1 entries; nei_dx holds x_j(+image) - x_i.
 //   e_atom[n], force[3n], virial[9n] (xx,yy,zz,xy,xz,yz,yx,zx,zy), fp_out[n*fp_stride] (optional),
 //   pair_g[3*npairs] (optional) receive the results.  Returns 0 on success.
+//   Atoms [0, n_eval) are evaluated (n_eval <= n, a prefix is used to time a bounded sample).
 int oracle_compute(int T, const int* spec, const double* rcuts, const double* params,
-                   int n, const int* type, const long* nei_off, const int* nei_j, const double* nei_dx,
+                   int n, int n_eval, const int* type, const long* nei_off, const int* nei_j, const double* nei_dx,
                    double* e_atom, double* force, double* virial, double* fp_out, int fp_stride, double* pair_g) {
     std::vector<Species> sp = parse_spec(T, spec, rcuts);
     std::vector<int> ntype;
@@ -587,7 +588,7 @@ int oracle_compute(int T, const int* spec, const double* rcuts, const double* pa
     std::vector<std::vector<double>> Astore;
     if (force) std::fill(force, force + 3 * (size_t)n, 0.0);
     if (virial) std::fill(virial, virial + 9 * (size_t)n, 0.0);
-    for (int i = 0; i < n; ++i) {
+    for (int i = 0; i < n_eval; ++i) {
         int ti = type[i];
         if (ti < 1 || ti > T) return 2;
         const Species& S = sp[ti - 1];

@@ -36,10 +36,10 @@ struct ThreadBuf {
     int status = 0;
 };
 
-void run_atoms(int tid, int nthreads, int n, const int* type, const long* nei_off, const int* nei_j,
+void run_atoms(int tid, int nthreads, int n_eval, const int* type, const long* nei_off, const int* nei_j,
                const double* nei_dx, double** hp, double** fpp, double** nnp, double** normp,
                long cache_per_nei, long cache_const, bool want_e, bool want_f, bool want_v, ThreadBuf& B) {
-    for (int i = tid; i < n; i += nthreads) {
+    for (int i = tid; i < n_eval; i += nthreads) {
         const long o = nei_off[i];
         const int nn = (int)(nei_off[i + 1] - o);
         B.dx.resize(nn + 1); B.dy.resize(nn + 1); B.dz.resize(nn + 1);
@@ -82,9 +82,10 @@ void run_atoms(int tid, int nthreads, int n, const int* type, const long* nei_of
 extern "C" {
 
 // Energies, forces and per-atom virials of one structure through the reference's
-// per-atom arithmetic.  Any of e_atom/force/virial may be NULL.  Returns the first
-// nonzero code of the reference function, or 0.
-int ref_compute(int T, double** hp, double** fpp, double** nnp, double** normp, int n, const int* type,
+// per-atom arithmetic.  Atoms [0, n_eval) are evaluated (n_eval <= n; a prefix is used
+// to time a bounded sample); output arrays hold n atoms.  Any of e_atom/force/virial
+// may be NULL.  Returns the first nonzero code of the reference function, or 0.
+int ref_compute(int T, double** hp, double** fpp, double** nnp, double** normp, int n, int n_eval, const int* type,
                 const long* nei_off, const int* nei_j, const double* nei_dx, long cache_per_nei, long cache_const,
                 int nthreads, double* e_atom, double* force, double* virial) {
     (void)T;
@@ -97,10 +98,10 @@ int ref_compute(int T, double** hp, double** fpp, double** nnp, double** normp, 
     }
     std::vector<std::thread> th;
     for (int t = 1; t < nthreads; ++t)
-        th.emplace_back(run_atoms, t, nthreads, n, type, nei_off, nei_j, nei_dx, hp, fpp, nnp, normp,
+        th.emplace_back(run_atoms, t, nthreads, n_eval, type, nei_off, nei_j, nei_dx, hp, fpp, nnp, normp,
                         cache_per_nei, cache_const, e_atom != nullptr, force != nullptr, virial != nullptr,
                         std::ref(bufs[t]));
-    run_atoms(0, nthreads, n, type, nei_off, nei_j, nei_dx, hp, fpp, nnp, normp, cache_per_nei, cache_const,
+    run_atoms(0, nthreads, n_eval, type, nei_off, nei_j, nei_dx, hp, fpp, nnp, normp, cache_per_nei, cache_const,
               e_atom != nullptr, force != nullptr, virial != nullptr, bufs[0]);
     for (auto& t : th) t.join();
     for (auto& B : bufs) if (B.status) return B.status;

@@ -1,0 +1,70 @@
+"""GPU path (through the C ABI) against the golden vectors of the reference's arithmetic.
+
+Tolerances (plain FP32 path; descriptors and network in FP32, displacements and all
+reductions in FP64):
+  * neighbour sets: bit-exact, (i, j, image) per pair;
+  * energies: |dE_i| <= 2e-5 * max(1, max|E|);
+  * forces and per-atom virials: max |d| <= 1e-3 * max(1e-2, max|ref|) and
+    RMS |d| <= 2e-4 * max(1e-2, max|ref|);
+  * descriptors: relative 1e-4 of each column's scale.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _nnap(model_json, precision="fp32"):
+    from jse_gb300.nnap import NNAP
+    return NNAP(model_json, precision=precision)
+
+
+class _S:
+    def __init__(self, c):
+        self.x, self.types, self.box, self.box_kind = c.x, c.types, c.box, c.box_kind
+
+
+def _close(got, ref, tol_max, tol_rms):
+    scale = max(1e-2, float(np.abs(ref).max()) if ref.size else 1.0)
+    d = np.abs(got - ref)
+    assert d.max() <= tol_max * scale, (d.max(), scale)
+    assert np.sqrt((d ** 2).mean()) <= tol_rms * scale
+
+
+def test_neighbor_sets_bit_exact(golden):
+    with _nnap(golden.model_json) as p:
+        off, j, img = p.neighborList(_S(golden))
+    got = set()
+    for i in range(len(golden.types)):
+        for k in range(off[i], off[i + 1]):
+            got.add((i, int(j[k])) + tuple(int(v) for v in img[k]))
+    assert got == golden.nl_set()
+
+
+def test_energy_force_virial_fp32(golden):
+    with _nnap(golden.model_json) as p:
+        o = p.calEnergyForceVirials(_S(golden))
+        assert p.lastLaunchCount() > 0
+    escale = max(1.0, float(np.abs(golden.energies).max()))
+    assert np.abs(o["energies"] - golden.energies).max() <= 2e-5 * escale
+    assert abs(o["energy"] - golden.energies.sum()) <= 2e-5 * escale * max(1, len(golden.types)) ** 0.5
+    _close(o["forces"], golden.forces, 1e-3, 2e-4)
+    _close(o["virials"], golden.virials, 1e-3, 2e-4)
+    np.testing.assert_allclose(o["virial"], golden.virials.sum(0), rtol=1e-3,
+                               atol=1e-4 * max(1.0, np.abs(golden.virials).sum(0).max()))
+
+
+def test_descriptors_fp32(golden):
+    with _nnap(golden.model_json) as p:
+        fp = p.calFp(_S(golden))
+    D = golden.fp.shape[1]
+    scale = np.maximum(np.abs(golden.fp).max(0), 1e-6)
+    assert (np.abs(fp[:, :D] - golden.fp) / scale).max() <= 1e-4
+
+
+def test_results_are_deterministic(golden):
+    with _nnap(golden.model_json) as p:
+        a = p.calEnergyForceVirials(_S(golden))
+        b = p.calEnergyForceVirials(_S(golden))
+    for k in ("energies", "forces", "virials", "virial"):
+        assert np.array_equal(a[k], b[k]), k
