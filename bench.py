@@ -292,6 +292,8 @@ def main():
         def device_step():
             pot.calEnergyForceVirialsBatch(structures)
 
+    bench_stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(bench_stream)
     pot.setProfiling(True)
     for _ in range(args.warmup):
         flush.zero_()

@@ -95,8 +95,8 @@ int nnap_compute(nnap_handle* h, int natoms, const double* x, const int* type, i
                  int flags, double* energy, double* energies, double* forces, double* virial, double* virials);
 
 /* Same computation on device-resident buffers; x, type, and every output are device
- * pointers, box stays a host array.  Work is ordered after `stream` (a cudaStream_t, may
- * be NULL) and `stream` is made to wait for the results.  The call synchronises the
+ * pointers, box stays a host array.  Work is ordered after `stream` (a cudaStream_t; NULL
+ * is CUDA's default stream) and `stream` is made to wait for the results.  The call synchronises the
  * handle's stream once, after the neighbour build, to validate the neighbour capacity
  * and read the species ranges; the rest is queued and the call returns before it ends. */
 int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int* d_type, int box_kind,

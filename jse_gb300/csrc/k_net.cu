@@ -20,7 +20,7 @@ constexpr int kNetAtoms = 8;
 constexpr int kNetWarps = 4;
 
 __device__ __forceinline__ float silu_and_grad(float z, float* grad) {
-    const float s = 1.f / (1.f + __expf(-z));
+    const float s = 1.f / (1.f + expf(-z));
     *grad = s * (1.f + z * (1.f - s));
     return z * s;
 }
@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
             float z[kNetAtoms];
 #pragma unroll
             for (int q = 0; q < kNetAtoms; ++q) z[q] = b[o];
+#pragma unroll 8
             for (int i = 0; i < in; ++i) {
                 const float wv = WT[(size_t)i * H + o];
                 const float4 x0 = *reinterpret_cast<const float4*>(cur + i * kNetAtoms);
@@ -113,6 +114,7 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
             float g[kNetAtoms];
 #pragma unroll
             for (int q = 0; q < kNetAtoms; ++q) g[q] = 0.f;
+#pragma unroll 8
             for (int o = 0; o < H; ++o) {
                 const float wv = W[(size_t)o * lin + i];
                 const float4 d0 = *reinterpret_cast<const float4*>(cur + o * kNetAtoms);

@@ -53,7 +53,7 @@ namespace {
 constexpr int kNbWarps = 4;       // must match k_struct.cu
 constexpr int kSortBlock = 256;   // must match k_struct.cu
 constexpr int kRedBlock = 256;    // must match k_struct.cu
-constexpr int kRedChunk = 4096;   // atoms per reduction chunk
+constexpr int kRedChunk = 1024;   // atoms per reduction chunk
 
 struct CudaFail : std::runtime_error {
     cudaError_t code;
@@ -142,6 +142,7 @@ struct nnap_handle {
     int M = 0;
     int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
     bool profiling = false;
+    cudaEvent_t order_ev = nullptr;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void mark(int k) {
         if (profiling) CK(cudaEventRecord(ev[k], stream));
@@ -668,6 +669,7 @@ int nnap_destroy(nnap_handle* h) {
     h->status.release(); h->xf.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release();
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
+    if (h->order_ev) cudaEventDestroy(h->order_ev);
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -765,20 +767,16 @@ int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int
         h->launches = 0;
         Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
         if (natoms && (!d_x || !d_type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
+        // NULL is CUDA's default stream; the handle's stream is ordered after the caller's
+        // work and the caller's stream waits for the results.
         cudaStream_t user = (cudaStream_t)stream;
-        cudaEvent_t ev = nullptr;
-        if (user) {  // order the handle's stream after the caller's work
-            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-            CK(cudaEventRecord(ev, user));
-            CK(cudaStreamWaitEvent(h->stream, ev, 0));
-        }
+        if (!h->order_ev) CK(cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming));
+        CK(cudaEventRecord(h->order_ev, user));
+        CK(cudaStreamWaitEvent(h->stream, h->order_ev, 0));
         evaluate(h, B, d_x, d_type, false);
         copy_out(h, B, flags, o, cudaMemcpyDeviceToDevice);
-        if (user) {
-            CK(cudaEventRecord(ev, h->stream));
-            CK(cudaStreamWaitEvent(user, ev, 0));
-            CK(cudaEventDestroy(ev));
-        }
+        CK(cudaEventRecord(h->order_ev, h->stream));
+        CK(cudaStreamWaitEvent(user, h->order_ev, 0));
         return NNAP_OK;
     });
 }
