@@ -14,7 +14,8 @@ enum : int {
     ERRBIT_CAPACITY = 1,    // a neighbour row overflowed its capacity
     ERRBIT_BAD_TYPE = 2,    // species outside 1..ntypes
     ERRBIT_NO_MIRROR = 4,   // a pair had no mirrored entry (asymmetric list)
-    ERRBIT_CELLS = 8        // an atom fell outside its structure's cell grid
+    ERRBIT_CELLS = 8,       // an atom fell outside its structure's cell grid
+    ERRBIT_TIMEOUT = 16     // a bounded device-side wait gave up
 };
 
 // One periodic structure of a batch, as the device sees it.
@@ -49,6 +50,7 @@ struct PairBufs {
     float4* dx;            // [n*M] (dx, dy, dz, bits of type_j)
     int* rev;              // [n*M] flat index of the mirrored entry
     float4* g;             // [n*M] pair gradient -dE_i/d(x_j - x_i)
+    uint16_t* grp;         // [n*M] cell-offset group of the entry (rows are sorted by group, then j)
     int* count;            // [n] true neighbour count (may exceed M on overflow)
 };
 

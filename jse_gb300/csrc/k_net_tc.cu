@@ -1,13 +1,446 @@
-// Tensor-core network kernel (mixed precision).  See net_tc.cuh.
+// Tensor-core evaluation of the per-species network and its input gradient (the
+// mixed-precision path), on the 5th-generation tensor cores (tcgen05, TMEM accumulators).
+//
+// Mathematics: normedNnForward / normedNnBackward (nnap_main.hpp:267-323) with two SiLU
+// hidden layers (nn_FeedForward.hpp:8-261):
+//   X  = (fp - mu)/sigma                      [128 x Dp]   Dp = D rounded up to 16
+//   Z1 = X W1^T + b1, A1 = silu(Z1)           [128 x H1]   GEMM 1 (N = H1, K = Dp)
+//   Z2 = A1 W2^T + b2, A2 = silu(Z2)          [128 x H2]   GEMM 2 (N = H2, K = H1)
+//   E  = (w_o . A2 + b_o) sigma_E + mu_E      (FP32 on the CUDA cores, FP64 output)
+//   dZ2 = sigma_E w_o * silu'(Z2)
+//   dA1 = dZ2 W2                              [128 x H1]   GEMM 3 (N = H1, K = H2)
+//   dZ1 = dA1 * silu'(Z1)
+//   dX  = dZ1 W1                              [128 x Dp]   GEMM 4 (N = Dp, K = H1)
+//   dE/dfp = dX / sigma
+// Operands are BF16 and every product is split as hi*hi + lo*hi + hi*lo with
+// x = hi + lo (both BF16), accumulated in FP32 in TMEM: three kind::f16 MMAs per
+// 16-wide K step keep the network error near FP32 level (about 1e-6 eV per atom)
+// while the arithmetic stays on the BF16 tensor pipe.
+//
+// One CTA of 128 threads owns a 128-atom tile; thread t owns row t (one atom) in every
+// epilogue, so TMEM lane t is read by thread t with tcgen05.ld 32x32b.  One thread
+// issues the MMAs; completion is signalled through an mbarrier (tcgen05.commit) whose
+// waits are bounded in time and raise ERRBIT_TIMEOUT instead of hanging.
+// Shared-memory operands use the no-swizzle K-major canonical layout: 8x8 core
+// matrices of 128 bytes, adjacent in K at LBO = 128 bytes and in M/N at
+// SBO = (K/8)*128 bytes.
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "net_tc.cuh"
 
 namespace nnapgb {
 
+namespace {
+
+constexpr int kTcThreads = 128;
+
+struct TCLayout {
+    int Dp, H1, H2;
+    // byte offsets inside the weight image (all multiples of 1024)
+    int w1, w2, w2t, w1t, fvec, bytes;  // each operand image holds hi then lo
+    int fmu, fisig, fb1, fb2, fwo;      // float offsets inside the FP32 vector block
+    int ncols;                          // TMEM columns allocated
+    int z1, z2, da1, dx;                // TMEM column offsets
+};
+
+__host__ __device__ inline int align1k(int b) { return (b + 1023) & ~1023; }
+
+TCLayout make_layout(int D, int H1, int H2) {
+    TCLayout L;
+    L.Dp = (D + 15) & ~15;
+    L.H1 = H1;
+    L.H2 = H2;
+    int off = 0;
+    L.w1 = off; off = align1k(off + 2 * 2 * H1 * L.Dp);
+    L.w2 = off; off = align1k(off + 2 * 2 * H2 * H1);
+    L.w2t = off; off = align1k(off + 2 * 2 * H1 * H2);
+    L.w1t = off; off = align1k(off + 2 * 2 * L.Dp * H1);
+    L.fvec = off;
+    L.fmu = 0;
+    L.fisig = L.Dp;
+    L.fb1 = 2 * L.Dp;
+    L.fb2 = L.fb1 + H1;
+    L.fwo = L.fb2 + H2;
+    off = align1k(off + 4 * (L.fwo + H2 + 4));
+    L.bytes = off;
+    L.z1 = 0;
+    L.z2 = H1;
+    L.da1 = H1 + H2;
+    L.dx = 2 * H1 + H2;
+    const int need = L.dx + L.Dp;
+    L.ncols = 32;
+    while (L.ncols < need) L.ncols *= 2;
+    return L;
+}
+
+// Element (r, k) of an R x K K-major operand in the no-swizzle core-matrix layout.
+inline size_t cm_index(int r, int k, int K) { return ((size_t)(r >> 3) * (K >> 3) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7); }
+
+uint16_t bf16_bits(float f) {
+    __nv_bfloat16 b = __float2bfloat16_rn(f);
+    uint16_t u;
+    std::memcpy(&u, &b, 2);
+    return u;
+}
+float bf16_val(uint16_t u) {
+    uint32_t w = (uint32_t)u << 16;
+    float f;
+    std::memcpy(&f, &w, 4);
+    return f;
+}
+
+// Write the hi and lo images of an R x K matrix M(r, k) (zero outside rows/cols given).
+template <class F>
+void put_operand(std::vector<uint8_t>& img, int byte_off, int R, int K, F&& M) {
+    uint16_t* hi = reinterpret_cast<uint16_t*>(img.data() + byte_off);
+    uint16_t* lo = hi + (size_t)R * K;
+    for (int r = 0; r < R; ++r)
+        for (int k = 0; k < K; ++k) {
+            const float v = (float)M(r, k);
+            const uint16_t h = bf16_bits(v);
+            const uint16_t l = bf16_bits(v - bf16_val(h));
+            hi[cm_index(r, k, K)] = h;
+            lo[cm_index(r, k, K)] = l;
+        }
+}
+
+// ------------------------------------------------------------------ device helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, int K) {
+    const uint64_t lbo = 128, sbo = (uint64_t)(K >> 3) * 128;
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version for this architecture
+    return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major, M = 128.
+__device__ __forceinline__ uint32_t make_idesc(int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Bounded wait on an mbarrier phase: gives up after ~2 s of device time.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > 4000000000LL) return false;
+    }
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// Split 8 FP32 values into BF16 hi/lo and store one 16-byte core-matrix row each.
+__device__ __forceinline__ void store_split8(uint8_t* hi_base, uint8_t* lo_base, int row, int k0, int K,
+                                             const float* v) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * q]), h1 = __float2bfloat16_rn(v[2 * q + 1]);
+        const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * q] - __bfloat162float(h0));
+        const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * q + 1] - __bfloat162float(h1));
+        h[q] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+        l[q] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+    }
+    const size_t off = (((size_t)(row >> 3) * (K >> 3) + (k0 >> 3)) * 64 + (row & 7) * 8) * 2;
+    *reinterpret_cast<uint4*>(hi_base + off) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4*>(lo_base + off) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Issue one split-BF16 GEMM: D[128 x N] (+)= A[128 x K] * B[N x K]^T.
+__device__ __forceinline__ void issue_gemm(uint32_t tmem_d, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi, uint32_t b_lo,
+                                           int K, int N) {
+    const uint32_t idesc = make_idesc(N);
+    for (int ks = 0; ks < K / 16; ++ks) {
+        const uint32_t step = ks * 256;  // two core matrices along K
+        const uint64_t ah = make_desc(a_hi + step, K), al = make_desc(a_lo + step, K);
+        const uint64_t bh = make_desc(b_hi + step, K), bl = make_desc(b_lo + step, K);
+        mma_bf16(tmem_d, ah, bh, idesc, ks > 0 ? 1u : 0u);
+        mma_bf16(tmem_d, al, bh, idesc, 1u);
+        mma_bf16(tmem_d, ah, bl, idesc, 1u);
+    }
+}
+
+__device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + expf(-z)); }
+
+struct TcParams {
+    const int* perm;
+    int s0, s1;
+    const float* fp;
+    int fp_stride, D;
+    float* gfp;
+    double* e_atom;
+    double mu_e, sigma_e;
+    float bo;
+    const uint8_t* img;  // weight image (global)
+    int* err;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int Dp = L.Dp, H1 = L.H1, H2 = L.H2;
+    uint8_t* sw = smem;                                       // weight image
+    uint8_t* sx = smem + L.bytes;                             // X / dZ1 operand (hi, lo)
+    const int xbytes = align1k(2 * 2 * 128 * (Dp > H1 ? Dp : H1));
+    uint8_t* sa = sx + xbytes;                                // A1 / dZ2 operand (hi, lo)
+    const int ab = 2 * 128 * (H1 > H2 ? H1 : H2);             // bytes of one (hi or lo) activation image
+    const float* fv = reinterpret_cast<const float*>(sw + L.fvec);
+
+    // stage the weight image
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(p.img);
+        uint4* dst = reinterpret_cast<uint4*>(sw);
+        for (int q = tid; q < L.bytes / 16; q += kTcThreads) dst[q] = src[q];
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                     "r"(L.ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tbase = tmem_base;
+    const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
+    const uint32_t mb = smem_u32(&mbar);
+    uint32_t phase = 0;
+    bool ok = true;
+
+    const uint32_t w1h = smem_u32(sw + L.w1), w1l = w1h + 2 * H1 * Dp;
+    const uint32_t w2h = smem_u32(sw + L.w2), w2l = w2h + 2 * H2 * H1;
+    const uint32_t w2th = smem_u32(sw + L.w2t), w2tl = w2th + 2 * H1 * H2;
+    const uint32_t w1th = smem_u32(sw + L.w1t), w1tl = w1th + 2 * Dp * H1;
+    const uint32_t xh = smem_u32(sx), xl = xh + 2 * 128 * (Dp > H1 ? Dp : H1);
+    const uint32_t ah = smem_u32(sa), al = ah + ab;
+    uint8_t* sx_lo = sx + 2 * 128 * (Dp > H1 ? Dp : H1);
+    uint8_t* sa_lo = sa + ab;
+
+    const int n = p.s1 - p.s0;
+    const int ntiles = (n + 127) / 128;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int row = tid;
+        const int slot = p.s0 + tile * 128 + row;
+        const bool valid = slot < p.s1;
+        // ---- X = (fp - mu) / sigma, split into hi / lo
+        const float* frow = p.fp + (size_t)(valid ? slot : p.s0) * p.fp_stride;
+        for (int k0 = 0; k0 < Dp; k0 += 8) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int k = k0 + q;
+                v[q] = (valid && k < p.D) ? (frow[k] - fv[L.fmu + k]) * fv[L.fisig + k] : 0.f;
+            }
+            store_split8(sx, sx_lo, row, k0, Dp, v);
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            issue_gemm(tbase + L.z1, xh, xl, w1h, w1l, Dp, H1);
+            mma_commit(mb);
+        }
+        ok = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1;
+        if (!ok) break;
+        fence_after();
+        // ---- A1 = silu(Z1 + b1)
+        for (int c0 = 0; c0 < H1; c0 += 16) {
+            float z[16];
+            tmem_ld16(tlane + L.z1 + c0, z);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const float zz = z[q] + fv[L.fb1 + c0 + q];
+                z[q] = zz * sigmoidf_(zz);
+            }
+            store_split8(sa, sa_lo, row, c0, H1, z);
+            store_split8(sa, sa_lo, row, c0 + 8, H1, z + 8);
+        }
+        fence_before();
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            issue_gemm(tbase + L.z2, ah, al, w2h, w2l, H1, H2);
+            mma_commit(mb);
+        }
+        ok = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1;
+        if (!ok) break;
+        fence_after();
+        // ---- energy and dZ2 = sigma_E w_o silu'(Z2 + b2)
+        const float se = (float)p.sigma_e;
+        float e = 0.f;
+        for (int c0 = 0; c0 < H2; c0 += 16) {
+            float z[16];
+            tmem_ld16(tlane + L.z2 + c0, z);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const float zz = z[q] + fv[L.fb2 + c0 + q];
+                const float s = sigmoidf_(zz);
+                const float wo = fv[L.fwo + c0 + q];
+                e += wo * (zz * s);
+                z[q] = se * wo * (s * (1.f + zz * (1.f - s)));
+            }
+            store_split8(sa, sa_lo, row, c0, H2, z);
+            store_split8(sa, sa_lo, row, c0 + 8, H2, z + 8);
+        }
+        if (valid) p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo) * p.sigma_e + p.mu_e;
+        fence_before();
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            issue_gemm(tbase + L.da1, ah, al, w2th, w2tl, H2, H1);
+            mma_commit(mb);
+        }
+        ok = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1;
+        if (!ok) break;
+        fence_after();
+        // ---- dZ1 = dA1 * silu'(Z1 + b1)
+        for (int c0 = 0; c0 < H1; c0 += 16) {
+            float g[16], z[16];
+            tmem_ld16(tlane + L.da1 + c0, g);
+            tmem_ld16(tlane + L.z1 + c0, z);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const float zz = z[q] + fv[L.fb1 + c0 + q];
+                const float s = sigmoidf_(zz);
+                g[q] *= s * (1.f + zz * (1.f - s));
+            }
+            store_split8(sx, sx_lo, row, c0, H1, g);
+            store_split8(sx, sx_lo, row, c0 + 8, H1, g + 8);
+        }
+        fence_before();
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            issue_gemm(tbase + L.dx, xh, xl, w1th, w1tl, H1, Dp);
+            mma_commit(mb);
+        }
+        ok = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1;
+        if (!ok) break;
+        fence_after();
+        // ---- dE/dfp = dX / sigma
+        float* grow = p.gfp + (size_t)(valid ? slot : p.s0) * p.fp_stride;
+        for (int c0 = 0; c0 < Dp; c0 += 16) {
+            float g[16];
+            tmem_ld16(tlane + L.dx + c0, g);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int k = c0 + q;
+                if (valid && k < p.D) grow[k] = g[q] * fv[L.fisig + k];
+            }
+        }
+        fence_before();
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicOr(p.err, ERRBIT_TIMEOUT);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L.ncols) : "memory");
+}
+
+}  // namespace
+
 bool net_tc_prepare(const Species& sp, NetTC& tc, std::string& why) {
-    (void)sp;
     tc.ready = false;
-    why = "the tensor-core network kernel is not available in this build";
-    return false;
+    if (sp.hidden.size() != 2) {
+        why = "the tensor-core network needs exactly two hidden layers";
+        return false;
+    }
+    const int D = sp.D, H1 = sp.hidden[0], H2 = sp.hidden[1];
+    if (D > 128 || H1 % 16 || H2 % 16 || H1 > 128 || H2 > 128 || H1 < 16 || H2 < 16) {
+        why = "the tensor-core network needs D <= 128 and hidden widths that are multiples of 16 up to 128";
+        return false;
+    }
+    const TCLayout L = make_layout(D, H1, H2);
+    std::vector<uint8_t> img(L.bytes, 0);
+    const int Dp = L.Dp;
+    auto W1 = [&](int o, int i) { return i < D ? sp.Wh[0][(size_t)o * D + i] : 0.0; };
+    auto W2 = [&](int o, int i) { return sp.Wh[1][(size_t)o * H1 + i]; };
+    put_operand(img, L.w1, H1, Dp, [&](int r, int k) { return W1(r, k); });         // GEMM1 B: [H1][Dp]
+    put_operand(img, L.w2, H2, H1, [&](int r, int k) { return W2(r, k); });         // GEMM2 B: [H2][H1]
+    put_operand(img, L.w2t, H1, H2, [&](int r, int k) { return W2(k, r); });        // GEMM3 B: [H1][H2]
+    put_operand(img, L.w1t, Dp, H1, [&](int r, int k) { return W1(k, r); });        // GEMM4 B: [Dp][H1]
+    float* fv = reinterpret_cast<float*>(img.data() + L.fvec);
+    for (int k = 0; k < Dp; ++k) {
+        fv[L.fmu + k] = k < D ? (float)sp.mu[k] : 0.f;
+        fv[L.fisig + k] = k < D ? (float)(1.0 / sp.sigma[k]) : 0.f;
+    }
+    for (int o = 0; o < H1; ++o) fv[L.fb1 + o] = (float)sp.bh[0][o];
+    for (int o = 0; o < H2; ++o) fv[L.fb2 + o] = (float)sp.bh[1][o];
+    for (int o = 0; o < H2; ++o) fv[L.fwo + o] = (float)sp.wo[o];
+    if (cudaMalloc(&tc.blob, img.size()) != cudaSuccess) {
+        why = "device allocation failed";
+        return false;
+    }
+    if (cudaMemcpy(tc.blob, img.data(), img.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        why = "copy of the network image failed";
+        return false;
+    }
+    tc.blob_bytes = img.size();
+    tc.D = D;
+    tc.Dp = Dp;
+    tc.H1 = H1;
+    tc.H2 = H2;
+    tc.bo = (float)sp.bo;
+    tc.ready = true;
+    return true;
 }
 
 void net_tc_release(NetTC& tc) {
@@ -16,11 +449,34 @@ void net_tc_release(NetTC& tc) {
     tc.ready = false;
 }
 
-cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, cudaStream_t st) {
-    (void)a;
-    (void)tc;
-    (void)st;
-    return cudaErrorNotSupported;
+cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_count, cudaStream_t st) {
+    if (!tc.ready) return cudaErrorNotSupported;
+    const int n = a.s1 - a.s0;
+    if (n <= 0) return cudaSuccess;
+    const TCLayout L = make_layout(tc.D, tc.H1, tc.H2);
+    const int xbytes = align1k(2 * 2 * 128 * (L.Dp > L.H1 ? L.Dp : L.H1));
+    const int abytes = align1k(2 * 2 * 128 * (L.H1 > L.H2 ? L.H1 : L.H2));
+    const size_t sm = (size_t)L.bytes + xbytes + abytes;
+    cudaError_t e = cudaFuncSetAttribute(k_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    TcParams p;
+    p.perm = a.perm;
+    p.s0 = a.s0;
+    p.s1 = a.s1;
+    p.fp = a.fp;
+    p.fp_stride = a.fp_stride;
+    p.D = tc.D;
+    p.gfp = a.gfp;
+    p.e_atom = a.e_atom;
+    p.mu_e = a.mu_e;
+    p.sigma_e = a.sigma_e;
+    p.bo = tc.bo;
+    p.img = reinterpret_cast<const uint8_t*>(tc.blob);
+    p.err = err;
+    const int ntiles = (n + 127) / 128;
+    const int grid = ntiles < sm_count ? ntiles : sm_count;
+    k_net_tc<<<grid, kTcThreads, sm, st>>>(p, L);
+    return cudaGetLastError();
 }
 
 }  // namespace nnapgb

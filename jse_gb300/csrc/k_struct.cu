@@ -75,8 +75,8 @@ __device__ __forceinline__ void image_shift(const StructDev& S, int na, int nb, 
 // candidate screen and the atom's cell, and count atoms per cell.
 __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ x,
                            const int* __restrict__ type, int n, int ntypes, double* __restrict__ xw,
-                           float4* __restrict__ xf, int* __restrict__ cell_of, int* __restrict__ cell_count,
-                           int* __restrict__ err) {
+                           float4* __restrict__ xf, float4* __restrict__ xlo, int* __restrict__ cell_of,
+                           int* __restrict__ cell_count, int* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const StructDev& st = S[sid[i]];
@@ -89,7 +89,10 @@ __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restric
         if (p[d] < 0.0 || p[d] >= 1.0) p[d] = ds(p[d], floor(p[d]));
     to_cartesian(st, p);
     xw[3 * i] = p[0]; xw[3 * i + 1] = p[1]; xw[3 * i + 2] = p[2];
-    xf[i] = make_float4((float)p[0], (float)p[1], (float)p[2], __int_as_float(t));
+    const float hx = (float)p[0], hy = (float)p[1], hz = (float)p[2];
+    xf[i] = make_float4(hx, hy, hz, __int_as_float(t));
+    // x = hi + lo exactly to 48 bits: the float-float form used by the neighbour test
+    xlo[i] = make_float4((float)ds(p[0], (double)hx), (float)ds(p[1], (double)hy), (float)ds(p[2], (double)hz), 0.f);
     double f[3] = {p[0], p[1], p[2]};
     to_direct(st, f);
     int c[3];
@@ -149,16 +152,51 @@ __global__ void k_fill_cells(const int* __restrict__ cell_of, int n, const int* 
 }
 
 // Order each cell's atoms by index so that every neighbour row is deterministic.
+// One warp per cell: up to 32 atoms are placed by rank; larger cells are sorted by lane 0.
 __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int* __restrict__ cell_atoms) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (c >= ncells) return;
-    const int b = cell_start[c], e = cell_start[c + 1];
-    for (int k = b + 1; k < e; ++k) {
-        const int v = cell_atoms[k];
-        int q = k - 1;
-        while (q >= b && cell_atoms[q] > v) { cell_atoms[q + 1] = cell_atoms[q]; --q; }
-        cell_atoms[q + 1] = v;
+    const int b = cell_start[c], e = cell_start[c + 1], m = e - b;
+    if (m <= 32) {
+        const int v = lane < m ? cell_atoms[b + lane] : 0x7fffffff;
+        int rank = 0;
+        for (int q = 0; q < m; ++q) {
+            const int u = __shfl_sync(0xffffffffu, v, q);
+            rank += (u < v) ? 1 : 0;
+        }
+        __syncwarp();
+        if (lane < m) cell_atoms[b + rank] = v;
+    } else if (lane == 0) {
+        for (int k = b + 1; k < e; ++k) {
+            const int v = cell_atoms[k];
+            int q = k - 1;
+            while (q >= b && cell_atoms[q] > v) { cell_atoms[q + 1] = cell_atoms[q]; --q; }
+            cell_atoms[q + 1] = v;
+        }
     }
+}
+
+// ----------------------------------------------------------------- float-float helpers
+// Error-free transformations on the FP32 pipe (the FP64 pipe of this GPU is narrow).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+// hi + lo += v
+__device__ __forceinline__ void ff_acc(float& hi, float& lo, float v) {
+    float s, e;
+    two_sum(hi, v, s, e);
+    hi = s;
+    lo += e;
+}
+// hi + lo += x * y (exact product)
+__device__ __forceinline__ void ff_acc_prod(float& hi, float& lo, float x, float y) {
+    const float p = x * y;
+    const float pe = fmaf(x, y, -p);
+    ff_acc(hi, lo, p);
+    lo += pe;
 }
 
 // ----------------------------------------------------------------- neighbour rows
@@ -170,12 +208,13 @@ constexpr int kNbWarps = 4;
 
 __global__ void __launch_bounds__(32 * kNbWarps)
 k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ xw,
-            const float4* __restrict__ xf, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
-            const int* __restrict__ cell_atoms, int n, PairBufs P, int* __restrict__ err, int* __restrict__ max_count) {
+            const float4* __restrict__ xf, const float4* __restrict__ xlo, const int* __restrict__ cell_of,
+            const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, int n, PairBufs P,
+            int* __restrict__ err, int* __restrict__ max_count) {
     __shared__ int s_incl[kNbWarps][32], s_start[kNbWarps][32];
     __shared__ uint32_t s_img[kNbWarps][32];
     __shared__ double s_sh[kNbWarps][32][3];
-    __shared__ float s_fsh[kNbWarps][32][3];
+    __shared__ float s_fsh[kNbWarps][32][3], s_flo[kNbWarps][32][3];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * kNbWarps + w;
     if (i >= n) return;
@@ -187,6 +226,9 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     const int noff = wa * wb * (2 * st.R[2] + 1);
     const double xi = xw[3 * i], yi = xw[3 * i + 1], zi = xw[3 * i + 2];
     const float4 fi = xf[i];
+    const float4 li = xlo[i];
+    const float rc2h = (float)st.rc2, rc2l = (float)(st.rc2 - (double)(float)st.rc2);
+    const float tol = 1e-10f * rc2h;  // float-float d^2 is accurate to ~1e-12 relative
     int cnt = 0;
     for (int o0 = 0; o0 < noff; o0 += 32) {
         const int o = o0 + lane;
@@ -206,7 +248,12 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             double sh[3];
             image_shift(st, na, nb, nc, sh);
 #pragma unroll
-            for (int d = 0; d < 3; ++d) { s_sh[w][lane][d] = sh[d]; s_fsh[w][lane][d] = (float)sh[d]; }
+            for (int d = 0; d < 3; ++d) {
+                const float h = (float)sh[d];
+                s_sh[w][lane][d] = sh[d];
+                s_fsh[w][lane][d] = h;
+                s_flo[w][lane][d] = (float)ds(sh[d], (double)h);
+            }
         }
         int incl = ccount;
 #pragma unroll
@@ -221,7 +268,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             const int cidx = cb + lane;
             bool acc = false;
             int j = 0, slot = 0;
-            double dxv = 0.0, dyv = 0.0, dzv = 0.0;
+            float ox = 0.f, oy = 0.f, oz = 0.f;
             if (cidx < total) {
                 int lo = 0, hi = 31;  // first slot with incl > cidx
                 while (lo < hi) {
@@ -238,11 +285,37 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     const float fy = (fj.y + s_fsh[w][slot][1]) - fi.y;
                     const float fz = (fj.z + s_fsh[w][slot][2]) - fi.z;
                     if (fx * fx + fy * fy + fz * fz < st.rc2_hi) {
-                        dxv = ds(da(xw[3 * j], s_sh[w][slot][0]), xi);
-                        dyv = ds(da(xw[3 * j + 1], s_sh[w][slot][1]), yi);
-                        dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
-                        const double d2 = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv));
-                        acc = d2 < st.rc2;
+                        // (x_j + shift) - x_i in float-float, then d^2 in float-float
+                        const float4 lj = xlo[j];
+                        float dh[3], dl[3];
+                        const float ajh[3] = {fj.x, fj.y, fj.z}, ajl[3] = {lj.x, lj.y, lj.z};
+                        const float aih[3] = {fi.x, fi.y, fi.z}, ail[3] = {li.x, li.y, li.z};
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            float s1, e1, s2, e2;
+                            two_sum(ajh[d], s_fsh[w][slot][d], s1, e1);
+                            two_sum(s1, -aih[d], s2, e2);
+                            const float lo = ((ajl[d] + s_flo[w][slot][d]) - ail[d]) + (e1 + e2);
+                            two_sum(s2, lo, dh[d], dl[d]);
+                        }
+                        float d2h = 0.f, d2l = 0.f;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            ff_acc_prod(d2h, d2l, dh[d], dh[d]);
+                            d2l += 2.f * dh[d] * dl[d];
+                        }
+                        const float diff = (d2h - rc2h) + (d2l - rc2l);
+                        if (fabsf(diff) > tol) {
+                            acc = diff < 0.f;
+                        } else {  // within 1e-10 of the cutoff: the exact FP64 test
+                            const double dxv = ds(da(xw[3 * j], s_sh[w][slot][0]), xi);
+                            const double dyv = ds(da(xw[3 * j + 1], s_sh[w][slot][1]), yi);
+                            const double dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
+                            acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
+                        }
+                        ox = dh[0] + dl[0];
+                        oy = dh[1] + dl[1];
+                        oz = dh[2] + dl[2];
                     }
                 }
             }
@@ -252,7 +325,8 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 if (pos < M) {
                     const size_t e = (size_t)i * M + pos;
                     P.key[e] = pair_key(j, s_img[w][slot]);
-                    P.dx[e] = make_float4((float)dxv, (float)dyv, (float)dzv, xf[j].w);
+                    P.dx[e] = make_float4(ox, oy, oz, xf[j].w);
+                    P.grp[e] = (uint16_t)(o0 + slot);
                 }
             }
             cnt += __popc(m);
@@ -267,28 +341,39 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
 }
 
 // Mirror index: for entry (i -> j, image n) the position of (j -> i, image -n) in j's row.
-__global__ void k_mirror(PairBufs P, int n, int* __restrict__ err) {
+// Rows are ordered by (cell-offset group, atom index); the mirrored entry lies in group
+// noff-1-g of j's row (the negated cell offset), so it is found by binary search.
+__global__ void k_mirror(const StructDev* __restrict__ S, const int* __restrict__ sid, PairBufs P, int n,
+                         int* __restrict__ err) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int M = P.M;
     const int i = (int)(t / M), k = (int)(t % M);
     if (i >= n) return;
     const int ci = min(P.count[i], M);
     if (k >= ci) return;
-    const uint64_t key = P.key[(size_t)i * M + k];
+    const StructDev& st = S[sid[i]];
+    const int noff = (2 * st.R[0] + 1) * (2 * st.R[1] + 1) * (2 * st.R[2] + 1);
+    const size_t e = (size_t)i * M + k;
+    const uint64_t key = P.key[e];
     const int j = (int)(key >> 32);
-    int na, nb, nc;
-    unpack_img((uint32_t)key, na, nb, nc);
-    const uint64_t want = pair_key(i, pack_img(-na, -nb, -nc));
+    const uint32_t want_g = (uint32_t)(noff - 1 - P.grp[e]);
+    const uint64_t want = ((uint64_t)want_g << 32) | (uint32_t)i;
     const int cj = min(P.count[j], M);
     const uint64_t* row = P.key + (size_t)j * M;
-    int found = -1;
-    for (int q = 0; q < cj; ++q)
-        if (row[q] == want) { found = q; break; }
-    if (found < 0) {
-        atomicOr(err, ERRBIT_NO_MIRROR);
-        P.rev[(size_t)i * M + k] = (int)((size_t)i * M + k);
+    const uint16_t* grow = P.grp + (size_t)j * M;
+    int lo = 0, hi = cj;  // first q with composite(q) >= want
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const uint64_t c = ((uint64_t)grow[mid] << 32) | (uint32_t)(row[mid] >> 32);
+        if (c < want) lo = mid + 1; else hi = mid;
+    }
+    int na, nb, nc;
+    unpack_img((uint32_t)key, na, nb, nc);
+    if (lo < cj && row[lo] == pair_key(i, pack_img(-na, -nb, -nc))) {
+        P.rev[e] = (int)((size_t)j * M + lo);
     } else {
-        P.rev[(size_t)i * M + k] = (int)((size_t)j * M + found);
+        atomicOr(err, ERRBIT_NO_MIRROR);
+        P.rev[e] = (int)e;
     }
 }
 
@@ -370,43 +455,42 @@ __global__ void k_type_scatter(const int* __restrict__ type, int n, int T, const
 }
 
 // ----------------------------------------------------------------- gather
-// One warp per atom a: F_a = sum_k (g[mirror(a,k)] - g[a,k]);
-// W_a = sum_k dx[mirror(a,k)] (x) g[mirror(a,k)], accumulated in FP64.
+// One thread per atom a: F_a = sum_k (g[mirror(a,k)] - g[a,k]);
+// W_a = sum_k dx[mirror(a,k)] (x) g[mirror(a,k)].  Sums are carried as float-float
+// pairs (exact products, error-free additions) and written as FP64.
 __global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double* __restrict__ virials) {
-    const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     const int M = P.M;
     const int cnt = min(P.count[a], M);
-    double f[3] = {0.0, 0.0, 0.0}, v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = lane; k < cnt; k += 32) {
-        const size_t e = (size_t)a * M + k;
-        const float4 go = P.g[e];
-        const int r = P.rev[e];
+    float fh[3] = {0.f, 0.f, 0.f}, fl[3] = {0.f, 0.f, 0.f};
+    float vh[9], vl[9];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) { vh[d] = 0.f; vl[d] = 0.f; }
+    const size_t row = (size_t)a * M;
+#pragma unroll 2
+    for (int k = 0; k < cnt; ++k) {
+        const float4 go = P.g[row + k];
+        const int r = P.rev[row + k];
         const float4 gr = P.g[r];
         const float4 dr = P.dx[r];
-        f[0] += (double)gr.x - (double)go.x;
-        f[1] += (double)gr.y - (double)go.y;
-        f[2] += (double)gr.z - (double)go.z;
-        const double x = dr.x, y = dr.y, z = dr.z, gx = gr.x, gy = gr.y, gz = gr.z;
-        v[0] += x * gx; v[1] += y * gy; v[2] += z * gz;
-        v[3] += x * gy; v[4] += x * gz; v[5] += y * gz;
-        v[6] += y * gx; v[7] += z * gx; v[8] += z * gy;
+        ff_acc(fh[0], fl[0], gr.x); ff_acc(fh[0], fl[0], -go.x);
+        ff_acc(fh[1], fl[1], gr.y); ff_acc(fh[1], fl[1], -go.y);
+        ff_acc(fh[2], fl[2], gr.z); ff_acc(fh[2], fl[2], -go.z);
+        ff_acc_prod(vh[0], vl[0], dr.x, gr.x);
+        ff_acc_prod(vh[1], vl[1], dr.y, gr.y);
+        ff_acc_prod(vh[2], vl[2], dr.z, gr.z);
+        ff_acc_prod(vh[3], vl[3], dr.x, gr.y);
+        ff_acc_prod(vh[4], vl[4], dr.x, gr.z);
+        ff_acc_prod(vh[5], vl[5], dr.y, gr.z);
+        ff_acc_prod(vh[6], vl[6], dr.y, gr.x);
+        ff_acc_prod(vh[7], vl[7], dr.z, gr.x);
+        ff_acc_prod(vh[8], vl[8], dr.z, gr.y);
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int d = 0; d < 3; ++d) forces[3 * (size_t)a + d] = (double)fh[d] + (double)fl[d];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) f[d] += __shfl_xor_sync(0xffffffffu, f[d], o);
-#pragma unroll
-        for (int d = 0; d < 9; ++d) v[d] += __shfl_xor_sync(0xffffffffu, v[d], o);
-    }
-    if (lane < 3) forces[3 * (size_t)a + lane] = lane == 0 ? f[0] : (lane == 1 ? f[1] : f[2]);
-    if (lane < 9) {
-        double out = v[0];
-#pragma unroll
-        for (int d = 1; d < 9; ++d) if (lane == d) out = v[d];
-        virials[9 * (size_t)a + lane] = out;
-    }
+    for (int d = 0; d < 9; ++d) virials[9 * (size_t)a + d] = (double)vh[d] + (double)vl[d];
 }
 
 // ----------------------------------------------------------------- per-structure totals
@@ -440,18 +524,19 @@ __global__ void k_reduce_chunks(const int* __restrict__ cb, const int* __restric
     }
 }
 
-// structure s owns chunks [sc[s], sc[s+1]).
+// structure s owns chunks [sc[s], sc[s+1]); one warp per structure, fixed summation order.
 __global__ void k_reduce_structs(const int* __restrict__ sc, int nstruct, const double* __restrict__ partial,
                                  double* __restrict__ energy, double* __restrict__ virial) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (s >= nstruct) return;
-    double t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int c = sc[s]; c < sc[s + 1]; ++c)
-#pragma unroll
-        for (int d = 0; d < 10; ++d) t[d] += partial[10 * (size_t)c + d];
-    energy[s] = t[0];
-#pragma unroll
-    for (int d = 0; d < 9; ++d) virial[9 * (size_t)s + d] = t[1 + d];
+    double t = 0.0;
+    const int nv = 10;
+    // lanes 0..9 each own one of the 10 totals and add the chunks in order
+    if (lane < nv)
+        for (int c = sc[s]; c < sc[s + 1]; ++c) t += partial[10 * (size_t)c + lane];
+    if (lane == 0) energy[s] = t;
+    else if (lane < nv) virial[9 * (size_t)s + lane - 1] = t;
 }
 
 }  // namespace nnapgb

@@ -12,6 +12,7 @@ namespace nnapgb {
 struct NetTC {
     bool ready = false;
     int D = 0, Dp = 0, H1 = 0, H2 = 0;
+    float bo = 0.f;           // output bias
     void* blob = nullptr;     // device: packed operand images and FP32 vectors
     size_t blob_bytes = 0;
 };
@@ -20,6 +21,7 @@ struct NetTC {
 // shape is outside what the kernel implements.
 bool net_tc_prepare(const Species& sp, NetTC& tc, std::string& why);
 void net_tc_release(NetTC& tc);
-cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, cudaStream_t st);
+// err receives ERRBIT_TIMEOUT if a bounded wait on the tensor cores gave up.
+cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_count, cudaStream_t st);
 
 }  // namespace nnapgb

@@ -32,14 +32,14 @@ using namespace nnapgb;
 
 namespace nnapgb {
 // k_struct.cu
-__global__ void k_wrap_bin(const StructDev*, const int*, const double*, const int*, int, int, double*, float4*, int*,
-                           int*, int*);
+__global__ void k_wrap_bin(const StructDev*, const int*, const double*, const int*, int, int, double*, float4*,
+                           float4*, int*, int*, int*);
 __global__ void k_scan_excl(const int*, int, int*);
 __global__ void k_fill_cells(const int*, int, const int*, int*, int*);
 __global__ void k_sort_cells(const int*, int, int*);
-__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const int*, const int*,
-                            const int*, int, PairBufs, int*, int*);
-__global__ void k_mirror(PairBufs, int, int*);
+__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const int*,
+                            const int*, const int*, int, PairBufs, int*, int*);
+__global__ void k_mirror(const StructDev*, const int*, PairBufs, int, int*);
 __global__ void k_type_hist(const int*, int, int, int*);
 __global__ void k_type_offsets(int*, int, int, int*);
 __global__ void k_type_scatter(const int*, int, int, const int*, int*);
@@ -133,7 +133,8 @@ struct nnap_handle {
     DevBuf<double> x, xw, e_atom, forces, virials, energy, virial, partial;
     DevBuf<int> type, sid, cell_of, cell_count, cell_fill, cell_start, cell_atoms, perm, block_counts, type_start;
     DevBuf<int> chunk_b, chunk_e, struct_chunks, status;
-    DevBuf<float4> xf;
+    DevBuf<float4> xf, xlo;
+    DevBuf<uint16_t> pgrp;
     DevBuf<StructDev> sdev;
     DevBuf<uint64_t> pkey;
     DevBuf<float4> pdx, pg;
@@ -143,6 +144,7 @@ struct nnap_handle {
     int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
     bool profiling = false;
     cudaEvent_t order_ev = nullptr;
+    int sm_count = 148;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void mark(int k) {
         if (profiling) CK(cudaEventRecord(ev[k], stream));
@@ -346,6 +348,7 @@ void grow_pairs(nnap_handle* h, int n, int M) {
     h->pdx.ensure(np);
     h->pg.ensure(np);
     h->prev.ensure(np);
+    h->pgrp.ensure(np);
 }
 
 PairBufs pair_bufs(nnap_handle* h) {
@@ -355,6 +358,7 @@ PairBufs pair_bufs(nnap_handle* h) {
     P.dx = h->pdx.p;
     P.rev = h->prev.p;
     P.g = h->pg.p;
+    P.grp = h->pgrp.p;
     P.count = h->pcount.p;
     return P;
 }
@@ -382,6 +386,7 @@ void build_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const in
     if (n) CK(cudaMemcpyAsync(h->sid.p, B.sid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
     h->xw.ensure(3 * (size_t)n);
     h->xf.ensure(n);
+    h->xlo.ensure(n);
     h->cell_of.ensure(n);
     h->cell_count.ensure(B.ncells);
     h->cell_fill.ensure(B.ncells);
@@ -399,21 +404,21 @@ void build_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const in
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
     if (n > 0) {
         k_wrap_bin<<<(n + 255) / 256, 256, 0, st>>>(h->sdev.p, h->sid.p, d_x, d_type, n, T, h->xw.p, h->xf.p,
-                                                    h->cell_of.p, h->cell_count.p, h->status.p);
+                                                    h->xlo.p, h->cell_of.p, h->cell_count.p, h->status.p);
         ++h->launches;
     }
     k_scan_excl<<<1, 1024, 0, st>>>(h->cell_count.p, B.ncells, h->cell_start.p);
     ++h->launches;
     if (n > 0) {
         k_fill_cells<<<(n + 255) / 256, 256, 0, st>>>(h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p);
-        k_sort_cells<<<(B.ncells + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
+        k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
         h->launches += 2;
     }
     for (int attempt = 0; attempt < 3; ++attempt) {
         CK(cudaMemsetAsync(h->status.p + 1, 0, sizeof(int), st));
         if (n > 0) {
             k_neighbors<<<(n + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
-                h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
+                h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
                 pair_bufs(h), h->status.p, h->status.p + 1);
             ++h->launches;
         }
@@ -442,7 +447,7 @@ void build_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const in
     (void)want_types;
     if (n > 0) {
         const long long tot = (long long)n * h->M;
-        k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(pair_bufs(h), n, h->status.p);
+        k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
         ++h->launches;
     }
 }
@@ -510,7 +515,7 @@ void network(nnap_handle* h, const std::vector<int>& ts) {
         a.e_atom = h->e_atom.p;
         a.gfp = h->gfp.p;
         if (h->precision == NNAP_PREC_MIXED) {
-            CK(launch_net_tc(a, nd.tc, h->stream));
+            CK(launch_net_tc(a, nd.tc, h->status.p, h->sm_count, h->stream));
         } else {
             CK(launch_net_fp32(a, h->stream));
         }
@@ -541,7 +546,7 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
     h->forces.ensure(3 * (size_t)std::max(n, 1));
     h->virials.ensure(9 * (size_t)std::max(n, 1));
     if (n > 0) {
-        k_gather<<<(n * 32 + 255) / 256, 256, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
+        k_gather<<<(n + 127) / 128, 128, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
         ++h->launches;
     }
     const int nchunks = (int)B.cb.size();
@@ -559,7 +564,7 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
         ++h->launches;
     }
     CK(cudaMemcpyAsync(h->struct_chunks.p, B.sc.data(), sizeof(int) * (B.nstruct + 1), cudaMemcpyHostToDevice, st));
-    k_reduce_structs<<<(B.nstruct + 127) / 128, 128, 0, st>>>(h->struct_chunks.p, B.nstruct, h->partial.p,
+    k_reduce_structs<<<(B.nstruct * 32 + 127) / 128, 128, 0, st>>>(h->struct_chunks.p, B.nstruct, h->partial.p,
                                                                h->energy.p, h->virial.p);
     ++h->launches;
     h->mark(5);
@@ -569,6 +574,7 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
 void check_after(nnap_handle* h) {
     CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    if (h->h_status[0] & ERRBIT_TIMEOUT) throw ApiFail(NNAP_ERR_TIMEOUT, "a bounded tensor-core wait gave up");
     if (h->h_status[0] & ERRBIT_NO_MIRROR) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
     if (h->h_status[0] & ERRBIT_CAPACITY) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour capacity exceeded");
 }
@@ -627,6 +633,7 @@ int nnap_create(const char* model_json, size_t len, int precision, int device, n
     try {
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        CK(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
         CK(cudaMallocHost(&h->h_status, sizeof(int) * (3 + kMaxTypes)));
         CK(upload_sh_constants());
         upload_model(h.get());
@@ -666,7 +673,7 @@ int nnap_destroy(nnap_handle* h) {
     h->type.release(); h->sid.release(); h->cell_of.release(); h->cell_count.release(); h->cell_fill.release();
     h->cell_start.release(); h->cell_atoms.release(); h->perm.release(); h->block_counts.release();
     h->type_start.release(); h->chunk_b.release(); h->chunk_e.release(); h->struct_chunks.release();
-    h->status.release(); h->xf.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
+    h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release();
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     if (h->order_ev) cudaEventDestroy(h->order_ev);

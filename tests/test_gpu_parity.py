@@ -68,3 +68,23 @@ def test_results_are_deterministic(golden):
         b = p.calEnergyForceVirials(_S(golden))
     for k in ("energies", "forces", "virials", "virial"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def _tc_shape_ok(model):
+    for m in model["models"]:
+        h = m.get("nn", {}).get("hidden_dims", [32, 32])
+        if len(h) != 2 or any(x % 16 for x in h):
+            return False
+    return True
+
+
+def test_energy_force_virial_mixed(golden):
+    """Mixed precision: split-BF16 tensor-core network (hi*hi + lo*hi + hi*lo, FP32 accumulation)."""
+    if not _tc_shape_ok(golden.model):
+        pytest.skip("network shape outside the tensor-core kernel (two hidden layers, widths multiple of 16)")
+    with _nnap(golden.model_json, "mixed") as p:
+        o = p.calEnergyForceVirials(_S(golden))
+    escale = max(1.0, float(np.abs(golden.energies).max()))
+    assert np.abs(o["energies"] - golden.energies).max() <= 2e-5 * escale
+    _close(o["forces"], golden.forces, 1e-3, 2e-4)
+    _close(o["virials"], golden.virials, 1e-3, 2e-4)
