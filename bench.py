@@ -273,24 +273,29 @@ def main():
     dev = torch.device("cuda", local)
     s = structures[0]
     single = len(structures) == 1
-
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    if single:
-        n = s.natoms
-        x_d = torch.from_numpy(np.ascontiguousarray(s.x)).to(dev)
-        t_d = torch.from_numpy(np.ascontiguousarray(s.types)).to(dev)
-        e_d = torch.zeros(1, dtype=torch.float64, device=dev)
-        f_d = torch.zeros((n, 3), dtype=torch.float64, device=dev)
-        v_d = torch.zeros(9, dtype=torch.float64, device=dev)
-        flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
+    nat = np.array([st.natoms for st in structures], dtype=np.int32)
+    kinds = np.array([st.box_kind for st in structures], dtype=np.int32)
+    boxes = np.ascontiguousarray(np.concatenate([np.asarray(st.box, dtype=np.float64).reshape(9) for st in structures]))
+    x_all = np.ascontiguousarray(np.concatenate([st.x for st in structures]))
+    t_all = np.ascontiguousarray(np.concatenate([st.types for st in structures]).astype(np.int32))
+    N = int(nat.sum())
+    S = len(structures)
+    x_d = torch.from_numpy(x_all).to(dev)
+    t_d = torch.from_numpy(t_all).to(dev)
+    e_d = torch.zeros(S, dtype=torch.float64, device=dev)
+    f_d = torch.zeros((N, 3), dtype=torch.float64, device=dev)
+    v_d = torch.zeros((S, 9), dtype=torch.float64, device=dev)
+    flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
 
-        def device_step():
-            st = torch.cuda.current_stream(dev).cuda_stream
-            pot.computeDevice(n, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
-                              f_d.data_ptr(), v_d.data_ptr(), 0, stream=st)
-    else:
-        def device_step():
-            pot.calEnergyForceVirialsBatch(structures)
+    def device_step():
+        st_ = torch.cuda.current_stream(dev).cuda_stream
+        if single:
+            pot.computeDevice(N, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
+                              f_d.data_ptr(), v_d.data_ptr(), 0, stream=st_)
+        else:
+            pot.computeBatchDevice(nat, x_d.data_ptr(), t_d.data_ptr(), kinds, boxes, flags, e_d.data_ptr(), 0,
+                                   f_d.data_ptr(), v_d.data_ptr(), 0, stream=st_)
 
     bench_stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(bench_stream)
@@ -305,7 +310,7 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
-    ms, stages, launches = [], np.zeros(5), 0
+    ms, stages, launches, stage_ok = [], np.zeros(5), 0, True
     t_wall = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
@@ -316,7 +321,11 @@ def main():
         e1.record()
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
-        stages += pot.stageTimes()
+        if stage_ok:
+            try:
+                stages += pot.stageTimes()
+            except Exception:
+                stage_ok = False
         launches += pot.lastLaunchCount()
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall
@@ -332,38 +341,52 @@ def main():
     stages /= args.steps
 
     # end to end through host buffers (pinned)
-    e2e = None
-    if single:
-        n = s.natoms
-        xh = torch.from_numpy(np.ascontiguousarray(s.x)).pin_memory().numpy()
-        th = torch.from_numpy(np.ascontiguousarray(s.types)).pin_memory().numpy()
-        fh = torch.zeros((n, 3), dtype=torch.float64).pin_memory().numpy()
-        eh = torch.zeros(1, dtype=torch.float64).pin_memory().numpy()
-        vh = torch.zeros(9, dtype=torch.float64).pin_memory().numpy()
-        from jse_gb300.nnap import _dptr, _iptr
-        box9 = np.ascontiguousarray(s.box, dtype=np.float64).reshape(9)
-        for _ in range(2):
-            pot._check(pot._L.nnap_compute(pot._handle(), n, _dptr(xh), _iptr(th), s.box_kind, _dptr(box9), flags,
-                                           _dptr(eh), None, _dptr(fh), _dptr(vh), None))
-        dts = []
-        for _ in range(args.steps):
-            flush.zero_()
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            pot._check(pot._L.nnap_compute(pot._handle(), n, _dptr(xh), _iptr(th), s.box_kind, _dptr(box9), flags,
-                                           _dptr(eh), None, _dptr(fh), _dptr(vh), None))
-            dts.append(time.perf_counter() - t0)
-        e2e = {"value": n * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": n * 24 + n * 4,
-               "d2h_bytes_per_step": 8 + n * 24 + 72}
-    else:
-        dts = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            pot.calEnergyForceVirialsBatch(structures)
-            dts.append(time.perf_counter() - t0)
-        nat = natoms_step
-        e2e = {"value": nat * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": nat * 28,
-               "d2h_bytes_per_step": nat * 32 + len(structures) * 80}
+    from jse_gb300.nnap import _dptr, _iptr
+    xh = torch.from_numpy(x_all).pin_memory().numpy()
+    th = torch.from_numpy(t_all).pin_memory().numpy()
+    fh = torch.zeros((N, 3), dtype=torch.float64).pin_memory().numpy()
+    eh = torch.zeros(S, dtype=torch.float64).pin_memory().numpy()
+    vh = torch.zeros((S, 9), dtype=torch.float64).pin_memory().numpy()
+
+    def host_step(p_):
+        p_._check(p_._L.nnap_compute_batch(p_._handle(), S, _iptr(nat), _dptr(xh), _iptr(th), _iptr(kinds),
+                                           _dptr(boxes), flags, _dptr(eh), None, _dptr(fh), _dptr(vh), None))
+
+    for _ in range(3):
+        host_step(pot)
+    dts = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        host_step(pot)
+        dts.append(time.perf_counter() - t0)
+    e2e = {"value": N * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": N * 28,
+           "d2h_bytes_per_step": S * 8 + N * 24 + S * 72}
+
+    # the plain GPU path on batches: one FP32 single-structure call per structure
+    plain = None
+    if not single:
+        with NNAP(model, precision="fp32", device=local) as pp:
+            pp.setGraphs(False)
+            offs = np.concatenate([[0], np.cumsum(nat)])
+
+            def plain_step():
+                for k, st_ in enumerate(structures):
+                    a, b = offs[k], offs[k + 1]
+                    pp._check(pp._L.nnap_compute(pp._handle(), int(nat[k]), _dptr(xh[a:b]), _iptr(th[a:b]),
+                                                 int(kinds[k]), _dptr(boxes[9 * k:9 * k + 9]), flags, _dptr(eh[k:k + 1]),
+                                                 None, _dptr(fh[a:b]), _dptr(vh[k]), None))
+            plain_step()
+            pts = []
+            for _ in range(max(1, min(args.steps, 5))):
+                t0 = time.perf_counter()
+                plain_step()
+                pts.append(time.perf_counter() - t0)
+            pv = N * len(pts) / sum(pts)
+            plain = {"value": pv, "unit": "atom-evals/s", "ms_per_step": 1e3 * sum(pts) / len(pts),
+                     "path": "plain FP32, one nnap_compute per structure, host buffers",
+                     "tuned_e2e_over_plain": e2e["value"] / pv}
 
     # roofline of the dominant stage
     peak, peak_kind, sm_max = load_peaks()
@@ -400,6 +423,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16+f32",
                 "data": "synthetic (seeded)", "config": config, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                 "clocks": clk, "gpu_launches": launches, "wall_s_timed": wall}
+        if plain is not None:
+            line["plain_gpu"] = plain
         print(json.dumps(line))
     pot.close()
     if dist:

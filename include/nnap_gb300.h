@@ -112,6 +112,14 @@ int nnap_compute_batch(nnap_handle* h, int nstruct, const int* natoms, const dou
                        const int* box_kind, const double* boxes, int flags, double* energy, double* energies,
                        double* forces, double* virial, double* virials);
 
+/* The batched form on device-resident buffers: d_x / d_type hold the concatenated
+ * structures; natoms, box_kind and boxes stay host arrays; every output is a device
+ * pointer with the layout of nnap_compute_batch.  Ordering as nnap_compute_device. */
+int nnap_compute_batch_device(nnap_handle* h, int nstruct, const int* natoms, const double* d_x, const int* d_type,
+                              const int* box_kind, const double* boxes, int flags, double* d_energy,
+                              double* d_energies, double* d_forces, double* d_virial, double* d_virials,
+                              void* stream);
+
 /* Descriptor vectors of every atom (NNAP.calFp, NNAP.java:596-632 -> jse_nnap_calFp,
  * nnap_interface.cpp:11-25).  fp is n x stride doubles, stride >= the largest
  * descriptor size; entries beyond an atom's own size are zero.  Host buffers. */
@@ -135,6 +143,10 @@ int nnap_last_launch_count(const nnap_handle* h, int* count);
  * forward; [2] network; [3] descriptors backward; [4] force/virial gather and FP64
  * reductions.  nnap_stage_times waits for the last call and returns milliseconds. */
 int nnap_set_profiling(nnap_handle* h, int on);
+/* CUDA-graph replay of repeated evaluations (on by default; no counterpart in the
+ * reference).  The first call of a layout (atom counts, box kinds, cell grids, buffer
+ * addresses) runs eagerly, the second is captured, later ones replay the graph. */
+int nnap_set_graphs(nnap_handle* h, int on);
 int nnap_stage_times(nnap_handle* h, double* ms5);
 
 #ifdef __cplusplus

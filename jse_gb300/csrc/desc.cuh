@@ -5,11 +5,14 @@
 
 namespace nnapgb {
 
-// Arguments of one descriptor launch: one sub-basis over a contiguous range of
-// species-sorted slots [s0, s1) whose species share the sub-basis shape.
+// Arguments of one descriptor launch: one sub-basis over the contiguous range of
+// species-sorted slots of a run of species sharing the sub-basis shape.  The range is
+// read on the device, so launches need no host knowledge of the species counts.
 struct DescArgs {
     const int* perm;        // slot -> atom
-    int s0, s1;
+    const int* range;       // device: first slot of each species, [ntypes + 1]
+    int t0, t1;             // species run [t0, t1): slots range[t0] .. range[t1]
+    int nmax;               // upper bound of the slot count (grid sizing)
     const int* type;        // 1-based species per atom
     PairBufs P;
     const float* W;         // [T][T][NP][N1] radial-fuse matrices, centre species major
@@ -17,7 +20,7 @@ struct DescArgs {
     float rcut;
     float* fp;              // descriptors by slot, row stride fp_stride
     int fp_stride, fp_off;  // column offset of this sub-basis
-    float* A;               // spherical only: [s - s0][NP][K] expansion coefficients
+    float* A;               // spherical only: [slot - range[t0]][NP][K] expansion coefficients
     const float* gfp;       // backward: dE/dfp by slot (same layout as fp)
     int accumulate;         // backward: add into P.g instead of overwriting
 };
@@ -26,10 +29,12 @@ cudaError_t upload_sh_constants();
 bool desc_supported(int kind, int lmax, int np, int n1);
 cudaError_t launch_descriptor(int kind, int lmax, int np, int n1, const DescArgs& a, bool fwd, cudaStream_t st);
 
-// Network over the slots [s0, s1) of one species.
+// Network over the slots of one species.
 struct NetArgs {
     const int* perm;
-    int s0, s1;
+    const int* range;       // device: first slot of each species, [ntypes + 1]
+    int t;                  // species (0-based): slots range[t] .. range[t+1]
+    int nmax;               // upper bound of the slot count (grid sizing)
     const float* fp;        // descriptors by slot
     int fp_stride;
     int D, nlayer;

@@ -157,7 +157,7 @@ __device__ __forceinline__ void load_fuse(const float* __restrict__ Wg, float* s
     for (int q = threadIdx.x; q < count; q += blockDim.x) sW[q] = Wg[q];
 }
 
-__device__ __forceinline__ int atom_of(const DescArgs& a, int warp) { return a.perm[a.s0 + warp]; }
+__device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { return a.perm[s0 + warp]; }
 
 }  // namespace
 
@@ -168,8 +168,9 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
     load_fuse<NP, N1>(a.W, sW, a.T * a.T * NP * N1);
     __syncthreads();
     const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (a.s0 + w >= a.s1) return;
-    const int at = atom_of(a, w);
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
     const float rc = a.rcut, irc = 1.f / a.rcut;
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
     for (int p = 0; p < NP; ++p)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc[p] += __shfl_xor_sync(0xffffffffu, acc[p], o);
-    float* out = a.fp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+    float* out = a.fp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
 #pragma unroll
     for (int p = 0; p < NP; ++p)
         if (lane == (p & 31)) out[p] = acc[p];
@@ -209,12 +210,13 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_bwd(DescArgs a) {
     load_fuse<NP, N1>(a.W, sW, a.T * a.T * NP * N1);
     __syncthreads();
     const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (a.s0 + w >= a.s1) return;
-    const int at = atom_of(a, w);
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
     const float rc = a.rcut, irc = 1.f / a.rcut;
-    const float* gf = a.gfp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+    const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
     float gfp[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) gfp[p] = gf[p];
@@ -275,10 +277,11 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * kDescWarps + wl;
-    if (a.s0 + w >= a.s1) return;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
     float* sY = smem + ((nW + 3) & ~3) + wl * S::FWD_WARP_FLOATS;  // [32][KS]
     float* sC = sY + 32 * S::KS;                                       // [32][NPS]
-    const int at = atom_of(a, w);
+    const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
     const float rc = a.rcut, irc = 1.f / a.rcut;
@@ -355,7 +358,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
             }
     }
     __syncwarp();
-    float* out = a.fp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+    float* out = a.fp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
     for (int e = lane; e < NP * (L + 1); e += 32) {
         const int p = e / (L + 1), l = e - p * (L + 1);
         float s = 0.f;
@@ -374,18 +377,19 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_bwd(DescArgs a) {
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * kDescWarps + wl;
-    if (a.s0 + w >= a.s1) return;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
     float* sG = smem + ((nW + 3) & ~3) + wl * S::BWD_WARP_FLOATS;  // [K][NPS]
     float* sY = sG + S::K * S::NPS;                                   // [K][32]
     float* sYt = sY + S::K * 32;                                      // [K][32]
-    const int at = atom_of(a, w);
+    const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
     const float rc = a.rcut, irc = 1.f / a.rcut;
     // G[p][lm] = 2 * 4pi/(2l+1) * dE/dfp[p][l] * A[p][lm], stored transposed
     {
         const float* Ain = a.A + (size_t)w * NP * S::K;
-        const float* gf = a.gfp + (size_t)(a.s0 + w) * a.fp_stride + a.fp_off;
+        const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
         for (int lm = lane; lm < S::K; lm += 32) {
             int l = 0;
             while ((l + 1) * (l + 1) <= lm) ++l;
@@ -512,7 +516,7 @@ namespace {
 
 template <int NP, int N1>
 cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
-    const int n = a.s1 - a.s0;
+    const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     const int grid = (n + kDescWarps - 1) / kDescWarps;
     const size_t sm = sizeof(float) * a.T * a.T * NP * N1;
@@ -524,7 +528,7 @@ cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
 template <int L, int NP, int N1>
 cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     using S = SphShape<L, NP>;
-    const int n = a.s1 - a.s0;
+    const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     const int grid = (n + kDescWarps - 1) / kDescWarps;
     const size_t wbytes = sizeof(float) * (((size_t)a.T * a.T * NP * N1 + 3) & ~(size_t)3);

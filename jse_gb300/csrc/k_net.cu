@@ -28,9 +28,10 @@ __device__ __forceinline__ float silu_and_grad(float z, float* grad) {
 __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp_floats) {
     extern __shared__ float smem[];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int slot0 = a.s0 + (blockIdx.x * kNetWarps + wl) * kNetAtoms;
-    if (slot0 >= a.s1) return;
-    const int na = min(kNetAtoms, a.s1 - slot0);
+    const int s0 = a.range[a.t], s1 = a.range[a.t + 1];
+    const int slot0 = s0 + (blockIdx.x * kNetWarps + wl) * kNetAtoms;
+    if (slot0 >= s1) return;
+    const int na = min(kNetAtoms, s1 - slot0);
     int Hmax = a.D;
     for (int l = 0; l < a.nlayer; ++l) Hmax = max(Hmax, a.H[l]);
     float* buf0 = smem + (size_t)wl * warp_floats;        // [Hmax][8]
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
 }  // namespace
 
 cudaError_t launch_net_fp32(const NetArgs& a, cudaStream_t st) {
-    const int n = a.s1 - a.s0;
+    const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     int Hmax = a.D;
     for (int l = 0; l < a.nlayer; ++l) Hmax = Hmax > a.H[l] ? Hmax : a.H[l];

@@ -206,7 +206,8 @@ __device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + expf(-
 
 struct TcParams {
     const int* perm;
-    int s0, s1;
+    const int* range;
+    int t;
     const float* fp;
     int fp_stride, D;
     float* gfp;
@@ -265,14 +266,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
     uint8_t* sx_lo = sx + 2 * 128 * (Dp > H1 ? Dp : H1);
     uint8_t* sa_lo = sa + ab;
 
-    const int n = p.s1 - p.s0;
-    const int ntiles = (n + 127) / 128;
+    const int s0 = p.range[p.t], s1 = p.range[p.t + 1];
+    const int ntiles = (s1 - s0 + 127) / 128;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const int row = tid;
-        const int slot = p.s0 + tile * 128 + row;
-        const bool valid = slot < p.s1;
+        const int slot = s0 + tile * 128 + row;
+        const bool valid = slot < s1;
         // ---- X = (fp - mu) / sigma, split into hi / lo
-        const float* frow = p.fp + (size_t)(valid ? slot : p.s0) * p.fp_stride;
+        const float* frow = p.fp + (size_t)(valid ? slot : s0) * p.fp_stride;
         for (int k0 = 0; k0 < Dp; k0 += 8) {
             float v[8];
 #pragma unroll
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         if (!ok) break;
         fence_after();
         // ---- dE/dfp = dX / sigma
-        float* grow = p.gfp + (size_t)(valid ? slot : p.s0) * p.fp_stride;
+        float* grow = p.gfp + (size_t)(valid ? slot : s0) * p.fp_stride;
         for (int c0 = 0; c0 < Dp; c0 += 16) {
             float g[16];
             tmem_ld16(tlane + L.dx + c0, g);
@@ -451,7 +452,7 @@ void net_tc_release(NetTC& tc) {
 
 cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_count, cudaStream_t st) {
     if (!tc.ready) return cudaErrorNotSupported;
-    const int n = a.s1 - a.s0;
+    const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     const TCLayout L = make_layout(tc.D, tc.H1, tc.H2);
     const int xbytes = align1k(2 * 2 * 128 * (L.Dp > L.H1 ? L.Dp : L.H1));
@@ -461,8 +462,8 @@ cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_co
     if (e != cudaSuccess) return e;
     TcParams p;
     p.perm = a.perm;
-    p.s0 = a.s0;
-    p.s1 = a.s1;
+    p.range = a.range;
+    p.t = a.t;
     p.fp = a.fp;
     p.fp_stride = a.fp_stride;
     p.D = tc.D;

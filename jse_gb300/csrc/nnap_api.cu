@@ -144,6 +144,14 @@ struct nnap_handle {
     int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
     bool profiling = false;
     cudaEvent_t order_ev = nullptr;
+    // launch-sequence cache (CUDA graph) and the layout it was sized for
+    bool use_graphs = true;
+    bool layout_ok = false;
+    int layout_runs = 0;
+    std::vector<long long> last_layout, gkey;
+    cudaGraphExec_t gexec = nullptr;
+    StructDev* h_sdev = nullptr;  // pinned staging of the structure descriptors
+    size_t h_sdev_cap = 0;
     int sm_count = 148;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     void mark(int k) {
@@ -343,7 +351,7 @@ struct Outputs {
 
 void grow_pairs(nnap_handle* h, int n, int M) {
     h->M = M;
-    const size_t np = (size_t)n * M;
+    const size_t np = (size_t)std::max(n, 1) * M;
     h->pkey.ensure(np);
     h->pdx.ensure(np);
     h->pg.ensure(np);
@@ -372,33 +380,80 @@ int initial_capacity(const Batch& B, double rc) {
     return std::max(32, (M + 7) & ~7);
 }
 
-// Runs the structure part of the pipeline up to the species sort and validates it.
-// On return: pair rows, mirror index and species slot order are ready on the device,
-// and type_start is known on the host.
-void build_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, std::vector<int>& type_start,
-                     bool want_types) {
+// A-arena rows: every (run, spherical sub-basis) owns n rows of P*K floats, indexed by
+// the slot offset inside its run, so no host knowledge of species counts is needed.
+size_t a_arena_size(nnap_handle* h, int n) {
+    size_t tot = 0;
+    for (auto& r : h->runs)
+        for (auto& s : r.subs)
+            if (s.kind == KIND_SPHERICAL) tot += (size_t)n * s.np * (s.lmax + 1) * (s.lmax + 1);
+    return tot;
+}
+
+// Size every buffer for the batch and upload the layout arrays that depend only on the
+// atom counts (structure of each atom, reduction chunks).  Runs outside graph capture.
+void prepare_layout(nnap_handle* h, const Batch& B) {
     const int n = B.natoms;
     const int T = h->model.ntypes();
-    cudaStream_t st = h->stream;
+    const int n1 = std::max(n, 1);
     h->sdev.ensure(B.nstruct);
-    h->sid.ensure(n);
-    CK(cudaMemcpyAsync(h->sdev.p, B.sd.data(), sizeof(StructDev) * B.nstruct, cudaMemcpyHostToDevice, st));
-    if (n) CK(cudaMemcpyAsync(h->sid.p, B.sid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
-    h->xw.ensure(3 * (size_t)n);
-    h->xf.ensure(n);
-    h->xlo.ensure(n);
-    h->cell_of.ensure(n);
+    h->sid.ensure(n1);
+    h->xw.ensure(3 * (size_t)n1);
+    h->xf.ensure(n1);
+    h->xlo.ensure(n1);
+    h->cell_of.ensure(n1);
     h->cell_count.ensure(B.ncells);
     h->cell_fill.ensure(B.ncells);
     h->cell_start.ensure(B.ncells + 1);
-    h->cell_atoms.ensure(n);
-    h->pcount.ensure(n);
-    h->perm.ensure(n);
+    h->cell_atoms.ensure(n1);
+    h->pcount.ensure(n1);
+    h->perm.ensure(n1);
     const int nb = (n + kSortBlock - 1) / kSortBlock;
     h->block_counts.ensure((size_t)std::max(nb, 1) * T);
     h->type_start.ensure(T + 1);
     h->status.ensure(2);
-    if (h->M == 0 || (size_t)n * h->M > h->pkey.cap) grow_pairs(h, n, std::max(h->M, initial_capacity(B, h->model.rcut_max)));
+    if (h->M == 0) h->M = initial_capacity(B, h->model.rcut_max);
+    grow_pairs(h, n, h->M);
+    h->fp.ensure((size_t)n1 * h->fp_stride);
+    h->gfp.ensure((size_t)n1 * h->fp_stride);
+    h->A.ensure(std::max<size_t>(a_arena_size(h, n), 1));
+    h->e_atom.ensure(n1);
+    h->forces.ensure(3 * (size_t)n1);
+    h->virials.ensure(9 * (size_t)n1);
+    const int nchunks = (int)B.cb.size();
+    h->chunk_b.ensure(std::max(nchunks, 1));
+    h->chunk_e.ensure(std::max(nchunks, 1));
+    h->struct_chunks.ensure(B.nstruct + 1);
+    h->partial.ensure(10 * (size_t)std::max(nchunks, 1));
+    h->energy.ensure(std::max(B.nstruct, 1));
+    h->virial.ensure(9 * (size_t)std::max(B.nstruct, 1));
+    if (h->h_sdev_cap < (size_t)B.nstruct) {
+        if (h->h_sdev) cudaFreeHost(h->h_sdev);
+        h->h_sdev = nullptr;
+        CK(cudaMallocHost(&h->h_sdev, sizeof(StructDev) * B.nstruct));
+        h->h_sdev_cap = B.nstruct;
+    }
+    cudaStream_t st = h->stream;
+    if (n) CK(cudaMemcpyAsync(h->sid.p, B.sid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    if (nchunks) {
+        CK(cudaMemcpyAsync(h->chunk_b.p, B.cb.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->chunk_e.p, B.ce.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(h->struct_chunks.p, B.sc.data(), sizeof(int) * (B.nstruct + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+}
+
+// Queue the whole evaluation on the handle's stream without any host synchronisation
+// (capturable into a CUDA graph).  The structure descriptors are copied from the pinned
+// staging array, so a replay picks up new boxes.
+void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+    const int n = B.natoms;
+    const int T = h->model.ntypes();
+    cudaStream_t st = h->stream;
+    const int nb = (n + kSortBlock - 1) / kSortBlock;
+    h->launches = 0;
+    h->mark(0);
+    CK(cudaMemcpyAsync(h->sdev.p, h->h_sdev, sizeof(StructDev) * B.nstruct, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * B.ncells, st));
     CK(cudaMemsetAsync(h->cell_fill.p, 0, sizeof(int) * B.ncells, st));
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
@@ -412,171 +467,172 @@ void build_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const in
     if (n > 0) {
         k_fill_cells<<<(n + 255) / 256, 256, 0, st>>>(h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p);
         k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
-        h->launches += 2;
-    }
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        CK(cudaMemsetAsync(h->status.p + 1, 0, sizeof(int), st));
-        if (n > 0) {
-            k_neighbors<<<(n + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
-                h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
-                pair_bufs(h), h->status.p, h->status.p + 1);
-            ++h->launches;
-        }
-        if (attempt == 0 && n > 0) {
-            k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
-            k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
-            k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
-            h->launches += 3;
-        }
-        CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
-        if (attempt == 0) CK(cudaMemcpyAsync(h->h_status + 2, h->type_start.p, sizeof(int) * (T + 1),
-                                             cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        const int bits = h->h_status[0];
-        if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
-        if (attempt == 0) {
-            type_start.assign(h->h_status + 2, h->h_status + 3 + T);
-            if (n == 0) type_start.assign(T + 1, 0);
-        }
-        const int maxc = h->h_status[1];
-        if (maxc <= h->M) break;
-        if (attempt == 2) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour capacity could not be established");
-        grow_pairs(h, n, ((int)std::ceil(maxc * 1.15) + 8 + 7) & ~7);
-        CK(cudaMemsetAsync(h->status.p, 0, sizeof(int), st));
-    }
-    (void)want_types;
-    if (n > 0) {
+        k_neighbors<<<(n + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
+            h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
+            pair_bufs(h), h->status.p, h->status.p + 1);
+        k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
+        k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
+        k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
         const long long tot = (long long)n * h->M;
         k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
-        ++h->launches;
+        h->launches += 7;
     }
-}
-
-void descriptors(nnap_handle* h, int n, const int* d_type, const std::vector<int>& ts, bool fwd) {
-    const int T = h->model.ntypes();
-    (void)T;
-    size_t a_off = 0;
-    for (auto& r : h->runs) {
-        const int s0 = ts[r.t0], s1 = ts[r.t1];
-        for (size_t k = 0; k < r.subs.size(); ++k) {
-            const SubShape& s = r.subs[k];
-            DescArgs a;
+    h->mark(1);
+    if (n > 0) CK(cudaMemsetAsync(h->fp.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
+    // descriptors forward, per run of species sharing a basis shape and per sub-basis
+    auto descriptors = [&](bool fwd) {
+        size_t a_off = 0;
+        for (auto& r : h->runs) {
+            for (size_t k = 0; k < r.subs.size(); ++k) {
+                const SubShape& s = r.subs[k];
+                DescArgs a;
+                a.perm = h->perm.p;
+                a.range = h->type_start.p;
+                a.t0 = r.t0;
+                a.t1 = r.t1;
+                a.nmax = n;
+                a.type = d_type;
+                a.P = pair_bufs(h);
+                a.W = r.W[k].p;
+                a.T = T;
+                a.rcut = (float)s.rcut;
+                a.fp = h->fp.p;
+                a.fp_stride = h->fp_stride;
+                a.fp_off = r.fp_off[k];
+                a.A = nullptr;
+                if (s.kind == KIND_SPHERICAL) {
+                    a.A = h->A.p + a_off;
+                    a_off += (size_t)n * s.np * (s.lmax + 1) * (s.lmax + 1);
+                }
+                a.gfp = h->gfp.p;
+                a.accumulate = k > 0;
+                if (n > 0) {
+                    CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, st));
+                    ++h->launches;
+                }
+            }
+        }
+    };
+    descriptors(true);
+    h->mark(2);
+    if (!fp_only && n > 0) {
+        for (int t = 0; t < T; ++t) {
+            const NetDev& nd = h->nets[t];
+            NetArgs a;
             a.perm = h->perm.p;
-            a.s0 = s0;
-            a.s1 = s1;
-            a.type = d_type;
-            a.P = pair_bufs(h);
-            a.W = r.W[k].p;
-            a.T = h->model.ntypes();
-            a.rcut = (float)s.rcut;
+            a.range = h->type_start.p;
+            a.t = t;
+            a.nmax = n;
             a.fp = h->fp.p;
             a.fp_stride = h->fp_stride;
-            a.fp_off = r.fp_off[k];
-            a.A = nullptr;
-            if (s.kind == KIND_SPHERICAL) {
-                a.A = h->A.p + a_off;
-                a_off += (size_t)(s1 - s0) * s.np * (s.lmax + 1) * (s.lmax + 1);
-            }
+            a.D = nd.D;
+            a.nlayer = nd.nlayer;
+            for (int l = 0; l < 4; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;
+            a.w = nd.w32.p;
+            a.mu_e = nd.mu_e;
+            a.sigma_e = nd.sigma_e;
+            a.e_atom = h->e_atom.p;
             a.gfp = h->gfp.p;
-            a.accumulate = k > 0;
-            if (s1 > s0) {
-                CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, h->stream));
-                ++h->launches;
-            }
+            if (h->precision == NNAP_PREC_MIXED) CK(launch_net_tc(a, nd.tc, h->status.p, h->sm_count, st));
+            else CK(launch_net_fp32(a, st));
+            ++h->launches;
         }
     }
-    (void)n;
-}
-
-size_t a_arena_size(nnap_handle* h, const std::vector<int>& ts) {
-    size_t tot = 0;
-    for (auto& r : h->runs)
-        for (auto& s : r.subs)
-            if (s.kind == KIND_SPHERICAL) tot += (size_t)(ts[r.t1] - ts[r.t0]) * s.np * (s.lmax + 1) * (s.lmax + 1);
-    return tot;
-}
-
-void network(nnap_handle* h, const std::vector<int>& ts) {
-    for (int t = 0; t < h->model.ntypes(); ++t) {
-        const NetDev& nd = h->nets[t];
-        NetArgs a;
-        a.perm = h->perm.p;
-        a.s0 = ts[t];
-        a.s1 = ts[t + 1];
-        if (a.s1 <= a.s0) continue;
-        a.fp = h->fp.p;
-        a.fp_stride = h->fp_stride;
-        a.D = nd.D;
-        a.nlayer = nd.nlayer;
-        for (int l = 0; l < 4; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;
-        a.w = nd.w32.p;
-        a.mu_e = nd.mu_e;
-        a.sigma_e = nd.sigma_e;
-        a.e_atom = h->e_atom.p;
-        a.gfp = h->gfp.p;
-        if (h->precision == NNAP_PREC_MIXED) {
-            CK(launch_net_tc(a, nd.tc, h->status.p, h->sm_count, h->stream));
-        } else {
-            CK(launch_net_fp32(a, h->stream));
-        }
-        ++h->launches;
-    }
-}
-
-// Full evaluation of a batch whose positions/types are already on the device.
-void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
-    const int n = B.natoms;
-    cudaStream_t st = h->stream;
-    std::vector<int> ts;
-    h->mark(0);
-    build_neighbors(h, B, d_x, d_type, ts, true);
-    h->mark(1);
-    h->fp.ensure((size_t)std::max(n, 1) * h->fp_stride);
-    h->gfp.ensure((size_t)std::max(n, 1) * h->fp_stride);
-    h->A.ensure(std::max<size_t>(a_arena_size(h, ts), 1));
-    if (n > 0) CK(cudaMemsetAsync(h->fp.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
-    descriptors(h, n, d_type, ts, true);
-    h->mark(2);
-    if (fp_only) return;
-    h->e_atom.ensure(std::max(n, 1));
-    network(h, ts);
     h->mark(3);
-    descriptors(h, n, d_type, ts, false);
+    if (!fp_only) descriptors(false);
     h->mark(4);
-    h->forces.ensure(3 * (size_t)std::max(n, 1));
-    h->virials.ensure(9 * (size_t)std::max(n, 1));
-    if (n > 0) {
-        k_gather<<<(n + 127) / 128, 128, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
+    if (!fp_only) {
+        if (n > 0) {
+            k_gather<<<(n + 127) / 128, 128, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
+            ++h->launches;
+        }
+        const int nchunks = (int)B.cb.size();
+        if (nchunks) {
+            k_reduce_chunks<<<nchunks, kRedBlock, 0, st>>>(h->chunk_b.p, h->chunk_e.p, h->e_atom.p, h->virials.p,
+                                                            h->partial.p);
+            ++h->launches;
+        }
+        k_reduce_structs<<<(B.nstruct * 32 + 127) / 128, 128, 0, st>>>(h->struct_chunks.p, B.nstruct, h->partial.p,
+                                                                        h->energy.p, h->virial.p);
         ++h->launches;
     }
-    const int nchunks = (int)B.cb.size();
-    h->chunk_b.ensure(std::max(nchunks, 1));
-    h->chunk_e.ensure(std::max(nchunks, 1));
-    h->struct_chunks.ensure(B.nstruct + 1);
-    h->partial.ensure(10 * (size_t)std::max(nchunks, 1));
-    h->energy.ensure(std::max(B.nstruct, 1));
-    h->virial.ensure(9 * (size_t)std::max(B.nstruct, 1));
-    if (nchunks) {
-        CK(cudaMemcpyAsync(h->chunk_b.p, B.cb.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(h->chunk_e.p, B.ce.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
-        k_reduce_chunks<<<nchunks, kRedBlock, 0, st>>>(h->chunk_b.p, h->chunk_e.p, h->e_atom.p, h->virials.p,
-                                                        h->partial.p);
-        ++h->launches;
-    }
-    CK(cudaMemcpyAsync(h->struct_chunks.p, B.sc.data(), sizeof(int) * (B.nstruct + 1), cudaMemcpyHostToDevice, st));
-    k_reduce_structs<<<(B.nstruct * 32 + 127) / 128, 128, 0, st>>>(h->struct_chunks.p, B.nstruct, h->partial.p,
-                                                               h->energy.p, h->virial.p);
-    ++h->launches;
     h->mark(5);
     CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
 }
 
-void check_after(nnap_handle* h) {
-    CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    if (h->h_status[0] & ERRBIT_TIMEOUT) throw ApiFail(NNAP_ERR_TIMEOUT, "a bounded tensor-core wait gave up");
-    if (h->h_status[0] & ERRBIT_NO_MIRROR) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
-    if (h->h_status[0] & ERRBIT_CAPACITY) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour capacity exceeded");
+// Identity of a launch sequence: what the captured graph depends on.
+std::vector<long long> layout_key(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+    std::vector<long long> k = {B.nstruct, B.natoms, B.ncells, h->M, (long long)(intptr_t)d_x,
+                                (long long)(intptr_t)d_type, fp_only ? 1 : 0, h->profiling ? 1 : 0};
+    for (auto& s : B.sd) {
+        k.push_back(s.n);
+        k.push_back(s.kind);
+        for (int d = 0; d < 3; ++d) { k.push_back(s.nc[d]); k.push_back(s.R[d]); }
+    }
+    return k;
+}
+
+void drop_graph(nnap_handle* h) {
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+    h->gkey.clear();
+}
+
+// Evaluate a planned batch whose inputs are on the device.  The first call of a layout
+// runs eagerly and validates the neighbour capacity; the second captures the launch
+// sequence into a CUDA graph; later calls replay it.  Synchronises before returning.
+void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+    const bool same_layout = h->layout_ok && h->last_layout == layout_key(h, B, nullptr, nullptr, fp_only);
+    if (!same_layout) {
+        drop_graph(h);
+        prepare_layout(h, B);
+        h->layout_ok = true;
+        h->last_layout = layout_key(h, B, nullptr, nullptr, fp_only);
+        h->layout_runs = 0;
+    }
+    std::memcpy(h->h_sdev, B.sd.data(), sizeof(StructDev) * B.nstruct);
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        const std::vector<long long> key = layout_key(h, B, d_x, d_type, fp_only);
+        if (h->gexec && h->gkey == key) {
+            CK(cudaGraphLaunch(h->gexec, h->stream));
+        } else if (h->use_graphs && h->layout_runs >= 1) {
+            drop_graph(h);
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue(h, B, d_x, d_type, fp_only);
+            } catch (...) {
+                cudaStreamEndCapture(h->stream, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            CK(cudaStreamEndCapture(h->stream, &g));
+            cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
+            cudaGraphDestroy(g);
+            CK(e);
+            h->gkey = key;
+            CK(cudaGraphLaunch(h->gexec, h->stream));
+        } else {
+            enqueue(h, B, d_x, d_type, fp_only);
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        ++h->layout_runs;
+        const int bits = h->h_status[0];
+        if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
+        if (bits & ERRBIT_TIMEOUT) throw ApiFail(NNAP_ERR_TIMEOUT, "a bounded tensor-core wait gave up");
+        const int maxc = h->h_status[1];
+        if (maxc <= h->M) {
+            if (bits & ERRBIT_NO_MIRROR) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
+            return;
+        }
+        // neighbour rows overflowed: grow the capacity and evaluate again
+        drop_graph(h);
+        grow_pairs(h, B.natoms, ((int)std::ceil(maxc * 1.15) + 8 + 7) & ~7);
+        h->last_layout = layout_key(h, B, nullptr, nullptr, fp_only);
+        h->layout_runs = 0;
+    }
+    throw ApiFail(NNAP_ERR_CAPACITY, "neighbour capacity could not be established");
 }
 
 void copy_out(nnap_handle* h, const Batch& B, int flags, const Outputs& o, cudaMemcpyKind kind) {
@@ -677,6 +733,8 @@ int nnap_destroy(nnap_handle* h) {
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release();
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     if (h->order_ev) cudaEventDestroy(h->order_ev);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->h_sdev) cudaFreeHost(h->h_sdev);
     if (h->h_status) cudaFreeHost(h->h_status);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -759,7 +817,7 @@ int nnap_compute_batch(nnap_handle* h, int nstruct, const int* natoms, const dou
         upload_inputs(h, B.natoms, x, type);
         evaluate(h, B, h->x.p, h->type.p, false);
         copy_out(h, B, flags, o, cudaMemcpyDeviceToHost);
-        check_after(h);
+        CK(cudaStreamSynchronize(h->stream));
         return NNAP_OK;
     });
 }
@@ -771,7 +829,6 @@ int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int
         if (!box) throw ApiFail(NNAP_ERR_ARG, "box is NULL");
         Outputs o{d_energy, d_energies, d_forces, d_virial, d_virials};
         check_outputs(flags, o);
-        h->launches = 0;
         Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
         if (natoms && (!d_x || !d_type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         // NULL is CUDA's default stream; the handle's stream is ordered after the caller's
@@ -784,6 +841,36 @@ int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int
         copy_out(h, B, flags, o, cudaMemcpyDeviceToDevice);
         CK(cudaEventRecord(h->order_ev, h->stream));
         CK(cudaStreamWaitEvent(user, h->order_ev, 0));
+        return NNAP_OK;
+    });
+}
+
+int nnap_compute_batch_device(nnap_handle* h, int nstruct, const int* natoms, const double* d_x, const int* d_type,
+                              const int* box_kind, const double* boxes, int flags, double* d_energy,
+                              double* d_energies, double* d_forces, double* d_virial, double* d_virials,
+                              void* stream) {
+    return guarded(h, [&]() -> int {
+        if (nstruct < 1 || !natoms || !box_kind || !boxes) throw ApiFail(NNAP_ERR_ARG, "invalid batch description");
+        Outputs o{d_energy, d_energies, d_forces, d_virial, d_virials};
+        check_outputs(flags, o);
+        Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
+        if (B.natoms && (!d_x || !d_type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
+        cudaStream_t user = (cudaStream_t)stream;
+        if (!h->order_ev) CK(cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming));
+        CK(cudaEventRecord(h->order_ev, user));
+        CK(cudaStreamWaitEvent(h->stream, h->order_ev, 0));
+        evaluate(h, B, d_x, d_type, false);
+        copy_out(h, B, flags, o, cudaMemcpyDeviceToDevice);
+        CK(cudaEventRecord(h->order_ev, h->stream));
+        CK(cudaStreamWaitEvent(user, h->order_ev, 0));
+        return NNAP_OK;
+    });
+}
+
+int nnap_set_graphs(nnap_handle* h, int on) {
+    return guarded(h, [&]() -> int {
+        h->use_graphs = on != 0;
+        if (!h->use_graphs) drop_graph(h);
         return NNAP_OK;
     });
 }
@@ -806,7 +893,7 @@ int nnap_compute_fp(nnap_handle* h, int natoms, const double* x, const int* type
             CK(cudaMemcpyAsync(f.data(), h->fp.p, sizeof(float) * f.size(), cudaMemcpyDeviceToHost, h->stream));
             CK(cudaMemcpyAsync(perm.data(), h->perm.p, sizeof(int) * natoms, cudaMemcpyDeviceToHost, h->stream));
         }
-        check_after(h);
+        CK(cudaStreamSynchronize(h->stream));
         for (int s = 0; s < natoms; ++s) {
             const int a = perm[s];
             const int D = h->model.sp[type[a] - 1].D;
@@ -824,8 +911,7 @@ int nnap_neighbor_list(nnap_handle* h, int natoms, const double* x, const int* t
         Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
         if (natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, natoms, x, type);
-        std::vector<int> ts;
-        build_neighbors(h, B, h->x.p, h->type.p, ts, false);
+        evaluate(h, B, h->x.p, h->type.p, true);
         std::vector<int> cnt(natoms);
         std::vector<uint64_t> keys((size_t)natoms * h->M);
         if (natoms) {
@@ -833,7 +919,7 @@ int nnap_neighbor_list(nnap_handle* h, int natoms, const double* x, const int* t
             CK(cudaMemcpyAsync(keys.data(), h->pkey.p, sizeof(uint64_t) * keys.size(), cudaMemcpyDeviceToHost,
                                h->stream));
         }
-        check_after(h);
+        CK(cudaStreamSynchronize(h->stream));
         long long t = 0;
         for (int i = 0; i < natoms; ++i) {
             counts[i] = cnt[i];

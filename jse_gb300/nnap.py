@@ -38,7 +38,7 @@ WANT_ENERGY, WANT_ENERGIES, WANT_FORCES, WANT_VIRIAL, WANT_VIRIALS = 1, 2, 4, 8,
 EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes", "nnap_rcut_max", "nnap_symbol",
            "nnap_descriptor_size", "nnap_last_error", "nnap_compute", "nnap_compute_device", "nnap_compute_batch",
            "nnap_compute_fp", "nnap_neighbor_list", "nnap_last_launch_count", "nnap_set_profiling",
-           "nnap_stage_times"]
+           "nnap_stage_times", "nnap_compute_batch_device", "nnap_set_graphs"]
 
 
 class IllegalStateError(RuntimeError):
@@ -81,6 +81,8 @@ def load_library(path: str = LIB_PATH):
     L.nnap_last_launch_count.argtypes = [P, ip]
     L.nnap_set_profiling.argtypes = [P, I]
     L.nnap_stage_times.argtypes = [P, dp]
+    L.nnap_compute_batch_device.argtypes = [P, I, ip, P, P, ip, dp, I, P, P, P, P, P, P]
+    L.nnap_set_graphs.argtypes = [P, I]
     _lib = L
     return L
 
@@ -182,6 +184,10 @@ class NNAP:
         v = C.c_int()
         self._check(self._L.nnap_last_launch_count(self._handle(), C.byref(v)))
         return v.value
+
+    def setGraphs(self, on: bool):
+        """CUDA-graph replay of repeated evaluations of the same layout (on by default)."""
+        self._check(self._L.nnap_set_graphs(self._handle(), 1 if on else 0))
 
     def setProfiling(self, on: bool):
         self._check(self._L.nnap_set_profiling(self._handle(), 1 if on else 0))
@@ -301,6 +307,18 @@ class NNAP:
             out.append(r)
             a0 += n
         return out
+
+    def computeBatchDevice(self, natoms, x_ptr: int, type_ptr: int, box_kinds, boxes, flags: int,
+                           energy_ptr: int = 0, energies_ptr: int = 0, forces_ptr: int = 0, virial_ptr: int = 0,
+                           virials_ptr: int = 0, stream: int = 0):
+        """Batched device-resident evaluation; natoms/box_kinds/boxes are host sequences."""
+        nat = np.ascontiguousarray(natoms, dtype=np.int32)
+        kd = np.ascontiguousarray(box_kinds, dtype=np.int32)
+        bx = np.ascontiguousarray(boxes, dtype=np.float64).reshape(-1)
+        self._check(self._L.nnap_compute_batch_device(self._handle(), len(nat), _iptr(nat), x_ptr, type_ptr,
+                                                      _iptr(kd), _dptr(bx), flags, energy_ptr or None,
+                                                      energies_ptr or None, forces_ptr or None, virial_ptr or None,
+                                                      virials_ptr or None, stream or None))
 
     def computeDevice(self, n: int, x_ptr: int, type_ptr: int, box, box_kind: int, flags: int, energy_ptr: int = 0,
                       energies_ptr: int = 0, forces_ptr: int = 0, virial_ptr: int = 0, virials_ptr: int = 0,

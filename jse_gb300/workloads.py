@@ -53,88 +53,40 @@ def _lmp_box(L: float, tilt: float) -> np.ndarray:
     return np.array([[L, 0.0, 0.0], [tilt * L, L, 0.0], [tilt * L, tilt * L, L]])
 
 
-def _rsa_fractional(n: int, box: np.ndarray, rmin: float, rng: np.random.Generator, max_rounds: int = 4000):
-    """Random sequential addition of ``n`` points with pair distance >= rmin under PBC.
+_RSA = None
 
-    Works on a grid in fractional coordinates whose cells are small enough that no two
-    accepted points can share a cell; each round proposes a batch of candidates, drops
-    those closer than ``rmin`` to an accepted point or to an earlier candidate of the same
-    batch, and accepts the rest.
-    """
-    A = box
-    inv = np.linalg.inv(A)  # fractional = cart @ inv
-    vol = abs(np.linalg.det(A))
-    h = np.array([vol / np.linalg.norm(np.cross(A[1], A[2])), vol / np.linalg.norm(np.cross(A[2], A[0])),
-                  vol / np.linalg.norm(np.cross(A[0], A[1]))])
-    nc = np.maximum(1, np.floor(np.linalg.norm(A, axis=1) * math.sqrt(3.0) * 1.15 / rmin)).astype(np.int64)
 
-    def diag_ok(ncv):
-        cell = A / ncv[:, None]
-        diags = [cell[0] + cell[1] + cell[2], cell[0] + cell[1] - cell[2], cell[0] - cell[1] + cell[2],
-                 -cell[0] + cell[1] + cell[2]]
-        return max(np.linalg.norm(d) for d in diags) < rmin * 0.999
+def _rsa_lib():
+    """The C generator (jse_gb300/csrc/rsa.c), compiled on first use."""
+    global _RSA
+    if _RSA is None:
+        import ctypes as C
+        import os
+        import subprocess
+        here = os.path.dirname(os.path.abspath(__file__))
+        src = os.path.join(here, "csrc", "rsa.c")
+        lib = os.path.join(here, "librsa.so")
+        if not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(src):
+            subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", src, "-o", lib, "-lm"], check=True)
+        L = C.CDLL(lib)
+        L.rsa_generate.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double, C.c_uint64, C.c_int,
+                                   C.POINTER(C.c_double)]
+        L.rsa_generate.restype = C.c_int
+        _RSA = L
+    return _RSA
 
-    while not diag_ok(nc):
-        nc = nc + 1
-    R = np.ceil(rmin * nc / h).astype(np.int64)
-    offs = np.stack(np.meshgrid(*[np.arange(-r, r + 1) for r in R], indexing="ij"), -1).reshape(-1, 3)
-    grid = -np.ones(int(nc.prod()), dtype=np.int64)
-    pos = np.zeros((n, 3))
-    frac = np.zeros((n, 3))
-    count = 0
-    rmin2 = rmin * rmin
 
-    def cell_index(c):
-        return c[..., 0] + nc[0] * (c[..., 1] + nc[1] * c[..., 2])
-
-    for _ in range(max_rounds):
-        if count >= n:
-            break
-        need = n - count
-        B = int(min(max(2 * need, 64), 8192))
-        s = rng.random((B, 3))
-        c = np.minimum((s * nc).astype(np.int64), nc - 1)
-        q = c[:, None, :] + offs[None, :, :]                       # (B, M, 3) neighbour cells
-        img = np.floor_divide(q, nc)
-        qc = q - img * nc
-        occ = grid[cell_index(qc)]                                 # (B, M)
-        has = occ >= 0
-        ok = np.ones(B, dtype=bool)
-        if has.any():
-            bi, mi = np.nonzero(has)
-            other = frac[occ[bi, mi]] + img[bi, mi]
-            d = (other - s[bi]) @ A
-            close = (d * d).sum(-1) < rmin2
-            ok[bi[close]] = False
-        # conflicts inside the batch: keep the earliest candidate per cell, then test neighbours
-        cand = np.nonzero(ok)[0]
-        if cand.size:
-            cid = cell_index(c[cand])
-            first = np.full(grid.size, np.iinfo(np.int64).max)
-            np.minimum.at(first, cid, cand)
-            keep = first[cid] == cand
-            cand = cand[keep]
-            ok[:] = False
-            ok[cand] = True
-            tmp = -np.ones(grid.size, dtype=np.int64)
-            tmp[cell_index(c[cand])] = cand
-            occ2 = tmp[cell_index(qc[cand])]                       # (C, M)
-            earlier = (occ2 >= 0) & (occ2 < cand[:, None])
-            if earlier.any():
-                ci, mi = np.nonzero(earlier)
-                other = s[occ2[ci, mi]] + img[cand[ci], mi]
-                d = (other - s[cand[ci]]) @ A
-                close = (d * d).sum(-1) < rmin2
-                ok[cand[ci[close]]] = False
-        acc = np.nonzero(ok)[0][:need]
-        k = acc.size
-        frac[count:count + k] = s[acc]
-        grid[cell_index(c[acc])] = np.arange(count, count + k)
-        count += k
-    if count < n:
-        raise RuntimeError("random sequential addition stalled at %d of %d points" % (count, n))
-    pos = frac @ A
-    return pos
+def _rsa(n: int, box: np.ndarray, rmin: float, seed: int) -> np.ndarray:
+    """Random sequential addition of ``n`` points with pair distance >= rmin under PBC."""
+    import ctypes as C
+    L = _rsa_lib()
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    out = np.zeros((max(n, 1), 3))
+    got = L.rsa_generate(n, b.ctypes.data_as(C.POINTER(C.c_double)), float(rmin), int(seed) & ((1 << 64) - 1),
+                         100000, out.ctypes.data_as(C.POINTER(C.c_double)))
+    if got != n:
+        raise RuntimeError("random sequential addition stalled at %d of %d points" % (got, n))
+    return out[:n]
 
 
 def random_liquid(n: int, density: float, fractions: Sequence[float], rmin: float, seed: int,
@@ -146,7 +98,7 @@ def random_liquid(n: int, density: float, fractions: Sequence[float], rmin: floa
         box, kind = np.diag([L, L, L]), BOX_ORTHO
     else:
         box, kind = _lmp_box(L, tilt), BOX_LMP
-    x = _rsa_fractional(n, box, rmin, rng)
+    x = _rsa(n, box, rmin, int(rng.integers(0, 2 ** 63)))
     counts = [int(round(f * n)) for f in fractions]
     counts[0] += n - sum(counts)
     types = np.concatenate([np.full(c, t + 1, dtype=np.int32) for t, c in enumerate(counts)])
