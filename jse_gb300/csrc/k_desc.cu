@@ -533,16 +533,19 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     const int grid = (n + kDescWarps - 1) / kDescWarps;
     const size_t wbytes = sizeof(float) * (((size_t)a.T * a.T * NP * N1 + 3) & ~(size_t)3);
     const size_t sm = wbytes + sizeof(float) * kDescWarps * (fwd ? S::FWD_WARP_FLOATS : S::BWD_WARP_FLOATS);
-    cudaError_t e;
-    if (fwd) {
-        e = cudaFuncSetAttribute(k_sph_fwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    // the shared-memory limit is raised once per kernel (before any graph capture: the
+    // first evaluation of a layout always runs eagerly)
+    static int limit_fwd = 0, limit_bwd = 0;
+    int& lim = fwd ? limit_fwd : limit_bwd;
+    if ((int)sm > lim) {
+        const cudaError_t e =
+            fwd ? cudaFuncSetAttribute(k_sph_fwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                : cudaFuncSetAttribute(k_sph_bwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
-        k_sph_fwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(k_sph_bwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        k_sph_bwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+        lim = (int)sm;
     }
+    if (fwd) k_sph_fwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    else k_sph_bwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
     return cudaGetLastError();
 }
 

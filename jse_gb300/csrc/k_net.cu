@@ -147,8 +147,12 @@ cudaError_t launch_net_fp32(const NetArgs& a, cudaStream_t st) {
     for (int l = 0; l < a.nlayer; ++l) Hmax = Hmax > a.H[l] ? Hmax : a.H[l];
     const int warp_floats = (2 + a.nlayer) * Hmax * kNetAtoms;
     const size_t sm = sizeof(float) * (size_t)warp_floats * kNetWarps;
-    cudaError_t e = cudaFuncSetAttribute(k_net_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
+    static int limit = 0;
+    if ((int)sm > limit) {
+        const cudaError_t e = cudaFuncSetAttribute(k_net_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        limit = (int)sm;
+    }
     const int per_block = kNetAtoms * kNetWarps;
     k_net_fp32<<<(n + per_block - 1) / per_block, 32 * kNetWarps, sm, st>>>(a, warp_floats);
     return cudaGetLastError();

@@ -458,8 +458,12 @@ cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_co
     const int xbytes = align1k(2 * 2 * 128 * (L.Dp > L.H1 ? L.Dp : L.H1));
     const int abytes = align1k(2 * 2 * 128 * (L.H1 > L.H2 ? L.H1 : L.H2));
     const size_t sm = (size_t)L.bytes + xbytes + abytes;
-    cudaError_t e = cudaFuncSetAttribute(k_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
+    static int limit = 0;
+    if ((int)sm > limit) {
+        const cudaError_t e = cudaFuncSetAttribute(k_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        limit = (int)sm;
+    }
     TcParams p;
     p.perm = a.perm;
     p.range = a.range;
