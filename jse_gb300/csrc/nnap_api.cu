@@ -154,8 +154,11 @@ struct nnap_handle {
     size_t h_sdev_cap = 0;
     int sm_count = 148;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool capturing = false;
     void mark(int k) {
-        if (profiling) CK(cudaEventRecord(ev[k], stream));
+        // inside stream capture an ordinary record is only a dependency marker; an external
+        // event node records the event when the graph runs
+        if (profiling) CK(cudaEventRecordWithFlags(ev[k], stream, capturing ? cudaEventRecordExternal : 0));
     }
 };
 
@@ -177,6 +180,7 @@ int guarded(nnap_handle* h, F&& f) {
     } catch (const ApiFail& e) {
         return fail(h, e.status, e.what());
     } catch (const CudaFail& e) {
+        cudaGetLastError();  // leave no error behind for the caller's next CUDA call
         return fail(h, NNAP_ERR_CUDA, e.what());
     } catch (const std::bad_alloc&) {
         return fail(h, NNAP_ERR_CAPACITY, "host allocation failed");
@@ -600,13 +604,17 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
             drop_graph(h);
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            h->capturing = true;
             try {
                 enqueue(h, B, d_x, d_type, fp_only);
             } catch (...) {
+                h->capturing = false;
                 cudaStreamEndCapture(h->stream, &g);
                 if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
                 throw;
             }
+            h->capturing = false;
             CK(cudaStreamEndCapture(h->stream, &g));
             cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
             cudaGraphDestroy(g);
