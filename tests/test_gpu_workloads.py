@@ -94,3 +94,21 @@ def test_batch_equals_single(precision):
             assert np.array_equal(o["virials"], b["virials"])
             np.testing.assert_allclose(o["energy"], b["energy"], rtol=1e-13)
             np.testing.assert_allclose(o["virial"], b["virial"], rtol=1e-12, atol=1e-12)
+
+
+def test_graph_replay_across_layout_changes():
+    """Alternating layouts on one handle: each call re-plans or replays the captured
+    launch sequence; results equal those of a fresh handle."""
+    from jse_gb300.nnap import NNAP
+    a = W.random_liquid(300, 0.06, [0.46, 0.46, 0.08], 2.0, 41)
+    b = W.random_liquid(500, 0.06, [0.46, 0.46, 0.08], 2.0, 42, tilt=0.1)
+    model = W.model_for("c2")
+    with NNAP(model, precision="mixed") as p:
+        ra = p.calEnergyForceVirials(a)
+        rb = p.calEnergyForceVirials(b)
+    with NNAP(model, precision="mixed") as p:
+        for _ in range(3):
+            for s, r in ((a, ra), (a, ra), (b, rb), (b, rb), (b, rb)):
+                o = p.calEnergyForceVirials(s)
+                assert np.array_equal(o["forces"], r["forces"])
+                assert o["energy"] == r["energy"]
