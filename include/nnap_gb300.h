@@ -149,6 +149,21 @@ int nnap_set_profiling(nnap_handle* h, int on);
 int nnap_set_graphs(nnap_handle* h, int on);
 int nnap_stage_times(nnap_handle* h, double* ms5);
 
+/* Per-atom neighbour counts of one structure without allocating any memory.  This entry
+ * point has no counterpart in the reference.  It is for callers that cannot call
+ * cudaMalloc when they need the answer: a program capturing a CUDA graph in global
+ * capture mode, or an engine that pre-reserves all device memory and forbids later
+ * allocations.  No handle is needed; rcut is the cutoff.  d_x (3n doubles), d_type
+ * (n ints) and d_counts (n ints) are device pointers; box is a host array.
+ * Its scratch is one fixed 2 MiB device array compiled into the library (held by every
+ * GPU that loads it): at most 16384 atoms and 16384 cells, larger inputs return
+ * NNAP_ERR_CAPACITY.  The first call on each device looks up that array's address and
+ * should come before any stream capture.  All calls share the array, so calls whose
+ * work overlaps on the GPU race.  Work is queued on `stream` (NULL: CUDA's default
+ * stream) and the call waits for it. */
+int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const int* d_type, int box_kind, const double* box,
+                                 double rcut, int* d_counts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
