@@ -49,7 +49,8 @@ typedef enum {
     NNAP_ERR_UNSUPPORTED = 5,  /* model shape without a compiled kernel               */
     NNAP_ERR_ARG = 6,          /* invalid argument (null pointer, bad size, bad box)  */
     NNAP_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up                  */
-    NNAP_ERR_DEAD = 8          /* handle already destroyed                            */
+    NNAP_ERR_DEAD = 8,         /* handle already destroyed                            */
+    NNAP_ERR_BUSY = 9          /* server budget or slots in use; retry after a release */
 } nnap_status;
 
 /* Precision modes.  NNAP_PREC_FP32 is the plain drop-in (FP32 descriptors and FP32
@@ -163,6 +164,41 @@ int nnap_stage_times(nnap_handle* h, double* ms5);
  * stream) and the call waits for it. */
 int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const int* d_type, int box_kind, const double* box,
                                  double rcut, int* d_counts, void* stream);
+
+/* ---------------------------------------------------------------- serving
+ * Resident structures evaluated by continuous batching (no counterpart in the
+ * reference, which evaluates one structure per call and rebuilds its neighbour list
+ * each time).  A server owns one handle until nnap_server_destroy: make no other call
+ * on that handle meanwhile, and destroy the server before the handle.
+ *
+ * nnap_server_admit makes a structure resident (its species, box and neighbour rows at
+ * rcut + skin stay on the device) and returns its slot.  nnap_server_step evaluates any
+ * set of slots together in one batched launch sequence; slots admitted since the last
+ * step join it, released ones leave it.  A slot's neighbour rows are rebuilt when it is
+ * new or when one of its atoms moved more than skin/2 (in the caller's coordinates)
+ * since its last rebuild; otherwise the stored rows are filtered at rcut, which gives
+ * exactly the full search's neighbour set.  Admission is refused with NNAP_ERR_BUSY
+ * while memory_budget bytes (the resident arrays plus the work buffers of a step over
+ * every resident atom) or max_structs slots (0: 4096) are in use, and with
+ * NNAP_ERR_CAPACITY for a structure that would not fit an empty server. */
+typedef struct nnap_server nnap_server;
+int nnap_server_create(nnap_handle* h, double skin, size_t memory_budget, int max_structs, nnap_server** out);
+int nnap_server_destroy(nnap_server* s);
+/* Admit one structure: natoms atoms, species type[natoms], box as in nnap_compute. */
+int nnap_server_admit(nnap_server* s, int natoms, const int* type, int box_kind, const double* box, int* slot);
+int nnap_server_release(nnap_server* s, int slot);
+/* Evaluate the listed slots (each at most once) at positions x, the slots' atoms
+ * concatenated in the order of `slots`.  Outputs as nnap_compute_batch, in the same
+ * order (energy[q], virial[9*q] per listed slot).  Host buffers, synchronous. */
+int nnap_server_step(nnap_server* s, int nslots, const int* slots, const double* x, int flags, double* energy,
+                     double* energies, double* forces, double* virial, double* virials);
+/* Neighbour list that the last step used for `slot` (layout of nnap_neighbor_list;
+ * neighbour indices local to the slot). */
+int nnap_server_neighbor_list(nnap_server* s, int slot, int* counts, long long cap, int* j, int* img,
+                              long long* total);
+/* out8: resident slots, resident atoms, resident bytes, work bytes, steps, slot
+ * rebuilds, neighbour-row capacity, memory budget. */
+int nnap_server_stats(const nnap_server* s, long long* out8);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,209 @@
+// Host-side internals shared by the C ABI translation units: error types, device
+// arrays, the handle (model upload, work buffers, launch-sequence cache) and the
+// stages of the evaluation pipeline.  Not part of the public interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/nnap_gb300.h"
+#include "common.cuh"
+#include "desc.cuh"
+#include "model.hpp"
+#include "net_tc.cuh"
+
+namespace nnapgb {
+
+// k_struct.cu
+__global__ void k_wrap_bin(const StructDev*, const int*, const double*, const int*, int, int, double*, float4*,
+                           float4*, int*, int*, int*);
+__global__ void k_scan_excl(const int*, int, int*);
+__global__ void k_fill_cells(const int*, int, const int*, int*, int*);
+__global__ void k_sort_cells(const int*, int, int*);
+__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const int*,
+                            const int*, const int*, int, PairBufs, int*, int*);
+__global__ void k_mirror(const StructDev*, const int*, PairBufs, int, int*);
+__global__ void k_type_hist(const int*, int, int, int*);
+__global__ void k_type_offsets(int*, int, int, int*);
+__global__ void k_type_scatter(const int*, int, int, const int*, int*);
+__global__ void k_gather(PairBufs, int, double*, double*);
+__global__ void k_reduce_chunks(const int*, const int*, const double*, const double*, double*);
+__global__ void k_reduce_structs(const int*, int, const double*, double*, double*);
+
+constexpr int kNbWarps = 4;       // must match k_struct.cu
+constexpr int kSortBlock = 256;   // must match k_struct.cu
+constexpr int kRedBlock = 256;    // must match k_struct.cu
+constexpr int kRedChunk = 1024;   // atoms per reduction chunk
+
+struct CudaFail : std::runtime_error {
+    cudaError_t code;
+    CudaFail(cudaError_t c, const char* what)
+        : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c) {}
+};
+struct ApiFail : std::runtime_error {
+    int status;
+    ApiFail(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+#define CK(call)                                            \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) throw ::nnapgb::CudaFail(e_, #call);   \
+    } while (0)
+
+// Grow-only device array.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    void ensure(size_t n) {
+        if (n <= cap) return;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n, 1);
+        CK(cudaMalloc(&p, want * sizeof(T)));
+        cap = want;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct SubShape {
+    int kind, lmax, np, n1;
+    double rcut;
+    bool operator==(const SubShape& o) const {
+        return kind == o.kind && lmax == o.lmax && np == o.np && n1 == o.n1 && rcut == o.rcut;
+    }
+};
+
+// Species t0..t1-1 sharing the sub-basis shapes (and descriptor length).
+struct Run {
+    int t0, t1;
+    std::vector<SubShape> subs;
+    std::vector<int> fp_off;
+    std::vector<DevBuf<float>> W;  // per sub: [T][T][NP][N1]
+};
+
+struct NetDev {
+    int D, nlayer;
+    int H[4];
+    DevBuf<float> w32;
+    double mu_e, sigma_e;
+    NetTC tc;  // tensor-core parameters (mixed precision)
+};
+
+// One planned evaluation: the structures, the structure of every atom and the
+// reduction chunks (chunk c covers atoms [cb[c], ce[c]); structure s owns chunks
+// [sc[s], sc[s+1])).
+struct Batch {
+    int nstruct = 0, natoms = 0, ncells = 0;
+    std::vector<StructDev> sd;
+    std::vector<int> sid, cb, ce, sc;
+};
+
+struct Outputs {
+    double *energy = nullptr, *energies = nullptr, *forces = nullptr, *virial = nullptr, *virials = nullptr;
+};
+
+}  // namespace nnapgb
+
+struct nnap_handle {
+    nnapgb::Model model;
+    int precision = NNAP_PREC_FP32;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool dead = false;
+    int launches = 0;
+    int fp_stride = 0;
+    std::vector<nnapgb::Run> runs;
+    std::vector<nnapgb::NetDev> nets;
+    // work buffers
+    nnapgb::DevBuf<double> x, xw, e_atom, forces, virials, energy, virial, partial;
+    nnapgb::DevBuf<int> type, sid, cell_of, cell_count, cell_fill, cell_start, cell_atoms, perm, block_counts,
+        type_start;
+    nnapgb::DevBuf<int> chunk_b, chunk_e, struct_chunks, status;
+    nnapgb::DevBuf<float4> xf, xlo;
+    nnapgb::DevBuf<uint16_t> pgrp;
+    nnapgb::DevBuf<nnapgb::StructDev> sdev;
+    nnapgb::DevBuf<uint64_t> pkey;
+    nnapgb::DevBuf<float4> pdx, pg;
+    nnapgb::DevBuf<int> prev, pcount;
+    nnapgb::DevBuf<float> fp, gfp, A;
+    int M = 0;
+    int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
+    bool profiling = false;
+    cudaEvent_t order_ev = nullptr;
+    // launch-sequence cache (CUDA graph) and the layout it was sized for
+    bool use_graphs = true;
+    bool layout_ok = false;
+    int layout_runs = 0;
+    std::vector<long long> last_layout, gkey;
+    cudaGraphExec_t gexec = nullptr;
+    nnapgb::StructDev* h_sdev = nullptr;  // pinned staging of the structure descriptors
+    size_t h_sdev_cap = 0;
+    int sm_count = 148;
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool capturing = false;
+    void mark(int k) {
+        // inside stream capture an ordinary record is only a dependency marker; an external
+        // event node records the event when the graph runs
+        if (profiling) CK(cudaEventRecordWithFlags(ev[k], stream, capturing ? cudaEventRecordExternal : 0));
+    }
+};
+
+namespace nnapgb {
+
+int fail(nnap_handle* h, int status, const std::string& m);
+
+// Run f() with the handle's device current and turn exceptions into status codes.
+template <class F>
+int guarded(nnap_handle* h, F&& f) {
+    if (!h) return NNAP_ERR_ARG;
+    if (h->dead) return fail(h, NNAP_ERR_DEAD, "this NNAP is dead");
+    h->err.clear();
+    try {
+        CK(cudaSetDevice(h->device));
+        return f();
+    } catch (const ApiFail& e) {
+        return fail(h, e.status, e.what());
+    } catch (const CudaFail& e) {
+        cudaGetLastError();  // leave no error behind for the caller's next CUDA call
+        return fail(h, NNAP_ERR_CUDA, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(h, NNAP_ERR_CAPACITY, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(h, NNAP_ERR_ARG, e.what());
+    }
+}
+
+// Structure descriptor for cutoff rc: box rows, cell grid, float screen bound.
+StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0);
+// Float screen bound for cutoff rc when image shifts reach Rm cells.
+float screen_bound(const StructDev& s, double rc, int Rm);
+// Neighbour capacity per atom for the densest structure of a batch at cutoff rc.
+int initial_capacity(const Batch& B, double rc);
+// Set the row capacity and size the pair buffers for n atoms.
+void grow_pairs(nnap_handle* h, int n, int M);
+PairBufs pair_bufs(nnap_handle* h);
+// Size every per-atom work buffer for n atoms, nstruct structures, ncells cells and
+// nchunks reduction chunks (no copies, no synchronisation).
+void ensure_work(nnap_handle* h, int n, int nstruct, int ncells, int nchunks);
+// Queue the species sort of the batch's atoms and the mirror index of the pair rows.
+void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type);
+// Queue descriptors, networks, descriptor gradients, the gather and the reductions.
+void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only);
+void check_outputs(int flags, const Outputs& o);
+// Forget the captured launch sequence of the handle.
+void drop_graph(nnap_handle* h);
+
+}  // namespace nnapgb

@@ -18,175 +18,18 @@
 #include <fstream>
 #include <memory>
 #include <sstream>
-#include <stdexcept>
 #include <string>
 #include <vector>
 
-#include "../../include/nnap_gb300.h"
-#include "common.cuh"
-#include "desc.cuh"
-#include "model.hpp"
-#include "net_tc.cuh"
+#include "api_internal.hpp"
 
 using namespace nnapgb;
 
 namespace nnapgb {
-// k_struct.cu
-__global__ void k_wrap_bin(const StructDev*, const int*, const double*, const int*, int, int, double*, float4*,
-                           float4*, int*, int*, int*);
-__global__ void k_scan_excl(const int*, int, int*);
-__global__ void k_fill_cells(const int*, int, const int*, int*, int*);
-__global__ void k_sort_cells(const int*, int, int*);
-__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const int*,
-                            const int*, const int*, int, PairBufs, int*, int*);
-__global__ void k_mirror(const StructDev*, const int*, PairBufs, int, int*);
-__global__ void k_type_hist(const int*, int, int, int*);
-__global__ void k_type_offsets(int*, int, int, int*);
-__global__ void k_type_scatter(const int*, int, int, const int*, int*);
-__global__ void k_gather(PairBufs, int, double*, double*);
-__global__ void k_reduce_chunks(const int*, const int*, const double*, const double*, double*);
-__global__ void k_reduce_structs(const int*, int, const double*, double*, double*);
-}  // namespace nnapgb
-
-namespace {
-
-constexpr int kNbWarps = 4;       // must match k_struct.cu
-constexpr int kSortBlock = 256;   // must match k_struct.cu
-constexpr int kRedBlock = 256;    // must match k_struct.cu
-constexpr int kRedChunk = 1024;   // atoms per reduction chunk
-
-struct CudaFail : std::runtime_error {
-    cudaError_t code;
-    CudaFail(cudaError_t c, const char* what)
-        : std::runtime_error(std::string(what) + ": " + cudaGetErrorString(c)), code(c) {}
-};
-struct ApiFail : std::runtime_error {
-    int status;
-    ApiFail(int s, const std::string& m) : std::runtime_error(m), status(s) {}
-};
-
-#define CK(call)                                            \
-    do {                                                    \
-        cudaError_t e_ = (call);                            \
-        if (e_ != cudaSuccess) throw CudaFail(e_, #call);   \
-    } while (0)
-
-// Grow-only device array.
-template <class T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t cap = 0;
-    void ensure(size_t n) {
-        if (n <= cap) return;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = std::max<size_t>(n, 1);
-        CK(cudaMalloc(&p, want * sizeof(T)));
-        cap = want;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-struct SubShape {
-    int kind, lmax, np, n1;
-    double rcut;
-    bool operator==(const SubShape& o) const {
-        return kind == o.kind && lmax == o.lmax && np == o.np && n1 == o.n1 && rcut == o.rcut;
-    }
-};
-
-// Species t0..t1-1 sharing the sub-basis shapes (and descriptor length).
-struct Run {
-    int t0, t1;
-    std::vector<SubShape> subs;
-    std::vector<int> fp_off;
-    std::vector<DevBuf<float>> W;  // per sub: [T][T][NP][N1]
-};
-
-struct NetDev {
-    int D, nlayer;
-    int H[4];
-    DevBuf<float> w32;
-    double mu_e, sigma_e;
-    NetTC tc;  // tensor-core parameters (mixed precision)
-};
-
-}  // namespace
-
-struct nnap_handle {
-    Model model;
-    int precision = NNAP_PREC_FP32;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    bool dead = false;
-    int launches = 0;
-    int fp_stride = 0;
-    std::vector<Run> runs;
-    std::vector<NetDev> nets;
-    // work buffers
-    DevBuf<double> x, xw, e_atom, forces, virials, energy, virial, partial;
-    DevBuf<int> type, sid, cell_of, cell_count, cell_fill, cell_start, cell_atoms, perm, block_counts, type_start;
-    DevBuf<int> chunk_b, chunk_e, struct_chunks, status;
-    DevBuf<float4> xf, xlo;
-    DevBuf<uint16_t> pgrp;
-    DevBuf<StructDev> sdev;
-    DevBuf<uint64_t> pkey;
-    DevBuf<float4> pdx, pg;
-    DevBuf<int> prev, pcount;
-    DevBuf<float> fp, gfp, A;
-    int M = 0;
-    int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
-    bool profiling = false;
-    cudaEvent_t order_ev = nullptr;
-    // launch-sequence cache (CUDA graph) and the layout it was sized for
-    bool use_graphs = true;
-    bool layout_ok = false;
-    int layout_runs = 0;
-    std::vector<long long> last_layout, gkey;
-    cudaGraphExec_t gexec = nullptr;
-    StructDev* h_sdev = nullptr;  // pinned staging of the structure descriptors
-    size_t h_sdev_cap = 0;
-    int sm_count = 148;
-    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    bool capturing = false;
-    void mark(int k) {
-        // inside stream capture an ordinary record is only a dependency marker; an external
-        // event node records the event when the graph runs
-        if (profiling) CK(cudaEventRecordWithFlags(ev[k], stream, capturing ? cudaEventRecordExternal : 0));
-    }
-};
-
-namespace {
 
 int fail(nnap_handle* h, int status, const std::string& m) {
     if (h) h->err = m;
     return status;
-}
-
-template <class F>
-int guarded(nnap_handle* h, F&& f) {
-    if (!h) return NNAP_ERR_ARG;
-    if (h->dead) return fail(h, NNAP_ERR_DEAD, "this NNAP is dead");
-    h->err.clear();
-    try {
-        CK(cudaSetDevice(h->device));
-        return f();
-    } catch (const ApiFail& e) {
-        return fail(h, e.status, e.what());
-    } catch (const CudaFail& e) {
-        cudaGetLastError();  // leave no error behind for the caller's next CUDA call
-        return fail(h, NNAP_ERR_CUDA, e.what());
-    } catch (const std::bad_alloc&) {
-        return fail(h, NNAP_ERR_CAPACITY, "host allocation failed");
-    } catch (const std::exception& e) {
-        return fail(h, NNAP_ERR_ARG, e.what());
-    }
 }
 
 // ------------------------------------------------------------------ model upload
@@ -279,6 +122,16 @@ void cross3(const double* u, const double* v, double* r) {
     r[2] = u[0] * v[1] - v[0] * u[1];
 }
 
+// Float bound for the candidate screen: rc^2 plus the worst rounding of the FP32
+// difference (x_j + shift) - x_i for image shifts up to Rm + 2 box lengths.
+float screen_bound(const StructDev& s, double rc, int Rm) {
+    double ext = 0.0;
+    for (int d = 0; d < 3; ++d) ext += std::fabs(s.a[d]) + std::fabs(s.b[d]) + std::fabs(s.c[d]);
+    const double eps = 16.0 * (ext * (2 + Rm)) * std::ldexp(1.0, -24);
+    const double margin = 2.0 * std::sqrt(3.0) * rc * eps + 3.0 * eps * eps + 16.0 * rc * rc * std::ldexp(1.0, -24);
+    return (float)(rc * rc + margin) * (1.0f + 1e-6f);
+}
+
 StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0) {
     if (kind < 0 || kind > 2) throw ApiFail(NNAP_ERR_ARG, "box_kind must be 0, 1 or 2");
     StructDev s;
@@ -298,20 +151,22 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
     if (!(s.vol > 0.0) || !std::isfinite(s.vol)) throw ApiFail(NNAP_ERR_ARG, "box must be right-handed with positive volume");
     auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
     const double h[3] = {s.vol / nrm(s.bc), s.vol / nrm(s.ca), s.vol / nrm(s.ab)};
-    double ext = 0.0;
     for (int d = 0; d < 3; ++d) {
         s.nc[d] = std::max(1, (int)std::floor(h[d] / rc));
         s.nc[d] = std::min(s.nc[d], 1024);
         s.R[d] = (int)std::floor(rc * s.nc[d] / h[d] + 1e-6) + 1;
         if (s.R[d] > 64) throw ApiFail(NNAP_ERR_ARG, "box too thin for the cutoff");
-        ext += std::fabs(s.a[d]) + std::fabs(s.b[d]) + std::fabs(s.c[d]);
     }
-    for (int d = 0; d < 3; ++d) { s.fa[d] = (float)s.a[d]; s.fb[d] = (float)s.b[d]; s.fc[d] = (float)s.c[d]; }
+    if ((2 * s.R[0] + 1) * (2 * s.R[1] + 1) * (2 * s.R[2] + 1) > 65535)
+        throw ApiFail(NNAP_ERR_ARG, "box too thin for the cutoff");
+    for (int d = 0; d < 3; ++d) {
+        s.fa[d] = (float)s.a[d]; s.fb[d] = (float)s.b[d]; s.fc[d] = (float)s.c[d];
+        s.la[d] = (float)(s.a[d] - (double)s.fa[d]);
+        s.lb[d] = (float)(s.b[d] - (double)s.fb[d]);
+        s.lc[d] = (float)(s.c[d] - (double)s.fc[d]);
+    }
     s.rc2 = rc * rc;
-    const int Rm = std::max(s.R[0], std::max(s.R[1], s.R[2]));
-    const double eps = 16.0 * (ext * (2 + Rm)) * std::ldexp(1.0, -24);
-    const double margin = 2.0 * std::sqrt(3.0) * rc * eps + 3.0 * eps * eps + 16.0 * rc * rc * std::ldexp(1.0, -24);
-    s.rc2_hi = (float)(rc * rc + margin) * (1.0f + 1e-6f);
+    s.rc2_hi = screen_bound(s, rc, std::max(s.R[0], std::max(s.R[1], s.R[2])));
     s.a0 = a0;
     s.n = n;
     s.c0 = c0;
@@ -319,12 +174,6 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
 }
 
 // ------------------------------------------------------------------ pipeline
-struct Batch {
-    int nstruct = 0, natoms = 0, ncells = 0;
-    std::vector<StructDev> sd;
-    std::vector<int> sid, cb, ce, sc;
-};
-
 Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes) {
     Batch B;
     B.nstruct = nstruct;
@@ -348,10 +197,6 @@ Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kind
     B.ncells = c0;
     return B;
 }
-
-struct Outputs {
-    double *energy = nullptr, *energies = nullptr, *forces = nullptr, *virial = nullptr, *virials = nullptr;
-};
 
 void grow_pairs(nnap_handle* h, int n, int M) {
     h->M = M;
@@ -394,21 +239,18 @@ size_t a_arena_size(nnap_handle* h, int n) {
     return tot;
 }
 
-// Size every buffer for the batch and upload the layout arrays that depend only on the
-// atom counts (structure of each atom, reduction chunks).  Runs outside graph capture.
-void prepare_layout(nnap_handle* h, const Batch& B) {
-    const int n = B.natoms;
+void ensure_work(nnap_handle* h, int n, int nstruct, int ncells, int nchunks) {
     const int T = h->model.ntypes();
     const int n1 = std::max(n, 1);
-    h->sdev.ensure(B.nstruct);
+    h->sdev.ensure(std::max(nstruct, 1));
     h->sid.ensure(n1);
     h->xw.ensure(3 * (size_t)n1);
     h->xf.ensure(n1);
     h->xlo.ensure(n1);
     h->cell_of.ensure(n1);
-    h->cell_count.ensure(B.ncells);
-    h->cell_fill.ensure(B.ncells);
-    h->cell_start.ensure(B.ncells + 1);
+    h->cell_count.ensure(std::max(ncells, 1));
+    h->cell_fill.ensure(std::max(ncells, 1));
+    h->cell_start.ensure(ncells + 1);
     h->cell_atoms.ensure(n1);
     h->pcount.ensure(n1);
     h->perm.ensure(n1);
@@ -416,7 +258,6 @@ void prepare_layout(nnap_handle* h, const Batch& B) {
     h->block_counts.ensure((size_t)std::max(nb, 1) * T);
     h->type_start.ensure(T + 1);
     h->status.ensure(2);
-    if (h->M == 0) h->M = initial_capacity(B, h->model.rcut_max);
     grow_pairs(h, n, h->M);
     h->fp.ensure((size_t)n1 * h->fp_stride);
     h->gfp.ensure((size_t)n1 * h->fp_stride);
@@ -424,13 +265,21 @@ void prepare_layout(nnap_handle* h, const Batch& B) {
     h->e_atom.ensure(n1);
     h->forces.ensure(3 * (size_t)n1);
     h->virials.ensure(9 * (size_t)n1);
-    const int nchunks = (int)B.cb.size();
     h->chunk_b.ensure(std::max(nchunks, 1));
     h->chunk_e.ensure(std::max(nchunks, 1));
-    h->struct_chunks.ensure(B.nstruct + 1);
+    h->struct_chunks.ensure(nstruct + 1);
     h->partial.ensure(10 * (size_t)std::max(nchunks, 1));
-    h->energy.ensure(std::max(B.nstruct, 1));
-    h->virial.ensure(9 * (size_t)std::max(B.nstruct, 1));
+    h->energy.ensure(std::max(nstruct, 1));
+    h->virial.ensure(9 * (size_t)std::max(nstruct, 1));
+}
+
+// Size every buffer for the batch and upload the layout arrays that depend only on the
+// atom counts (structure of each atom, reduction chunks).  Runs outside graph capture.
+void prepare_layout(nnap_handle* h, const Batch& B) {
+    const int n = B.natoms;
+    const int nchunks = (int)B.cb.size();
+    if (h->M == 0) h->M = initial_capacity(B, h->model.rcut_max);
+    ensure_work(h, n, B.nstruct, B.ncells, nchunks);
     if (h->h_sdev_cap < (size_t)B.nstruct) {
         if (h->h_sdev) cudaFreeHost(h->h_sdev);
         h->h_sdev = nullptr;
@@ -447,20 +296,14 @@ void prepare_layout(nnap_handle* h, const Batch& B) {
     CK(cudaStreamSynchronize(st));
 }
 
-// Queue the whole evaluation on the handle's stream without any host synchronisation
-// (capturable into a CUDA graph).  The structure descriptors are copied from the pinned
-// staging array, so a replay picks up new boxes.
-void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+// Cell list and neighbour rows of every atom of the batch (cutoff and cell grid from
+// the structure descriptors already on the device).
+void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type) {
     const int n = B.natoms;
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
-    const int nb = (n + kSortBlock - 1) / kSortBlock;
-    h->launches = 0;
-    h->mark(0);
-    CK(cudaMemcpyAsync(h->sdev.p, h->h_sdev, sizeof(StructDev) * B.nstruct, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * B.ncells, st));
     CK(cudaMemsetAsync(h->cell_fill.p, 0, sizeof(int) * B.ncells, st));
-    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
     if (n > 0) {
         k_wrap_bin<<<(n + 255) / 256, 256, 0, st>>>(h->sdev.p, h->sid.p, d_x, d_type, n, T, h->xw.p, h->xf.p,
                                                     h->xlo.p, h->cell_of.p, h->cell_count.p, h->status.p);
@@ -474,16 +317,30 @@ void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_typ
         k_neighbors<<<(n + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
             h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
             pair_bufs(h), h->status.p, h->status.p + 1);
-        k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
-        k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
-        k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
-        const long long tot = (long long)n * h->M;
-        k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
-        h->launches += 7;
+        h->launches += 3;
     }
-    h->mark(1);
+}
+
+void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
+    const int n = B.natoms;
+    if (n <= 0) return;
+    const int T = h->model.ntypes();
+    cudaStream_t st = h->stream;
+    const int nb = (n + kSortBlock - 1) / kSortBlock;
+    k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
+    k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
+    k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
+    const long long tot = (long long)n * h->M;
+    k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
+    h->launches += 4;
+}
+
+void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only) {
+    const int n = B.natoms;
+    const int T = h->model.ntypes();
+    cudaStream_t st = h->stream;
     if (n > 0) CK(cudaMemsetAsync(h->fp.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
-    // descriptors forward, per run of species sharing a basis shape and per sub-basis
+    // descriptors, per run of species sharing a basis shape and per sub-basis
     auto descriptors = [&](bool fwd) {
         size_t a_off = 0;
         for (auto& r : h->runs) {
@@ -561,6 +418,21 @@ void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_typ
         ++h->launches;
     }
     h->mark(5);
+}
+
+// Queue the whole evaluation on the handle's stream without any host synchronisation
+// (capturable into a CUDA graph).  The structure descriptors are copied from the pinned
+// staging array, so a replay picks up new boxes.
+void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+    cudaStream_t st = h->stream;
+    h->launches = 0;
+    h->mark(0);
+    CK(cudaMemcpyAsync(h->sdev.p, h->h_sdev, sizeof(StructDev) * B.nstruct, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
+    enqueue_neighbors(h, B, d_x, d_type);
+    enqueue_species_mirror(h, B, d_type);
+    h->mark(1);
+    enqueue_eval(h, B, d_type, fp_only);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
 }
@@ -675,7 +547,7 @@ void upload_inputs(nnap_handle* h, int n, const double* x, const int* type) {
     }
 }
 
-}  // namespace
+}  // namespace nnapgb
 
 // =================================================================== C ABI
 extern "C" {

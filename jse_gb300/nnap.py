@@ -31,14 +31,16 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libnnap_gb300.so")
 
 NNAP_OK, NNAP_ERR_BAD_MODEL, NNAP_ERR_BAD_TYPE, NNAP_ERR_CAPACITY, NNAP_ERR_CUDA, NNAP_ERR_UNSUPPORTED, \
-    NNAP_ERR_ARG, NNAP_ERR_TIMEOUT, NNAP_ERR_DEAD = range(9)
+    NNAP_ERR_ARG, NNAP_ERR_TIMEOUT, NNAP_ERR_DEAD, NNAP_ERR_BUSY = range(10)
 PREC = {"fp32": 0, "single": 0, "mixed": 1}
 WANT_ENERGY, WANT_ENERGIES, WANT_FORCES, WANT_VIRIAL, WANT_VIRIALS = 1, 2, 4, 8, 16
 
 EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes", "nnap_rcut_max", "nnap_symbol",
            "nnap_descriptor_size", "nnap_last_error", "nnap_compute", "nnap_compute_device", "nnap_compute_batch",
            "nnap_compute_fp", "nnap_neighbor_list", "nnap_last_launch_count", "nnap_set_profiling",
-           "nnap_stage_times", "nnap_compute_batch_device", "nnap_set_graphs"]
+           "nnap_stage_times", "nnap_compute_batch_device", "nnap_set_graphs", "nnap_neighbor_counts_noalloc",
+           "nnap_server_create", "nnap_server_destroy", "nnap_server_admit", "nnap_server_release",
+           "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats"]
 
 
 class IllegalStateError(RuntimeError):
@@ -83,6 +85,13 @@ def load_library(path: str = LIB_PATH):
     L.nnap_stage_times.argtypes = [P, dp]
     L.nnap_compute_batch_device.argtypes = [P, I, ip, P, P, ip, dp, I, P, P, P, P, P, P]
     L.nnap_set_graphs.argtypes = [P, I]
+    L.nnap_server_create.argtypes = [P, D, S, I, C.POINTER(P)]
+    L.nnap_server_destroy.argtypes = [P]
+    L.nnap_server_admit.argtypes = [P, I, ip, I, dp, ip]
+    L.nnap_server_release.argtypes = [P, I]
+    L.nnap_server_step.argtypes = [P, I, ip, dp, I, dp, dp, dp, dp, dp]
+    L.nnap_server_neighbor_list.argtypes = [P, I, ip, C.c_longlong, ip, ip, C.POINTER(C.c_longlong)]
+    L.nnap_server_stats.argtypes = [P, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 

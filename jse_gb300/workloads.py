@@ -200,3 +200,16 @@ def model_for(config: str, seed: int = 11, norm_mu=None, norm_sigma=None) -> dic
     if config == "c3":
         return write_model(["A", "B"], C3_BASIS, [64, 64], seed, norm_mu, norm_sigma, -3.0, 0.1)
     raise ValueError(config)
+
+
+def c5_pool(count: int = 512, seed: int = 5, sigma: float = 1.0) -> List[Structure]:
+    """Structures for the serving workload: n ~ log-normal (median 500, log-sd ``sigma``)
+    clipped to [50, 20000]; ternary liquids as the 32000-atom workload (cubic box,
+    density 0.060 /A^3, fractions 0.46/0.46/0.08, min separation 2.0 A).  Requests draw
+    their starting structure from this pool."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        n = int(min(20000, max(50, round(math.exp(math.log(500.0) + sigma * rng.standard_normal())))))
+        out.append(random_liquid(n, 0.060, [0.46, 0.46, 0.08], 2.0, seed * 100003 + k))
+    return out
