@@ -217,6 +217,52 @@ def cpu_reference(structures, model: dict, budget_s: float = 12.0, threads: int 
                               if ref is not None else "FP64 oracle port, 1 thread")}
 
 
+# ----------------------------------------------------------------------------- serving
+def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2)) -> dict:
+    """Continuous-batching serving of ``nreq`` requests of 20 evaluations each.
+
+    Requests start from structures of a 256-structure pool (n ~ log-normal, median 500,
+    log-sd 1.0, clipped to [50, 20000]; ternary liquids at 0.060 /A^3) and move every
+    coordinate by N(0, 0.01^2) A between evaluations.  The server keeps neighbour rows at
+    rcut + 0.5 A, admits by a 120 GB budget and at most 1024 resident structures.  The
+    capacity is the request rate of a saturated run (every request queued at once); the
+    Poisson runs offer fractions of it.  Latencies are wall-clock, host buffers, and
+    include queueing."""
+    from jse_gb300.nnap import NNAP
+    from jse_gb300.serve import GaussianMoves, NNAPServer, RequestLoop, poisson_requests
+    pool = W.c5_pool(256)
+    model = normalised_model("c5", [max(pool, key=lambda q: q.natoms)], "mixed")
+    moves = GaussianMoves(sigma=0.01, seed=7)
+    out = {"requests": nreq, "evaluations_per_request": 20, "skin_A": 0.5, "memory_budget_GB": 120,
+           "max_resident": 1024, "pool": "256 structures, n ~ lognormal(median 500, sd 1.0) in [50, 20000]",
+           "mean_atoms": float(np.mean([p.natoms for p in pool]))}
+    with NNAP(model, precision="mixed", device=device) as p:
+        def run(rate):
+            with NNAPServer(p, skin=0.5, memory_budget=120e9, max_structs=1024) as srv:
+                reqs = poisson_requests(pool, nreq, rate, nsteps=20, seed=11)
+                st = RequestLoop(srv, reqs, moves=moves).run()
+                ss = srv.stats()
+                st["rebuilds_per_request"] = ss["rebuilds"] / max(1, nreq)
+                return st
+        # warm the pool allocator and kernels, then saturate
+        with NNAPServer(p, skin=0.5, memory_budget=120e9, max_structs=1024) as srv:
+            RequestLoop(srv, poisson_requests(pool, 64, float("inf"), nsteps=3, seed=1), moves=moves).run()
+        sat = run(float("inf"))
+        cap = sat["req_per_s"]
+        out["capacity_req_s"] = cap
+        out["capacity_atom_evals_s"] = sat["atom_evals_per_s"]
+        runs = []
+        for f in loads:
+            st = run(f * cap)
+            runs.append({"load": f, "offered_req_s": f * cap, "achieved_req_s": st["req_per_s"],
+                         "atom_evals_s": st["atom_evals_per_s"], "request_p50_ms": st["request_p50_ms"],
+                         "request_p99_ms": st["request_p99_ms"], "eval_p50_ms": st["eval_p50_ms"],
+                         "eval_p99_ms": st["eval_p99_ms"], "max_active": st["max_active"],
+                         "rebuilds_per_request": st["rebuilds_per_request"]})
+        out["runs"] = runs
+    return out
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -225,8 +271,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="liquid32k", choices=["liquid32k", "fcc4000", "glass1m", "batch1024"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-requests", type=int, default=5000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -364,29 +412,35 @@ def main():
     e2e = {"value": N * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": N * 28,
            "d2h_bytes_per_step": S * 8 + N * 24 + S * 72}
 
-    # the plain GPU path on batches: one FP32 single-structure call per structure
-    plain = None
-    if not single:
-        with NNAP(model, precision="fp32", device=local) as pp:
+    # the plain GPU path: one FP32 single-structure nnap_compute per structure
+    with NNAP(model, precision="fp32", device=local) as pp:
+        if not single:
             pp.setGraphs(False)
-            offs = np.concatenate([[0], np.cumsum(nat)])
+        offs = np.concatenate([[0], np.cumsum(nat)])
 
-            def plain_step():
-                for k, st_ in enumerate(structures):
-                    a, b = offs[k], offs[k + 1]
-                    pp._check(pp._L.nnap_compute(pp._handle(), int(nat[k]), _dptr(xh[a:b]), _iptr(th[a:b]),
-                                                 int(kinds[k]), _dptr(boxes[9 * k:9 * k + 9]), flags, _dptr(eh[k:k + 1]),
-                                                 None, _dptr(fh[a:b]), _dptr(vh[k]), None))
+        def plain_step():
+            for k in range(S):
+                a, b = offs[k], offs[k + 1]
+                pp._check(pp._L.nnap_compute(pp._handle(), int(nat[k]), _dptr(xh[a:b]), _iptr(th[a:b]),
+                                             int(kinds[k]), _dptr(boxes[9 * k:9 * k + 9]), flags, _dptr(eh[k:k + 1]),
+                                             None, _dptr(fh[a:b]), _dptr(vh[k]), None))
+        for _ in range(3):
             plain_step()
-            pts = []
-            for _ in range(max(1, min(args.steps, 5))):
-                t0 = time.perf_counter()
-                plain_step()
-                pts.append(time.perf_counter() - t0)
-            pv = N * len(pts) / sum(pts)
-            plain = {"value": pv, "unit": "atom-evals/s", "ms_per_step": 1e3 * sum(pts) / len(pts),
-                     "path": "plain FP32, one nnap_compute per structure, host buffers",
-                     "tuned_e2e_over_plain": e2e["value"] / pv}
+        pts = []
+        for _ in range(max(1, min(args.steps, 5) if not single else args.steps)):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            plain_step()
+            pts.append(time.perf_counter() - t0)
+        pv = N * len(pts) / sum(pts)
+        plain = {"value": pv, "unit": "atom-evals/s", "ms_per_step": 1e3 * sum(pts) / len(pts),
+                 "path": "plain FP32, one nnap_compute per structure, host buffers",
+                 "tuned_e2e_over_plain": e2e["value"] / pv}
+
+    serving = None
+    if rank == 0 and not args.no_serve and args.workload == "liquid32k":
+        serving = serve_measurement(local, args.serve_requests)
 
     # roofline of the dominant stage
     peak, peak_kind, sm_max = load_peaks()
@@ -423,8 +477,9 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16+f32",
                 "data": "synthetic (seeded)", "config": config, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
                 "clocks": clk, "gpu_launches": launches, "wall_s_timed": wall}
-        if plain is not None:
-            line["plain_gpu"] = plain
+        line["plain_gpu"] = plain
+        if serving is not None:
+            line["serving"] = serving
         print(json.dumps(line))
     pot.close()
     if dist:
