@@ -152,9 +152,61 @@ __device__ __forceinline__ void sph_harm(const Angles& an, float* Y, float* Yt, 
     }
 }
 
+// Radial-fuse matrices in shared memory with rows padded to N1P = N1 rounded up to 4,
+// so a row is read with float4 loads: sW[(tc * T + tn) * NP * N1P + p * N1P + n].
+template <int N1>
+struct Fuse {
+    static constexpr int N1P = (N1 + 3) & ~3;
+};
+
 template <int NP, int N1>
-__device__ __forceinline__ void load_fuse(const float* __restrict__ Wg, float* sW, int count) {
-    for (int q = threadIdx.x; q < count; q += blockDim.x) sW[q] = Wg[q];
+__device__ __forceinline__ void load_fuse(const float* __restrict__ Wg, float* sW, int T) {
+    constexpr int N1P = Fuse<N1>::N1P;
+    const int count = T * T * NP * N1P;
+    for (int q = threadIdx.x; q < count; q += blockDim.x) {
+        const int row = q / N1P, n = q - row * N1P;
+        sW[q] = n < N1 ? Wg[row * N1 + n] : 0.f;
+    }
+}
+
+// out[p] = sum_n Wt[p][n] * v[n]
+template <int NP, int N1>
+__device__ __forceinline__ void fuse_apply(const float* __restrict__ Wt, const float* v, float* out) {
+    constexpr int N1P = Fuse<N1>::N1P;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float4* row = reinterpret_cast<const float4*>(Wt + p * N1P);
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < N1P / 4; ++q) {
+            const float4 w = row[q];
+            s += w.x * v[4 * q];
+            if (4 * q + 1 < N1) s += w.y * v[4 * q + 1];
+            if (4 * q + 2 < N1) s += w.z * v[4 * q + 2];
+            if (4 * q + 3 < N1) s += w.w * v[4 * q + 3];
+        }
+        out[p] = s;
+    }
+}
+
+// out[n] = sum_p u[p] * Wt[p][n]
+template <int NP, int N1>
+__device__ __forceinline__ void fuse_apply_t(const float* __restrict__ Wt, const float* u, float* out) {
+    constexpr int N1P = Fuse<N1>::N1P;
+#pragma unroll
+    for (int n = 0; n < N1; ++n) out[n] = 0.f;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float4* row = reinterpret_cast<const float4*>(Wt + p * N1P);
+#pragma unroll
+        for (int q = 0; q < N1P / 4; ++q) {
+            const float4 w = row[q];
+            out[4 * q] += u[p] * w.x;
+            if (4 * q + 1 < N1) out[4 * q + 1] += u[p] * w.y;
+            if (4 * q + 2 < N1) out[4 * q + 2] += u[p] * w.z;
+            if (4 * q + 3 < N1) out[4 * q + 3] += u[p] * w.w;
+        }
+    }
 }
 
 __device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { return a.perm[s0 + warp]; }
@@ -165,7 +217,7 @@ __device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { re
 template <int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
     extern __shared__ float sW[];
-    load_fuse<NP, N1>(a.W, sW, a.T * a.T * NP * N1);
+    load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
     const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
@@ -183,16 +235,11 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
         if (r >= rc) continue;
         const int tn = __float_as_int(d.w) - 1;
         const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
-        float T[N1];
+        float T[N1], sv[NP];
         cheby_f<N1>(1.f - 2.f * u, T);
-        const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+        fuse_apply<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, T, sv);
 #pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            float s = 0.f;
-#pragma unroll
-            for (int n = 0; n < N1; ++n) s += Wt[p * N1 + n] * T[n];
-            acc[p] += fc * s;
-        }
+        for (int p = 0; p < NP; ++p) acc[p] += fc * sv[p];
     }
 #pragma unroll
     for (int p = 0; p < NP; ++p)
@@ -207,7 +254,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
 template <int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescWarps) k_radial_bwd(DescArgs a) {
     extern __shared__ float sW[];
-    load_fuse<NP, N1>(a.W, sW, a.T * a.T * NP * N1);
+    load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
     const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
@@ -233,15 +280,13 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_bwd(DescArgs a) {
             float T[N1], TG[N1];
             cheby_f<N1>(x, T);
             cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
-            const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+            float v[N1];
+            fuse_apply_t<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, gfp, v);
             float dfc = 0.f, drn = 0.f;
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                float s = 0.f, sg = 0.f;
-#pragma unroll
-                for (int n = 0; n < N1; ++n) { s += Wt[p * N1 + n] * T[n]; sg += Wt[p * N1 + n] * TG[n]; }
-                dfc += gfp[p] * s;
-                drn += gfp[p] * sg;
+            for (int n = 0; n < N1; ++n) {
+                dfc += v[n] * T[n];
+                drn += v[n] * TG[n];
             }
             const float gr = dfc * fcg + fc * drn;
             g = make_float4(gr * d.x, gr * d.y, gr * d.z, 0.f);
@@ -271,9 +316,9 @@ template <int L, int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
     using S = SphShape<L, NP>;
     extern __shared__ float smem[];
-    const int nW = a.T * a.T * NP * N1;
+    const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
     float* sW = smem;
-    load_fuse<NP, N1>(a.W, sW, nW);
+    load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * kDescWarps + wl;
@@ -285,11 +330,13 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
     const float rc = a.rcut, irc = 1.f / a.rcut;
-    float acc[NP][S::COLS];
+    // accumulators in packed pairs of channels (p = 2h, 2h + 1) for paired FP32 FMAs
+    constexpr int NH = (NP + 1) / 2;
+    float2 acc[NH][S::COLS];
 #pragma unroll
-    for (int p = 0; p < NP; ++p)
+    for (int h = 0; h < NH; ++h)
 #pragma unroll
-        for (int c = 0; c < S::COLS; ++c) acc[p][c] = 0.f;
+        for (int c = 0; c < S::COLS; ++c) acc[h][c] = make_float2(0.f, 0.f);
     for (int base = 0; base < cnt; base += 32) {
         const int k = base + lane;
         float c[NP];
@@ -304,16 +351,11 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
                 valid = true;
                 const int tn = __float_as_int(d.w) - 1;
                 const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
-                float T[N1];
+                float T[N1], sv[NP];
                 cheby_f<N1>(1.f - 2.f * u, T);
-                const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+                fuse_apply<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, T, sv);
 #pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    float s = 0.f;
-#pragma unroll
-                    for (int n = 0; n < N1; ++n) s += Wt[p * N1 + n] * T[n];
-                    c[p] = fc * s;
-                }
+                for (int p = 0; p < NP; ++p) c[p] = fc * sv[p];
                 const Angles an = angles_f(d.x, d.y, d.z, r);
                 sph_harm<L, false>(an, y, nullptr, 1);
             }
@@ -322,24 +364,26 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
 #pragma unroll
             for (int q = 0; q < S::K; ++q) y[q] = 0.f;
 #pragma unroll
-        for (int p = 0; p < NP; ++p) sC[lane * S::NPS + p] = c[p];
+        for (int p = 0; p < S::NPS; ++p) sC[lane * S::NPS + p] = p < NP ? c[p] : 0.f;
         __syncwarp();
         const int nk = min(32, cnt - base);
         for (int kk = 0; kk < nk; ++kk) {
-            float cv[S::NPS];
+            float2 cv[NH];
             const float4* crow = reinterpret_cast<const float4*>(sC + kk * S::NPS);
 #pragma unroll
             for (int q = 0; q < S::NPS / 4; ++q) {
                 const float4 v = crow[q];
-                cv[4 * q] = v.x; cv[4 * q + 1] = v.y; cv[4 * q + 2] = v.z; cv[4 * q + 3] = v.w;
+                if (2 * q < NH) cv[2 * q] = make_float2(v.x, v.y);
+                if (2 * q + 1 < NH) cv[2 * q + 1] = make_float2(v.z, v.w);
             }
             const float* yrow = sY + kk * S::KS;
 #pragma unroll
             for (int col = 0; col < S::COLS; ++col) {
                 const int lm = lane + 32 * col;
                 const float yv = lm < S::K ? yrow[lm] : 0.f;
+                const float2 yy = make_float2(yv, yv);
 #pragma unroll
-                for (int p = 0; p < NP; ++p) acc[p][col] += cv[p] * yv;
+                for (int h = 0; h < NH; ++h) acc[h][col] = __ffma2_rn(cv[h], yy, acc[h][col]);
             }
         }
         __syncwarp();
@@ -353,8 +397,9 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
         if (lm < S::K)
 #pragma unroll
             for (int p = 0; p < NP; ++p) {
-                Aout[p * S::K + lm] = acc[p][col];
-                sA2[p * S::K + lm] = acc[p][col] * acc[p][col];
+                const float v = (p & 1) ? acc[p >> 1][col].y : acc[p >> 1][col].x;
+                Aout[p * S::K + lm] = v;
+                sA2[p * S::K + lm] = v * v;
             }
     }
     __syncwarp();
@@ -367,21 +412,29 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
     }
 }
 
+// Backward, one warp per atom slot, one neighbour per lane.  For each neighbour,
+//   dY_lm = sum_p c_p G[p][lm]        (chain into theta and phi),
+//   dc_p  = sum_lm G[p][lm] Y_lm      (chain into fc and the radial functions),
+// with c_p = fc Rnp_p.  G rows are read from shared memory as broadcast float4 loads;
+// Y and dY/dtheta of the lane's neighbour sit in a lane column of shared memory.  Only
+// c and dc stay live through the lm loop: the radial sums are formed again afterwards
+// as v_n = sum_p dc_p W[p][n], so dfc = v . T and drn = v . dT.  Registers stay at or
+// below 128 per thread (four CTAs of four warps per SM).
 template <int L, int NP, int N1>
-__global__ void __launch_bounds__(32 * kDescWarps) k_sph_bwd(DescArgs a) {
+__global__ void __launch_bounds__(32 * kDescWarps, 4) k_sph_bwd(DescArgs a) {
     using S = SphShape<L, NP>;
     extern __shared__ float smem[];
-    const int nW = a.T * a.T * NP * N1;
+    const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
     float* sW = smem;
-    load_fuse<NP, N1>(a.W, sW, nW);
+    load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * kDescWarps + wl;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
-    float* sG = smem + ((nW + 3) & ~3) + wl * S::BWD_WARP_FLOATS;  // [K][NPS]
-    float* sY = sG + S::K * S::NPS;                                   // [K][32]
-    float* sYt = sY + S::K * 32;                                      // [K][32]
+    float* sG = smem + nW + wl * S::BWD_WARP_FLOATS;  // [K][NPS]
+    float* sY = sG + S::K * S::NPS;                  // [K][32]
+    float* sYt = sY + S::K * 32;                     // [K][32]
     const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
@@ -403,95 +456,97 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_bwd(DescArgs a) {
     }
     for (int base = 0; base < cnt; base += 32) {
         const int k = base + lane;
-        float c[NP], rnp[NP], rnpg[NP];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) { c[p] = 0.f; rnp[p] = 0.f; rnpg[p] = 0.f; }
+        float c[NP];
         float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-        float r = 1.f, fc = 0.f, fcg = 0.f;
-        Angles an;
-        an.ct = an.st = an.sp = 0.f; an.cp = 1.f; an.dxy = 0.f; an.pole = true;
+        float r = 1.f;
         bool valid = false;
         if (k < cnt) {
             d = a.P.dx[(size_t)at * M + k];
             r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
             valid = r < rc;
         }
+        const int tn = valid ? __float_as_int(d.w) - 1 : 0;
+        const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P;
         if (valid) {
-            const int tn = __float_as_int(d.w) - 1;
-            const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1;
-            fc = fc2 * fc2;
-            fcg = 8.f * fc1 * fc2 * irc * irc;
-            const float x = 1.f - 2.f * u;
-            float T[N1], TG[N1];
-            cheby_f<N1>(x, T);
-            cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
-            const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * N1;
+            const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
+            float T[N1], sv[NP];
+            cheby_f<N1>(1.f - 2.f * u, T);
+            fuse_apply<NP, N1>(Wt, T, sv);
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                float s = 0.f, sg = 0.f;
-#pragma unroll
-                for (int n = 0; n < N1; ++n) { s += Wt[p * N1 + n] * T[n]; sg += Wt[p * N1 + n] * TG[n]; }
-                rnp[p] = s; rnpg[p] = sg; c[p] = fc * s;
-            }
-            an = angles_f(d.x, d.y, d.z, r);
+            for (int p = 0; p < NP; ++p) c[p] = fc * sv[p];
+            const Angles an = angles_f(d.x, d.y, d.z, r);
             sph_harm<L, true>(an, sY + lane, sYt + lane, 32);
         } else {
 #pragma unroll
+            for (int p = 0; p < NP; ++p) c[p] = 0.f;
+#pragma unroll 7
             for (int q = 0; q < S::K; ++q) { sY[q * 32 + lane] = 0.f; sYt[q * 32 + lane] = 0.f; }
         }
-        float dc[NP];
+        // c and dc in packed channel pairs (p = 2h, 2h + 1); padded G columns are zero
+        constexpr int NH = (NP + 1) / 2;
+        float2 c2[NH], dc2[NH];
 #pragma unroll
-        for (int p = 0; p < NP; ++p) dc[p] = 0.f;
+        for (int h = 0; h < NH; ++h) {
+            c2[h] = make_float2(c[2 * h], 2 * h + 1 < NP ? c[2 * h + 1] : 0.f);
+            dc2[h] = make_float2(0.f, 0.f);
+        }
         float gth = 0.f, gph = 0.f;
+        // one G row: returns dY_lm and adds G[.][lm] * Y_lm into dc
+        auto row = [&](int lm) -> float {
+            const float4* gr = reinterpret_cast<const float4*>(sG + lm * S::NPS);
+            const float yv = sY[lm * 32 + lane];
+            const float2 yy = make_float2(yv, yv);
+            float2 dY = make_float2(0.f, 0.f);
 #pragma unroll
+            for (int q = 0; q < S::NPS / 4; ++q) {
+                const float4 g = gr[q];
+                if (2 * q < NH) {
+                    const float2 ga = make_float2(g.x, g.y);
+                    dY = __ffma2_rn(c2[2 * q], ga, dY);
+                    dc2[2 * q] = __ffma2_rn(ga, yy, dc2[2 * q]);
+                }
+                if (2 * q + 1 < NH) {
+                    const float2 gb = make_float2(g.z, g.w);
+                    dY = __ffma2_rn(c2[2 * q + 1], gb, dY);
+                    dc2[2 * q + 1] = __ffma2_rn(gb, yy, dc2[2 * q + 1]);
+                }
+            }
+            return dY.x + dY.y;
+        };
+#pragma unroll 1
         for (int l = 0; l <= L; ++l) {
             const int c0 = l * l + l;
-            {
-                const float4* gr = reinterpret_cast<const float4*>(sG + c0 * S::NPS);
-                float gv[S::NPS];
-#pragma unroll
-                for (int q = 0; q < S::NPS / 4; ++q) {
-                    const float4 v = gr[q];
-                    gv[4 * q] = v.x; gv[4 * q + 1] = v.y; gv[4 * q + 2] = v.z; gv[4 * q + 3] = v.w;
-                }
-                const float yv = sY[c0 * 32 + lane], ytv = sYt[c0 * 32 + lane];
-                float dY = 0.f;
-#pragma unroll
-                for (int p = 0; p < NP; ++p) { dY += c[p] * gv[p]; dc[p] += gv[p] * yv; }
-                gth += dY * ytv;
-            }
-#pragma unroll
+            gth += row(c0) * sYt[c0 * 32 + lane];
+#pragma unroll 1
             for (int m = 1; m <= l; ++m) {
-                const float4* gp4 = reinterpret_cast<const float4*>(sG + (c0 + m) * S::NPS);
-                const float4* gm4 = reinterpret_cast<const float4*>(sG + (c0 - m) * S::NPS);
-                float gp[S::NPS], gm[S::NPS];
-#pragma unroll
-                for (int q = 0; q < S::NPS / 4; ++q) {
-                    const float4 v = gp4[q], u = gm4[q];
-                    gp[4 * q] = v.x; gp[4 * q + 1] = v.y; gp[4 * q + 2] = v.z; gp[4 * q + 3] = v.w;
-                    gm[4 * q] = u.x; gm[4 * q + 1] = u.y; gm[4 * q + 2] = u.z; gm[4 * q + 3] = u.w;
-                }
-                const float yp = sY[(c0 + m) * 32 + lane], ym = sY[(c0 - m) * 32 + lane];
-                const float ytp = sYt[(c0 + m) * 32 + lane], ytm = sYt[(c0 - m) * 32 + lane];
-                float dYp = 0.f, dYm = 0.f;
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    dYp += c[p] * gp[p];
-                    dYm += c[p] * gm[p];
-                    dc[p] += gp[p] * yp + gm[p] * ym;
-                }
-                gth += dYp * ytp + dYm * ytm;
-                gph += (float)m * (dYm * yp - dYp * ym);
+                const float dYp = row(c0 + m);
+                const float dYm = row(c0 - m);
+                gth += dYp * sYt[(c0 + m) * 32 + lane] + dYm * sYt[(c0 - m) * 32 + lane];
+                gph += (float)m * (dYm * sY[(c0 + m) * 32 + lane] - dYp * sY[(c0 - m) * 32 + lane]);
             }
         }
         if (k < cnt) {
             const size_t e = (size_t)at * M + k;
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (valid) {
+                const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
+                const float fcg = 8.f * fc1 * fc2 * irc * irc;
+                const float x = 1.f - 2.f * u;
+                float T[N1], TG[N1], v[N1];
+                cheby_f<N1>(x, T);
+                cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+                float dc[NP];
+#pragma unroll
+                for (int p = 0; p < NP; ++p) dc[p] = (p & 1) ? dc2[p >> 1].y : dc2[p >> 1].x;
+                fuse_apply_t<NP, N1>(Wt, dc, v);
                 float dfc = 0.f, drn = 0.f;
 #pragma unroll
-                for (int p = 0; p < NP; ++p) { dfc += dc[p] * rnp[p]; drn += dc[p] * rnpg[p]; }
+                for (int n = 0; n < N1; ++n) {
+                    dfc += v[n] * T[n];
+                    drn += v[n] * TG[n];
+                }
                 const float gr = dfc * fcg + fc * drn;
+                const Angles an = angles_f(d.x, d.y, d.z, r);
                 const float ir = 1.f / r;
                 const float tpx = -an.ct * an.cp * ir, tpy = -an.ct * an.sp * ir, tpz = an.st * ir;
                 const float ppx = an.pole ? 0.f : an.sp / an.dxy, ppy = an.pole ? 0.f : -an.cp / an.dxy;
@@ -508,6 +563,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_bwd(DescArgs a) {
                 a.P.g[e] = g;
             }
         }
+        __syncwarp();
     }
 }
 
@@ -519,7 +575,16 @@ cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     const int grid = (n + kDescWarps - 1) / kDescWarps;
-    const size_t sm = sizeof(float) * a.T * a.T * NP * N1;
+    const size_t sm = sizeof(float) * a.T * a.T * NP * Fuse<N1>::N1P;
+    static int limit_fwd = 0, limit_bwd = 0;  // raised once, before any graph capture
+    int& lim = fwd ? limit_fwd : limit_bwd;
+    if ((int)sm > lim && sm > 48 * 1024) {
+        const cudaError_t e =
+            fwd ? cudaFuncSetAttribute(k_radial_fwd<NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                : cudaFuncSetAttribute(k_radial_bwd<NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        lim = (int)sm;
+    }
     if (fwd) k_radial_fwd<NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
     else k_radial_bwd<NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
     return cudaGetLastError();
@@ -531,7 +596,7 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     const int grid = (n + kDescWarps - 1) / kDescWarps;
-    const size_t wbytes = sizeof(float) * (((size_t)a.T * a.T * NP * N1 + 3) & ~(size_t)3);
+    const size_t wbytes = sizeof(float) * ((size_t)a.T * a.T * NP * Fuse<N1>::N1P);
     const size_t sm = wbytes + sizeof(float) * kDescWarps * (fwd ? S::FWD_WARP_FLOATS : S::BWD_WARP_FLOATS);
     // the shared-memory limit is raised once per kernel (before any graph capture: the
     // first evaluation of a layout always runs eagerly)
