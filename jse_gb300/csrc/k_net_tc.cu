@@ -204,17 +204,20 @@ __device__ __forceinline__ void issue_gemm(uint32_t tmem_d, uint32_t a_hi, uint3
 
 __device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + expf(-z)); }
 
+// Species t0 .. t0+nt-1 of one launch; all share one layout (D, H1, H2).  Tiles are
+// numbered species by species; a CTA stages a species' weights when its next tile
+// belongs to another species than the last one.
 struct TcParams {
     const int* perm;
-    const int* range;
-    int t;
+    const int* range;     // device: first slot of each species
+    int t0, nt;
     const float* fp;
     int fp_stride, D;
     float* gfp;
     double* e_atom;
-    double mu_e, sigma_e;
-    float bo;
-    const uint8_t* img;  // weight image (global)
+    const uint8_t* img[kMaxTypes];  // weight image per species (global)
+    float bo[kMaxTypes];
+    double mu_e[kMaxTypes], sigma_e[kMaxTypes];
     int* err;
 };
 
@@ -222,6 +225,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
+    __shared__ int s_tstart[kMaxTypes + 1];
     const int tid = threadIdx.x, warp = tid >> 5;
     const int Dp = L.Dp, H1 = L.H1, H2 = L.H2;
     uint8_t* sw = smem;                                       // weight image
@@ -231,11 +235,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
     const int ab = 2 * 128 * (H1 > H2 ? H1 : H2);             // bytes of one (hi or lo) activation image
     const float* fv = reinterpret_cast<const float*>(sw + L.fvec);
 
-    // stage the weight image
-    {
-        const uint4* src = reinterpret_cast<const uint4*>(p.img);
-        uint4* dst = reinterpret_cast<uint4*>(sw);
-        for (int q = tid; q < L.bytes / 16; q += kTcThreads) dst[q] = src[q];
+    if (tid == 0) {
+        s_tstart[0] = 0;
+        for (int t = 0; t < p.nt; ++t)
+            s_tstart[t + 1] = s_tstart[t] + (p.range[p.t0 + t + 1] - p.range[p.t0 + t] + 127) / 128;
     }
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
@@ -266,9 +269,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
     uint8_t* sx_lo = sx + 2 * 128 * (Dp > H1 ? Dp : H1);
     uint8_t* sa_lo = sa + ab;
 
-    const int s0 = p.range[p.t], s1 = p.range[p.t + 1];
-    const int ntiles = (s1 - s0 + 127) / 128;
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    const int total = s_tstart[p.nt];
+    int staged = -1;
+    for (int gt = blockIdx.x; gt < total && ok; gt += gridDim.x) {
+        int ts = 0;
+        while (gt >= s_tstart[ts + 1]) ++ts;
+        const int tile = gt - s_tstart[ts];
+        if (ts != staged) {  // stage this species' weight image (no MMA is in flight here)
+            __syncthreads();
+            const uint4* src = reinterpret_cast<const uint4*>(p.img[ts]);
+            uint4* dst = reinterpret_cast<uint4*>(sw);
+            for (int q = tid; q < L.bytes / 16; q += kTcThreads) dst[q] = src[q];
+            fence_async_smem();
+            __syncthreads();
+            staged = ts;
+        }
+        const int s0 = p.range[p.t0 + ts], s1 = p.range[p.t0 + ts + 1];
         const int row = tid;
         const int slot = s0 + tile * 128 + row;
         const bool valid = slot < s1;
@@ -319,7 +335,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         if (!ok) break;
         fence_after();
         // ---- energy and dZ2 = sigma_E w_o silu'(Z2 + b2)
-        const float se = (float)p.sigma_e;
+        const float se = (float)p.sigma_e[ts];
         float e = 0.f;
         for (int c0 = 0; c0 < H2; c0 += 16) {
             float z[16];
@@ -335,7 +351,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
             store_split8(sa, sa_lo, row, c0, H2, z);
             store_split8(sa, sa_lo, row, c0 + 8, H2, z + 8);
         }
-        if (valid) p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo) * p.sigma_e + p.mu_e;
+        if (valid) p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
         fence_before();
         fence_async_smem();
         __syncthreads();
@@ -450,11 +466,16 @@ void net_tc_release(NetTC& tc) {
     tc.ready = false;
 }
 
-cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_count, cudaStream_t st) {
-    if (!tc.ready) return cudaErrorNotSupported;
-    const int n = a.nmax;
+cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int* err, int sm_count,
+                          cudaStream_t st) {
+    if (nt < 1 || nt > kMaxTypes) return cudaErrorInvalidValue;
+    for (int k = 0; k < nt; ++k) {
+        if (!tc[k]->ready) return cudaErrorNotSupported;
+        if (tc[k]->D != tc[0]->D || tc[k]->H1 != tc[0]->H1 || tc[k]->H2 != tc[0]->H2) return cudaErrorInvalidValue;
+    }
+    const int n = a[0].nmax;
     if (n <= 0) return cudaSuccess;
-    const TCLayout L = make_layout(tc.D, tc.H1, tc.H2);
+    const TCLayout L = make_layout(tc[0]->D, tc[0]->H1, tc[0]->H2);
     const int xbytes = align1k(2 * 2 * 128 * (L.Dp > L.H1 ? L.Dp : L.H1));
     const int abytes = align1k(2 * 2 * 128 * (L.H1 > L.H2 ? L.H1 : L.H2));
     const size_t sm = (size_t)L.bytes + xbytes + abytes;
@@ -465,20 +486,24 @@ cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_co
         limit = (int)sm;
     }
     TcParams p;
-    p.perm = a.perm;
-    p.range = a.range;
-    p.t = a.t;
-    p.fp = a.fp;
-    p.fp_stride = a.fp_stride;
-    p.D = tc.D;
-    p.gfp = a.gfp;
-    p.e_atom = a.e_atom;
-    p.mu_e = a.mu_e;
-    p.sigma_e = a.sigma_e;
-    p.bo = tc.bo;
-    p.img = reinterpret_cast<const uint8_t*>(tc.blob);
+    std::memset(&p, 0, sizeof p);
+    p.perm = a[0].perm;
+    p.range = a[0].range;
+    p.t0 = a[0].t;
+    p.nt = nt;
+    p.fp = a[0].fp;
+    p.fp_stride = a[0].fp_stride;
+    p.D = tc[0]->D;
+    p.gfp = a[0].gfp;
+    p.e_atom = a[0].e_atom;
+    for (int k = 0; k < nt; ++k) {
+        p.img[k] = reinterpret_cast<const uint8_t*>(tc[k]->blob);
+        p.bo[k] = tc[k]->bo;
+        p.mu_e[k] = a[k].mu_e;
+        p.sigma_e[k] = a[k].sigma_e;
+    }
     p.err = err;
-    const int ntiles = (n + 127) / 128;
+    const int ntiles = (n + 127) / 128 + nt;  // upper bound of the tiles over all species
     const int grid = ntiles < sm_count ? ntiles : sm_count;
     k_net_tc<<<grid, kTcThreads, sm, st>>>(p, L);
     return cudaGetLastError();

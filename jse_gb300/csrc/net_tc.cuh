@@ -21,7 +21,10 @@ struct NetTC {
 // shape is outside what the kernel implements.
 bool net_tc_prepare(const Species& sp, NetTC& tc, std::string& why);
 void net_tc_release(NetTC& tc);
-// err receives ERRBIT_TIMEOUT if a bounded wait on the tensor cores gave up.
-cudaError_t launch_net_tc(const NetArgs& a, const NetTC& tc, int* err, int sm_count, cudaStream_t st);
+// One launch over nt consecutive species a[k].t = a[0].t + k, all with the same network
+// shape (D, H1, H2).  err receives ERRBIT_TIMEOUT if a bounded wait on the tensor cores
+// gave up.
+cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int* err, int sm_count,
+                          cudaStream_t st);
 
 }  // namespace nnapgb

@@ -377,9 +377,10 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     descriptors(true);
     h->mark(2);
     if (!fp_only && n > 0) {
+        std::vector<NetArgs> args(T);
         for (int t = 0; t < T; ++t) {
             const NetDev& nd = h->nets[t];
-            NetArgs a;
+            NetArgs& a = args[t];
             a.perm = h->perm.p;
             a.range = h->type_start.p;
             a.t = t;
@@ -394,9 +395,23 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
             a.sigma_e = nd.sigma_e;
             a.e_atom = h->e_atom.p;
             a.gfp = h->gfp.p;
-            if (h->precision == NNAP_PREC_MIXED) CK(launch_net_tc(a, nd.tc, h->status.p, h->sm_count, st));
-            else CK(launch_net_fp32(a, st));
-            ++h->launches;
+            if (h->precision != NNAP_PREC_MIXED) {
+                CK(launch_net_fp32(a, st));
+                ++h->launches;
+            }
+        }
+        if (h->precision == NNAP_PREC_MIXED) {
+            // one launch per run of consecutive species with the same network shape
+            for (int t = 0; t < T;) {
+                int u = t + 1;
+                const NetTC& a0 = h->nets[t].tc;
+                while (u < T && h->nets[u].tc.D == a0.D && h->nets[u].tc.H1 == a0.H1 && h->nets[u].tc.H2 == a0.H2) ++u;
+                const NetTC* tcs[kMaxTypes];
+                for (int k = t; k < u; ++k) tcs[k - t] = &h->nets[k].tc;
+                CK(launch_net_tc(&args[t], tcs, u - t, h->status.p, h->sm_count, st));
+                ++h->launches;
+                t = u;
+            }
         }
     }
     h->mark(3);
