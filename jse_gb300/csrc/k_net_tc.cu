@@ -36,7 +36,8 @@ namespace nnapgb {
 
 namespace {
 
-constexpr int kTcThreads = 128;
+constexpr int kRowSplit = 4;                 // threads per tile row in the epilogues
+constexpr int kTcThreads = 128 * kRowSplit;  // warp w reads TMEM lanes 32 * (w % 4) ..
 
 struct TCLayout {
     int Dp, H1, H2;
@@ -227,6 +228,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
     __shared__ uint32_t tmem_base;
     __shared__ int s_tstart[kMaxTypes + 1];
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int part = tid >> 7;  // column share of this thread in the epilogues
+    __shared__ float s_e[kRowSplit][128];
     const int Dp = L.Dp, H1 = L.H1, H2 = L.H2;
     uint8_t* sw = smem;                                       // weight image
     uint8_t* sx = smem + L.bytes;                             // X / dZ1 operand (hi, lo)
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
     __syncthreads();
     fence_after();
     const uint32_t tbase = tmem_base;
-    const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
+    const uint32_t tlane = tbase + ((uint32_t)((warp & 3) * 32) << 16);
     const uint32_t mb = smem_u32(&mbar);
     uint32_t phase = 0;
     bool ok = true;
@@ -285,12 +288,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
             staged = ts;
         }
         const int s0 = p.range[p.t0 + ts], s1 = p.range[p.t0 + ts + 1];
-        const int row = tid;
+        const int row = tid & 127;
         const int slot = s0 + tile * 128 + row;
         const bool valid = slot < s1;
         // ---- X = (fp - mu) / sigma, split into hi / lo
         const float* frow = p.fp + (size_t)(valid ? slot : s0) * p.fp_stride;
-        for (int k0 = 0; k0 < Dp; k0 += 8) {
+        for (int k0 = 8 * part; k0 < Dp; k0 += 8 * kRowSplit) {
             float v[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -311,7 +314,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         if (!ok) break;
         fence_after();
         // ---- A1 = silu(Z1 + b1)
-        for (int c0 = 0; c0 < H1; c0 += 16) {
+        for (int c0 = 16 * part; c0 < H1; c0 += 16 * kRowSplit) {
             float z[16];
             tmem_ld16(tlane + L.z1 + c0, z);
 #pragma unroll
@@ -337,7 +340,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         // ---- energy and dZ2 = sigma_E w_o silu'(Z2 + b2)
         const float se = (float)p.sigma_e[ts];
         float e = 0.f;
-        for (int c0 = 0; c0 < H2; c0 += 16) {
+        for (int c0 = 16 * part; c0 < H2; c0 += 16 * kRowSplit) {
             float z[16];
             tmem_ld16(tlane + L.z2 + c0, z);
 #pragma unroll
@@ -351,7 +354,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
             store_split8(sa, sa_lo, row, c0, H2, z);
             store_split8(sa, sa_lo, row, c0 + 8, H2, z + 8);
         }
-        if (valid) p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
+        s_e[part][row] = e;
         fence_before();
         fence_async_smem();
         __syncthreads();
@@ -364,8 +367,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         phase ^= 1;
         if (!ok) break;
         fence_after();
+        if (part == 0 && valid) {  // energy: the four column shares added in a fixed order
+            float e = s_e[0][row];
+#pragma unroll
+            for (int q = 1; q < kRowSplit; ++q) e += s_e[q][row];
+            p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
+        }
         // ---- dZ1 = dA1 * silu'(Z1 + b1)
-        for (int c0 = 0; c0 < H1; c0 += 16) {
+        for (int c0 = 16 * part; c0 < H1; c0 += 16 * kRowSplit) {
             float g[16], z[16];
             tmem_ld16(tlane + L.da1 + c0, g);
             tmem_ld16(tlane + L.z1 + c0, z);
@@ -392,7 +401,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         fence_after();
         // ---- dE/dfp = dX / sigma
         float* grow = p.gfp + (size_t)(valid ? slot : s0) * p.fp_stride;
-        for (int c0 = 0; c0 < Dp; c0 += 16) {
+        for (int c0 = 16 * part; c0 < Dp; c0 += 16 * kRowSplit) {
             float g[16];
             tmem_ld16(tlane + L.dx + c0, g);
 #pragma unroll
