@@ -278,13 +278,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from jse_gb300.replicas import barrier, init_from_env, max_over_ranks, whole_job_rate
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("gloo")
+    dist, rank, world = init_from_env("gloo")
 
     structures, cfg = make_workload(args.workload)
     natoms_step = sum(s.natoms for s in structures)
@@ -355,8 +351,7 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.2)
-    if dist:
-        dist.barrier()
+    barrier(dist)
     torch.cuda.synchronize(dev)
     ms, stages, launches, stage_ok = [], np.zeros(5), 0, True
     t_wall = time.perf_counter()
@@ -377,15 +372,10 @@ def main():
         launches += pot.lastLaunchCount()
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall
-    if dist:
-        dist.barrier()
+    barrier(dist)
     clk = clocks.stop()
-    t_dev = sum(ms) / 1e3
-    if dist:
-        tt = torch.tensor([t_dev])
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt[0])
-    value = natoms_step * args.steps * world / t_dev
+    t_dev = max_over_ranks(sum(ms) / 1e3, dist)
+    value = whole_job_rate(natoms_step, args.steps, world, t_dev)
     stages /= args.steps
 
     # end to end through host buffers (pinned)
