@@ -97,9 +97,10 @@ int nnap_compute(nnap_handle* h, int natoms, const double* x, const int* type, i
 
 /* Same computation on device-resident buffers; x, type, and every output are device
  * pointers, box stays a host array.  Work is ordered after `stream` (a cudaStream_t; NULL
- * is CUDA's default stream) and `stream` is made to wait for the results.  The call synchronises the
- * handle's stream once, after the neighbour build, to validate the neighbour capacity
- * and read the species ranges; the rest is queued and the call returns before it ends. */
+ * is CUDA's default stream) and `stream` is made to wait for the results.  The whole
+ * evaluation is queued without intermediate host synchronisation; the call then waits
+ * for it once, to read the error and neighbour-capacity word (an overflowing capacity
+ * is grown and the evaluation repeated). */
 int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int* d_type, int box_kind,
                         const double* box, int flags, double* d_energy, double* d_energies, double* d_forces,
                         double* d_virial, double* d_virials, void* stream);
@@ -148,6 +149,20 @@ int nnap_set_profiling(nnap_handle* h, int on);
  * reference).  The first call of a layout (atom counts, box kinds, cell grids, buffer
  * addresses) runs eagerly, the second is captured, later ones replay the graph. */
 int nnap_set_graphs(nnap_handle* h, int on);
+/* Launch-shape autotuning (no counterpart in the reference).  Evaluations are grouped
+ * into atom-count buckets, natoms in [2^b, 2^(b+1)).  With autotuning on, the first
+ * evaluation of a bucket that has no shapes yet times the candidates of each stage on
+ * the caller's own batch (warps per CTA 2/4/8 of the descriptor forward, descriptor
+ * backward and neighbour kernels; 64/128/256 threads per CTA of the gather; 2 or 4
+ * threads per row of the tensor-core network) and keeps the fastest; later evaluations
+ * of the bucket reuse them.  Off by default; untuned buckets use 4, 4, 4, 128, 4. */
+int nnap_set_autotune(nnap_handle* h, int on);
+/* Shapes used for natoms atoms: [descriptor forward warps, descriptor backward warps,
+ * neighbour warps, gather threads, network threads per row]; *tuned = 1 when the
+ * bucket has tuned (or installed) shapes, 0 for the defaults.  tuned may be NULL. */
+int nnap_get_tuning(nnap_handle* h, int natoms, int* shapes5, int* tuned);
+/* Install shapes for the bucket of natoms (e.g. saved from an earlier run). */
+int nnap_set_tuning(nnap_handle* h, int natoms, const int* shapes5);
 int nnap_stage_times(nnap_handle* h, double* ms5);
 
 /* Per-atom neighbour counts of one structure without allocating any memory.  This entry

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -35,7 +36,15 @@ __global__ void k_gather(PairBufs, int, double*, double*);
 __global__ void k_reduce_chunks(const int*, const int*, const double*, const double*, double*);
 __global__ void k_reduce_structs(const int*, int, const double*, double*, double*);
 
-constexpr int kNbWarps = 4;       // must match k_struct.cu
+// Launch shapes chosen per atom-count bucket by the autotuner (defaults below).
+struct Tuning {
+    int desc_fwd_warps = 4;  // warps per CTA of the descriptor forward kernels
+    int desc_bwd_warps = 4;  // warps per CTA of the descriptor backward kernels
+    int nb_warps = 4;        // warps per CTA of the neighbour kernel
+    int gather_block = 128;  // threads per CTA of the force / virial gather
+    int net_split = 4;       // threads per tile row of the tensor-core network (2 or 4)
+};
+constexpr int kTuneParams = 5;
 constexpr int kSortBlock = 256;   // must match k_struct.cu
 constexpr int kRedBlock = 256;    // must match k_struct.cu
 constexpr int kRedChunk = 1024;   // atoms per reduction chunk
@@ -153,6 +162,10 @@ struct nnap_handle {
     size_t h_sdev_cap = 0;
     int sm_count = 148;
     cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // launch shapes: the ones in use, and the autotuner's choice per atom-count bucket
+    nnapgb::Tuning tune;
+    bool autotune = false;
+    std::map<int, nnapgb::Tuning> tuned;
     bool capturing = false;
     void mark(int k) {
         // inside stream capture an ordinary record is only a dependency marker; an external

@@ -23,6 +23,7 @@ struct DescArgs {
     float* A;               // spherical only: [slot - range[t0]][NP][K] expansion coefficients
     const float* gfp;       // backward: dE/dfp by slot (same layout as fp)
     int accumulate;         // backward: add into P.g instead of overwriting
+    int warps;              // warps per CTA (2, 4 or 8; one atom slot per warp)
 };
 
 cudaError_t upload_sh_constants();

@@ -57,7 +57,7 @@ cudaError_t upload_sh_constants() {
 
 namespace {
 
-constexpr int kDescWarps = 4;
+constexpr int kDescMaxWarps = 8;  // warps per CTA are a launch parameter (2, 4 or 8)
 constexpr float kPi4 = 12.566370614359172f;
 
 __host__ __device__ constexpr int tri(int l, int m) { return l * (l + 1) / 2 + m; }
@@ -215,11 +215,11 @@ __device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { re
 
 // =========================================================================== radial
 template <int NP, int N1>
-__global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
+__global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
     extern __shared__ float sW[];
     load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
-    const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
     const int at = atom_of(a, s0, w);
@@ -252,11 +252,11 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_radial_fwd(DescArgs a) {
 }
 
 template <int NP, int N1>
-__global__ void __launch_bounds__(32 * kDescWarps) k_radial_bwd(DescArgs a) {
+__global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_bwd(DescArgs a) {
     extern __shared__ float sW[];
     load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
-    const int w = blockIdx.x * kDescWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
     const int at = atom_of(a, s0, w);
@@ -313,7 +313,7 @@ struct SphShape {
 };
 
 template <int L, int NP, int N1>
-__global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
+__global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
     using S = SphShape<L, NP>;
     extern __shared__ float smem[];
     const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
     load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = blockIdx.x * kDescWarps + wl;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wl;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
     float* sY = smem + ((nW + 3) & ~3) + wl * S::FWD_WARP_FLOATS;  // [32][KS]
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(32 * kDescWarps) k_sph_fwd(DescArgs a) {
 // as v_n = sum_p dc_p W[p][n], so dfc = v . T and drn = v . dT.  Registers stay at or
 // below 128 per thread (four CTAs of four warps per SM).
 template <int L, int NP, int N1>
-__global__ void __launch_bounds__(32 * kDescWarps, 4) k_sph_bwd(DescArgs a) {
+__global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
     using S = SphShape<L, NP>;
     extern __shared__ float smem[];
     const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(32 * kDescWarps, 4) k_sph_bwd(DescArgs a) {
     load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = blockIdx.x * kDescWarps + wl;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wl;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
     float* sG = smem + nW + wl * S::BWD_WARP_FLOATS;  // [K][NPS]
@@ -574,7 +574,8 @@ template <int NP, int N1>
 cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
-    const int grid = (n + kDescWarps - 1) / kDescWarps;
+    const int wpc = a.warps;
+    const int grid = (n + wpc - 1) / wpc;
     const size_t sm = sizeof(float) * a.T * a.T * NP * Fuse<N1>::N1P;
     static int limit_fwd = 0, limit_bwd = 0;  // raised once, before any graph capture
     int& lim = fwd ? limit_fwd : limit_bwd;
@@ -585,8 +586,8 @@ cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    if (fwd) k_radial_fwd<NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
-    else k_radial_bwd<NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    if (fwd) k_radial_fwd<NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
+    else k_radial_bwd<NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
     return cudaGetLastError();
 }
 
@@ -595,9 +596,10 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     using S = SphShape<L, NP>;
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
-    const int grid = (n + kDescWarps - 1) / kDescWarps;
+    const int wpc = a.warps;
+    const int grid = (n + wpc - 1) / wpc;
     const size_t wbytes = sizeof(float) * ((size_t)a.T * a.T * NP * Fuse<N1>::N1P);
-    const size_t sm = wbytes + sizeof(float) * kDescWarps * (fwd ? S::FWD_WARP_FLOATS : S::BWD_WARP_FLOATS);
+    const size_t sm = wbytes + sizeof(float) * wpc * (fwd ? S::FWD_WARP_FLOATS : S::BWD_WARP_FLOATS);
     // the shared-memory limit is raised once per kernel (before any graph capture: the
     // first evaluation of a layout always runs eagerly)
     static int limit_fwd = 0, limit_bwd = 0;
@@ -609,8 +611,8 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    if (fwd) k_sph_fwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
-    else k_sph_bwd<L, NP, N1><<<grid, 32 * kDescWarps, sm, st>>>(a);
+    if (fwd) k_sph_fwd<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
+    else k_sph_bwd<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -39,8 +39,8 @@ namespace {
 
 using namespace ::nnapgb::tc;
 
-constexpr int kRowSplit = 4;                 // threads per tile row in the epilogues
-constexpr int kTcThreads = 128 * kRowSplit;  // warp w reads TMEM lanes 32 * (w % 4) ..
+// SPLIT threads per tile row in the epilogues (a launch parameter: 2 or 4); warp w
+// reads TMEM lanes 32 * (w % 4) .. 32 * (w % 4) + 31.
 
 struct TCLayout {
     int Dp, H1, H2;
@@ -131,14 +131,15 @@ struct TcParams {
     int* err;
 };
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L) {
+template <int SPLIT>
+__global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout L) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int s_tstart[kMaxTypes + 1];
     const int tid = threadIdx.x, warp = tid >> 5;
     const int part = tid >> 7;  // column share of this thread in the epilogues
-    __shared__ float s_e[kRowSplit][128];
+    __shared__ float s_e[SPLIT][128];
     const int Dp = L.Dp, H1 = L.H1, H2 = L.H2;
     uint8_t* sw = smem;                                       // weight image
     uint8_t* sx = smem + L.bytes;                             // X / dZ1 operand (hi, lo)
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
             __syncthreads();
             const uint4* src = reinterpret_cast<const uint4*>(p.img[ts]);
             uint4* dst = reinterpret_cast<uint4*>(sw);
-            for (int q = tid; q < L.bytes / 16; q += kTcThreads) dst[q] = src[q];
+            for (int q = tid; q < L.bytes / 16; q += (128 * SPLIT)) dst[q] = src[q];
             fence_async_smem();
             __syncthreads();
             staged = ts;
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         const bool valid = slot < s1;
         // ---- X = (fp - mu) / sigma, split into hi / lo
         const float* frow = p.fp + (size_t)(valid ? slot : s0) * p.fp_stride;
-        for (int k0 = 8 * part; k0 < Dp; k0 += 8 * kRowSplit) {
+        for (int k0 = 8 * part; k0 < Dp; k0 += 8 * SPLIT) {
             float v[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         if (!ok) break;
         fence_after();
         // ---- A1 = silu(Z1 + b1)
-        for (int c0 = 16 * part; c0 < H1; c0 += 16 * kRowSplit) {
+        for (int c0 = 16 * part; c0 < H1; c0 += 16 * SPLIT) {
             float z[16];
             tmem_ld16(tlane + L.z1 + c0, z);
 #pragma unroll
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         // ---- energy and dZ2 = sigma_E w_o silu'(Z2 + b2)
         const float se = (float)p.sigma_e[ts];
         float e = 0.f;
-        for (int c0 = 16 * part; c0 < H2; c0 += 16 * kRowSplit) {
+        for (int c0 = 16 * part; c0 < H2; c0 += 16 * SPLIT) {
             float z[16];
             tmem_ld16(tlane + L.z2 + c0, z);
 #pragma unroll
@@ -279,11 +280,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         if (part == 0 && valid) {  // energy: the four column shares added in a fixed order
             float e = s_e[0][row];
 #pragma unroll
-            for (int q = 1; q < kRowSplit; ++q) e += s_e[q][row];
+            for (int q = 1; q < SPLIT; ++q) e += s_e[q][row];
             p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
         }
         // ---- dZ1 = dA1 * silu'(Z1 + b1)
-        for (int c0 = 16 * part; c0 < H1; c0 += 16 * kRowSplit) {
+        for (int c0 = 16 * part; c0 < H1; c0 += 16 * SPLIT) {
             float g[16], z[16];
             tmem_ld16(tlane + L.da1 + c0, g);
             tmem_ld16(tlane + L.z1 + c0, z);
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_net_tc(TcParams p, TCLayout L
         fence_after();
         // ---- dE/dfp = dX / sigma
         float* grow = p.gfp + (size_t)(valid ? slot : s0) * p.fp_stride;
-        for (int c0 = 16 * part; c0 < Dp; c0 += 16 * kRowSplit) {
+        for (int c0 = 16 * part; c0 < Dp; c0 += 16 * SPLIT) {
             float g[16];
             tmem_ld16(tlane + L.dx + c0, g);
 #pragma unroll
@@ -384,7 +385,7 @@ void net_tc_release(NetTC& tc) {
     tc.ready = false;
 }
 
-cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int* err, int sm_count,
+cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int* err, int sm_count, int split,
                           cudaStream_t st) {
     if (nt < 1 || nt > kMaxTypes) return cudaErrorInvalidValue;
     for (int k = 0; k < nt; ++k) {
@@ -397,9 +398,13 @@ cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int*
     const int xbytes = align1k(2 * 2 * 128 * (L.Dp > L.H1 ? L.Dp : L.H1));
     const int abytes = align1k(2 * 2 * 128 * (L.H1 > L.H2 ? L.H1 : L.H2));
     const size_t sm = (size_t)L.bytes + xbytes + abytes;
-    static int limit = 0;
+    if (split != 2 && split != 4) return cudaErrorInvalidValue;
+    static int limit2 = 0, limit4 = 0;  // raised once per instantiation, before any graph capture
+    int& limit = split == 2 ? limit2 : limit4;
     if ((int)sm > limit) {
-        const cudaError_t e = cudaFuncSetAttribute(k_net_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        const cudaError_t e =
+            split == 2 ? cudaFuncSetAttribute(k_net_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                       : cudaFuncSetAttribute(k_net_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         limit = (int)sm;
     }
@@ -423,7 +428,8 @@ cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int*
     p.err = err;
     const int ntiles = (n + 127) / 128 + nt;  // upper bound of the tiles over all species
     const int grid = ntiles < sm_count ? ntiles : sm_count;
-    k_net_tc<<<grid, kTcThreads, sm, st>>>(p, L);
+    if (split == 2) k_net_tc<2><<<grid, 256, sm, st>>>(p, L);
+    else k_net_tc<4><<<grid, 512, sm, st>>>(p, L);
     return cudaGetLastError();
 }
 

@@ -133,19 +133,19 @@ __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int
 // of 32 cells the candidates are spread over the lanes, screened in FP32 against
 // rc^2 plus a rounding margin, and confirmed with the exact FP64 test.  Accepted
 // pairs are compacted in candidate order with a ballot, so rows are deterministic.
-constexpr int kNbWarps = 4;
+constexpr int kNbMaxWarps = 8;  // warps per CTA are a launch parameter (2, 4 or 8)
 
-__global__ void __launch_bounds__(32 * kNbWarps)
+__global__ void __launch_bounds__(32 * kNbMaxWarps)
 k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ xw,
             const float4* __restrict__ xf, const float4* __restrict__ xlo, const int* __restrict__ cell_of,
             const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, int n, PairBufs P,
             int* __restrict__ err, int* __restrict__ max_count) {
-    __shared__ int s_incl[kNbWarps][32], s_start[kNbWarps][32];
-    __shared__ uint32_t s_img[kNbWarps][32];
-    __shared__ double s_sh[kNbWarps][32][3];
-    __shared__ float s_fsh[kNbWarps][32][3], s_flo[kNbWarps][32][3];
+    __shared__ int s_incl[kNbMaxWarps][32], s_start[kNbMaxWarps][32];
+    __shared__ uint32_t s_img[kNbMaxWarps][32];
+    __shared__ double s_sh[kNbMaxWarps][32][3];
+    __shared__ float s_fsh[kNbMaxWarps][32][3], s_flo[kNbMaxWarps][32][3];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = blockIdx.x * kNbWarps + w;
+    const int i = blockIdx.x * (blockDim.x >> 5) + w;
     if (i >= n) return;
     const StructDev& st = S[sid[i]];
     const int M = P.M;

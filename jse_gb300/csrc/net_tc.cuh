@@ -24,7 +24,8 @@ void net_tc_release(NetTC& tc);
 // One launch over nt consecutive species a[k].t = a[0].t + k, all with the same network
 // shape (D, H1, H2).  err receives ERRBIT_TIMEOUT if a bounded wait on the tensor cores
 // gave up.
-cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int* err, int sm_count,
+// split: threads per tile row in the epilogues (2 or 4).
+cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int* err, int sm_count, int split,
                           cudaStream_t st);
 
 }  // namespace nnapgb

@@ -314,7 +314,8 @@ void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const 
     if (n > 0) {
         k_fill_cells<<<(n + 255) / 256, 256, 0, st>>>(h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p);
         k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
-        k_neighbors<<<(n + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
+        const int nw = h->tune.nb_warps;
+        k_neighbors<<<(n + nw - 1) / nw, 32 * nw, 0, st>>>(
             h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
             pair_bufs(h), h->status.p, h->status.p + 1);
         h->launches += 3;
@@ -367,6 +368,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 }
                 a.gfp = h->gfp.p;
                 a.accumulate = k > 0;
+                a.warps = fwd ? h->tune.desc_fwd_warps : h->tune.desc_bwd_warps;
                 if (n > 0) {
                     CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, st));
                     ++h->launches;
@@ -408,7 +410,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 while (u < T && h->nets[u].tc.D == a0.D && h->nets[u].tc.H1 == a0.H1 && h->nets[u].tc.H2 == a0.H2) ++u;
                 const NetTC* tcs[kMaxTypes];
                 for (int k = t; k < u; ++k) tcs[k - t] = &h->nets[k].tc;
-                CK(launch_net_tc(&args[t], tcs, u - t, h->status.p, h->sm_count, st));
+                CK(launch_net_tc(&args[t], tcs, u - t, h->status.p, h->sm_count, h->tune.net_split, st));
                 ++h->launches;
                 t = u;
             }
@@ -419,7 +421,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     h->mark(4);
     if (!fp_only) {
         if (n > 0) {
-            k_gather<<<(n + 127) / 128, 128, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
+            const int gb = h->tune.gather_block;
+            k_gather<<<(n + gb - 1) / gb, gb, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
             ++h->launches;
         }
         const int nchunks = (int)B.cb.size();
@@ -455,7 +458,9 @@ void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_typ
 // Identity of a launch sequence: what the captured graph depends on.
 std::vector<long long> layout_key(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
     std::vector<long long> k = {B.nstruct, B.natoms, B.ncells, h->M, (long long)(intptr_t)d_x,
-                                (long long)(intptr_t)d_type, fp_only ? 1 : 0, h->profiling ? 1 : 0};
+                                (long long)(intptr_t)d_type, fp_only ? 1 : 0, h->profiling ? 1 : 0,
+                                h->tune.desc_fwd_warps, h->tune.desc_bwd_warps, h->tune.nb_warps,
+                                h->tune.gather_block, h->tune.net_split};
     for (auto& s : B.sd) {
         k.push_back(s.n);
         k.push_back(s.kind);
@@ -470,10 +475,100 @@ void drop_graph(nnap_handle* h) {
     h->gkey.clear();
 }
 
+// Atom-count bucket of the autotuner: natoms in [2^b, 2^(b+1)).
+int size_bucket(int natoms) {
+    int b = 0;
+    while (b < 30 && (2 << b) <= natoms) ++b;
+    return b;
+}
+
+bool valid_tuning(const Tuning& t) {
+    auto in = [](int v, std::initializer_list<int> c) { return std::find(c.begin(), c.end(), v) != c.end(); };
+    return in(t.desc_fwd_warps, {2, 4, 8}) && in(t.desc_bwd_warps, {2, 4, 8}) && in(t.nb_warps, {2, 4, 8}) &&
+           in(t.gather_block, {64, 128, 256}) && in(t.net_split, {2, 4});
+}
+
+// Device milliseconds of the five stages of one eager evaluation with the current shapes.
+void stage_ms(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, double* ms) {
+    enqueue(h, B, d_x, d_type, false);
+    CK(cudaStreamSynchronize(h->stream));
+    const int bits = h->h_status[0];
+    if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
+    if (bits & ERRBIT_TIMEOUT) throw ApiFail(NNAP_ERR_TIMEOUT, "a bounded tensor-core wait gave up");
+    for (int k = 0; k < 5; ++k) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, h->ev[k], h->ev[k + 1]));
+        ms[k] = t;
+    }
+}
+
+// Stage-by-stage search over the launch shapes: for each parameter in turn, every
+// candidate is timed (one warm-up, best of two) on the stage it governs with the other
+// parameters at their best values so far.  The inputs are the caller's own batch.
+Tuning tune_launches(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type) {
+    for (auto& e : h->ev)
+        if (!e) CK(cudaEventCreate(&e));
+    const bool prof = h->profiling;
+    h->profiling = true;
+    drop_graph(h);
+    Tuning best = h->tune;
+    auto score = [&](const Tuning& t, int stage) {
+        h->tune = t;
+        double ms[5], lo = 1e300;
+        stage_ms(h, B, d_x, d_type, ms);
+        for (int r = 0; r < 2; ++r) {
+            stage_ms(h, B, d_x, d_type, ms);
+            lo = std::min(lo, ms[stage]);
+        }
+        return lo;
+    };
+    struct Param {
+        int Tuning::*field;
+        int stage;
+        std::vector<int> cand;
+    };
+    std::vector<Param> params = {{&Tuning::nb_warps, 0, {2, 4, 8}},
+                                 {&Tuning::desc_fwd_warps, 1, {2, 4, 8}},
+                                 {&Tuning::desc_bwd_warps, 3, {2, 4, 8}},
+                                 {&Tuning::gather_block, 4, {64, 128, 256}}};
+    if (h->precision == NNAP_PREC_MIXED) params.push_back({&Tuning::net_split, 2, {2, 4}});
+    try {
+        for (auto& p : params) {
+            int bv = best.*(p.field);
+            double bt = 1e300;
+            for (int v : p.cand) {
+                Tuning t = best;
+                t.*(p.field) = v;
+                const double x = score(t, p.stage);
+                if (x < bt) {
+                    bt = x;
+                    bv = v;
+                }
+            }
+            best.*(p.field) = bv;
+        }
+    } catch (...) {
+        h->profiling = prof;
+        throw;
+    }
+    h->profiling = prof;
+    h->tune = best;
+    return best;
+}
+
 // Evaluate a planned batch whose inputs are on the device.  The first call of a layout
 // runs eagerly and validates the neighbour capacity; the second captures the launch
 // sequence into a CUDA graph; later calls replay it.  Synchronises before returning.
 void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only) {
+    // launch shapes of this atom-count bucket (tuned now if autotuning is on and the bucket is new)
+    int tune_bucket = -1;
+    {
+        const int b = size_bucket(B.natoms);
+        auto it = h->tuned.find(b);
+        if (it != h->tuned.end()) h->tune = it->second;
+        else if (h->autotune && !fp_only && B.natoms > 0) tune_bucket = b;
+        else h->tune = Tuning();
+    }
     const bool same_layout = h->layout_ok && h->last_layout == layout_key(h, B, nullptr, nullptr, fp_only);
     if (!same_layout) {
         drop_graph(h);
@@ -519,6 +614,14 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
         const int maxc = h->h_status[1];
         if (maxc <= h->M) {
             if (bits & ERRBIT_NO_MIRROR) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
+            if (tune_bucket >= 0) {
+                h->tuned[tune_bucket] = tune_launches(h, B, d_x, d_type);
+                // the outputs of this call come from the chosen shapes
+                enqueue(h, B, d_x, d_type, fp_only);
+                CK(cudaStreamSynchronize(h->stream));
+                h->last_layout = layout_key(h, B, nullptr, nullptr, fp_only);
+                h->layout_runs = 1;
+            }
             return;
         }
         // neighbour rows overflowed: grow the capacity and evaluate again
@@ -758,6 +861,45 @@ int nnap_compute_batch_device(nnap_handle* h, int nstruct, const int* natoms, co
         copy_out(h, B, flags, o, cudaMemcpyDeviceToDevice);
         CK(cudaEventRecord(h->order_ev, h->stream));
         CK(cudaStreamWaitEvent(user, h->order_ev, 0));
+        return NNAP_OK;
+    });
+}
+
+int nnap_set_autotune(nnap_handle* h, int on) {
+    return guarded(h, [&]() -> int {
+        h->autotune = on != 0;
+        return NNAP_OK;
+    });
+}
+
+int nnap_get_tuning(nnap_handle* h, int natoms, int* shapes5, int* tuned) {
+    if (!shapes5) return NNAP_ERR_ARG;
+    return guarded(h, [&]() -> int {
+        auto it = h->tuned.find(size_bucket(natoms));
+        const Tuning t = it != h->tuned.end() ? it->second : Tuning();
+        shapes5[0] = t.desc_fwd_warps;
+        shapes5[1] = t.desc_bwd_warps;
+        shapes5[2] = t.nb_warps;
+        shapes5[3] = t.gather_block;
+        shapes5[4] = t.net_split;
+        if (tuned) *tuned = it != h->tuned.end() ? 1 : 0;
+        return NNAP_OK;
+    });
+}
+
+int nnap_set_tuning(nnap_handle* h, int natoms, const int* shapes5) {
+    if (!shapes5) return NNAP_ERR_ARG;
+    return guarded(h, [&]() -> int {
+        Tuning t;
+        t.desc_fwd_warps = shapes5[0];
+        t.desc_bwd_warps = shapes5[1];
+        t.nb_warps = shapes5[2];
+        t.gather_block = shapes5[3];
+        t.net_split = shapes5[4];
+        if (!valid_tuning(t)) throw ApiFail(NNAP_ERR_ARG, "launch shapes outside the tuned candidates");
+        h->tuned[size_bucket(natoms)] = t;
+        drop_graph(h);
+        h->layout_ok = false;
         return NNAP_OK;
     });
 }

@@ -345,7 +345,8 @@ void step_impl(nnap_server* s, int nslots, const int* ids, const double* x, int 
             k_fill_cells<<<(nb_atoms + 255) / 256, 256, 0, st>>>(h->cell_of.p, nb_atoms, h->cell_start.p,
                                                                  h->cell_fill.p, h->cell_atoms.p);
             k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
-            k_neighbors<<<(nb_atoms + kNbWarps - 1) / kNbWarps, 32 * kNbWarps, 0, st>>>(
+            const int nw = h->tune.nb_warps;
+            k_neighbors<<<(nb_atoms + nw - 1) / nw, 32 * nw, 0, st>>>(
                 s->sdev_build.p, sid, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p,
                 nb_atoms, pair_bufs(h), h->status.p, h->status.p + 1);
             k_verlet_store<<<(unsigned)(((size_t)nb_atoms * 32 + 127) / 128), 128, 0, st>>>(s->dslots.p, sid,

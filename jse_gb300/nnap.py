@@ -40,7 +40,8 @@ EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes"
            "nnap_compute_fp", "nnap_neighbor_list", "nnap_last_launch_count", "nnap_set_profiling",
            "nnap_stage_times", "nnap_compute_batch_device", "nnap_set_graphs", "nnap_neighbor_counts_noalloc",
            "nnap_server_create", "nnap_server_destroy", "nnap_server_admit", "nnap_server_release",
-           "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats"]
+           "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats", "nnap_set_autotune",
+           "nnap_get_tuning", "nnap_set_tuning"]
 
 
 class IllegalStateError(RuntimeError):
@@ -85,6 +86,9 @@ def load_library(path: str = LIB_PATH):
     L.nnap_stage_times.argtypes = [P, dp]
     L.nnap_compute_batch_device.argtypes = [P, I, ip, P, P, ip, dp, I, P, P, P, P, P, P]
     L.nnap_set_graphs.argtypes = [P, I]
+    L.nnap_set_autotune.argtypes = [P, I]
+    L.nnap_get_tuning.argtypes = [P, I, ip, ip]
+    L.nnap_set_tuning.argtypes = [P, I, ip]
     L.nnap_server_create.argtypes = [P, D, S, I, C.POINTER(P)]
     L.nnap_server_destroy.argtypes = [P]
     L.nnap_server_admit.argtypes = [P, I, ip, I, dp, ip]
@@ -197,6 +201,25 @@ class NNAP:
     def setGraphs(self, on: bool):
         """CUDA-graph replay of repeated evaluations of the same layout (on by default)."""
         self._check(self._L.nnap_set_graphs(self._handle(), 1 if on else 0))
+
+    def setAutotune(self, on: bool):
+        """Tune launch shapes on the first evaluation of each atom-count bucket."""
+        self._check(self._L.nnap_set_autotune(self._handle(), 1 if on else 0))
+
+    TUNING_KEYS = ("desc_fwd_warps", "desc_bwd_warps", "nb_warps", "gather_block", "net_split")
+
+    def tuning(self, natoms: int) -> dict:
+        """Launch shapes used for ``natoms`` atoms (and whether they were tuned)."""
+        v = np.zeros(5, dtype=np.int32)
+        t = C.c_int()
+        self._check(self._L.nnap_get_tuning(self._handle(), int(natoms), _iptr(v), C.byref(t)))
+        d = dict(zip(self.TUNING_KEYS, (int(x) for x in v)))
+        d["tuned"] = bool(t.value)
+        return d
+
+    def setTuning(self, natoms: int, shapes: dict):
+        v = np.array([shapes[k] for k in self.TUNING_KEYS], dtype=np.int32)
+        self._check(self._L.nnap_set_tuning(self._handle(), int(natoms), _iptr(v)))
 
     def setProfiling(self, on: bool):
         self._check(self._L.nnap_set_profiling(self._handle(), 1 if on else 0))

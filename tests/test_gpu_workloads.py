@@ -112,3 +112,27 @@ def test_graph_replay_across_layout_changes():
                 o = p.calEnergyForceVirials(s)
                 assert np.array_equal(o["forces"], r["forces"])
                 assert o["energy"] == r["energy"]
+
+
+def test_autotuned_shapes_give_the_same_results():
+    """Launch shapes chosen by the autotuner change no neighbour row and no per-atom
+    arithmetic order except the network's energy split (<= 1e-9 eV/atom apart)."""
+    from jse_gb300.nnap import NNAP
+    s = W.random_liquid(3000, 0.060, [0.46, 0.46, 0.08], 2.0, 61, tilt=0.1)
+    model = W.model_for("c2")
+    with NNAP(model, precision="mixed") as p:
+        ref = p.calEnergyForceVirials(s, per_atom_virial=False)
+        assert p.tuning(s.natoms)["tuned"] is False
+        p.setAutotune(True)
+        got = p.calEnergyForceVirials(s, per_atom_virial=False)
+        t = p.tuning(s.natoms)
+        assert t["tuned"] is True
+        assert t["desc_fwd_warps"] in (2, 4, 8) and t["gather_block"] in (64, 128, 256) and t["net_split"] in (2, 4)
+        again = p.calEnergyForceVirials(s, per_atom_virial=False)
+        p.setTuning(100000, {"desc_fwd_warps": 8, "desc_bwd_warps": 2, "nb_warps": 8, "gather_block": 64,
+                             "net_split": 2})
+        assert p.tuning(120000)["tuned"] is True and p.tuning(120000)["nb_warps"] == 8
+    n = s.natoms
+    assert abs(got["energy"] - ref["energy"]) / n <= 1e-9
+    assert np.max(np.abs(got["forces"] - ref["forces"])) <= 1e-6
+    assert np.array_equal(got["forces"], again["forces"])
