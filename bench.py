@@ -275,6 +275,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-requests", type=int, default=5000)
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -314,7 +315,7 @@ def main():
     torch.cuda.set_device(local)
     model = normalised_model(cfg, structures, args.precision)
     pot = NNAP(model, precision=args.precision, device=local)
-    pot.setAutotune(True)  # launch shapes picked on the first (warm-up) step of the workload's size bucket
+    pot.setAutotune(not args.no_autotune)  # shapes picked on the first warm-up step of the size bucket
     dev = torch.device("cuda", local)
     s = structures[0]
     single = len(structures) == 1
