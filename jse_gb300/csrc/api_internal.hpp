@@ -110,13 +110,12 @@ struct NetDev {
     NetTC tc;  // tensor-core parameters (mixed precision)
 };
 
-// One planned evaluation: the structures, the structure of every atom and the
-// reduction chunks (chunk c covers atoms [cb[c], ce[c]); structure s owns chunks
-// [sc[s], sc[s+1])).
+// One planned evaluation: the structures and the reduction chunks (chunk c covers atoms
+// [cb[c], ce[c]); structure s owns chunks [sc[s], sc[s+1])).
 struct Batch {
     int nstruct = 0, natoms = 0, ncells = 0;
     std::vector<StructDev> sd;
-    std::vector<int> sid, cb, ce, sc;
+    std::vector<int> cb, ce, sc;
 };
 
 struct Outputs {
@@ -149,6 +148,8 @@ struct nnap_handle {
     nnapgb::DevBuf<int> prev, pcount;
     nnapgb::DevBuf<float> fp, gfp, A;
     int M = 0;
+    int GS = 0;                  // cell-offset groups per atom + 1 kept by k_neighbors (0: none)
+    nnapgb::DevBuf<int> gstart;  // [n][GS] group starts of each neighbour row
     int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
     bool profiling = false;
     cudaEvent_t order_ev = nullptr;

@@ -53,6 +53,8 @@ struct PairBufs {
     float4* g;             // [n*M] pair gradient -dE_i/d(x_j - x_i)
     uint16_t* grp;         // [n*M] cell-offset group of the entry (rows are sorted by group, then j)
     int* count;            // [n] true neighbour count (may exceed M on overflow)
+    int* gstart;           // [n][GS] row position where each cell-offset group starts (GS = 0: not kept)
+    int GS;                // groups per atom + 1 (largest offset count of the batch + 1), or 0
 };
 
 }  // namespace nnapgb

@@ -144,6 +144,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     __shared__ uint32_t s_img[kNbMaxWarps][32];
     __shared__ double s_sh[kNbMaxWarps][32][3];
     __shared__ float s_fsh[kNbMaxWarps][32][3], s_flo[kNbMaxWarps][32][3];
+    __shared__ int s_acc[kNbMaxWarps][32];  // accepted entries per cell-offset group of the batch
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + w;
     if (i >= n) return;
@@ -159,8 +160,11 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     const float rc2h = (float)st.rc2, rc2l = (float)(st.rc2 - (double)(float)st.rc2);
     const float tol = 1e-10f * rc2h;  // float-float d^2 is accurate to ~1e-12 relative
     int cnt = 0;
+    const bool keep_groups = P.GS > noff;
     for (int o0 = 0; o0 < noff; o0 += 32) {
         const int o = o0 + lane;
+        const int cnt0 = cnt;
+        s_acc[w][lane] = 0;
         int ccount = 0;
         if (o < noff) {
             const int oa = o % wa - st.R[0], ob = (o / wa) % wb - st.R[1], oc = o / (wa * wb) - st.R[2];
@@ -257,12 +261,25 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     P.dx[e] = make_float4(ox, oy, oz, xf[j].w);
                     P.grp[e] = (uint16_t)(o0 + slot);
                 }
+                if (keep_groups) atomicAdd(&s_acc[w][slot], 1);
             }
             cnt += __popc(m);
         }
         __syncwarp();
+        if (keep_groups) {  // start of each group of this batch: cnt0 + accepted entries of earlier groups
+            const int a = s_acc[w][lane];
+            int incl2 = a;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl2, d);
+                if (lane >= d) incl2 += u;
+            }
+            if (o < noff) P.gstart[(size_t)i * P.GS + o] = cnt0 + incl2 - a;
+        }
+        __syncwarp();
     }
     if (lane == 0) {
+        if (keep_groups) P.gstart[(size_t)i * P.GS + noff] = cnt;
         P.count[i] = cnt;
         if (cnt > M) atomicOr(err, ERRBIT_CAPACITY);
         atomicMax(max_count, cnt);
@@ -271,38 +288,55 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
 
 // Mirror index: for entry (i -> j, image n) the position of (j -> i, image -n) in j's row.
 // Rows are ordered by (cell-offset group, atom index); the mirrored entry lies in group
-// noff-1-g of j's row (the negated cell offset), so it is found by binary search.
+// noff-1-g of j's row (the negated cell offset).  With group starts kept, it is found
+// by a scan of that group (a few entries); otherwise by binary search on (group, atom).
+// One warp per row.
 __global__ void k_mirror(const StructDev* __restrict__ S, const int* __restrict__ sid, PairBufs P, int n,
                          int* __restrict__ err) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int M = P.M;
-    const int i = (int)(t / M), k = (int)(t % M);
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (i >= n) return;
+    const int M = P.M;
     const int ci = min(P.count[i], M);
-    if (k >= ci) return;
     const StructDev& st = S[sid[i]];
     const int noff = (2 * st.R[0] + 1) * (2 * st.R[1] + 1) * (2 * st.R[2] + 1);
-    const size_t e = (size_t)i * M + k;
-    const uint64_t key = P.key[e];
-    const int j = (int)(key >> 32);
-    const uint32_t want_g = (uint32_t)(noff - 1 - P.grp[e]);
-    const uint64_t want = ((uint64_t)want_g << 32) | (uint32_t)i;
-    const int cj = min(P.count[j], M);
-    const uint64_t* row = P.key + (size_t)j * M;
-    const uint16_t* grow = P.grp + (size_t)j * M;
-    int lo = 0, hi = cj;  // first q with composite(q) >= want
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        const uint64_t c = ((uint64_t)grow[mid] << 32) | (uint32_t)(row[mid] >> 32);
-        if (c < want) lo = mid + 1; else hi = mid;
-    }
-    int na, nb, nc;
-    unpack_img((uint32_t)key, na, nb, nc);
-    if (lo < cj && row[lo] == pair_key(i, pack_img(-na, -nb, -nc))) {
-        P.rev[e] = (int)((size_t)j * M + lo);
-    } else {
-        atomicOr(err, ERRBIT_NO_MIRROR);
-        P.rev[e] = (int)e;
+    const bool groups = P.GS > noff;
+    for (int k = lane; k < ci; k += 32) {
+        const size_t e = (size_t)i * M + k;
+        const uint64_t key = P.key[e];
+        const int j = (int)(key >> 32);
+        const int want_g = noff - 1 - P.grp[e];
+        int na, nb, nc;
+        unpack_img((uint32_t)key, na, nb, nc);
+        const uint64_t target = pair_key(i, pack_img(-na, -nb, -nc));
+        const int cj = min(P.count[j], M);
+        const uint64_t* row = P.key + (size_t)j * M;
+        int found = -1;
+        if (groups) {
+            const int* gs = P.gstart + (size_t)j * P.GS;
+            const int lo = min(gs[want_g], cj), hi = min(gs[want_g + 1], cj);
+            for (int q = lo; q < hi; ++q)
+                if (row[q] == target) {
+                    found = q;
+                    break;
+                }
+        } else {
+            const uint16_t* grow = P.grp + (size_t)j * M;
+            const uint64_t want = ((uint64_t)(uint32_t)want_g << 32) | (uint32_t)i;
+            int lo = 0, hi = cj;  // first q with composite(q) >= want
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                const uint64_t c = ((uint64_t)grow[mid] << 32) | (uint32_t)(row[mid] >> 32);
+                if (c < want) lo = mid + 1; else hi = mid;
+            }
+            if (lo < cj && row[lo] == target) found = lo;
+        }
+        if (found >= 0) {
+            P.rev[e] = (int)((size_t)j * M + found);
+        } else {
+            atomicOr(err, ERRBIT_NO_MIRROR);
+            P.rev[e] = (int)e;
+        }
     }
 }
 

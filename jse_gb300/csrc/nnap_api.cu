@@ -184,7 +184,6 @@ Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kind
         if (natoms[s] < 0) throw ApiFail(NNAP_ERR_ARG, "negative atom count");
         StructDev d = make_struct(kinds[s], boxes + 9 * s, rc, a0, natoms[s], c0);
         B.sd.push_back(d);
-        for (int k = 0; k < natoms[s]; ++k) B.sid.push_back(s);
         for (int b = 0; b < natoms[s]; b += kRedChunk) {
             B.cb.push_back(a0 + b);
             B.ce.push_back(a0 + std::min(natoms[s], b + kRedChunk));
@@ -217,6 +216,8 @@ PairBufs pair_bufs(nnap_handle* h) {
     P.g = h->pg.p;
     P.grp = h->pgrp.p;
     P.count = h->pcount.p;
+    P.gstart = h->GS ? h->gstart.p : nullptr;
+    P.GS = h->GS;
     return P;
 }
 
@@ -280,6 +281,11 @@ void prepare_layout(nnap_handle* h, const Batch& B) {
     const int nchunks = (int)B.cb.size();
     if (h->M == 0) h->M = initial_capacity(B, h->model.rcut_max);
     ensure_work(h, n, B.nstruct, B.ncells, nchunks);
+    // group starts of the neighbour rows, for the mirror search (kept up to 127 offset groups)
+    int gs = 0;
+    for (auto& d : B.sd) gs = std::max(gs, (2 * d.R[0] + 1) * (2 * d.R[1] + 1) * (2 * d.R[2] + 1) + 1);
+    h->GS = gs <= 128 ? gs : 0;
+    if (h->GS) h->gstart.ensure((size_t)std::max(n, 1) * h->GS);
     if (h->h_sdev_cap < (size_t)B.nstruct) {
         if (h->h_sdev) cudaFreeHost(h->h_sdev);
         h->h_sdev = nullptr;
@@ -287,7 +293,12 @@ void prepare_layout(nnap_handle* h, const Batch& B) {
         h->h_sdev_cap = B.nstruct;
     }
     cudaStream_t st = h->stream;
-    if (n) CK(cudaMemcpyAsync(h->sid.p, B.sid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    if (n) {  // structure of every atom: built only when the layout changes
+        std::vector<int> sid((size_t)n);
+        for (int q = 0; q < B.nstruct; ++q) std::fill(sid.begin() + B.sd[q].a0, sid.begin() + B.sd[q].a0 + B.sd[q].n, q);
+        CK(cudaMemcpyAsync(h->sid.p, sid.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+    }
     if (nchunks) {
         CK(cudaMemcpyAsync(h->chunk_b.p, B.cb.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(h->chunk_e.p, B.ce.data(), sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
@@ -331,8 +342,8 @@ void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
     k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
     k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
     k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
-    const long long tot = (long long)n * h->M;
-    k_mirror<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
+    k_mirror<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n,
+                                                                      h->status.p);
     h->launches += 4;
 }
 
@@ -728,7 +739,7 @@ int nnap_destroy(nnap_handle* h) {
     h->cell_start.release(); h->cell_atoms.release(); h->perm.release(); h->block_counts.release();
     h->type_start.release(); h->chunk_b.release(); h->chunk_e.release(); h->struct_chunks.release();
     h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
-    h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release();
+    h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->gstart.release();
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     if (h->order_ev) cudaEventDestroy(h->order_ev);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);

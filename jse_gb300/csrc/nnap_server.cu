@@ -281,6 +281,7 @@ void step_impl(nnap_server* s, int nslots, const int* ids, const double* x, int 
         const int nchunks = (int)B.cb.size();
         // buffers: the handle's work arrays at row capacity Mv, then the server's own
         h->M = s->Mv;
+        h->GS = 0;  // filtered rows keep no group starts: the mirror search bisects
         ensure_work(h, N, nslots, B.ncells, nchunks);
         drop_graph(h);
         h->layout_ok = false;
