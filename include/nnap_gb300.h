@@ -136,6 +136,26 @@ int nnap_compute_fp(nnap_handle* h, int natoms, const double* x, const int* type
 int nnap_neighbor_list(nnap_handle* h, int natoms, const double* x, const int* type, int box_kind,
                        const double* box, int* counts, long long cap, int* j, int* img, long long* total);
 
+/* LAMMPS-style evaluation: one call per force evaluation of a LAMMPS pair style.  It
+ * replaces the reference's jse_nnap_lammps2cuda + jse_nnap_computeLammpsCuda +
+ * jse_nnap_cuda2lammps sequence (nnap_interface_cuda.cu:319-483, driven by
+ * NNAP.java:919-1030 for PairNNAP_gpu).  Inputs are LAMMPS's own arrays:
+ *   inum local atoms ilist[inum] with full neighbour lists numneigh[i] / firstneigh[i]
+ *   (indices into 0..nall-1; special-bond bits above 0x1FFFFFFF are masked off);
+ *   x: nall x 3 doubles (local then ghost atoms, ghosts already at their image
+ *   positions); type: nall LAMMPS types, mapped through type_map[type] to 1-based NNAP
+ *   species (type_map NULL: identity; it must cover every type value present).
+ * A pair is kept when |x_j - x_i|^2 < rcut^2 (FP64).  Results are ADDED to LAMMPS's
+ * accumulators, as cuda2lammps does: f (nall x 3, ghosts included, for LAMMPS's reverse
+ * communication), *eng_vdwl (eflag), eatom[i] (eflag_atom), virial[6] (vflag: xx, yy,
+ * zz, xy, xz, yz), vatom (nall x 6, vflag_atom) and cvatom (nall x 9, cvflag_atom:
+ * xx, yy, zz, xy, xz, yz, yx, zx, zy), the pair term dx (x) g assigned to the neighbour.
+ * The scatter is atomic-free and deterministic.  Host buffers, synchronous. */
+int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int* ilist, const int* numneigh,
+                        const int* const* firstneigh, const double* x, const int* type, const int* type_map,
+                        int eflag, int vflag, int eflag_atom, int vflag_atom, int cvflag_atom, double* f,
+                        double* eng_vdwl, double* eatom, double* virial, double* vatom, double* cvatom);
+
 /* Number of this library's kernels launched by the last compute call on the handle. */
 int nnap_last_launch_count(const nnap_handle* h, int* count);
 

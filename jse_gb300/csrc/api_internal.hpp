@@ -148,6 +148,10 @@ struct nnap_handle {
     nnapgb::DevBuf<int> prev, pcount;
     nnapgb::DevBuf<float> fp, gfp, A;
     int M = 0;
+    // LAMMPS-style boundary: caller's atoms (local + ghost), list, targets of the scatter
+    nnapgb::DevBuf<double> lmp_x, lmp_forces, lmp_virials;
+    nnapgb::DevBuf<int> lmp_type, lmp_ilist, lmp_off, lmp_idx, lmp_rowtype, lmp_rowof, lmp_tcount, lmp_tstart,
+        lmp_tfill, lmp_tlist;
     int GS = 0;                  // cell-offset groups per atom + 1 kept by k_neighbors (0: none)
     nnapgb::DevBuf<int> gstart;  // [n][GS] group starts of each neighbour row
     int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
@@ -212,10 +216,13 @@ PairBufs pair_bufs(nnap_handle* h);
 // Size every per-atom work buffer for n atoms, nstruct structures, ncells cells and
 // nchunks reduction chunks (no copies, no synchronisation).
 void ensure_work(nnap_handle* h, int n, int nstruct, int ncells, int nchunks);
+// Queue the species sort of n rows (slots ordered by species, stable).
+void enqueue_species(nnap_handle* h, int n, const int* d_type);
 // Queue the species sort of the batch's atoms and the mirror index of the pair rows.
 void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type);
-// Queue descriptors, networks, descriptor gradients, the gather and the reductions.
-void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only);
+// Queue descriptors, networks and descriptor gradients; with gather, also the
+// force / virial gather over mirrored rows and the per-structure reductions.
+void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather);
 void check_outputs(int flags, const Outputs& o);
 // Forget the captured launch sequence of the handle.
 void drop_graph(nnap_handle* h);

@@ -333,8 +333,7 @@ void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const 
     }
 }
 
-void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
-    const int n = B.natoms;
+void enqueue_species(nnap_handle* h, int n, const int* d_type) {
     if (n <= 0) return;
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
@@ -342,12 +341,19 @@ void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
     k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
     k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
     k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
-    k_mirror<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(h->sdev.p, h->sid.p, pair_bufs(h), n,
-                                                                      h->status.p);
-    h->launches += 4;
+    h->launches += 3;
 }
 
-void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only) {
+void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
+    const int n = B.natoms;
+    if (n <= 0) return;
+    enqueue_species(h, n, d_type);
+    k_mirror<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, h->stream>>>(
+        h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
+    ++h->launches;
+}
+
+void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather) {
     const int n = B.natoms;
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
@@ -430,7 +436,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     h->mark(3);
     if (!fp_only) descriptors(false);
     h->mark(4);
-    if (!fp_only) {
+    if (!fp_only && gather) {
         if (n > 0) {
             const int gb = h->tune.gather_block;
             k_gather<<<(n + gb - 1) / gb, gb, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
@@ -461,7 +467,7 @@ void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_typ
     enqueue_neighbors(h, B, d_x, d_type);
     enqueue_species_mirror(h, B, d_type);
     h->mark(1);
-    enqueue_eval(h, B, d_type, fp_only);
+    enqueue_eval(h, B, d_type, fp_only, true);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
 }
@@ -740,6 +746,10 @@ int nnap_destroy(nnap_handle* h) {
     h->type_start.release(); h->chunk_b.release(); h->chunk_e.release(); h->struct_chunks.release();
     h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->gstart.release();
+    for (auto* b : {&h->lmp_x, &h->lmp_forces, &h->lmp_virials}) b->release();
+    for (auto* b : {&h->lmp_type, &h->lmp_ilist, &h->lmp_off, &h->lmp_idx, &h->lmp_rowtype, &h->lmp_rowof,
+                    &h->lmp_tcount, &h->lmp_tstart, &h->lmp_tfill, &h->lmp_tlist})
+        b->release();
     for (auto& e : h->ev) if (e) cudaEventDestroy(e);
     if (h->order_ev) cudaEventDestroy(h->order_ev);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);

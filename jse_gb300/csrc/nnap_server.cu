@@ -363,7 +363,7 @@ void step_impl(nnap_server* s, int nslots, const int* ids, const double* x, int 
         }
         enqueue_species_mirror(h, B, tb);
         h->mark(1);
-        enqueue_eval(h, B, tb, false);
+        enqueue_eval(h, B, tb, false, true);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
         // outputs in batch order into pinned staging

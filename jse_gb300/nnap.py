@@ -41,7 +41,7 @@ EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes"
            "nnap_stage_times", "nnap_compute_batch_device", "nnap_set_graphs", "nnap_neighbor_counts_noalloc",
            "nnap_server_create", "nnap_server_destroy", "nnap_server_admit", "nnap_server_release",
            "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats", "nnap_set_autotune",
-           "nnap_get_tuning", "nnap_set_tuning"]
+           "nnap_get_tuning", "nnap_set_tuning", "nnap_compute_lammps"]
 
 
 class IllegalStateError(RuntimeError):
@@ -86,6 +86,8 @@ def load_library(path: str = LIB_PATH):
     L.nnap_stage_times.argtypes = [P, dp]
     L.nnap_compute_batch_device.argtypes = [P, I, ip, P, P, ip, dp, I, P, P, P, P, P, P]
     L.nnap_set_graphs.argtypes = [P, I]
+    L.nnap_compute_lammps.argtypes = [P, I, I, ip, ip, C.POINTER(ip), dp, ip, ip, I, I, I, I, I, dp, dp, dp, dp,
+                                      dp, dp]
     L.nnap_set_autotune.argtypes = [P, I]
     L.nnap_get_tuning.argtypes = [P, I, ip, ip]
     L.nnap_set_tuning.argtypes = [P, I, ip]
@@ -339,6 +341,34 @@ class NNAP:
             out.append(r)
             a0 += n
         return out
+
+    def computeLammps(self, ilist, neighbors, x, types, type_map=None, eflag=True, vflag=True, eflag_atom=True,
+                      vflag_atom=False, cvflag_atom=True) -> dict:
+        """LAMMPS-style evaluation (``PairNNAP_gpu``): ``ilist`` local atoms, ``neighbors[i]``
+        the full list of local atom i (indices into the nall = len(x) local + ghost atoms),
+        ``types`` LAMMPS types (mapped through ``type_map`` when given).  Returns fresh
+        accumulators: forces on every atom (ghosts included), eng, eatom, virial[6],
+        vatom (nall x 6), cvatom (nall x 9)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        il = np.ascontiguousarray(ilist, dtype=np.int32)
+        nall = len(x)
+        lists = [np.ascontiguousarray(neighbors[i], dtype=np.int32) if i < len(neighbors) and neighbors[i] is not None
+                 else np.zeros(0, dtype=np.int32) for i in range(nall)]
+        num = np.array([len(a) for a in lists], dtype=np.int32)
+        ptrs = (C.POINTER(C.c_int) * max(nall, 1))(*[_iptr(a) for a in lists])
+        tm = None if type_map is None else np.ascontiguousarray(type_map, dtype=np.int32)
+        f = np.zeros((nall, 3))
+        eng = np.zeros(1)
+        eatom = np.zeros(nall)
+        vir = np.zeros(6)
+        vatom = np.zeros((nall, 6))
+        cvatom = np.zeros((nall, 9))
+        self._check(self._L.nnap_compute_lammps(self._handle(), len(il), nall, _iptr(il), _iptr(num), ptrs, _dptr(x),
+                                                _iptr(t), _iptr(tm), int(eflag), int(vflag), int(eflag_atom),
+                                                int(vflag_atom), int(cvflag_atom), _dptr(f), _dptr(eng), _dptr(eatom),
+                                                _dptr(vir), _dptr(vatom), _dptr(cvatom)))
+        return {"forces": f, "eng": float(eng[0]), "eatom": eatom, "virial": vir, "vatom": vatom, "cvatom": cvatom}
 
     def computeBatchDevice(self, natoms, x_ptr: int, type_ptr: int, box_kinds, boxes, flags: int,
                            energy_ptr: int = 0, energies_ptr: int = 0, forces_ptr: int = 0, virial_ptr: int = 0,
