@@ -496,22 +496,23 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
             const float4* gr = reinterpret_cast<const float4*>(sG + lm * S::NPS);
             const float yv = sY[lm * 32 + lane];
             const float2 yy = make_float2(yv, yv);
-            float2 dY = make_float2(0.f, 0.f);
+            // two independent partial sums keep the dependent FMA chain short
+            float2 dYa = make_float2(0.f, 0.f), dYb = make_float2(0.f, 0.f);
 #pragma unroll
             for (int q = 0; q < S::NPS / 4; ++q) {
                 const float4 g = gr[q];
                 if (2 * q < NH) {
                     const float2 ga = make_float2(g.x, g.y);
-                    dY = __ffma2_rn(c2[2 * q], ga, dY);
+                    dYa = __ffma2_rn(c2[2 * q], ga, dYa);
                     dc2[2 * q] = __ffma2_rn(ga, yy, dc2[2 * q]);
                 }
                 if (2 * q + 1 < NH) {
                     const float2 gb = make_float2(g.z, g.w);
-                    dY = __ffma2_rn(c2[2 * q + 1], gb, dY);
+                    dYb = __ffma2_rn(c2[2 * q + 1], gb, dYb);
                     dc2[2 * q + 1] = __ffma2_rn(gb, yy, dc2[2 * q + 1]);
                 }
             }
-            return dY.x + dY.y;
+            return (dYa.x + dYb.x) + (dYa.y + dYb.y);
         };
 #pragma unroll 1
         for (int l = 0; l <= L; ++l) {
