@@ -178,14 +178,14 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             ccount = cell_start[cid + 1] - cs;
             s_start[w][lane] = cs;
             s_img[w][lane] = pack_img(na, nb, nc);
-            double sh[3];
-            image_shift(st, na, nb, nc, sh);
+            double sh[3] = {0.0, 0.0, 0.0};  // the zero image has an exactly zero shift
+            if (na | nb | nc) image_shift(st, na, nb, nc, sh);
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 const float h = (float)sh[d];
                 s_sh[w][lane][d] = sh[d];
                 s_fsh[w][lane][d] = h;
-                s_flo[w][lane][d] = (float)ds(sh[d], (double)h);
+                s_flo[w][lane][d] = (na | nb | nc) ? (float)ds(sh[d], (double)h) : 0.f;
             }
         }
         int incl = ccount;

@@ -8,8 +8,9 @@ A periodic structure is turned into LAMMPS's form:
   entries.
 After LAMMPS's reverse communication (ghost forces and per-atom virials added to their
 owners), the results must equal nnap_compute's: per-atom energies, forces, the global
-virial and the per-atom virials.  They differ only by FP32 rounding of displacements
-taken from other coordinates (tolerances below).  Two calls give identical results.
+virial and the per-atom virials.  They differ only by FP32 rounding: displacements come
+from other coordinates and rows are summed in another order (tolerances below).  Two
+calls give identical results.
 """
 import numpy as np
 import pytest
@@ -19,7 +20,7 @@ from oracle import native as ON
 
 pytestmark = pytest.mark.gpu
 
-E_TOL = 1e-6   # eV per atom
+E_TOL = 1e-5   # eV per atom: two FP32 descriptor sums in different orders (the path's energy target)
 F_TOL = 1e-4   # eV/A, largest component
 V_TOL = 1e-4   # eV, largest per-atom virial component
 
