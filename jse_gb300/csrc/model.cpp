@@ -247,6 +247,68 @@ int kind_of(const std::string& s) {
     return -1;
 }
 
+// SharedFeedForward.load + updateParameters_ (SharedFeedForward.java:162-339): the base
+// network with, in each hidden layer, its first H - S rows and biases replaced by the
+// species' own values (zeros when absent); the output layer is the base's when the last
+// shared dimension is 1, else the species' own.
+void load_shared_network(Species& sp, const Species& base, const JValue& m) {
+    if (m.get("shared_flags")) bad("shared in layer nn is invalid now");
+    if (const JValue* in = m.get("input_dim"))
+        if (in->as_int() != sp.D) bad("input dimension mismatch");
+    if (sp.D != base.D) bad("input dimensions mismatch for shared nn");
+    const JValue* shv = m.get_any({"shared_hidden_dims", "shared_nnarch"});
+    if (!shv) bad("key shared_hidden_dims required for shared_feed_forward");
+    std::vector<int> sh;
+    for (auto& e : shv->arr) sh.push_back(e.as_int());
+    const size_t L = base.hidden.size();
+    if (sh.size() == L) sh.push_back(0);
+    if (sh.size() != L + 1) bad("the number of hidden layers mismatch");
+    const JValue* hw = m.get("hidden_weights");
+    const JValue* hb = m.get("hidden_biases");
+    if (hw && hw->arr.size() != L) bad("the number of hidden weights mismatch");
+    if (hb && hb->arr.size() != L) bad("the number of hidden biases mismatch");
+    sp.hidden = base.hidden;
+    sp.Wh = base.Wh;
+    sp.bh = base.bh;
+    int fan = sp.D;
+    for (size_t l = 0; l < L; ++l) {
+        const int H = base.hidden[l];
+        if (sh[l] < 0 || sh[l] > H) bad("invalid shared dimension");
+        const int U = H - sh[l];
+        for (int o = 0; o < U; ++o) {
+            for (int i = 0; i < fan; ++i) sp.Wh[l][(size_t)o * fan + i] = 0.0;
+            sp.bh[l][o] = 0.0;
+        }
+        if (hw) {
+            const JValue& rows = hw->arr[l];
+            if ((int)rows.arr.size() != U) bad("nrows of hidden weight mismatch");
+            for (int o = 0; o < U; ++o) {
+                if ((int)rows.arr[o].arr.size() != fan) bad("ncols of hidden weight mismatch");
+                for (int i = 0; i < fan; ++i) sp.Wh[l][(size_t)o * fan + i] = rows.arr[o].arr[i].as_num();
+            }
+        }
+        if (hb) {
+            std::vector<double> v = num_list(hb->arr[l], "hidden_biases");
+            if ((int)v.size() != U) bad("size of hidden bias mismatch");
+            for (int o = 0; o < U; ++o) sp.bh[l][o] = v[o];
+        }
+        fan = H;
+    }
+    if (sh[L] != 0 && sh[L] != 1) bad("invalid shared output dimension");
+    if (sh[L] == 1) {
+        sp.wo = base.wo;
+        sp.bo = base.bo;
+    } else {
+        sp.wo.assign(fan, 0.0);
+        sp.bo = 0.0;
+        if (const JValue* ow = m.get("output_weight")) {
+            sp.wo = num_list(*ow, "output_weight");
+            if ((int)sp.wo.size() != fan) bad("size of output weight mismatch");
+        }
+        if (const JValue* ob = m.get("output_bias")) sp.bo = ob->as_num();
+    }
+}
+
 void load_network(Species& sp, const JValue* nnv) {
     static const JValue empty_obj = [] { JValue v; v.kind = JValue::OBJ; return v; }();
     const JValue& m = nnv ? *nnv : empty_obj;
@@ -308,6 +370,9 @@ Model load_model(const char* text, size_t len) {
     M.sp.resize(T);
     double mu_e = 0.0, sig_e = 1.0;
     bool have_mu = false, have_sig = false;
+    // bases: concrete ones first; mirror and shared ones refer to them (Basis.java:22-66)
+    enum { PLAIN = 0, MIRROR = 1, SHARE = 2 };
+    std::vector<int> bkind(T, PLAIN), bsrc(T, 0), nn_plain(T, 0);
     for (int t = 0; t < T; ++t) {
         const JValue& mm = models->arr[t];
         Species& sp = M.sp[t];
@@ -329,22 +394,84 @@ Model load_model(const char* text, size_t len) {
                 sp.subs.push_back(load_sub(k, T, sm));
             }
         } else if (bt == "mirror" || bt == "mirror_basis" || bt == "share" || bt == "shared_basis") {
-            bad("mirror/shared bases are not supported");
+            const bool mirror = bt == "mirror" || bt == "mirror_basis";
+            const JValue* src = bm->get(mirror ? "mirror" : "share");
+            if (!src) bad(mirror ? "key mirror required for mirror_basis" : "key share required for shared_basis");
+            bkind[t] = mirror ? MIRROR : SHARE;
+            bsrc[t] = src->as_int();
         } else {
             int k = kind_of(bt);
             if (k < 0) bad("unsupported basis type: " + bt);
             sp.subs.push_back(load_sub(k, T, bm ? *bm : empty));
         }
-        int off = 0;
-        for (auto& b : sp.subs) { b.fp_off = off; off += b.size; M.rcut_max = std::max(M.rcut_max, b.rcut); }
-        sp.D = off;
-        load_network(sp, mm.get("nn"));
         if (!have_sig) if (const JValue* v = mm.get("norm_sigma_eng")) { sig_e = v->as_num(); have_sig = true; }
         if (!have_mu) if (const JValue* v = mm.get("norm_mu_eng")) { mu_e = v->as_num(); have_mu = true; }
     }
     for (int t = 0; t < T; ++t) {
-        const JValue& mm = models->arr[t];
+        if (bkind[t] == PLAIN) continue;
+        const int s = bsrc[t];
+        // a mirror or shared basis of a mirror or shared basis reads an empty parameter
+        // block in the reference's generated code, so only concrete sources are accepted
+        if (s < 1 || s > T || bkind[s - 1] != PLAIN) bad("the source of a mirror or shared basis must be a plain basis");
+        M.sp[t].subs = M.sp[s - 1].subs;
+        if (bkind[t] == MIRROR) {
+            // neighbours of the centre's own species and of the mirrored one swap roles
+            // (nnap_main.hpp:40-48): W_t[tn] = W_s[sigma(tn)], sigma exchanging t+1 and s
+            for (auto& b : M.sp[t].subs) {
+                const size_t blk = (size_t)b.np * (b.nmax + 1);
+                const std::vector<double> W0 = b.W;
+                for (int tn = 1; tn <= T; ++tn) {
+                    const int from = tn == s ? t + 1 : (tn == t + 1 ? s : tn);
+                    std::copy(W0.begin() + (size_t)(from - 1) * blk, W0.begin() + (size_t)from * blk,
+                              b.W.begin() + (size_t)(tn - 1) * blk);
+                }
+            }
+        }
+    }
+    for (int t = 0; t < T; ++t) {
         Species& sp = M.sp[t];
+        int off = 0;
+        for (auto& b : sp.subs) { b.fp_off = off; off += b.size; M.rcut_max = std::max(M.rcut_max, b.rcut); }
+        sp.D = off;
+    }
+    // networks: plain feed-forward ones first; a mirror species takes its source's network
+    // unchanged, a shared one merges its own rows into its base's (NeuralNetwork.java:24-65)
+    for (int t = 0; t < T; ++t) {
+        const JValue* nnv = models->arr[t].get("nn");
+        if (bkind[t] == MIRROR) {
+            if (nnv) bad("nn data of a mirror basis must be empty");
+            continue;
+        }
+        if (nnv && nnv->get("type") && nnv->get("type")->as_str() == "shared_feed_forward") continue;
+        load_network(M.sp[t], nnv);
+        nn_plain[t] = 1;
+    }
+    for (int t = 0; t < T; ++t) {
+        if (nn_plain[t]) continue;
+        Species& sp = M.sp[t];
+        const JValue* nnv = models->arr[t].get("nn");
+        const int s = bkind[t] == MIRROR ? bsrc[t] : (nnv->get("share") ? nnv->get("share")->as_int() : 0);
+        if (s < 1 || s > T || !nn_plain[s - 1]) bad("a shared network needs a plain feed_forward source");
+        const Species& base = M.sp[s - 1];
+        if (bkind[t] == MIRROR) {
+            sp.hidden = base.hidden;
+            sp.Wh = base.Wh;
+            sp.bh = base.bh;
+            sp.wo = base.wo;
+            sp.bo = base.bo;
+        } else {
+            load_shared_network(sp, base, *nnv);
+        }
+    }
+    for (int t = 0; t < T; ++t) {
+        const JValue* mmp = &models->arr[t];
+        Species& sp = M.sp[t];
+        if (bkind[t] == MIRROR) {  // normalisation of the mirrored species (NNAP.java:281-289)
+            if (mmp->get("ref_eng")) bad("ref_eng of a mirror basis must be empty");
+            if (mmp->get_any({"norm_vec", "norm_sigma", "norm_mu"})) bad("normalisation of a mirror basis must be empty");
+            mmp = &models->arr[bsrc[t] - 1];
+        }
+        const JValue& mm = *mmp;
         const double ref = mm.get("ref_eng") ? mm.get("ref_eng")->as_num() : 0.0;
         sp.mu_e = mu_e + ref;
         sp.sigma_e = sig_e;

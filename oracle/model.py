@@ -255,6 +255,8 @@ def _internal_fuse(sb: SubBasis, fuse_w, fuse_size, rfuse_w, scale, ws) -> np.nd
 @dataclass
 class Basis:
     subs: List[SubBasis]
+    kind: str = "plain"    # "plain" (single or merged), "mirror" or "share"
+    src: int = 0           # mirror / share: the 1-based species whose basis is used
 
     @property
     def size(self) -> int:
@@ -295,6 +297,66 @@ class FeedForward:
         """``hidden W | output W | hidden b | output b`` (FeedForward.java:310-316)."""
         return np.concatenate([w.reshape(-1) for w in self.hidden_weights] + [self.output_weight] +
                               list(self.hidden_biases) + [np.array([self.output_bias])])
+
+
+def _load_shared_nn(D: int, base: FeedForward, m: dict) -> FeedForward:
+    """``SharedFeedForward.load`` + ``updateParameters_`` (SharedFeedForward.java:162-339):
+    the base network with, per hidden layer, its first H - S rows (and biases) replaced
+    by the species' own values (zeros when absent); the output layer is the base's when
+    the last shared dimension is 1, else the species' own."""
+    if m.get("shared_flags") is not None:
+        raise ValueError("shared in layer nn is invalid now")
+    ind = _get(m, "input_dim")
+    if ind is not None and int(ind) != D:
+        raise ValueError("input dimension mismatch: %d vs %d" % (int(ind), D))
+    if D != base.input_dim:
+        raise ValueError("input dimensions mismatch for shared nn")
+    sh = _get(m, "shared_hidden_dims", "shared_nnarch")
+    if sh is None:
+        raise ValueError("Key `shared_hidden_dims` required for shared_feed_forward")
+    sh = [int(v) for v in sh]
+    L = len(base.hidden_dims)
+    if len(sh) == L:
+        sh = sh + [0]
+    if len(sh) - 1 != L:
+        raise ValueError("the number of hidden layers mismatch")
+    hw, hb = m.get("hidden_weights"), m.get("hidden_biases")
+    if hw is not None and len(hw) != L:
+        raise ValueError("the number of hidden weights mismatch")
+    if hb is not None and len(hb) != L:
+        raise ValueError("the number of hidden biases mismatch")
+    ws, bs, fan = [], [], D
+    for i, h in enumerate(base.hidden_dims):
+        if sh[i] < 0 or sh[i] > h:
+            raise ValueError("invalid shared dimension")
+        u = h - sh[i]
+        w = base.hidden_weights[i].copy()
+        b = base.hidden_biases[i].copy()
+        if hw is None or u == 0:
+            own_w = np.zeros((u, fan))
+        else:
+            own_w = np.asarray(hw[i], dtype=np.float64)
+        if own_w.shape != (u, fan):
+            raise ValueError("hidden weight %d shape mismatch" % i)
+        own_b = np.zeros(u) if hb is None else np.asarray(hb[i], dtype=np.float64)
+        if own_b.shape != (u,):
+            raise ValueError("hidden bias %d size mismatch" % i)
+        w[:u] = own_w
+        b[:u] = own_b
+        ws.append(w)
+        bs.append(b)
+        fan = h
+    if sh[L] not in (0, 1):
+        raise ValueError("invalid shared output dimension")
+    if sh[L] == 1:
+        ow, ob = base.output_weight.copy(), base.output_bias
+    else:
+        ow = np.asarray(m["output_weight"], dtype=np.float64) if m.get("output_weight") is not None \
+            else np.zeros(fan)
+        if ow.shape != (fan,):
+            raise ValueError("output weight size mismatch")
+        ob = float(m.get("output_bias", 0.0) or 0.0)
+    return FeedForward(D, list(base.hidden_dims), ws, bs, ow, ob)
 
 
 def _load_nn(D: int, m: dict) -> FeedForward:
@@ -387,17 +449,59 @@ def load(source) -> PackedModel:
                     raise ValueError("unsupported merged basis type %r" % st)
                 subs.append(_load_sub(kind, T, sm))
             basis.append(Basis(subs))
+        elif bt in ("mirror", "mirror_basis", "share", "shared_basis"):
+            basis.append(None)  # resolved below, after every concrete basis (Basis.java:50-66)
         else:
             raise ValueError("unsupported basis type %r" % bt)
-    nns = []
-    for mm, b in zip(models, basis):
+    for t, mm in enumerate(models):
+        if basis[t] is not None:
+            continue
+        bm = mm["basis"]
+        mirror = bm["type"] in ("mirror", "mirror_basis")
+        key = "mirror" if mirror else "share"
+        if bm.get(key) is None:
+            raise ValueError("Key `%s` required" % key)
+        src = int(bm[key])
+        if not 1 <= src <= T or basis[src - 1] is None or basis[src - 1].kind != "plain":
+            # a mirror or shared basis of a mirror or shared basis reads an empty parameter
+            # block in the reference's generated code, so only plain sources are accepted
+            raise ValueError("the source of a mirror or shared basis must be a plain basis")
+        basis[t] = Basis(basis[src - 1].subs, "mirror" if mirror else "share", src)
+    nns = [None] * T
+    for t, (mm, b) in enumerate(zip(models, basis)):
         if mm.get("torch") is not None:
             raise ValueError("torch model is invalid")
-        nns.append(_load_nn(b.size, mm.get("nn") or {}))
+        if b.kind == "mirror":
+            if mm.get("nn") is not None:
+                raise ValueError("nn data in mirror ModelInfo MUST be empty")
+            continue
+        nm = mm.get("nn") or {}
+        if _get(nm, "type", default="feed_forward") == "shared_feed_forward":
+            continue
+        nns[t] = _load_nn(b.size, nm)
+    plain = [n is not None for n in nns]  # plain feed_forward networks (the only valid bases)
+    for t, (mm, b) in enumerate(zip(models, basis)):
+        if plain[t]:
+            continue
+        src = b.src if b.kind == "mirror" else int((mm.get("nn") or {}).get("share", 0))
+        if not 1 <= src <= T or not plain[src - 1]:
+            raise ValueError("a shared network needs a plain feed_forward source")
+        if b.kind == "mirror":  # SharedFeedForward.full: every layer shared
+            base = nns[src - 1]
+            nns[t] = FeedForward(base.input_dim, list(base.hidden_dims), [w.copy() for w in base.hidden_weights],
+                                 [v.copy() for v in base.hidden_biases], base.output_weight.copy(), base.output_bias)
+        else:
+            nns[t] = _load_shared_nn(b.size, nns[src - 1], mm["nn"])
     sig_e = next((mm["norm_sigma_eng"] for mm in models if mm.get("norm_sigma_eng") is not None), 1.0)
     mu_e = next((mm["norm_mu_eng"] for mm in models if mm.get("norm_mu_eng") is not None), 0.0)
     norms = []
     for mm, b in zip(models, basis):
+        if b.kind == "mirror":  # a mirror species takes its source's normalisation (NNAP.java:281-289)
+            if mm.get("ref_eng") is not None:
+                raise ValueError("ref_eng in mirror_basis MUST be empty")
+            if _get(mm, "norm_vec", "norm_sigma", "norm_mu") is not None:
+                raise ValueError("norm_vec/norm_sigma/norm_mu in mirror_basis MUST be empty")
+            mm = models[b.src - 1]
         D = b.size
         ref = float(mm.get("ref_eng") or 0.0)
         sig = _get(mm, "norm_sigma", "norm_vec")

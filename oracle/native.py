@@ -57,7 +57,9 @@ def pack(model: PackedModel):
             fp_off += sb.size
         nn_off = add(nn.cparam)
         norm_off = add(model.norm[t])
-        spec += [len(b.subs), b.size, len(nn.hidden_dims)] + list(nn.hidden_dims) + [nn_off, norm_off] + sub_entries
+        mirror = b.src if b.kind == "mirror" else 0
+        spec += [len(b.subs), b.size, mirror, len(nn.hidden_dims)] + list(nn.hidden_dims) + [nn_off, norm_off] + \
+            sub_entries
     return (np.asarray(spec, dtype=np.int32), np.asarray(rcuts, dtype=np.float64),
             np.concatenate(blocks) if blocks else np.zeros(0))
 

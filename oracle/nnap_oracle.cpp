@@ -232,7 +232,7 @@ inline double cutoff_grad(double r, double rc) { double u = 1.0 - (r / rc) * (r 
 // params (doubles): all parameter blocks; rcut per sub in rcut[] (flattened per species).
 struct Sub { int kind, nmax, lmax, np, param_off, fp_off; double rcut; };
 struct Species {
-    int D, nlayer, nn_off, norm_off;
+    int D, mirror, nlayer, nn_off, norm_off;  // mirror: 1-based species whose basis is mirrored (0: none)
     std::vector<int> hidden;
     std::vector<Sub> subs;
 };
@@ -243,6 +243,7 @@ std::vector<Species> parse_spec(int T, const int* spec, const double* rcuts) {
     for (int t = 0; t < T; ++t) {
         int nsub = spec[k++];
         sp[t].D = spec[k++];
+        sp[t].mirror = spec[k++];
         sp[t].nlayer = spec[k++];
         for (int i = 0; i < sp[t].nlayer; ++i) sp[t].hidden.push_back(spec[k++]);
         sp[t].nn_off = spec[k++];
@@ -598,6 +599,9 @@ int oracle_compute(int T, const int* spec, const double* rcuts, const double* pa
         for (int j = 0; j < nn; ++j) {
             int tj = type[nei_j[o + j]];
             if (tj < 1 || tj > T) return 2;
+            // a mirror basis sees its own species and the mirrored one swapped
+            // (nnap_main.hpp:40-48, MirrorBasis.java)
+            if (S.mirror) tj = tj == S.mirror ? ti : (tj == ti ? S.mirror : tj);
             ntype[j] = tj;
         }
         const double* ndx = nei_dx + 3 * o;

@@ -186,12 +186,16 @@ def gen_map(model) -> Dict[str, object]:
     ``WTypeBasis.updateGenMap`` (WTypeBasis.java:669-676),
     ``SphericalChebyshev.updateGenMap`` (SphericalChebyshev.java:122-128),
     ``Chebyshev.updateGenMap`` (Chebyshev.java:88-91),
-    ``MergedBasis.updateGenMapInternal`` (MergedBasis.java:149-160) and
+    ``MergedBasis.updateGenMapInternal`` (MergedBasis.java:149-160),
+    ``MirrorBasis.updateGenMap`` / ``SharedBasis.updateGenMap`` (MirrorBasis.java:30-38,
+    SharedBasis.java:30-38) and
     ``FeedForward.updateGenMap`` (FeedForward.java:332-347).
     ``model`` is an :class:`oracle.model.PackedModel`.
     """
     T = model.ntypes
-    bsig = [tuple(sb.genkey() for sb in b.subs) for b in model.basis]
+    # a mirror or shared basis has its own gen map: the kind, the source species and the
+    # source's internal keys (MirrorBasis.java / SharedBasis.java hasSameGenMap)
+    bsig = [(b.kind, b.src, tuple(sb.genkey() for sb in b.subs)) for b in model.basis]
     nsig = [tuple([n.input_dim] + list(n.hidden_dims)) for n in model.nn]
     g: Dict[str, object] = {"NNAPGEN_NTYPES": T}
     g["[FP TYPE]"] = _switch_groups(bsig, lambda a, b: a == b)
@@ -201,7 +205,14 @@ def gen_map(model) -> Dict[str, object]:
     gidx = 0
     for grp in g["[FP NN TYPE]"]:
         b = model.basis[grp[0] - 1]
-        g["[FP MERGE %d]" % gidx] = True
+        if b.kind == "mirror":    # MirrorBasis.updateGenMap
+            g["[FP MIRROR %d]" % gidx] = True
+            g["%d:NNAPGEN_FP_MIRROR_TYPE" % gidx] = b.src
+        elif b.kind == "share":   # SharedBasis.updateGenMap
+            g["[FP SHARE %d]" % gidx] = True
+            g["%d:NNAPGEN_FP_SHARED_TYPE" % gidx] = b.src
+        else:                     # MergedBasis.updateGenMap
+            g["[FP MERGE %d]" % gidx] = True
         g["[FP MERGE SIZE %d]" % gidx] = len(b.subs)
         g["%d:NNAPGEN_FP_SIZE" % gidx] = b.size
         for mi, sb in enumerate(b.subs):

@@ -119,11 +119,31 @@ def cases():
     xs = np.array([[1.0, 1.0, 1.0], [3.2, 1.1, 0.9], [2.0, 3.0, 1.5], [15.0, 15.0, 15.0], [-1.0, 31.5, 7.0]])
     s = W.Structure(xs, np.array([1, 2, 1, 2, 1], dtype=np.int32), np.diag([30.0, 30.0, 30.0]), W.BOX_ORTHO)
     out["isolated_and_unwrapped"] = (W.write_model(["A", "B"], _sph(4, 3, 5.0), [8, 8], 42), s)
+    # mirror and shared bases with a partly shared network: B mirrors A (its own species and
+    # A swapped among the neighbours, A's network and normalisation), C uses A's basis and
+    # shares A's network except the first 4 rows of the first hidden layer and the output
+    s3 = W.random_liquid(120, 0.06, [0.4, 0.4, 0.2], 2.0, 28)
+    for name, basis in (("mirror_share_sph", _sph(3, 2, 5.0, "full")),
+                        ("mirror_share_radial", {"type": "chebyshev", "nmax": 3, "rcut": 5.5, "wtype": "full"})):
+        m = _model(["A", "B", "C"], basis, [8, 8], 43)
+        D = OM.load(m).basis[0].size
+        nrm = _normalised(json.loads(json.dumps(m)), s3)["models"][0]
+        m["models"][0].update({k: nrm[k] for k in ("norm_mu", "norm_sigma", "ref_eng")})
+        m["models"][1] = {"symbol": "B", "basis": {"type": "mirror", "mirror": 1}}
+        m["models"][2]["basis"] = {"type": "share", "share": 1}
+        m["models"][2]["nn"] = {"type": "shared_feed_forward", "share": 1, "shared_hidden_dims": [4, 8],
+                                "hidden_weights": [rng.normal(0, D ** -0.5, (4, D)).tolist(), []],
+                                "hidden_biases": [rng.normal(0, 0.3, 4).tolist(), []],
+                                "output_weight": rng.normal(0, 0.35, 8).tolist(), "output_bias": 0.2}
+        out[name] = (m, s3)
     return out
 
 
 def main():
+    only = set(sys.argv[1:])  # optional case names: regenerate only those
     for name, (model, s) in cases().items():
+        if only and name not in only:
+            continue
         pm = OM.load(model)
         o = ON.compute(pm, s.x, s.types, s.box_kind, s.box)
         nl = o["nl"]

@@ -67,3 +67,60 @@ def test_null_arguments_are_rejected():
     L = _lib()
     assert L.nnap_create(None, 0, 0, 0, None) == 6  # NNAP_ERR_ARG
     assert L.nnap_destroy(None) == 6
+
+
+def _mirror_model():
+    import numpy as np
+    z = np.load(os.path.join(ROOT, "tests", "golden", "mirror_share_sph.npz"))
+    return json.loads(str(z["model_json"]))
+
+
+def _bad_mirror(mut):
+    m = _mirror_model()
+    mut(m)
+    return m
+
+
+MIRROR_BAD = [
+    _bad_mirror(lambda m: m["models"][1]["basis"].update(mirror=2)),            # mirror of a mirror basis
+    _bad_mirror(lambda m: m["models"][1]["basis"].update(mirror=3)),            # mirror of a shared basis
+    _bad_mirror(lambda m: m["models"][1]["basis"].pop("mirror")),               # no source
+    _bad_mirror(lambda m: m["models"][1].update(nn={"hidden_dims": [8, 8]})),   # a mirror has no network
+    _bad_mirror(lambda m: m["models"][1].update(ref_eng=0.5)),                  # nor its own normalisation
+    _bad_mirror(lambda m: m["models"][1].update(norm_mu=[0.0])),
+    _bad_mirror(lambda m: m["models"][2]["basis"].update(share=7)),             # source out of range
+    _bad_mirror(lambda m: m["models"][2]["nn"].update(share=2)),                # base network is not plain
+    _bad_mirror(lambda m: m["models"][2]["nn"].pop("shared_hidden_dims")),
+    _bad_mirror(lambda m: m["models"][2]["nn"].update(shared_hidden_dims=[9, 8])),
+    _bad_mirror(lambda m: m["models"][2]["nn"]["hidden_weights"][0].pop()),      # 3 own rows instead of 4
+    _bad_mirror(lambda m: m["models"][2]["nn"].update(shared_flags=[True, False])),
+]
+
+
+@pytest.mark.parametrize("model", MIRROR_BAD)
+def test_invalid_mirror_and_shared_models_are_rejected(model):
+    """Mirror / shared bases and shared networks: the GPU loader and the oracle's restatement
+    of the reference loader both refuse the same malformed files."""
+    from oracle import model as OM
+    L = _lib()
+    h = C.c_void_p()
+    b = json.dumps(model).encode()
+    assert L.nnap_create(b, len(b), 0, 0, C.byref(h)) == 1  # NNAP_ERR_BAD_MODEL
+    with pytest.raises((ValueError, KeyError, TypeError)):
+        OM.load(model)
+
+
+def test_valid_mirror_and_shared_model_passes_the_loader():
+    """The well-formed model gets past model loading (without a GPU, creation then stops at
+    the first CUDA call with NNAP_ERR_CUDA rather than NNAP_ERR_BAD_MODEL)."""
+    from oracle import model as OM
+    m = _mirror_model()
+    pm = OM.load(m)
+    assert [b.kind for b in pm.basis] == ["plain", "mirror", "share"]
+    L = _lib()
+    h = C.c_void_p()
+    b = json.dumps(m).encode()
+    rc = L.nnap_create(b, len(b), 0, 0, C.byref(h))
+    if rc == 0:
+        L.nnap_destroy(h)
+    assert rc != 1
