@@ -44,14 +44,15 @@ METRIC = "NNAP E+F atom-evals/s"
 
 
 # ----------------------------------------------------------------------------- workloads
-def make_workload(name: str):
-    """Structures and a model-factory taking per-species normalisation statistics."""
+def make_workload(name: str, atoms: int = 0):
+    """Structures and a model-factory taking per-species normalisation statistics.  ``atoms``
+    resizes the liquid and glass workloads (same density and composition), for profiling."""
     if name == "liquid32k":
-        return [W.c2_structure()], "c2"
+        return [W.c2_structure(atoms) if atoms else W.c2_structure()], "c2"
     if name == "fcc4000":
         return [W.c1_structure()], "c1"
     if name == "glass1m":
-        return [W.c3_structure()], "c3"
+        return [W.c3_structure(atoms) if atoms else W.c3_structure()], "c3"
     if name == "batch1024":
         return W.c4_structures(), "c4"
     raise SystemExit("unknown workload " + name)
@@ -276,6 +277,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--serve-requests", type=int, default=5000)
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (profiling runs)")
+    ap.add_argument("--atoms", type=int, default=0, help="resize the liquid / glass workload (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -283,7 +285,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist, rank, world = init_from_env("gloo")
 
-    structures, cfg = make_workload(args.workload)
+    structures, cfg = make_workload(args.workload, args.atoms)
     natoms_step = sum(s.natoms for s in structures)
     config = {"workload": args.workload, "structures": len(structures), "atoms_per_step": natoms_step,
               "precision": args.precision, "l2": "flushed between steps (256 MiB write)",
