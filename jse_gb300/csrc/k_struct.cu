@@ -418,12 +418,28 @@ __global__ void k_type_scatter(const int* __restrict__ type, int n, int T, const
 }
 
 // ----------------------------------------------------------------- gather
-// One thread per atom a: F_a = sum_k (g[mirror(a,k)] - g[a,k]);
-// W_a = sum_k dx[mirror(a,k)] (x) g[mirror(a,k)].  Sums are carried as float-float
-// pairs (exact products, error-free additions) and written as FP64.
+// Eight lanes per atom a: F_a = sum_k (g[mirror(a,k)] - g[a,k]);
+// W_a = sum_k dx[mirror(a,k)] (x) g[mirror(a,k)], with dx[mirror(a,k)] = -dx[a,k] (the
+// mirrored displacement is the negated one; both are the same exact value rounded to
+// nearest, which is symmetric under negation).  Each lane sums every eighth entry of the
+// row as float-float pairs (exact products, error-free additions); the eight partial
+// sums are combined by a fixed xor butterfly, so the result does not depend on timing.
+// Own-row loads are coalesced; only g of the mirrored entry is a scattered load.
+constexpr int kGatherLanes = 8;
+
+__device__ __forceinline__ void ff_merge(float& h, float& l, unsigned mask, int off) {
+    const float oh = __shfl_xor_sync(mask, h, off), ol = __shfl_xor_sync(mask, l, off);
+    float s, e;
+    two_sum(h, oh, s, e);
+    h = s;
+    l = (l + ol) + e;
+}
+
 __global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double* __restrict__ virials) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= n) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = t / kGatherLanes, sub = t & (kGatherLanes - 1);
+    if (a >= n) return;  // all eight lanes of an atom leave together
+    const unsigned mask = 0xFFu << ((threadIdx.x & 31) & ~(kGatherLanes - 1));
     const int M = P.M;
     const int cnt = min(P.count[a], M);
     float fh[3] = {0.f, 0.f, 0.f}, fl[3] = {0.f, 0.f, 0.f};
@@ -431,29 +447,37 @@ __global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double*
 #pragma unroll
     for (int d = 0; d < 9; ++d) { vh[d] = 0.f; vl[d] = 0.f; }
     const size_t row = (size_t)a * M;
-#pragma unroll 2
-    for (int k = 0; k < cnt; ++k) {
+    for (int k = sub; k < cnt; k += kGatherLanes) {
         const float4 go = P.g[row + k];
-        const int r = P.rev[row + k];
-        const float4 gr = P.g[r];
-        const float4 dr = P.dx[r];
+        const float4 dn = P.dx[row + k];
+        const float4 gr = P.g[P.rev[row + k]];
+        const float dx = -dn.x, dy = -dn.y, dz = -dn.z;
         ff_acc(fh[0], fl[0], gr.x); ff_acc(fh[0], fl[0], -go.x);
         ff_acc(fh[1], fl[1], gr.y); ff_acc(fh[1], fl[1], -go.y);
         ff_acc(fh[2], fl[2], gr.z); ff_acc(fh[2], fl[2], -go.z);
-        ff_acc_prod(vh[0], vl[0], dr.x, gr.x);
-        ff_acc_prod(vh[1], vl[1], dr.y, gr.y);
-        ff_acc_prod(vh[2], vl[2], dr.z, gr.z);
-        ff_acc_prod(vh[3], vl[3], dr.x, gr.y);
-        ff_acc_prod(vh[4], vl[4], dr.x, gr.z);
-        ff_acc_prod(vh[5], vl[5], dr.y, gr.z);
-        ff_acc_prod(vh[6], vl[6], dr.y, gr.x);
-        ff_acc_prod(vh[7], vl[7], dr.z, gr.x);
-        ff_acc_prod(vh[8], vl[8], dr.z, gr.y);
+        ff_acc_prod(vh[0], vl[0], dx, gr.x);
+        ff_acc_prod(vh[1], vl[1], dy, gr.y);
+        ff_acc_prod(vh[2], vl[2], dz, gr.z);
+        ff_acc_prod(vh[3], vl[3], dx, gr.y);
+        ff_acc_prod(vh[4], vl[4], dx, gr.z);
+        ff_acc_prod(vh[5], vl[5], dy, gr.z);
+        ff_acc_prod(vh[6], vl[6], dy, gr.x);
+        ff_acc_prod(vh[7], vl[7], dz, gr.x);
+        ff_acc_prod(vh[8], vl[8], dz, gr.y);
     }
 #pragma unroll
-    for (int d = 0; d < 3; ++d) forces[3 * (size_t)a + d] = (double)fh[d] + (double)fl[d];
+    for (int off = kGatherLanes / 2; off > 0; off >>= 1) {
 #pragma unroll
-    for (int d = 0; d < 9; ++d) virials[9 * (size_t)a + d] = (double)vh[d] + (double)vl[d];
+        for (int d = 0; d < 3; ++d) ff_merge(fh[d], fl[d], mask, off);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) ff_merge(vh[d], vl[d], mask, off);
+    }
+    if (sub == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) forces[3 * (size_t)a + d] = (double)fh[d] + (double)fl[d];
+#pragma unroll
+        for (int d = 0; d < 9; ++d) virials[9 * (size_t)a + d] = (double)vh[d] + (double)vl[d];
+    }
 }
 
 // ----------------------------------------------------------------- per-structure totals

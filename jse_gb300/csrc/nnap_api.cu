@@ -438,8 +438,9 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     h->mark(4);
     if (!fp_only && gather) {
         if (n > 0) {
-            const int gb = h->tune.gather_block;
-            k_gather<<<(n + gb - 1) / gb, gb, 0, st>>>(pair_bufs(h), n, h->forces.p, h->virials.p);
+            const int gb = h->tune.gather_block;  // threads per CTA, eight per atom
+            k_gather<<<(unsigned)(((size_t)n * 8 + gb - 1) / gb), gb, 0, st>>>(pair_bufs(h), n, h->forces.p,
+                                                                               h->virials.p);
             ++h->launches;
         }
         const int nchunks = (int)B.cb.size();
