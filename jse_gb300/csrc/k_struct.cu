@@ -176,6 +176,17 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             const int cid = st.c0 + c0 + st.nc[0] * (c1 + st.nc[1] * c2);
             const int cs = cell_start[cid];
             ccount = cell_start[cid + 1] - cs;
+            if (st.kind == 0) {
+                // orthogonal box: a lower bound of the distance from atom i to the target
+                // cell (unwrapped cell q spans [q, q+1) cell widths); cells beyond the screen
+                // bound (rc^2 plus its rounding margin) hold no neighbour and are skipped
+                const float wx = st.fa[0] / (float)st.nc[0], wy = st.fb[1] / (float)st.nc[1],
+                            wz = st.fc[2] / (float)st.nc[2];
+                const float gx = fmaxf(0.f, fmaxf((float)q0 * wx - fi.x, fi.x - (float)(q0 + 1) * wx));
+                const float gy = fmaxf(0.f, fmaxf((float)q1 * wy - fi.y, fi.y - (float)(q1 + 1) * wy));
+                const float gz = fmaxf(0.f, fmaxf((float)q2 * wz - fi.z, fi.z - (float)(q2 + 1) * wz));
+                if (gx * gx + gy * gy + gz * gz > st.rc2_hi) ccount = 0;
+            }
             s_start[w][lane] = cs;
             s_img[w][lane] = pack_img(na, nb, nc);
             double sh[3] = {0.0, 0.0, 0.0};  // the zero image has an exactly zero shift
