@@ -27,6 +27,8 @@ struct StructDev {
     float fa[3], fb[3], fc[3];    // float box rows for the candidate screen
     float rc2_hi;                 // float screen bound (rc^2 plus rounding margin)
     float la[3], lb[3], lc[3];    // low parts of the box rows: a = fa + la to ~48 bits
+    float iv[3][3];               // rows b x c, c x a, a x b over the volume: direct coordinates
+    float smin2;                  // squared smallest singular value of the box matrix (0: unknown)
     int kind;                     // 0 orthogonal, 1 LAMMPS lower-triangular, 2 general prism
     int a0, n;                    // atom range in the batch
     int c0;                       // first cell of this structure in the global cell arrays

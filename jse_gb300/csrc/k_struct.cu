@@ -157,6 +157,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     const double xi = xw[3 * i], yi = xw[3 * i + 1], zi = xw[3 * i + 2];
     const float4 fi = xf[i];
     const float4 li = xlo[i];
+
     const float rc2h = (float)st.rc2, rc2l = (float)(st.rc2 - (double)(float)st.rc2);
     const float tol = 1e-10f * rc2h;  // float-float d^2 is accurate to ~1e-12 relative
     int cnt = 0;
@@ -186,6 +187,21 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 const float gy = fmaxf(0.f, fmaxf((float)q1 * wy - fi.y, fi.y - (float)(q1 + 1) * wy));
                 const float gz = fmaxf(0.f, fmaxf((float)q2 * wz - fi.z, fi.z - (float)(q2 + 1) * wz));
                 if (gx * gx + gy * gy + gz * gz > st.rc2_hi) ccount = 0;
+            } else if (st.smin2 > 0.f) {
+                // skewed box: the gap in direct coordinates times the box's smallest
+                // singular value bounds the Cartesian distance from below (the atom's
+                // direct coordinates are formed here, so they hold no register in the
+                // candidate loop)
+                const int q[3] = {q0, q1, q2};
+                float g2 = 0.f;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float ui = st.iv[d][0] * fi.x + st.iv[d][1] * fi.y + st.iv[d][2] * fi.z;
+                    const float inv_n = 1.f / (float)st.nc[d];
+                    const float g = fmaxf(0.f, fmaxf((float)q[d] * inv_n - ui, ui - (float)(q[d] + 1) * inv_n));
+                    g2 += g * g;
+                }
+                if (st.smin2 * g2 > st.rc2_hi) ccount = 0;
             }
             s_start[w][lane] = cs;
             s_img[w][lane] = pack_img(na, nb, nc);

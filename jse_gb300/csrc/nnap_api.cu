@@ -122,6 +122,38 @@ void cross3(const double* u, const double* v, double* r) {
     r[2] = u[0] * v[1] - v[0] * u[1];
 }
 
+// Smallest eigenvalue of G = H H^T for the box matrix H (rows a, b, c): the squared
+// smallest singular value, so |u H| >= sqrt of it times |u| for any direct-coordinate
+// vector u.  Cyclic Jacobi rotations on the symmetric 3 x 3 matrix.
+double smallest_sq_singular(const StructDev& s) {
+    const double* r[3] = {s.a, s.b, s.c};
+    double G[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) G[i][j] = r[i][0] * r[j][0] + r[i][1] * r[j][1] + r[i][2] * r[j][2];
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        const double off = G[0][1] * G[0][1] + G[0][2] * G[0][2] + G[1][2] * G[1][2];
+        const double diag = G[0][0] * G[0][0] + G[1][1] * G[1][1] + G[2][2] * G[2][2];
+        if (off <= 1e-30 * diag) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (G[p][q] == 0.0) continue;
+                const double th = 0.5 * std::atan2(2.0 * G[p][q], G[q][q] - G[p][p]);
+                const double c = std::cos(th), sn = std::sin(th);
+                for (int k = 0; k < 3; ++k) {  // columns p, q
+                    const double gp = G[k][p], gq = G[k][q];
+                    G[k][p] = c * gp - sn * gq;
+                    G[k][q] = sn * gp + c * gq;
+                }
+                for (int k = 0; k < 3; ++k) {  // rows p, q
+                    const double gp = G[p][k], gq = G[q][k];
+                    G[p][k] = c * gp - sn * gq;
+                    G[q][k] = sn * gp + c * gq;
+                }
+            }
+    }
+    return std::max(0.0, std::min(G[0][0], std::min(G[1][1], G[2][2])));
+}
+
 // Float bound for the candidate screen: rc^2 plus the worst rounding of the FP32
 // difference (x_j + shift) - x_i for image shifts up to Rm + 2 box lengths.
 float screen_bound(const StructDev& s, double rc, int Rm) {
@@ -167,6 +199,12 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
     }
     s.rc2 = rc * rc;
     s.rc2_hi = screen_bound(s, rc, std::max(s.R[0], std::max(s.R[1], s.R[2])));
+    for (int d = 0; d < 3; ++d) {
+        s.iv[0][d] = (float)(s.bc[d] / s.vol);
+        s.iv[1][d] = (float)(s.ca[d] / s.vol);
+        s.iv[2][d] = (float)(s.ab[d] / s.vol);
+    }
+    s.smin2 = (float)(smallest_sq_singular(s) * (1.0 - 1e-5));
     s.a0 = a0;
     s.n = n;
     s.c0 = c0;
