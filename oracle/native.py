@@ -207,6 +207,48 @@ class RefLib:
             raise RuntimeError("reference per-atom function returned %d" % code)
         return {"energies": e, "energy": float(e.sum()), "forces": f, "virials": v, "virial": v.sum(axis=0)}
 
+    def train_grad(self, types, nl: NeighborList, bgrad_e=None, bgrad_f=None, bgrad_w=None, nthreads: int = 1):
+        """Parameter gradients of L = bE.E + bF.F + bW.W through the reference's training pair
+        (ref_train_grad in ref_driver.cpp); returns per-species lists ``grad_fp`` and ``grad_nn``
+        in the reference's C-level parameter layouts."""
+        m = self.model
+        T = m.ntypes
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        n = len(types)
+        fp_size = np.array([m.basis[t].param.size for t in range(T)], dtype=np.int64)
+        nn_size = np.array([m.nn[t].cparam.size for t in range(T)], dtype=np.int64)
+        per, const = 0, 0
+        for t in range(T):
+            p, c = 0, 0
+            for sb in m.basis[t].subs:
+                K = (max(sb.lmax, sb.l3max, sb.l4max) + 1) ** 2 if sb.kind == "spherical_chebyshev" else 1
+                p += 2 + 2 * (sb.nmax + 1) + 2 * sb.size_np + 3 * K
+                c += 3 * sb.size_np * K
+            nnw = m.nn[t].input_dim + sum(m.nn[t].hidden_dims)
+            per, const = max(per, p), max(const, c + 4 * nnw)
+        const += 64
+        be = None if bgrad_e is None else np.ascontiguousarray(bgrad_e, dtype=np.float64).reshape(n)
+        bf = None if bgrad_f is None else np.ascontiguousarray(bgrad_f, dtype=np.float64).reshape(n, 3)
+        bw = None if bgrad_w is None else np.ascontiguousarray(bgrad_w, dtype=np.float64).reshape(9)
+        gfp = np.zeros(max(int(fp_size.sum()), 1))
+        gnn = np.zeros(max(int(nn_size.sum()), 1))
+        dx = np.ascontiguousarray(nl.dx, dtype=np.float64)
+        nul = C.POINTER(C.c_double)()
+        code = self.lib.ref_train_grad(T, self.hp, self.fpp, self.nnp, self.nrm, n, _p(types, C.c_int),
+                                       _p(nl.offsets, C.c_long), _p(nl.j, C.c_int), _p(dx, C.c_double),
+                                       C.c_long(per), C.c_long(const), nthreads,
+                                       nul if be is None else _p(be, C.c_double),
+                                       nul if bf is None else _p(bf, C.c_double),
+                                       nul if bw is None else _p(bw, C.c_double),
+                                       _p(fp_size, C.c_long), _p(nn_size, C.c_long),
+                                       _p(gfp, C.c_double), _p(gnn, C.c_double))
+        if code != 0:
+            raise RuntimeError("reference training functions returned %d" % code)
+        of = np.concatenate([[0], np.cumsum(fp_size)])
+        on = np.concatenate([[0], np.cumsum(nn_size)])
+        return {"grad_fp": [gfp[of[t]:of[t + 1]].copy() for t in range(T)],
+                "grad_nn": [gnn[on[t]:on[t + 1]].copy() for t in range(T)]}
+
     def fp(self, types, nl: NeighborList):
         types = np.ascontiguousarray(types, dtype=np.int32)
         n = len(types)

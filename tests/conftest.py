@@ -33,6 +33,9 @@ class Case:
         self.xw = z["xw"]
         self.nl_offsets, self.nl_j, self.nl_img = z["nl_offsets"], z["nl_j"], z["nl_img"]
         self.energies, self.forces, self.virials, self.fp = z["energies"], z["forces"], z["virials"], z["fp"]
+        # training gradients of L = bE.E + bF.F + bW.W (reference C-level parameter layouts)
+        self.train_be, self.train_bf, self.train_bw = z["train_be"], z["train_bf"], z["train_bw"]
+        self.train_grad_fp, self.train_grad_nn = z["train_grad_fp"], z["train_grad_nn"]
 
     def nl_set(self):
         out = set()

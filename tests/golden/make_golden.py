@@ -13,7 +13,10 @@ driver (``oracle/ref_driver.cpp``) scatters energies, forces and per-atom virial
 like ``NNAP.calEnergyForceVirial``.  Descriptors come from ``jse_nnap_calFp``.
 
 Each ``<case>.npz`` holds the model JSON text, the structure, the neighbour set
-(offsets, j, image) and the reference's FP64 outputs.
+(offsets, j, image) and the reference's FP64 outputs, including the parameter
+gradients of a seeded energy / force / virial loss through the reference's training
+pair ``jse_nnap_forwardEnergyForce`` / ``jse_nnap_backwardEnergyForce``
+(``train_*`` keys; ``ref_train_grad`` in ``oracle/ref_driver.cpp``).
 """
 from __future__ import annotations
 
@@ -150,11 +153,18 @@ def main():
         ref = ON.RefLib(pm)
         r = ref.compute(s.types, nl)
         fp = ref.fp(s.types, nl)
+        # training gradients of L = bE.E + bF.F + bW.W for seeded upstream gradients
+        n = len(s.types)
+        rng = np.random.default_rng(len(name) * 7919 + n)
+        be, bf, bw = rng.normal(size=n), rng.normal(size=(n, 3)), rng.normal(size=9)
+        tg = ref.train_grad(s.types, nl, be, bf, bw)
         np.savez_compressed(
             os.path.join(HERE, name + ".npz"),
             model_json=np.array(json.dumps(model)), x=s.x, types=s.types, box=s.box, box_kind=np.array(s.box_kind),
             xw=o["xw"], nl_offsets=nl.offsets, nl_j=nl.j, nl_img=nl.img,
-            energies=r["energies"], forces=r["forces"], virials=r["virials"], fp=fp)
+            energies=r["energies"], forces=r["forces"], virials=r["virials"], fp=fp,
+            train_be=be, train_bf=bf, train_bw=bw, train_grad_fp=np.concatenate(tg["grad_fp"]),
+            train_grad_nn=np.concatenate(tg["grad_nn"]))
         print("%-24s n=%4d pairs=%6d E=%.10f" % (name, len(s.types), len(nl.j), r["energy"]))
 
 
