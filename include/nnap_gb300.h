@@ -156,6 +156,33 @@ int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int* ilist, co
                         int eflag, int vflag, int eflag_atom, int vflag_atom, int cvflag_atom, double* f,
                         double* eng_vdwl, double* eatom, double* virial, double* vatom, double* cvatom);
 
+/* Parameter counts of species `type` (1-based): *fp_size entries of its basis's C-level
+ * parameters (the internal radial-fuse matrices of its sub-bases, [t_nei][np][n] each,
+ * WTypeBasis.cptrParameterSize, WTypeBasis.java:609-611) and *nn_size of its network
+ * (hidden W [out][in] per layer | output W | hidden b per layer | output b,
+ * FeedForward.mountCptrParameter, FeedForward.java:310-316). */
+int nnap_param_sizes(const nnap_handle* h, int type, int* fp_size, int* nn_size);
+
+/* Force-training gradients: dL/dparameters of
+ *   L = sum_i bE_i E_i + sum_i bF_i . F_i + sum_s sum_ab bW_sab W_sab
+ * over a batch of structures (E per-atom energies, F forces, W_s the total virial of
+ * structure s, components xx, yy, zz, xy, xz, yz, yx, zx, zy).  Replaces the per-atom
+ * training pair jse_nnap_forwardEnergyForce + jse_nnap_backwardEnergyForce
+ * (nnap_interface.cpp:142-232) as TrainerNNAP drives it (TrainerNNAP.java:1006-1175:
+ * every pair (i, j) receives bF_j - bF_i plus the stress terms as the upstream gradient
+ * of its g_ij, and bE_i as that of E_i).  Batch layout as nnap_compute_batch.
+ * bgrad_energies (n), bgrad_forces (3n) and bgrad_virial (9 per structure) may each be
+ * NULL (zero).  grad_nn receives, concatenated over species, the network gradients in
+ * the layout of nnap_param_sizes; grad_fp (may be NULL) the basis gradients, which are
+ * zero for every weight type without trainable radial weights (the reference computes
+ * none either).  Models with fused radial weights (wtype fuse, rfuse, exfuse) and a
+ * non-NULL grad_fp return NNAP_ERR_UNSUPPORTED.  Arithmetic is FP32 with FP64 sums of
+ * fixed chunks, whatever the handle's precision.  Host buffers, synchronous. */
+int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const double* x, const int* type,
+                          const int* box_kind, const double* boxes, const double* bgrad_energies,
+                          const double* bgrad_forces, const double* bgrad_virial, double* grad_fp,
+                          double* grad_nn);
+
 /* Number of this library's kernels launched by the last compute call on the handle. */
 int nnap_last_launch_count(const nnap_handle* h, int* count);
 

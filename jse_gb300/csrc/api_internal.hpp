@@ -17,6 +17,7 @@
 #include "desc.cuh"
 #include "model.hpp"
 #include "net_tc.cuh"
+#include "train.cuh"
 
 namespace nnapgb {
 
@@ -152,6 +153,12 @@ struct nnap_handle {
     nnapgb::DevBuf<double> lmp_x, lmp_forces, lmp_virials;
     nnapgb::DevBuf<int> lmp_type, lmp_ilist, lmp_off, lmp_idx, lmp_rowtype, lmp_rowof, lmp_tcount, lmp_tstart,
         lmp_tfill, lmp_tlist;
+    // force-training gradients: directional derivatives, upstream gradients, per-slot
+    // network records, chunk partials and the FP64 result
+    nnapgb::DevBuf<float> tu, trec, tpart, tbW;
+    nnapgb::DevBuf<float4> tbF;
+    nnapgb::DevBuf<double> tbFd, tbE, tgrad;
+    nnapgb::DevBuf<nnapgb::GradTile> ttiles;
     int GS = 0;                  // cell-offset groups per atom + 1 kept by k_neighbors (0: none)
     nnapgb::DevBuf<int> gstart;  // [n][GS] group starts of each neighbour row
     int* h_status = nullptr;  // pinned: [0]=err bits [1]=max count [2..]=type_start
@@ -163,6 +170,7 @@ struct nnap_handle {
     int layout_runs = 0;
     std::vector<long long> last_layout, gkey;
     cudaGraphExec_t gexec = nullptr;
+    int glaunches = 0;  // kernel launches of the captured sequence
     nnapgb::StructDev* h_sdev = nullptr;  // pinned staging of the structure descriptors
     size_t h_sdev_cap = 0;
     int sm_count = 148;
@@ -223,6 +231,16 @@ void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type);
 // Queue descriptors, networks and descriptor gradients; with gather, also the
 // force / virial gather over mirrored rows and the per-structure reductions.
 void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather);
+// Run the whole launch sequence of a batch (neighbours, species order, descriptors and,
+// unless fp_only, networks, pair gradients and reductions), growing the neighbour
+// capacity and repeating as needed; returns after the stream has drained.
+void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only);
+// Plan a batch: structure descriptors, cell grids and reduction chunks.
+Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes);
+// Copy host positions and species into the handle's device buffers.
+void upload_inputs(nnap_handle* h, int n, const double* x, const int* type);
+// Bytes of the spherical expansion-coefficient arena for n atom slots.
+size_t a_arena_size(nnap_handle* h, int n);
 void check_outputs(int flags, const Outputs& o);
 // Forget the captured launch sequence of the handle.
 void drop_graph(nnap_handle* h);

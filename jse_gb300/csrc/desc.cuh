@@ -26,6 +26,12 @@ struct DescArgs {
     int warps;              // warps per CTA (2, 4 or 8; one atom slot per warp)
 };
 
+// Compiled shapes.  Radial: (NP, N1).  Spherical: (L, NP, N1).
+#define NNAP_RADIAL_SHAPES(X) X(11, 11) X(12, 6) X(4, 4) X(8, 4) X(12, 4) X(18, 9)
+#define NNAP_SPH_SHAPES(X)                                                                    \
+    X(6, 18, 9) X(4, 18, 9) X(4, 5, 5) X(2, 4, 4) X(2, 8, 4) X(2, 12, 4) X(3, 5, 4) X(2, 16, 4) \
+    X(3, 10, 5) X(6, 9, 9) X(4, 9, 9) X(3, 8, 4) X(4, 10, 5)
+
 cudaError_t upload_sh_constants();
 bool desc_supported(int kind, int lmax, int np, int n1);
 cudaError_t launch_descriptor(int kind, int lmax, int np, int n1, const DescArgs& a, bool fwd, cudaStream_t st);

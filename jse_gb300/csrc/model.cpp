@@ -238,6 +238,7 @@ SubBasis load_sub(int kind, int T, const JValue& m) {
         default: bad("invalid wtype");
     }
     b.size = kind == KIND_RADIAL ? NP : NP * (b.lmax + 1);
+    b.fused = tw == WT_RFUSE || tw == WT_FUSE || tw == WT_EXFUSE;
     return b;
 }
 

@@ -17,6 +17,7 @@ struct SubBasis {
     int nmax = 5, lmax = 0, np = 0;
     int fp_off = 0, size = 0;
     double rcut = 6.0;
+    bool fused = false;     // wtype fuse / rfuse / exfuse: the matrix is a trainable parameter
     std::vector<double> W;  // T * np * (nmax+1)
 };
 

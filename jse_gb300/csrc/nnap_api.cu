@@ -638,6 +638,7 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
         const std::vector<long long> key = layout_key(h, B, d_x, d_type, fp_only);
         if (h->gexec && h->gkey == key) {
             CK(cudaGraphLaunch(h->gexec, h->stream));
+            h->launches = h->glaunches;
         } else if (h->use_graphs && h->layout_runs >= 1) {
             drop_graph(h);
             cudaGraph_t g = nullptr;
@@ -658,6 +659,7 @@ void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_ty
             cudaGraphDestroy(g);
             CK(e);
             h->gkey = key;
+            h->glaunches = h->launches;
             CK(cudaGraphLaunch(h->gexec, h->stream));
         } else {
             enqueue(h, B, d_x, d_type, fp_only);
@@ -746,6 +748,7 @@ int nnap_create(const char* model_json, size_t len, int precision, int device, n
         CK(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
         CK(cudaMallocHost(&h->h_status, sizeof(int) * (3 + kMaxTypes)));
         CK(upload_sh_constants());
+        CK(upload_sh_constants_train());
         upload_model(h.get());
     } catch (const ApiFail& e) {
         std::fprintf(stderr, "nnap_create: %s\n", e.what());

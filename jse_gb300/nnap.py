@@ -98,6 +98,8 @@ def load_library(path: str = LIB_PATH):
     L.nnap_server_step.argtypes = [P, I, ip, dp, I, dp, dp, dp, dp, dp]
     L.nnap_server_neighbor_list.argtypes = [P, I, ip, C.c_longlong, ip, ip, C.POINTER(C.c_longlong)]
     L.nnap_server_stats.argtypes = [P, C.POINTER(C.c_longlong)]
+    L.nnap_param_sizes.argtypes = [P, I, ip, ip]
+    L.nnap_train_grad_batch.argtypes = [P, I, ip, dp, ip, ip, dp, dp, dp, dp, dp, dp]
     _lib = L
     return L
 
@@ -340,6 +342,53 @@ class NNAP:
                 r["virials"] = va[a0:a0 + n]
             out.append(r)
             a0 += n
+        return out
+
+    def paramSizes(self, t: int):
+        """(basis parameters, network parameters) of species t (1-based), C-level layouts."""
+        a, b = C.c_int(0), C.c_int(0)
+        self._check(self._L.nnap_param_sizes(self._handle(), int(t), C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def backwardEnergyForceBatch(self, structures: Sequence, bgrad_energies=None, bgrad_forces=None,
+                                 bgrad_virial=None, want_fp: bool = False) -> dict:
+        """Parameter gradients of L = sum bE.E + sum bF.F + sum bW.W over a batch of structures.
+
+        The structure-level form of the reference's training pair forwardEnergyForce /
+        backwardEnergyForce (NNAP.java:823-869) as TrainerNNAP drives it: ``bgrad_energies``
+        holds dL/dE_i per atom, ``bgrad_forces`` dL/dF_i (n x 3), ``bgrad_virial`` dL/dW per
+        structure (9 components xx, yy, zz, xy, xz, yz, yx, zx, zy); each may be None.
+        Returns per-species lists ``grad_nn`` (hidden W | output W | hidden b | output b)
+        and, with ``want_fp``, ``grad_fp`` (radial-fuse matrices)."""
+        xs, ts, kinds, boxes, ns = [], [], [], [], []
+        for s in structures:
+            x, t, box, kind = _unpack(s)
+            xs.append(x); ts.append(t); kinds.append(kind); boxes.append(box); ns.append(len(t))
+        S = len(ns)
+        x = np.ascontiguousarray(np.concatenate(xs)) if S else np.zeros((0, 3))
+        t = np.ascontiguousarray(np.concatenate(ts)).astype(np.int32)
+        nat = np.asarray(ns, dtype=np.int32)
+        kd = np.asarray(kinds, dtype=np.int32)
+        bx = np.ascontiguousarray(np.concatenate(boxes))
+        N = int(nat.sum())
+        be = None if bgrad_energies is None else np.ascontiguousarray(bgrad_energies, dtype=np.float64).reshape(N)
+        bf = None if bgrad_forces is None else np.ascontiguousarray(bgrad_forces, dtype=np.float64).reshape(N, 3)
+        bw = None if bgrad_virial is None else np.ascontiguousarray(bgrad_virial, dtype=np.float64).reshape(S, 9)
+        T = self.ntypes()
+        sizes = [self.paramSizes(k + 1) for k in range(T)]
+        gfp = np.zeros(max(sum(a for a, _ in sizes), 1)) if want_fp else None
+        gnn = np.zeros(max(sum(b for _, b in sizes), 1))
+        self._check(self._L.nnap_train_grad_batch(self._handle(), S, _iptr(nat), _dptr(x), _iptr(t), _iptr(kd),
+                                                  _dptr(bx), _dptr(be), _dptr(bf), _dptr(bw), _dptr(gfp),
+                                                  _dptr(gnn)))
+        out = {"grad_nn": [], "grad_fp": [] if want_fp else None}
+        on = of = 0
+        for a, b in sizes:
+            out["grad_nn"].append(gnn[on:on + b].copy())
+            on += b
+            if want_fp:
+                out["grad_fp"].append(gfp[of:of + a].copy())
+                of += a
         return out
 
     def computeLammps(self, ilist, neighbors, x, types, type_map=None, eflag=True, vflag=True, eflag_atom=True,
