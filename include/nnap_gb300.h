@@ -173,11 +173,14 @@ int nnap_param_sizes(const nnap_handle* h, int type, int* fp_size, int* nn_size)
  * of its g_ij, and bE_i as that of E_i).  Batch layout as nnap_compute_batch.
  * bgrad_energies (n), bgrad_forces (3n) and bgrad_virial (9 per structure) may each be
  * NULL (zero).  grad_nn receives, concatenated over species, the network gradients in
- * the layout of nnap_param_sizes; grad_fp (may be NULL) the basis gradients, which are
- * zero for every weight type without trainable radial weights (the reference computes
- * none either).  Models with fused radial weights (wtype fuse, rfuse, exfuse) and a
- * non-NULL grad_fp return NNAP_ERR_UNSUPPORTED.  Arithmetic is FP32 with FP64 sums of
- * fixed chunks, whatever the handle's precision.  Host buffers, synchronous. */
+ * the layout of nnap_param_sizes; grad_fp (may be NULL) the basis gradients in the same
+ * way: for sub-bases with trainable radial weights (wtype fuse, rfuse, exfuse, and
+ * post-fused ones) the gradient of the internal radial-fuse matrix, added to the species
+ * that owns the parameters (a mirror or shared basis's gradient goes to its source, as
+ * in nnap_main.hpp:398-445); zero for the other weight types, for which the reference
+ * computes none.  Arithmetic is FP32 with FP64 sums over fixed partitions of the atoms,
+ * whatever the handle's precision, so repeated calls return identical results.  Host
+ * buffers, synchronous. */
 int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const double* x, const int* type,
                           const int* box_kind, const double* boxes, const double* bgrad_energies,
                           const double* bgrad_forces, const double* bgrad_virial, double* grad_fp,

@@ -155,9 +155,9 @@ struct nnap_handle {
         lmp_tfill, lmp_tlist;
     // force-training gradients: directional derivatives, upstream gradients, per-slot
     // network records, chunk partials and the FP64 result
-    nnapgb::DevBuf<float> tu, trec, tpart, tbW;
+    nnapgb::DevBuf<float> tu, trec, tpart, tbW, tdA, tgfp, tdfp, twpart;
     nnapgb::DevBuf<float4> tbF;
-    nnapgb::DevBuf<double> tbFd, tbE, tgrad;
+    nnapgb::DevBuf<double> tbFd, tbE, tgrad, twgrad;
     nnapgb::DevBuf<nnapgb::GradTile> ttiles;
     int GS = 0;                  // cell-offset groups per atom + 1 kept by k_neighbors (0: none)
     nnapgb::DevBuf<int> gstart;  // [n][GS] group starts of each neighbour row

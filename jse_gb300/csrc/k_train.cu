@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(32 * kJvpWarps) k_sph_jvp(JvpArgs ja) {
     }
     // A dA products (A from the forward pass) into the freed Y tiles, then the l sums
     const float* Ain = a.A + (size_t)w * NP * S::K;
+    float* dAout = ja.dA ? ja.dA + (size_t)w * NP * S::K : nullptr;
     float* sP = sY;  // [NP][K]
 #pragma unroll
     for (int col = 0; col < S::COLS; ++col) {
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(32 * kJvpWarps) k_sph_jvp(JvpArgs ja) {
             for (int p = 0; p < NP; ++p) {
                 const float v = (p & 1) ? acc[p >> 1][col].y : acc[p >> 1][col].x;
                 sP[p * S::K + lm] = Ain[p * S::K + lm] * v;
+                if (dAout) dAout[p * S::K + lm] = v;
             }
     }
     __syncwarp();
@@ -418,7 +420,15 @@ __global__ void __launch_bounds__(128) k_net_train(NetTrainArgs a, int warp_floa
         for (int k = lane; k < H * kTrainAtoms; k += 32) t0[k] = aH[k] * silu_g(z[k]);
         __syncwarp();
         put_rec(a.rec, a.V, slot0, na, roff[l], H, t0, lane);
-        if (l > 0) mv_bwd(Wr[l], in_of[l], H, t0, ab + zoff[l - 1], lane);
+        if (l > 0) {
+            mv_bwd(Wr[l], in_of[l], H, t0, ab + zoff[l - 1], lane);
+        } else if (a.gfp) {  // dE/dfp = (W_1^T aZ_1) / sigma
+            mv_bwd(Wr[0], D, H, t0, t1, lane);
+            __syncwarp();
+            for (int q = 0; q < na; ++q)
+                for (int i = lane; i < D; i += 32)
+                    a.gfp[(size_t)(slot0 + q) * a.fp_stride + i] = t1[i * kTrainAtoms + q] * isig[i];
+        }
         __syncwarp();
     }
     // force term: U_l forward, bz_l into the aH_l buffers
@@ -461,7 +471,17 @@ __global__ void __launch_bounds__(128) k_net_train(NetTrainArgs a, int warp_floa
         for (int l = L - 1; l >= 0; --l) {
             const int H = a.H[l];
             put_rec(a.rec, a.V, slot0, na, roff[l] + H, H, dz, lane);
-            if (l == 0) break;
+            if (l == 0) {
+                if (a.dfp) {  // dL/dfp = (W_1^T dZ_1) / sigma
+                    float* nd = (dz == t0) ? t1 : t0;
+                    mv_bwd(Wr[0], D, H, dz, nd, lane);
+                    __syncwarp();
+                    for (int q = 0; q < na; ++q)
+                        for (int i = lane; i < D; i += 32)
+                            a.dfp[(size_t)(slot0 + q) * a.fp_stride + i] = nd[i * kTrainAtoms + q] * isig[i];
+                }
+                break;
+            }
             float* nd = (dz == t0) ? t1 : t0;
             mv_bwd(Wr[l], in_of[l], H, dz, nd, lane);
             __syncwarp();
@@ -608,6 +628,190 @@ __global__ void k_train_final(ReduceArgs a) {
     a.grad[a.goff[t] + p] = s;
 }
 
+// =========================================================================== radial-fuse gradients
+namespace {
+
+constexpr int kWgWarps = 4;
+
+template <int L, int NP, int N1, bool SPH>
+struct WgShape {
+    static constexpr int K = SPH ? (L + 1) * (L + 1) : 1;
+    static constexpr int KS = K | 1;
+    static constexpr int NPS = (NP + 3) & ~3;
+    static constexpr int N1P = (N1 + 3) & ~3;
+    static constexpr int PN = NP * N1;
+    // M1, M2 [K][NPS] | Y, D_b Y [32][KS] | Gc, Gdc [32][NPS] | fc T, D_b(fc T) [32][N1P] | tn [32]
+    static constexpr int FIXED = (SPH ? 2 * K * NPS + 2 * 32 * KS : 0) + 2 * 32 * NPS + 2 * 32 * N1P + 32;
+    __host__ __device__ static int warp_floats(int T) { return (FIXED + T * PN + 3) & ~3; }
+};
+
+}  // namespace
+
+// One warp per atom slot (slots s0 + w, s0 + w + G, ... of warp w).  Lanes evaluate one
+// neighbour each: fc T_n and D_b(fc T_n), and the loss gradients of c_j and D_b c_j,
+//   spherical  Gc[p] = sum_lm M1[lm][p] Y_lm + M2[lm][p] D_b Y_lm,  Gdc[p] = sum_lm M2[lm][p] Y_lm,
+//              M1 = 2 k_l (dfp[p][l] A - gfp[p][l] D_b A),  M2 = -2 k_l gfp[p][l] A,  k_l = 4 pi/(2l+1)
+//   radial     Gc[p] = dfp[p],  Gdc[p] = -gfp[p]
+// (restating backwardAnlm with GRAD_PARAM and backwardBackwardAnlm, basis_SphericalChebyshev.hpp:353-617,
+// with backwardRnp / backwardBackwardRnp, nnap_util.hpp:282-313).  Lanes then own entries
+// (p, n) of the [T][NP][N1] block of the centre's species and add Gc fcT + Gdc D_b(fcT) of
+// each neighbour into the entry of its species, in neighbour order.
+template <int L, int NP, int N1, bool SPH>
+__global__ void __launch_bounds__(32 * kWgWarps) k_wgrad(WgradArgs g) {
+    using S = WgShape<L, NP, N1, SPH>;
+    const DescArgs& a = g.j.d;
+    extern __shared__ float smem[];
+    const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
+    float* sW = smem;
+    load_fuse<NP, N1>(a.W, sW, a.T);
+    __syncthreads();
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wl;
+    if (w >= g.G) return;
+    float* base = smem + ((nW + 3) & ~3) + (size_t)wl * S::warp_floats(a.T);
+    float* sM1 = base;
+    float* sM2 = sM1 + (SPH ? S::K * S::NPS : 0);
+    float* sY = sM2 + (SPH ? S::K * S::NPS : 0);
+    float* sD = sY + (SPH ? 32 * S::KS : 0);
+    float* sGc = sD + (SPH ? 32 * S::KS : 0);
+    float* sGd = sGc + 32 * S::NPS;
+    float* sF = sGd + 32 * S::NPS;
+    float* sV = sF + 32 * S::N1P;
+    int* sTn = reinterpret_cast<int*>(sV + 32 * S::N1P);
+    float* sAcc = reinterpret_cast<float*>(sTn + 32);
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    const int Tr = a.t1 - a.t0;
+    const int TPN = a.T * S::PN;
+    float* part = g.partial + (size_t)w * Tr * TPN;
+    const float rc = a.rcut;
+    for (int slot = s0 + w; slot < s1; slot += g.G) {
+        const int at = a.perm[slot];
+        const int tc = a.type[at] - 1;
+        const int M = a.P.M, cnt = min(a.P.count[at], M);
+        const float* gf = g.gfp + (size_t)slot * a.fp_stride + a.fp_off;
+        const float* df = g.dfp + (size_t)slot * a.fp_stride + a.fp_off;
+        if (SPH) {
+            const float* Ain = a.A + (size_t)(slot - s0) * NP * S::K;
+            const float* dAin = g.dA + (size_t)(slot - s0) * NP * S::K;
+            for (int lm = lane; lm < S::K; lm += 32) {
+                int l = 0;
+                while ((l + 1) * (l + 1) <= lm) ++l;
+                const float k2 = 2.f * kPi4 / (float)(2 * l + 1);
+                for (int p = 0; p < S::NPS; ++p) {
+                    float m1 = 0.f, m2 = 0.f;
+                    if (p < NP) {
+                        const float av = Ain[p * S::K + lm], dav = dAin[p * S::K + lm];
+                        const float gv = gf[p * (L + 1) + l], dv = df[p * (L + 1) + l];
+                        m1 = k2 * (dv * av - gv * dav);
+                        m2 = -k2 * gv * av;
+                    }
+                    sM1[lm * S::NPS + p] = m1;
+                    sM2[lm * S::NPS + p] = m2;
+                }
+            }
+        }
+        for (int e = lane; e < TPN; e += 32) sAcc[e] = 0.f;
+        __syncwarp();
+        for (int b0 = 0; b0 < cnt; b0 += 32) {
+            const int k = b0 + lane;
+            float gc[NP], gd[NP], fT[N1], v[N1];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) { gc[p] = 0.f; gd[p] = 0.f; }
+#pragma unroll
+            for (int n = 0; n < N1; ++n) { fT[n] = 0.f; v[n] = 0.f; }
+            int tn = 0;
+            bool valid = false;
+            float* y = sY + lane * S::KS;
+            float* dy = sD + lane * S::KS;
+            if (k < cnt) {
+                const size_t e = (size_t)at * M + k;
+                const float4 d = a.P.dx[e];
+                const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+                if (r < rc) {
+                    valid = true;
+                    tn = __float_as_int(d.w) - 1;
+                    const float3 b = pair_upstream(g.j, at, e, d);
+                    const float db = d.x * b.x + d.y * b.y + d.z * b.z;
+                    radial_dir<N1>(r, rc, db, fT, v);
+                    if (SPH) {
+                        const Angles an = angles_f(d.x, d.y, d.z, r);
+                        sph_harm<(SPH ? L : 0), true>(an, y, dy, 1);
+                        const float ir = 1.f / r;
+                        const float dth = an.ct * an.cp * ir * b.x + an.ct * an.sp * ir * b.y - an.st * ir * b.z;
+                        const float dph = an.pole ? 0.f : (-an.sp * b.x + an.cp * b.y) / an.dxy;
+#pragma unroll
+                        for (int l = 0; l <= (SPH ? L : 0); ++l) {
+                            const int c0 = l * l + l;
+                            dy[c0] *= dth;
+#pragma unroll
+                            for (int m = 1; m <= l; ++m) {
+                                const float yp = y[c0 + m], ym = y[c0 - m];
+                                dy[c0 + m] = dy[c0 + m] * dth - (float)m * ym * dph;
+                                dy[c0 - m] = dy[c0 - m] * dth + (float)m * yp * dph;
+                            }
+                        }
+#pragma unroll 1
+                        for (int lm = 0; lm < S::K; ++lm) {
+                            const float yv = y[lm], dyv = dy[lm];
+                            const float4* m1 = reinterpret_cast<const float4*>(sM1 + lm * S::NPS);
+                            const float4* m2 = reinterpret_cast<const float4*>(sM2 + lm * S::NPS);
+#pragma unroll
+                            for (int q = 0; q < S::NPS / 4; ++q) {
+                                const float4 x1 = m1[q], x2 = m2[q];
+                                const float a1[4] = {x1.x, x1.y, x1.z, x1.w}, a2[4] = {x2.x, x2.y, x2.z, x2.w};
+#pragma unroll
+                                for (int c = 0; c < 4; ++c) {
+                                    const int p = 4 * q + c;
+                                    if (p < NP) {
+                                        gc[p] += a1[c] * yv + a2[c] * dyv;
+                                        gd[p] += a2[c] * yv;
+                                    }
+                                }
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int p = 0; p < NP; ++p) { gc[p] = df[p]; gd[p] = -gf[p]; }
+                    }
+                }
+            }
+            (void)valid;
+#pragma unroll
+            for (int p = 0; p < S::NPS; ++p) {
+                sGc[lane * S::NPS + p] = p < NP ? gc[p] : 0.f;
+                sGd[lane * S::NPS + p] = p < NP ? gd[p] : 0.f;
+            }
+#pragma unroll
+            for (int n = 0; n < S::N1P; ++n) {
+                sF[lane * S::N1P + n] = n < N1 ? fT[n] : 0.f;
+                sV[lane * S::N1P + n] = n < N1 ? v[n] : 0.f;
+            }
+            sTn[lane] = tn;
+            __syncwarp();
+            const int nk = min(32, cnt - b0);
+            for (int e = lane; e < S::PN; e += 32) {
+                const int p = e / N1, n = e - p * N1;
+                for (int kk = 0; kk < nk; ++kk) {
+                    const float c = sGc[kk * S::NPS + p] * sF[kk * S::N1P + n] + sGd[kk * S::NPS + p] * sV[kk * S::N1P + n];
+                    sAcc[sTn[kk] * S::PN + e] += c;
+                }
+            }
+            __syncwarp();
+        }
+        float* dst = part + (size_t)(tc - a.t0) * TPN;
+        for (int e = lane; e < TPN; e += 32) dst[e] += sAcc[e];
+        __syncwarp();
+    }
+}
+
+__global__ void k_wgrad_final(const float* __restrict__ partial, int G, int per, double* __restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= per) return;
+    double s = 0.0;
+    for (int w = 0; w < G; ++w) s += (double)partial[(size_t)w * per + e];
+    out[e] = s;
+}
+
 // =========================================================================== launchers
 namespace {
 
@@ -646,6 +850,44 @@ cudaError_t launch_sph_jvp(const JvpArgs& a, cudaStream_t st) {
 }
 
 }  // namespace
+
+namespace {
+
+template <int L, int NP, int N1, bool SPH>
+cudaError_t launch_wgrad_t(const WgradArgs& g, cudaStream_t st) {
+    using S = WgShape<L, NP, N1, SPH>;
+    if (g.G <= 0) return cudaSuccess;
+    const size_t wf = ((size_t)g.j.d.T * g.j.d.T * NP * Fuse<N1>::N1P + 3) & ~(size_t)3;
+    const size_t sm = sizeof(float) * (wf + (size_t)kWgWarps * S::warp_floats(g.j.d.T));
+    if (sm > 227 * 1024) return cudaErrorInvalidValue;
+    static int lim = 0;
+    if ((int)sm > lim) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_wgrad<L, NP, N1, SPH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        lim = (int)sm;
+    }
+    k_wgrad<L, NP, N1, SPH><<<(g.G + kWgWarps - 1) / kWgWarps, 32 * kWgWarps, sm, st>>>(g);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_wgrad(int kind, int lmax, int np, int n1, const WgradArgs& a, cudaStream_t st) {
+#define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return launch_wgrad_t<0, P_, N_, false>(a, st);
+#define S_CASE(L_, P_, N_) if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return launch_wgrad_t<L_, P_, N_, true>(a, st);
+    NNAP_RADIAL_SHAPES(R_CASE)
+    NNAP_SPH_SHAPES(S_CASE)
+#undef R_CASE
+#undef S_CASE
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_wgrad_final(const float* partial, int G, int per, double* out, cudaStream_t st) {
+    if (per <= 0) return cudaSuccess;
+    k_wgrad_final<<<(per + 255) / 256, 256, 0, st>>>(partial, G, per, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_train_prep(const double* bF, int n, float4* bFf, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;

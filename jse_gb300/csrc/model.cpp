@@ -415,6 +415,8 @@ Model load_model(const char* text, size_t len) {
         // block in the reference's generated code, so only concrete sources are accepted
         if (s < 1 || s > T || bkind[s - 1] != PLAIN) bad("the source of a mirror or shared basis must be a plain basis");
         M.sp[t].subs = M.sp[s - 1].subs;
+        M.sp[t].basis_src = s;
+        M.sp[t].basis_mirror = bkind[t] == MIRROR;
         if (bkind[t] == MIRROR) {
             // neighbours of the centre's own species and of the mirrored one swap roles
             // (nnap_main.hpp:40-48): W_t[tn] = W_s[sigma(tn)], sigma exchanging t+1 and s

@@ -32,6 +32,8 @@ struct Species {
     double bo = 0.0;                         // output bias
     std::vector<double> mu, sigma;           // descriptor normalisation
     double mu_e = 0.0, sigma_e = 1.0;        // energy denormalisation (mu includes ref_eng)
+    int basis_src = 0;                       // mirror / shared basis: 1-based source species (0: own)
+    bool basis_mirror = false;               // the basis is a mirror of basis_src's
 };
 
 struct Model {

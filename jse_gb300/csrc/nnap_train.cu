@@ -51,7 +51,17 @@ std::vector<GradTile> grad_tiles(const Species& sp) {
     return t;
 }
 
-void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const double* bF, const double* bW) {
+bool any_fused(const Model& m) {
+    for (auto& sp : m.sp)
+        for (auto& b : sp.subs)
+            if (b.fused) return true;
+    return false;
+}
+
+// Queue the training passes.  With want_w, also the radial-fuse gradients: one FP64
+// block [t1 - t0][T][NP][N1] per run of species and sub-basis in h->twgrad, in run order.
+void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const double* bF, const double* bW,
+                   bool want_w) {
     const Model& m = h->model;
     const int n = B.natoms, T = m.ntypes(), n1 = std::max(n, 1);
     cudaStream_t st = h->stream;
@@ -100,6 +110,15 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
         dbE = h->tbE.p;
     }
     if (n) CK(cudaMemsetAsync(h->tu.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
+    if (want_w) {
+        const size_t an = std::max<size_t>(a_arena_size(h, n), 1);
+        h->tdA.ensure(an);
+        h->tgfp.ensure((size_t)n1 * h->fp_stride);
+        h->tdfp.ensure((size_t)n1 * h->fp_stride);
+        CK(cudaMemsetAsync(h->tdA.p, 0, sizeof(float) * an, st));
+        CK(cudaMemsetAsync(h->tgfp.p, 0, sizeof(float) * (size_t)n1 * h->fp_stride, st));
+        CK(cudaMemsetAsync(h->tdfp.p, 0, sizeof(float) * (size_t)n1 * h->fp_stride, st));
+    }
     // descriptor directional derivatives, per run of species and sub-basis (A arena as the forward)
     size_t a_off = 0;
     for (auto& r : h->runs) {
@@ -132,6 +151,7 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             ja.bW = dbW;
             ja.sid = h->sid.p;
             ja.u = h->tu.p;
+            ja.dA = (want_w && s.kind == KIND_SPHERICAL) ? h->tdA.p + (a.A - h->A.p) : nullptr;
             if (n > 0 && (dbF || dbW)) {
                 CK(launch_jvp(s.kind, s.lmax, s.np, s.n1, ja, st));
                 ++h->launches;
@@ -157,6 +177,8 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
         a.bE = dbE;
         a.rec = h->trec.p;
         a.V = Vmax;
+        a.gfp = want_w ? h->tgfp.p : nullptr;
+        a.dfp = want_w ? h->tdfp.p : nullptr;
         CK(launch_net_train(a, st));
         ++h->launches;
     }
@@ -190,7 +212,109 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
         CK(launch_train_reduce(ra, st));
         h->launches += 2;
     }
+    if (want_w) {
+        // warps of the radial-fuse gradient launches: enough to fill the GPU, with the
+        // partial blocks bounded to about 64 M floats
+        size_t wtot = 0, per_max = 1;
+        for (auto& r : h->runs)
+            for (auto& sh : r.subs) {
+                const size_t per = (size_t)(r.t1 - r.t0) * T * sh.np * sh.n1;
+                wtot += per;
+                per_max = std::max(per_max, per);
+            }
+        int G = (int)std::min<size_t>(4096, std::max<size_t>(1, ((size_t)64 << 20) / per_max));
+        G = std::max(4, std::min(G, ((n + 3) / 4) * 4));
+        h->twpart.ensure((size_t)G * per_max);
+        h->twgrad.ensure(std::max<size_t>(wtot, 1));
+        size_t a_off = 0, w_off = 0;
+        for (auto& r : h->runs) {
+            for (size_t k = 0; k < r.subs.size(); ++k) {
+                const SubShape& sh = r.subs[k];
+                const size_t per = (size_t)(r.t1 - r.t0) * T * sh.np * sh.n1;
+                WgradArgs g;
+                DescArgs& a = g.j.d;
+                a.perm = h->perm.p;
+                a.range = h->type_start.p;
+                a.t0 = r.t0;
+                a.t1 = r.t1;
+                a.nmax = n;
+                a.type = h->type.p;
+                a.P = pair_bufs(h);
+                a.W = r.W[k].p;
+                a.T = T;
+                a.rcut = (float)sh.rcut;
+                a.fp = h->fp.p;
+                a.fp_stride = h->fp_stride;
+                a.fp_off = r.fp_off[k];
+                a.A = nullptr;
+                g.dA = nullptr;
+                if (sh.kind == KIND_SPHERICAL) {
+                    a.A = h->A.p + a_off;
+                    g.dA = h->tdA.p + a_off;
+                    a_off += (size_t)n * sh.np * (sh.lmax + 1) * (sh.lmax + 1);
+                }
+                a.gfp = nullptr;
+                a.accumulate = 0;
+                a.warps = 4;
+                g.j.bF = dbF;
+                g.j.bW = dbW;
+                g.j.sid = h->sid.p;
+                g.j.u = nullptr;
+                g.j.dA = nullptr;
+                g.gfp = h->tgfp.p;
+                g.dfp = h->tdfp.p;
+                g.partial = h->twpart.p;
+                g.G = G;
+                CK(cudaMemsetAsync(h->twpart.p, 0, sizeof(float) * (size_t)G * per, st));
+                if (n > 0) {
+                    CK(launch_wgrad(sh.kind, sh.lmax, sh.np, sh.n1, g, st));
+                    ++h->launches;
+                }
+                CK(launch_wgrad_final(h->twpart.p, G, (int)per, h->twgrad.p + w_off, st));
+                ++h->launches;
+                w_off += per;
+            }
+        }
+    }
     CK(cudaGetLastError());
+}
+
+// Scatter the per-run blocks of h->twgrad (already on the host as w) into the caller's
+// layout: per species its sub-bases' matrices [tn][np][n].  A mirror or shared basis
+// uses its source's parameters (nnap_main.hpp:410-420: the gradient goes to the source
+// species), a mirror with the neighbour species t and source exchanged.
+void scatter_wgrad(const nnap_handle* h, const std::vector<double>& w, double* grad_fp) {
+    const Model& m = h->model;
+    const int T = m.ntypes();
+    std::vector<size_t> off(T + 1, 0);
+    for (int t = 0; t < T; ++t) {
+        size_t f = 0;
+        for (auto& b : m.sp[t].subs) f += b.W.size();
+        off[t + 1] = off[t] + f;
+    }
+    std::fill(grad_fp, grad_fp + off[T], 0.0);
+    size_t w_off = 0;
+    for (auto& r : h->runs) {
+        for (size_t k = 0; k < r.subs.size(); ++k) {
+            const SubShape& sh = r.subs[k];
+            const size_t blk = (size_t)sh.np * sh.n1;
+            for (int tc = r.t0; tc < r.t1; ++tc) {
+                const Species& sp = m.sp[tc];
+                const int o = sp.basis_src ? sp.basis_src - 1 : tc;
+                if (!m.sp[o].subs[k].fused) continue;
+                size_t sub_off = 0;
+                for (size_t q = 0; q < k; ++q) sub_off += m.sp[o].subs[q].W.size();
+                for (int tn = 0; tn < T; ++tn) {
+                    int tt = tn;
+                    if (sp.basis_mirror) tt = tn == o ? tc : (tn == tc ? o : tn);
+                    const double* src = w.data() + w_off + ((size_t)(tc - r.t0) * T + tn) * blk;
+                    double* dst = grad_fp + off[o] + sub_off + (size_t)tt * blk;
+                    for (size_t e = 0; e < blk; ++e) dst[e] += src[e];
+                }
+            }
+            w_off += (size_t)(r.t1 - r.t0) * T * blk;
+        }
+    }
 }
 
 }  // namespace
@@ -218,26 +342,33 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         if (!grad_nn) throw ApiFail(NNAP_ERR_ARG, "grad_nn is NULL");
         const Model& m = h->model;
         const int T = m.ntypes();
-        if (grad_fp)
-            for (auto& sp : m.sp)
-                for (auto& b : sp.subs)
-                    if (b.fused)
-                        throw ApiFail(NNAP_ERR_UNSUPPORTED,
-                                      "gradients of fused radial weights (wtype fuse/rfuse/exfuse) are not computed");
+        const bool want_w = grad_fp && any_fused(m);
         h->launches = 0;
         Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, B.natoms, x, type);
         evaluate(h, B, h->x.p, h->type.p, true);
-        train_enqueue(h, B, bgrad_energies, bgrad_forces, bgrad_virial);
+        train_enqueue(h, B, bgrad_energies, bgrad_forces, bgrad_virial, want_w);
         int Ptot = 0;
         for (int t = 0; t < T; ++t) Ptot += net_params(m.sp[t]);
         if (Ptot) CK(cudaMemcpyAsync(grad_nn, h->tgrad.p, sizeof(double) * Ptot, cudaMemcpyDeviceToHost, h->stream));
+        std::vector<double> w;
+        if (want_w) {
+            size_t wtot = 0;
+            for (auto& r : h->runs)
+                for (auto& sh : r.subs) wtot += (size_t)(r.t1 - r.t0) * T * sh.np * sh.n1;
+            w.resize(wtot);
+            CK(cudaMemcpyAsync(w.data(), h->twgrad.p, sizeof(double) * wtot, cudaMemcpyDeviceToHost, h->stream));
+        }
         CK(cudaStreamSynchronize(h->stream));
         if (grad_fp) {
-            size_t F = 0;
-            for (int t = 0; t < T; ++t) F += fp_params(m.sp[t]);
-            std::memset(grad_fp, 0, sizeof(double) * F);
+            if (want_w) {
+                scatter_wgrad(h, w, grad_fp);
+            } else {
+                size_t F = 0;
+                for (int t = 0; t < T; ++t) F += fp_params(m.sp[t]);
+                std::memset(grad_fp, 0, sizeof(double) * F);
+            }
         }
         return NNAP_OK;
     });

@@ -18,6 +18,7 @@ struct JvpArgs {
     const float* bW;        // [nstruct][9] upstream virial gradients or NULL
     const int* sid;         // [n] structure of each atom
     float* u;               // [slots][fp_stride] directional derivatives
+    float* dA;              // spherical, or NULL: D_b A stored like d.A
 };
 
 // Per-slot records of one species' network pass (see k_net_train):
@@ -40,6 +41,23 @@ struct NetTrainArgs {
     const double* bE;       // [n] upstream per-atom energy gradients (by atom) or NULL
     float* rec;             // [slots][V]
     int V;
+    float* gfp;             // or NULL: dE/dfp by slot (fp layout)
+    float* dfp;             // or NULL: dL/dfp by slot, energy and force terms (fp layout)
+};
+
+// Gradient of the radial-fuse matrices W[tc][tn][p][n] of one sub-basis over a run of
+// species, from the per-atom dE/dfp (gfp), dL/dfp (dfp) and, spherical, A and D_b A:
+//   dL/dW[tc][tn][p][n] = sum over pairs (i, j) with types (tc, tn) of
+//       Gc_j[p] fc T_n(r_j) + Gdc_j[p] D_b(fc T_n)(r_j)
+// with Gc, Gdc the loss gradients of c_j = fc Rnp_j and of its directional derivative.
+// Warp w processes slots s0 + w, s0 + w + G, ... and owns partial[w][tc - t0][T][NP][N1].
+struct WgradArgs {
+    JvpArgs j;              // geometry, upstream gradients and j.d.A
+    const float* dA;        // spherical: D_b A from the directional-derivative pass
+    const float* gfp;
+    const float* dfp;
+    float* partial;         // [G][t1 - t0][T][NP][N1], zeroed before the launch
+    int G;                  // warps of the launch
 };
 
 // One tile of a species' parameter gradient: a 64 x 64 block (o0, i0) of layer `layer`'s
@@ -71,5 +89,8 @@ cudaError_t launch_train_prep(const double* bF, int n, float4* bFf, cudaStream_t
 cudaError_t launch_jvp(int kind, int lmax, int np, int n1, const JvpArgs& a, cudaStream_t st);
 cudaError_t launch_net_train(const NetTrainArgs& a, cudaStream_t st);
 cudaError_t launch_train_reduce(const ReduceArgs& a, cudaStream_t st);
+cudaError_t launch_wgrad(int kind, int lmax, int np, int n1, const WgradArgs& a, cudaStream_t st);
+// out[e] = sum over w < G of partial[w * per + e] (FP64, in w order), e < per.
+cudaError_t launch_wgrad_final(const float* partial, int G, int per, double* out, cudaStream_t st);
 
 }  // namespace nnapgb

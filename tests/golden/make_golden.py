@@ -139,6 +139,12 @@ def cases():
                                 "hidden_biases": [rng.normal(0, 0.3, 4).tolist(), []],
                                 "output_weight": rng.normal(0, 0.35, 8).tolist(), "output_bias": 0.2}
         out[name] = (m, s3)
+    # fused radial weights behind a mirror and a shared basis: their gradients belong to A
+    fw3 = rng.uniform(-1, 1, 3 * 3).tolist()
+    m = _model(["A", "B", "C"], _sph(3, 2, 5.0, "fuse", fuse_size=3, fuse_weight=fw3), [8, 8], 44)
+    m["models"][1] = {"symbol": "B", "basis": {"type": "mirror", "mirror": 1}}
+    m["models"][2]["basis"] = {"type": "share", "share": 1}
+    out["mirror_share_fuse"] = (m, s3)
     return out
 
 
