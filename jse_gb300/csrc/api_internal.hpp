@@ -101,6 +101,10 @@ struct Run {
     std::vector<SubShape> subs;
     std::vector<int> fp_off;
     std::vector<DevBuf<float>> W;  // per sub: [T][T][NP][N1]
+    // per sub: sparse form of W ([T][T][N1][kNz] rows and weights), empty when a column
+    // has more than kNz nonzero rows or N1 >= NP (the backward then stays in NP space)
+    std::vector<DevBuf<int>> nzp;
+    std::vector<DevBuf<float>> nzw;
 };
 
 struct NetDev {

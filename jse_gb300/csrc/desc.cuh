@@ -24,7 +24,13 @@ struct DescArgs {
     const float* gfp;       // backward: dE/dfp by slot (same layout as fp)
     int accumulate;         // backward: add into P.g instead of overwriting
     int warps;              // warps per CTA (2, 4 or 8; one atom slot per warp)
+    // spherical backward: sparse form of W, [T][T][N1][kNz] nonzero rows p (-1: none) and
+    // their weights, or NULL (the kernel then works in the space of the NP channels)
+    const int* nz_p;
+    const float* nz_w;
 };
+
+constexpr int kNz = 4;  // nonzero rows per column of a fuse matrix kept in the sparse form
 
 // Compiled shapes.  Radial: (NP, N1).  Spherical: (L, NP, N1).
 #define NNAP_RADIAL_SHAPES(X) X(11, 11) X(12, 6) X(4, 4) X(8, 4) X(12, 4) X(18, 9)

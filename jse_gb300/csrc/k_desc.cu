@@ -393,6 +393,193 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
     }
 }
 
+// Backward in the space of the radial functions (used when every column of the fuse
+// matrices has at most kNz nonzero rows and N1 < NP, e.g. the default, full, exfull and
+// fuse weight types).  With Gh[tn][lm][n] = sum_p W[tc][tn][p][n] G[p][lm], formed once per
+// atom from the sparse fuse table,
+//   dY_lm = sum_p c_p G[p][lm] = fc sum_n T_n Gh[tn][lm][n],
+//   v_n   = sum_p W[p][n] dc_p = sum_lm Gh[tn][lm][n] Y_lm,
+// so the per-neighbour products run over N1 instead of NP channels, and c, dc are never
+// formed.  Y and dY/dtheta are formed row by row from the lane's Legendre column in
+// shared memory with cos/sin(m phi) recurrences, instead of being stored.
+template <int L, int NP, int N1>
+struct SphNShape {
+    static constexpr int K = (L + 1) * (L + 1);
+    static constexpr int NT = L * (L + 1) / 2 + L + 1;      // Legendre entries
+    static constexpr int N1P = (N1 + 3) & ~3;
+    static constexpr int NPS = (NP + 3) & ~3;
+    static constexpr int SCR = (K * NPS > NT * 32 ? K * NPS : NT * 32);
+    static int warp_floats(int T) { return T * K * N1P + SCR; }
+};
+
+template <int L, int NP, int N1>
+__global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a) {
+    using S = SphNShape<L, NP, N1>;
+    extern __shared__ float smem[];
+    const int T = a.T;
+    const int ntab = T * T * N1 * kNz;
+    int* sNp = reinterpret_cast<int*>(smem);
+    float* sNw = smem + ntab;
+    for (int q = threadIdx.x; q < ntab; q += blockDim.x) {
+        sNp[q] = a.nz_p[q];
+        sNw[q] = a.nz_w[q];
+    }
+    __syncthreads();
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wl;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    float* sGh = smem + ((2 * ntab + 3) & ~3) + (size_t)wl * (T * S::K * S::N1P + S::SCR);  // [T][K][N1P]
+    float* scr = sGh + T * S::K * S::N1P;   // G [K][NPS], then the Legendre columns [NT][32]
+    const int at = a.perm[s0 + w];
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut, irc = 1.f / a.rcut;
+    {
+        // G[p][lm] = 2 * 4pi/(2l+1) * dE/dfp[p][l] * A[p][lm], transposed into scr
+        const float* Ain = a.A + (size_t)w * NP * S::K;
+        const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+        for (int lm = lane; lm < S::K; lm += 32) {
+            int l = 0;
+            while ((l + 1) * (l + 1) <= lm) ++l;
+            const float coef = 2.f * kPi4 / (float)(2 * l + 1);
+#pragma unroll
+            for (int p = 0; p < NP; ++p) scr[lm * S::NPS + p] = coef * gf[p * (L + 1) + l] * Ain[p * S::K + lm];
+        }
+        __syncwarp();
+        // Gh[tn][lm][n] from the sparse fuse table of (tc, tn)
+        for (int idx = lane; idx < T * S::K; idx += 32) {
+            const int tn = idx / S::K, lm = idx - tn * S::K;
+            const int* np_ = sNp + (size_t)(tc * T + tn) * N1 * kNz;
+            const float* nw = sNw + (size_t)(tc * T + tn) * N1 * kNz;
+            float* out = sGh + (size_t)idx * S::N1P;
+#pragma unroll
+            for (int n = 0; n < S::N1P; ++n) {
+                float v = 0.f;
+                if (n < N1) {
+#pragma unroll
+                    for (int z = 0; z < kNz; ++z) {
+                        const int pp = np_[n * kNz + z];
+                        if (pp >= 0) v += nw[n * kNz + z] * scr[lm * S::NPS + pp];
+                    }
+                }
+                out[n] = v;
+            }
+        }
+        __syncwarp();
+    }
+    float* sP = scr;  // [NT][32], one Legendre column per lane
+    const float r2 = 1.41421356237309515f;
+    constexpr int H2 = S::N1P / 2;
+    for (int base = 0; base < cnt; base += 32) {
+        const int k = base + lane;
+        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        float r = 1.f;
+        bool valid = false;
+        if (k < cnt) {
+            d = a.P.dx[(size_t)at * M + k];
+            r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+            valid = r < rc;
+        }
+        const int tn = valid ? __float_as_int(d.w) - 1 : 0;
+        const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = valid ? fc2 * fc2 : 0.f;
+        const float x = 1.f - 2.f * u;
+        float Tn[S::N1P];
+        cheby_f<N1>(x, Tn);
+#pragma unroll
+        for (int n = N1; n < S::N1P; ++n) Tn[n] = 0.f;
+        const Angles an = angles_f(d.x, d.y, d.z, r);
+        {
+            float Pv[S::NT];
+            legendre_f<L>(an.ct, an.st, Pv);
+#pragma unroll
+            for (int q = 0; q < S::NT; ++q) sP[q * 32 + lane] = valid ? Pv[q] : 0.f;
+        }
+        __syncwarp();
+        float2 T2[H2], v2[H2];
+#pragma unroll
+        for (int h = 0; h < H2; ++h) {
+            T2[h] = make_float2(Tn[2 * h], Tn[2 * h + 1]);
+            v2[h] = make_float2(0.f, 0.f);
+        }
+        const float* gh = sGh + (size_t)tn * S::K * S::N1P;
+        // one Gh row: returns dY_lm and adds Gh[lm][n] * y into v
+        auto row = [&](int lm, float y) -> float {
+            const float4* gr = reinterpret_cast<const float4*>(gh + lm * S::N1P);
+            const float2 yy = make_float2(y, y);
+            float2 da = make_float2(0.f, 0.f), db = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < S::N1P / 4; ++q) {
+                const float4 g = gr[q];
+                const float2 ga = make_float2(g.x, g.y), gb = make_float2(g.z, g.w);
+                da = __ffma2_rn(T2[2 * q], ga, da);
+                db = __ffma2_rn(T2[2 * q + 1], gb, db);
+                v2[2 * q] = __ffma2_rn(ga, yy, v2[2 * q]);
+                v2[2 * q + 1] = __ffma2_rn(gb, yy, v2[2 * q + 1]);
+            }
+            return fc * ((da.x + db.x) + (da.y + db.y));
+        };
+        const float cp = an.cp, sp = an.sp;
+        float gth = 0.f, gph = 0.f;
+#pragma unroll 1
+        for (int l = 0; l <= L; ++l) {
+            const int c0 = l * l + l, tl = l * (l + 1) / 2;
+            const float p0 = sP[tl * 32 + lane];
+            const float p1 = l >= 1 ? sP[(tl + 1) * 32 + lane] : 0.f;
+            // m = 0: dP/dtheta = (dup P_{l,1} + ddn P_{l,1}) / 2 (P_{l,-1} = -P_{l,1})
+            gth += row(c0, p0) * (0.5f * (c_dup[tl] + c_ddn[tl]) * p1);
+            float cmm = 1.f, cmv = cp, smm = 0.f, smv = sp;
+            float pmm = p0, pmv = p1;
+#pragma unroll 1
+            for (int m = 1; m <= l; ++m) {
+                const int t = tl + m;
+                const float pmp = m + 1 <= l ? sP[(t + 1) * 32 + lane] : 0.f;
+                const float dpt = 0.5f * (c_dup[t] * pmp - c_ddn[t] * pmm);
+                const float yp = r2 * pmv * cmv, ym = r2 * pmv * smv;
+                const float dYp = row(c0 + m, yp);
+                const float dYm = row(c0 - m, ym);
+                gth += r2 * dpt * (dYp * cmv + dYm * smv);
+                gph += (float)m * (dYm * yp - dYp * ym);
+                const float cn = 2.f * cp * cmv - cmm, sn = 2.f * cp * smv - smm;
+                cmm = cmv; cmv = cn; smm = smv; smv = sn;
+                pmm = pmv; pmv = pmp;
+            }
+        }
+        __syncwarp();  // the Legendre columns are rewritten by the next batch
+        if (k < cnt) {
+            const size_t e = (size_t)at * M + k;
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (valid) {
+                const float fcg = 8.f * fc1 * fc2 * irc * irc;
+                float TG[N1];
+                cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+                float dfc = 0.f, drn = 0.f;
+#pragma unroll
+                for (int n = 0; n < N1; ++n) {
+                    const float vn = (n & 1) ? v2[n >> 1].y : v2[n >> 1].x;
+                    dfc += vn * Tn[n];
+                    drn += vn * TG[n];
+                }
+                const float gr = dfc * fcg + fc * drn;
+                const float ir = 1.f / r;
+                const float tpx = -an.ct * an.cp * ir, tpy = -an.ct * an.sp * ir, tpz = an.st * ir;
+                const float ppx = an.pole ? 0.f : an.sp / an.dxy, ppy = an.pole ? 0.f : -an.cp / an.dxy;
+                g.x = gr * d.x + gth * tpx + gph * ppx;
+                g.y = gr * d.y + gth * tpy + gph * ppy;
+                g.z = gr * d.z + gth * tpz;
+            }
+            if (a.accumulate) {
+                if (valid) {
+                    const float4 o = a.P.g[e];
+                    a.P.g[e] = make_float4(o.x + g.x, o.y + g.y, o.z + g.z, 0.f);
+                }
+            } else {
+                a.P.g[e] = g;
+            }
+        }
+    }
+}
+
 // =========================================================================== dispatch
 namespace {
 
@@ -418,10 +605,30 @@ cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
 }
 
 template <int L, int NP, int N1>
+cudaError_t launch_sph_bwd_n(const DescArgs& a, cudaStream_t st) {
+    using S = SphNShape<L, NP, N1>;
+    const int wpc = a.warps;
+    const int grid = (a.nmax + wpc - 1) / wpc;
+    const size_t sm = sizeof(float) * (((size_t)2 * a.T * a.T * N1 * kNz + 3) / 4 * 4 +
+                                       (size_t)wpc * S::warp_floats(a.T));
+    if (sm > 227 * 1024) return cudaErrorInvalidValue;
+    static int lim = 0;
+    if ((int)sm > lim) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_sph_bwd_n<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        lim = (int)sm;
+    }
+    k_sph_bwd_n<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L, int NP, int N1>
 cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     using S = SphShape<L, NP>;
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
+    if (!fwd && a.nz_p && a.nz_w && N1 < NP) return launch_sph_bwd_n<L, NP, N1>(a, st);
     const int wpc = a.warps;
     const int grid = (n + wpc - 1) / wpc;
     const size_t wbytes = sizeof(float) * ((size_t)a.T * a.T * NP * Fuse<N1>::N1P);

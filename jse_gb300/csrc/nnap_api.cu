@@ -74,6 +74,31 @@ void upload_model(nnap_handle* h) {
             r.W.emplace_back();
             r.W.back().ensure(W.size());
             CK(cudaMemcpy(r.W.back().p, W.data(), W.size() * sizeof(float), cudaMemcpyHostToDevice));
+            // sparse columns for the radial-space backward
+            std::vector<int> zp((size_t)T * T * s.n1 * kNz, -1);
+            std::vector<float> zw(zp.size(), 0.f);
+            bool sparse = s.kind == KIND_SPHERICAL && s.n1 < s.np;
+            for (int tc = r.t0; tc < r.t1 && sparse; ++tc)
+                for (int tn = 0; tn < T && sparse; ++tn)
+                    for (int n = 0; n < s.n1 && sparse; ++n) {
+                        int z = 0;
+                        for (int p = 0; p < s.np; ++p) {
+                            const float v = W[(((size_t)tc * T + tn) * s.np + p) * s.n1 + n];
+                            if (v == 0.f) continue;
+                            if (z == kNz) { sparse = false; break; }
+                            const size_t q = (((size_t)tc * T + tn) * s.n1 + n) * kNz + z++;
+                            zp[q] = p;
+                            zw[q] = v;
+                        }
+                    }
+            r.nzp.emplace_back();
+            r.nzw.emplace_back();
+            if (sparse) {
+                r.nzp.back().ensure(zp.size());
+                r.nzw.back().ensure(zw.size());
+                CK(cudaMemcpy(r.nzp.back().p, zp.data(), zp.size() * sizeof(int), cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(r.nzw.back().p, zw.data(), zw.size() * sizeof(float), cudaMemcpyHostToDevice));
+            }
         }
         h->runs.push_back(std::move(r));
         t = u;
@@ -424,6 +449,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.gfp = h->gfp.p;
                 a.accumulate = k > 0;
                 a.warps = fwd ? h->tune.desc_fwd_warps : h->tune.desc_bwd_warps;
+                a.nz_p = r.nzp[k].p;
+                a.nz_w = r.nzw[k].p;
                 if (n > 0) {
                     CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, st));
                     ++h->launches;

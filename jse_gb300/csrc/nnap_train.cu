@@ -147,6 +147,8 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             a.gfp = nullptr;
             a.accumulate = 0;
             a.warps = 4;
+            a.nz_p = nullptr;
+            a.nz_w = nullptr;
             ja.bF = dbF;
             ja.bW = dbW;
             ja.sid = h->sid.p;
@@ -256,6 +258,8 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
                 a.gfp = nullptr;
                 a.accumulate = 0;
                 a.warps = 4;
+                a.nz_p = nullptr;
+                a.nz_w = nullptr;
                 g.j.bF = dbF;
                 g.j.bW = dbW;
                 g.j.sid = h->sid.p;
