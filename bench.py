@@ -264,6 +264,56 @@ def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2))
     return out
 
 
+# ----------------------------------------------------------------------------- training
+def train_measurement(device: int, s, model: dict, steps: int = 5, cpu: bool = True) -> dict:
+    """Force-training gradients (nnap_train_grad_batch) of one structure: dL/dparameters of
+    L = bE.E + bF.F + bW.W for seeded upstream gradients, host buffers in and out, FP32.
+    The CPU baseline runs the reference's training pair (jse_nnap_forwardEnergyForce +
+    jse_nnap_backwardEnergyForce per atom, oracle/_ref -O3 -ffast-math, all host threads)
+    on a 2000-atom structure of the same liquid."""
+    import torch
+    from jse_gb300.nnap import NNAP
+    n = s.natoms
+    rng = np.random.default_rng(17)
+    be, bf, bw = rng.normal(size=n), rng.normal(size=(n, 3)), rng.normal(size=(1, 9))
+    out = {"unit": "atom-evals/s", "atoms": n, "path": "nnap_train_grad_batch, host buffers, FP32 (network "
+           "parameter gradients of an energy + force + virial loss)"}
+    with NNAP(model, precision="fp32", device=device) as p:
+        for _ in range(3):
+            p.backwardEnergyForceBatch([s], be, bf, bw)
+        dts = []
+        for _ in range(steps):
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            p.backwardEnergyForceBatch([s], be, bf, bw)
+            dts.append(time.perf_counter() - t0)
+        out["gpu_launches"] = p.lastLaunchCount()
+    out["value"] = n * len(dts) / sum(dts)
+    out["ms_per_step"] = 1e3 * sum(dts) / len(dts)
+    if cpu:
+        try:
+            from oracle import model as OM, native as ON
+            pm = OM.load(model)
+            ref = ON.RefLib(pm, fast=True)
+            smp = W.random_liquid(2000, 0.060, [0.46, 0.46, 0.08], 2.0, 5)
+            nl = ON.neighbors(ON.wrap(smp.x, smp.box_kind, smp.box), smp.box_kind, smp.box, pm.rcut_max)
+            r2 = np.random.default_rng(18)
+            args = (smp.types, nl, r2.normal(size=2000), r2.normal(size=(2000, 3)), r2.normal(size=9))
+            threads = os.cpu_count() or 1
+            ref.train_grad(*args, nthreads=threads)
+            t0 = time.perf_counter()
+            reps = 0
+            while time.perf_counter() - t0 < 5.0:
+                ref.train_grad(*args, nthreads=threads)
+                reps += 1
+            v = 2000 * reps / (time.perf_counter() - t0)
+            out["cpu_baseline"] = {"value": v, "unit": "atom-evals/s", "kind": "reference", "cores": threads,
+                                   "sample": "2000-atom liquid of the same density and species, %d repeats" % reps}
+        except Exception as ex:
+            out["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    return out
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -275,6 +325,9 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-train", action="store_true", help="skip the training-gradient measurement")
+    ap.add_argument("--only-train", action="store_true", help="run only the training-gradient measurement "
+                    "(profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=5000)
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (profiling runs)")
     ap.add_argument("--atoms", type=int, default=0, help="resize the liquid / glass workload (profiling runs)")
@@ -316,6 +369,11 @@ def main():
     from jse_gb300.nnap import NNAP, WANT_ENERGY, WANT_FORCES, WANT_VIRIAL
     torch.cuda.set_device(local)
     model = normalised_model(cfg, structures, args.precision)
+    if args.only_train:
+        if rank == 0:
+            print(json.dumps({"training": train_measurement(local, structures[0], model, steps=args.steps,
+                                                             cpu=not args.no_cpu_baseline)}))
+        return
     pot = NNAP(model, precision=args.precision, device=local)
     pot.setAutotune(not args.no_autotune)  # shapes picked on the first warm-up step of the size bucket
     dev = torch.device("cuda", local)
@@ -435,6 +493,9 @@ def main():
     serving = None
     if rank == 0 and not args.no_serve and args.workload == "liquid32k":
         serving = serve_measurement(local, args.serve_requests)
+    training = None
+    if rank == 0 and not args.no_train and args.workload == "liquid32k":
+        training = train_measurement(local, s, model, cpu=not args.no_cpu_baseline)
 
     # roofline of the dominant stage
     peak, peak_kind, sm_max = load_peaks()
@@ -475,6 +536,8 @@ def main():
         line["plain_gpu"] = plain
         if serving is not None:
             line["serving"] = serving
+        if training is not None:
+            line["training"] = training
         print(json.dumps(line))
     pot.close()
     if dist:
