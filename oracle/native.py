@@ -10,7 +10,7 @@ from typing import Optional
 
 import numpy as np
 
-from . import build
+from . import bispectrum, build
 from .model import PackedModel
 
 _LIB = None
@@ -50,9 +50,18 @@ def pack(model: PackedModel):
         fp_off = 0
         for sb in b.subs:
             po = add(sb.param)
-            sub_entries += [0 if sb.kind == "chebyshev" else 1, sb.nmax, sb.lmax, sb.size_np, po, fp_off]
-            if sb.kind == "spherical_chebyshev" and (sb.l3max or sb.l4max):
-                raise NotImplementedError("bispectrum columns are not restated in the oracle")
+            if sb.kind == "spherical_chebyshev":
+                cols = bispectrum.column_terms(sb.l3max, sb.l4max)
+                tab = []
+                for terms in cols:
+                    tab.append(len(terms))
+                    for idx, coef in terms:
+                        tab += [len(idx)] + list(idx) + [-1] * (4 - len(idx)) + [coef]
+                io = add(np.asarray(tab, dtype=np.float64)) if tab else 0
+                L = max(sb.lmax, sb.l3max, sb.l4max)
+                sub_entries += [1, sb.nmax, L, sb.size_np, po, fp_off, sb.lmax + 1, len(cols), io]
+            else:
+                sub_entries += [0, sb.nmax, 0, sb.size_np, po, fp_off, 1, 0, 0]
             rcuts.append(sb.rcut)
             fp_off += sb.size
         nn_off = add(nn.cparam)

@@ -228,9 +228,14 @@ inline double cutoff_grad(double r, double rc) { double u = 1.0 - (r / rc) * (r 
 // ---------------------------------------------------------------- model description
 // spec (ints) per species t, concatenated:
 //   [nsub, D, nlayer, h_1..h_nlayer, nn_off, norm_off,
-//    then per sub: kind(0 radial,1 sph), nmax, lmax, np, param_off, fp_off]
+//    then per sub: kind(0 radial,1 sph), nmax, L, np, param_off, fp_off, nl2, ninv, inv_off]
+// L is the largest l of the expansion (max of lmax, l3max, l4max); nl2 = lmax + 1
+// power-spectrum columns and ninv invariant columns per channel follow each other
+// (calSphL2/L3/L4 of basis_SphericalChebyshev.hpp:321-351).  The invariant columns are
+// polynomials in A stored at params[inv_off]: per column [nterms, then per term
+// (order, i1, i2, i3, i4, coefficient)], i4 unused for order 3.
 // params (doubles): all parameter blocks; rcut per sub in rcut[] (flattened per species).
-struct Sub { int kind, nmax, lmax, np, param_off, fp_off; double rcut; };
+struct Sub { int kind, nmax, lmax, np, param_off, fp_off, nl2, ninv, inv_off; double rcut; };
 struct Species {
     int D, mirror, nlayer, nn_off, norm_off;  // mirror: 1-based species whose basis is mirrored (0: none)
     std::vector<int> hidden;
@@ -252,6 +257,7 @@ std::vector<Species> parse_spec(int T, const int* spec, const double* rcuts) {
             Sub b;
             b.kind = spec[k++]; b.nmax = spec[k++]; b.lmax = spec[k++]; b.np = spec[k++];
             b.param_off = spec[k++]; b.fp_off = spec[k++];
+            b.nl2 = spec[k++]; b.ninv = spec[k++]; b.inv_off = spec[k++];
             b.rcut = rcuts[ri++];
             sp[t].subs.push_back(b);
         }
@@ -309,12 +315,27 @@ void descriptor_forward(const Species& S, int T, const double* params, int nn, c
                     for (int k = 0; k < K; ++k) A[(size_t)p * K + k] += c * Y[k];
                 }
             }
-            for (int p = 0; p < NP; ++p)
-                for (int l = 0; l <= L; ++l) {
+            const int SL = b.nl2 + b.ninv;
+            for (int p = 0; p < NP; ++p) {
+                for (int l = 0; l < b.nl2; ++l) {
                     double s = 0.0;
                     for (int m = -l; m <= l; ++m) { double a = A[(size_t)p * K + l * l + l + m]; s += a * a; }
-                    fp[b.fp_off + p * (L + 1) + l] = kPi4 / (2.0 * l + 1.0) * s;
+                    fp[b.fp_off + p * SL + l] = kPi4 / (2.0 * l + 1.0) * s;
                 }
+                // three- and four-body invariants: sum of coefficient x product of A entries
+                const double* tab = params + b.inv_off;
+                const double* Ap = A.data() + (size_t)p * K;
+                for (int c = 0; c < b.ninv; ++c) {
+                    const int nt = (int)*tab++;
+                    double s = 0.0;
+                    for (int q = 0; q < nt; ++q, tab += 6) {
+                        double prod = tab[5] * Ap[(int)tab[1]] * Ap[(int)tab[2]] * Ap[(int)tab[3]];
+                        if ((int)tab[0] == 4) prod *= Ap[(int)tab[4]];
+                        s += prod;
+                    }
+                    fp[b.fp_off + p * SL + b.nl2 + c] = s;
+                }
+            }
         }
     }
 }
@@ -404,15 +425,34 @@ void descriptor_backward(const Species& S, const double* params, int nn, const i
         } else {
             const int L = b.lmax, K = (L + 1) * (L + 1);
             const std::vector<double>& A = Astore[si];
-            std::vector<double> G((size_t)NP * K);
-            for (int p = 0; p < NP; ++p)
-                for (int l = 0; l <= L; ++l) {
-                    double coef = 2.0 * kPi4 / (2.0 * l + 1.0) * gfp[b.fp_off + p * (L + 1) + l];
+            std::vector<double> G((size_t)NP * K, 0.0);
+            const int SL = b.nl2 + b.ninv;
+            for (int p = 0; p < NP; ++p) {
+                for (int l = 0; l < b.nl2; ++l) {
+                    double coef = 2.0 * kPi4 / (2.0 * l + 1.0) * gfp[b.fp_off + p * SL + l];
                     for (int m = -l; m <= l; ++m) {
                         int k = l * l + l + m;
                         G[(size_t)p * K + k] = coef * A[(size_t)p * K + k];
                     }
                 }
+                // d(invariant)/dA: each factor of a product in turn
+                const double* tab = params + b.inv_off;
+                const double* Ap = A.data() + (size_t)p * K;
+                double* Gp = G.data() + (size_t)p * K;
+                for (int c = 0; c < b.ninv; ++c) {
+                    const int nt = (int)*tab++;
+                    const double g = gfp[b.fp_off + p * SL + b.nl2 + c];
+                    for (int q = 0; q < nt; ++q, tab += 6) {
+                        const int ord = (int)tab[0];
+                        for (int f = 0; f < ord; ++f) {
+                            double prod = g * tab[5];
+                            for (int o = 0; o < ord; ++o)
+                                if (o != f) prod *= Ap[(int)tab[1 + o]];
+                            Gp[(int)tab[1 + f]] += prod;
+                        }
+                    }
+                }
+            }
             std::vector<double> Y(K), Yt(K), Yp(K), dY(K);
             for (int j = 0; j < nn; ++j) {
                 const double* d = ndx + 3 * j;

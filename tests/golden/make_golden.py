@@ -145,6 +145,12 @@ def cases():
     m["models"][1] = {"symbol": "B", "basis": {"type": "mirror", "mirror": 1}}
     m["models"][2]["basis"] = {"type": "share", "share": 1}
     out["mirror_share_fuse"] = (m, s3)
+    # three- and four-body invariant columns (l3max / l4max), including an expansion whose
+    # largest l comes from l3max rather than lmax
+    s2 = W.random_liquid(120, 0.06, [0.5, 0.5], 2.0, 26)
+    out["sph_bispectrum"] = (_model(["A", "B"], _sph(3, 3, 5.0, "full", l3max=3, l4max=2), [8, 8], 45), s2)
+    s1 = W.random_liquid(100, 0.06, [1.0], 2.0, 29)
+    out["sph_bispectrum_high"] = (_model(["A"], _sph(4, 2, 5.0, "default", l3max=4, l4max=3), [8, 8], 46), s1)
     return out
 
 
