@@ -90,8 +90,10 @@ struct DevBuf {
 struct SubShape {
     int kind, lmax, np, n1;
     double rcut;
+    int nl2, l3, l4, ninv;  // power-spectrum columns, l3max, l4max, invariant columns
     bool operator==(const SubShape& o) const {
-        return kind == o.kind && lmax == o.lmax && np == o.np && n1 == o.n1 && rcut == o.rcut;
+        return kind == o.kind && lmax == o.lmax && np == o.np && n1 == o.n1 && rcut == o.rcut && nl2 == o.nl2 &&
+               l3 == o.l3 && l4 == o.l4;
     }
 };
 
@@ -105,6 +107,11 @@ struct Run {
     // has more than kNz nonzero rows or N1 >= NP (the backward then stays in NP space)
     std::vector<DevBuf<int>> nzp;
     std::vector<DevBuf<float>> nzw;
+    // per sub: invariant-column terms (indices into A, -1 past the order; coefficients)
+    // and each column's first term, [ninv + 1]
+    std::vector<DevBuf<int4>> inv_idx;
+    std::vector<DevBuf<float>> inv_coef;
+    std::vector<DevBuf<int>> inv_start;
 };
 
 struct NetDev {
@@ -151,7 +158,7 @@ struct nnap_handle {
     nnapgb::DevBuf<uint64_t> pkey;
     nnapgb::DevBuf<float4> pdx, pg;
     nnapgb::DevBuf<int> prev, pcount;
-    nnapgb::DevBuf<float> fp, gfp, A;
+    nnapgb::DevBuf<float> fp, gfp, A, Gx;  // Gx: invariant-column part of dE/dA (when present)
     int M = 0;
     // LAMMPS-style boundary: caller's atoms (local + ghost), list, targets of the scatter
     nnapgb::DevBuf<double> lmp_x, lmp_forces, lmp_virials;

@@ -28,7 +28,31 @@ struct DescArgs {
     // their weights, or NULL (the kernel then works in the space of the NP channels)
     const int* nz_p;
     const float* nz_w;
+    // spherical: power-spectrum columns per channel (l < nl2) and descriptor columns per
+    // channel (sl = nl2 + invariant columns); Gx, or NULL: the invariant columns' part of
+    // dE/dA, [slot - range[t0]][NP][K] like A, added to the power-spectrum part
+    int nl2, sl;
+    const float* Gx;
 };
+
+// Invariant (l3max / l4max) columns of one spherical sub-basis over a run of species:
+// one warp per atom slot, lanes over channels.
+struct InvArgs {
+    const int* perm;
+    const int* range;
+    int t0, t1, nmax;
+    const float* A;          // [slot - range[t0]][NP][K]
+    int NP, K;
+    const int4* idx;         // term factors (indices into a channel's K entries, -1 unused)
+    const float* coef;
+    const int* start;        // [ncol + 1] first term of each column
+    int ncol;
+    float* fp;               // forward output (by slot)
+    const float* gfp;        // backward input: dE/dfp (by slot)
+    int fp_stride, fp_off, nl2, sl;
+    float* Gx;               // backward output, layout of A
+};
+cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st);
 
 constexpr int kNz = 4;  // nonzero rows per column of a fuse matrix kept in the sparse form
 

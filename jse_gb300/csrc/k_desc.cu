@@ -229,11 +229,11 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
     }
     __syncwarp();
     float* out = a.fp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
-    for (int e = lane; e < NP * (L + 1); e += 32) {
-        const int p = e / (L + 1), l = e - p * (L + 1);
+    for (int e = lane; e < NP * a.nl2; e += 32) {
+        const int p = e / a.nl2, l = e - p * a.nl2;
         float s = 0.f;
         for (int m = 0; m <= 2 * l; ++m) s += sA2[p * S::K + l * l + m];
-        out[e] = kPi4 / (float)(2 * l + 1) * s;
+        out[p * a.sl + l] = kPi4 / (float)(2 * l + 1) * s;
     }
 }
 
@@ -271,9 +271,14 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
         for (int lm = lane; lm < S::K; lm += 32) {
             int l = 0;
             while ((l + 1) * (l + 1) <= lm) ++l;
-            const float coef = 2.f * kPi4 / (float)(2 * l + 1);
+            const float coef = l < a.nl2 ? 2.f * kPi4 / (float)(2 * l + 1) : 0.f;
+            const int lc = l < a.nl2 ? l : 0;
 #pragma unroll
-            for (int p = 0; p < NP; ++p) sG[lm * S::NPS + p] = coef * gf[p * (L + 1) + l] * Ain[p * S::K + lm];
+            for (int p = 0; p < NP; ++p) {
+                float v = coef * gf[p * a.sl + lc] * Ain[p * S::K + lm];
+                if (a.Gx) v += a.Gx[(size_t)w * NP * S::K + p * S::K + lm];
+                sG[lm * S::NPS + p] = v;
+            }
 #pragma unroll
             for (int p = NP; p < S::NPS; ++p) sG[lm * S::NPS + p] = 0.f;
         }
@@ -442,9 +447,14 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
         for (int lm = lane; lm < S::K; lm += 32) {
             int l = 0;
             while ((l + 1) * (l + 1) <= lm) ++l;
-            const float coef = 2.f * kPi4 / (float)(2 * l + 1);
+            const float coef = l < a.nl2 ? 2.f * kPi4 / (float)(2 * l + 1) : 0.f;
+            const int lc = l < a.nl2 ? l : 0;
 #pragma unroll
-            for (int p = 0; p < NP; ++p) scr[lm * S::NPS + p] = coef * gf[p * (L + 1) + l] * Ain[p * S::K + lm];
+            for (int p = 0; p < NP; ++p) {
+                float v = coef * gf[p * a.sl + lc] * Ain[p * S::K + lm];
+                if (a.Gx) v += a.Gx[(size_t)w * NP * S::K + p * S::K + lm];
+                scr[lm * S::NPS + p] = v;
+            }
         }
         __syncwarp();
         // Gh[tn][lm][n] from the sparse fuse table of (tc, tn)
@@ -578,6 +588,70 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
             }
         }
     }
+}
+
+// =========================================================================== invariants
+// Columns: sum over the column's terms of coefficient x product of a channel's A entries
+// (calSphL3 / calSphL4, basis_SphericalUtil.hpp:395-467).  Backward: dE/dA of each
+// product, one factor at a time (calGradSphL3 / L4).  One lane owns one channel, so each
+// sum runs in term order and the results do not depend on scheduling.
+__global__ void __launch_bounds__(128) k_inv_fwd(InvArgs a) {
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    float* out = a.fp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    for (int p = lane; p < a.NP; p += 32) {
+        const float* Ap = a.A + ((size_t)w * a.NP + p) * a.K;
+        for (int c = 0; c < a.ncol; ++c) {
+            float s = 0.f;
+            for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
+                const int4 t = a.idx[q];
+                float v = a.coef[q] * Ap[t.x] * Ap[t.y] * Ap[t.z];
+                if (t.w >= 0) v *= Ap[t.w];
+                s += v;
+            }
+            out[p * a.sl + a.nl2 + c] = s;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_inv_bwd(InvArgs a) {
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    for (int p = lane; p < a.NP; p += 32) {
+        const float* Ap = a.A + ((size_t)w * a.NP + p) * a.K;
+        float* Gp = a.Gx + ((size_t)w * a.NP + p) * a.K;
+        for (int k = 0; k < a.K; ++k) Gp[k] = 0.f;
+        for (int c = 0; c < a.ncol; ++c) {
+            const float g = gf[p * a.sl + a.nl2 + c];
+            for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
+                const int4 t = a.idx[q];
+                const float cg = g * a.coef[q];
+                const float x = Ap[t.x], y = Ap[t.y], z = Ap[t.z];
+                if (t.w < 0) {
+                    Gp[t.x] += cg * y * z;
+                    Gp[t.y] += cg * x * z;
+                    Gp[t.z] += cg * x * y;
+                } else {
+                    const float u = Ap[t.w];
+                    Gp[t.x] += cg * y * z * u;
+                    Gp[t.y] += cg * x * z * u;
+                    Gp[t.z] += cg * x * y * u;
+                    Gp[t.w] += cg * x * y * z;
+                }
+            }
+        }
+    }
+}
+
+cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st) {
+    if (a.nmax <= 0 || a.ncol <= 0) return cudaSuccess;
+    const int grid = (a.nmax + 3) / 4;
+    if (fwd) k_inv_fwd<<<grid, 128, 0, st>>>(a);
+    else k_inv_bwd<<<grid, 128, 0, st>>>(a);
+    return cudaGetLastError();
 }
 
 // =========================================================================== dispatch

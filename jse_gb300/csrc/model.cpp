@@ -11,6 +11,8 @@
 //   that carries them).
 #include "model.hpp"
 
+#include <algorithm>
+
 #include <cmath>
 #include <stdexcept>
 
@@ -117,7 +119,8 @@ SubBasis load_sub(int kind, int T, const JValue& m) {
         l3 = (int)num_or(m, "l3max", 0);
         l4 = (int)num_or(m, "l4max", 0);
         if (b.lmax < 0 || b.lmax > 12) bad("lmax must be in [0, 12]");
-        if (l3 != 0 || l4 != 0) bad("l3max/l4max > 0 (bispectrum columns) are not supported");
+        if (l3 < 0 || l3 > 6) bad("l3max must be in [0, 6]");
+        if (l4 < 0 || l4 > 3) bad("l4max must be in [0, 3]");
         if (bool_or(m, {"noradial"}, false)) bad("noradial is invalid");
         if (!bool_or(m, {"l3cross"}, true) || !bool_or(m, {"l4cross"}, true)) bad("no l3cross/l4cross is invalid");
     }
@@ -237,7 +240,15 @@ SubBasis load_sub(int kind, int T, const JValue& m) {
             break;
         default: bad("invalid wtype");
     }
-    b.size = kind == KIND_RADIAL ? NP : NP * (b.lmax + 1);
+    if (kind == KIND_SPHERICAL) {
+        // the expansion runs to the largest l any column needs (SphericalChebyshev.java:39-44)
+        b.nl2 = b.lmax + 1;
+        b.l3max = l3;
+        b.l4max = l4;
+        b.inv = invariant_columns(l3, l4);
+        b.lmax = std::max(b.lmax, std::max(l3, l4));
+    }
+    b.size = kind == KIND_RADIAL ? NP : NP * (b.nl2 + (int)b.inv.size());
     b.fused = tw == WT_RFUSE || tw == WT_FUSE || tw == WT_EXFUSE;
     return b;
 }

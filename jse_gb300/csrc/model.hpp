@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include "invariants.hpp"
+
 namespace nnapgb {
 
 enum { KIND_RADIAL = 0, KIND_SPHERICAL = 1 };
@@ -14,7 +16,11 @@ enum { KIND_RADIAL = 0, KIND_SPHERICAL = 1 };
 // sub-basis start at fp_off within the species' descriptor.
 struct SubBasis {
     int kind = KIND_SPHERICAL;
-    int nmax = 5, lmax = 0, np = 0;
+    // lmax: largest l of the expansion A (the largest of the file's lmax, l3max, l4max);
+    // nl2: power-spectrum columns per channel (the file's lmax + 1), followed by the
+    // invariant columns inv (l3max / l4max) of the same channel
+    int nmax = 5, lmax = 0, np = 0, nl2 = 1, l3max = 0, l4max = 0;
+    std::vector<std::vector<InvTerm>> inv;
     int fp_off = 0, size = 0;
     double rcut = 6.0;
     bool fused = false;     // wtype fuse / rfuse / exfuse: the matrix is a trainable parameter

@@ -44,8 +44,11 @@ void upload_model(nnap_handle* h) {
     for (int t = 0; t < T;) {
         Run r;
         r.t0 = t;
+        auto shape = [](const SubBasis& b) {
+            return SubShape{b.kind, b.lmax, b.np, b.nmax + 1, b.rcut, b.nl2, b.l3max, b.l4max, (int)b.inv.size()};
+        };
         for (auto& b : m.sp[t].subs) {
-            r.subs.push_back({b.kind, b.lmax, b.np, b.nmax + 1, b.rcut});
+            r.subs.push_back(shape(b));
             r.fp_off.push_back(b.fp_off);
         }
         int u = t + 1;
@@ -53,7 +56,7 @@ void upload_model(nnap_handle* h) {
             const auto& su = m.sp[u].subs;
             bool same = su.size() == r.subs.size() && m.sp[u].D == m.sp[t].D;
             for (size_t k = 0; same && k < su.size(); ++k)
-                same = r.subs[k] == SubShape{su[k].kind, su[k].lmax, su[k].np, su[k].nmax + 1, su[k].rcut};
+                same = r.subs[k] == shape(su[k]);
             if (!same) break;
             ++u;
         }
@@ -91,6 +94,29 @@ void upload_model(nnap_handle* h) {
                             zw[q] = v;
                         }
                     }
+            // invariant-column terms (the same for every species of the run)
+            r.inv_idx.emplace_back();
+            r.inv_coef.emplace_back();
+            r.inv_start.emplace_back();
+            if (s.ninv) {
+                const auto& cols = m.sp[r.t0].subs[k].inv;
+                std::vector<int4> ti;
+                std::vector<float> tc;
+                std::vector<int> cs{0};
+                for (auto& col : cols) {
+                    for (auto& q : col) {
+                        ti.push_back(make_int4(q.idx[0], q.idx[1], q.idx[2], q.idx[3]));
+                        tc.push_back((float)q.coeff);
+                    }
+                    cs.push_back((int)ti.size());
+                }
+                r.inv_idx.back().ensure(ti.size());
+                r.inv_coef.back().ensure(tc.size());
+                r.inv_start.back().ensure(cs.size());
+                CK(cudaMemcpy(r.inv_idx.back().p, ti.data(), ti.size() * sizeof(int4), cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(r.inv_coef.back().p, tc.data(), tc.size() * sizeof(float), cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(r.inv_start.back().p, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice));
+            }
             r.nzp.emplace_back();
             r.nzw.emplace_back();
             if (sparse) {
@@ -326,6 +352,10 @@ void ensure_work(nnap_handle* h, int n, int nstruct, int ncells, int nchunks) {
     h->fp.ensure((size_t)n1 * h->fp_stride);
     h->gfp.ensure((size_t)n1 * h->fp_stride);
     h->A.ensure(std::max<size_t>(a_arena_size(h, n), 1));
+    bool inv = false;
+    for (auto& r : h->runs)
+        for (auto& sh : r.subs) inv = inv || sh.ninv > 0;
+    if (inv) h->Gx.ensure(std::max<size_t>(a_arena_size(h, n), 1));
     h->e_atom.ensure(n1);
     h->forces.ensure(3 * (size_t)n1);
     h->virials.ensure(9 * (size_t)n1);
@@ -442,6 +472,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.fp_stride = h->fp_stride;
                 a.fp_off = r.fp_off[k];
                 a.A = nullptr;
+                a.Gx = nullptr;
+                size_t this_off = a_off;
                 if (s.kind == KIND_SPHERICAL) {
                     a.A = h->A.p + a_off;
                     a_off += (size_t)n * s.np * (s.lmax + 1) * (s.lmax + 1);
@@ -451,9 +483,43 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.warps = fwd ? h->tune.desc_fwd_warps : h->tune.desc_bwd_warps;
                 a.nz_p = r.nzp[k].p;
                 a.nz_w = r.nzw[k].p;
+                a.nl2 = s.nl2;
+                a.sl = s.nl2 + s.ninv;
+                // invariant columns: forward after the expansion, their dE/dA before the backward
+                InvArgs ia;
+                if (s.ninv && n > 0) {
+                    ia.perm = h->perm.p;
+                    ia.range = h->type_start.p;
+                    ia.t0 = r.t0;
+                    ia.t1 = r.t1;
+                    ia.nmax = n;
+                    ia.A = a.A;
+                    ia.NP = s.np;
+                    ia.K = (s.lmax + 1) * (s.lmax + 1);
+                    ia.idx = r.inv_idx[k].p;
+                    ia.coef = r.inv_coef[k].p;
+                    ia.start = r.inv_start[k].p;
+                    ia.ncol = s.ninv;
+                    ia.fp = h->fp.p;
+                    ia.gfp = h->gfp.p;
+                    ia.fp_stride = h->fp_stride;
+                    ia.fp_off = r.fp_off[k];
+                    ia.nl2 = s.nl2;
+                    ia.sl = a.sl;
+                    ia.Gx = h->Gx.p + this_off;
+                    if (!fwd) {
+                        CK(launch_invariants(ia, false, st));
+                        ++h->launches;
+                        a.Gx = ia.Gx;
+                    }
+                }
                 if (n > 0) {
                     CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, st));
                     ++h->launches;
+                    if (fwd && s.ninv) {
+                        CK(launch_invariants(ia, true, st));
+                        ++h->launches;
+                    }
                 }
             }
         }
@@ -805,16 +871,26 @@ int nnap_destroy(nnap_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     h->dead = true;
-    for (auto& r : h->runs)
+    for (auto& r : h->runs) {
         for (auto& w : r.W) w.release();
+        for (auto& b : r.nzp) b.release();
+        for (auto& b : r.nzw) b.release();
+        for (auto& b : r.inv_idx) b.release();
+        for (auto& b : r.inv_coef) b.release();
+        for (auto& b : r.inv_start) b.release();
+    }
     for (auto& nd : h->nets) { nd.w32.release(); net_tc_release(nd.tc); }
+    for (auto* b : {&h->tu, &h->trec, &h->tpart, &h->tbW, &h->tdA, &h->tgfp, &h->tdfp, &h->twpart}) b->release();
+    for (auto* b : {&h->tbFd, &h->tbE, &h->tgrad, &h->twgrad}) b->release();
+    h->tbF.release();
+    h->ttiles.release();
     h->x.release(); h->xw.release(); h->e_atom.release(); h->forces.release(); h->virials.release();
     h->energy.release(); h->virial.release(); h->partial.release();
     h->type.release(); h->sid.release(); h->cell_of.release(); h->cell_count.release(); h->cell_fill.release();
     h->cell_start.release(); h->cell_atoms.release(); h->perm.release(); h->block_counts.release();
     h->type_start.release(); h->chunk_b.release(); h->chunk_e.release(); h->struct_chunks.release();
     h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
-    h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->gstart.release();
+    h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->Gx.release(); h->gstart.release();
     for (auto* b : {&h->lmp_x, &h->lmp_forces, &h->lmp_virials}) b->release();
     for (auto* b : {&h->lmp_type, &h->lmp_ilist, &h->lmp_off, &h->lmp_idx, &h->lmp_rowtype, &h->lmp_rowof,
                     &h->lmp_tcount, &h->lmp_tstart, &h->lmp_tfill, &h->lmp_tlist})

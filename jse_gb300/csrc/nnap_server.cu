@@ -120,10 +120,13 @@ size_t work_bytes_per_atom(const nnap_server* s) {
     size_t b = (size_t)s->Mv * (8 + 16 + 4 + 16 + 2);
     b += (size_t)h->fp_stride * 4 * 2;
     size_t a = 0;
+    bool inv = false;
     for (auto& r : h->runs)
-        for (auto& sb : r.subs)
+        for (auto& sb : r.subs) {
             if (sb.kind == KIND_SPHERICAL) a += (size_t)sb.np * (sb.lmax + 1) * (sb.lmax + 1);
-    b += a * 4;
+            inv = inv || sb.ninv > 0;
+        }
+    b += a * 4 * (inv ? 2 : 1);  // A, and its invariant-column gradient when present
     b += 24 + 24 + 32 + 16 + 4 * 8 + 8 + 24 + 72;
     return b;
 }

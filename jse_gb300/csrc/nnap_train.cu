@@ -149,6 +149,9 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             a.warps = 4;
             a.nz_p = nullptr;
             a.nz_w = nullptr;
+            a.nl2 = s.nl2;
+            a.sl = s.nl2 + s.ninv;
+            a.Gx = nullptr;
             ja.bF = dbF;
             ja.bW = dbW;
             ja.sid = h->sid.p;
@@ -260,6 +263,9 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
                 a.warps = 4;
                 a.nz_p = nullptr;
                 a.nz_w = nullptr;
+                a.nl2 = sh.nl2;
+                a.sl = sh.nl2 + sh.ninv;
+                a.Gx = nullptr;
                 g.j.bF = dbF;
                 g.j.bW = dbW;
                 g.j.sid = h->sid.p;
@@ -347,6 +353,11 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         const Model& m = h->model;
         const int T = m.ntypes();
         const bool want_w = grad_fp && any_fused(m);
+        for (auto& sp : m.sp)
+            for (auto& b : sp.subs)
+                if (!b.inv.empty())
+                    throw ApiFail(NNAP_ERR_UNSUPPORTED,
+                                  "training gradients of the l3max / l4max invariant columns are not implemented");
         h->launches = 0;
         Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
