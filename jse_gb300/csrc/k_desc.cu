@@ -413,7 +413,7 @@ struct SphNShape {
     static constexpr int NT = L * (L + 1) / 2 + L + 1;      // Legendre entries
     static constexpr int N1P = (N1 + 3) & ~3;
     static constexpr int NPS = (NP + 3) & ~3;
-    static constexpr int SCR = (K * NPS > NT * 32 ? K * NPS : NT * 32);
+    static constexpr int SCR = ((K * NP > NT * 32 ? K * NP : NT * 32) + 3) & ~3;  // keeps float4 rows aligned
     static int warp_floats(int T) { return T * K * N1P + SCR; }
 };
 
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
     float* sGh = smem + ((2 * ntab + 3) & ~3) + (size_t)wl * (T * S::K * S::N1P + S::SCR);  // [T][K][N1P]
-    float* scr = sGh + T * S::K * S::N1P;   // G [K][NPS], then the Legendre columns [NT][32]
+    float* scr = sGh + T * S::K * S::N1P;   // G [NP][K], then the Legendre columns [NT][32]
     const int at = a.perm[s0 + w];
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
@@ -450,31 +450,34 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
             const float coef = l < a.nl2 ? 2.f * kPi4 / (float)(2 * l + 1) : 0.f;
             const int lc = l < a.nl2 ? l : 0;
 #pragma unroll
-            for (int p = 0; p < NP; ++p) {
+            for (int p = 0; p < NP; ++p) {  // lanes over lm: conflict-free [p][K] stores
                 float v = coef * gf[p * a.sl + lc] * Ain[p * S::K + lm];
                 if (a.Gx) v += a.Gx[(size_t)w * NP * S::K + p * S::K + lm];
-                scr[lm * S::NPS + p] = v;
+                scr[p * S::K + lm] = v;
             }
         }
         __syncwarp();
-        // Gh[tn][lm][n] from the sparse fuse table of (tc, tn)
+        // Gh[tn][lm][n] from the sparse fuse table of (tc, tn); lanes over lm read G rows
+        // without conflicts and write their Gh rows as float4
         for (int idx = lane; idx < T * S::K; idx += 32) {
             const int tn = idx / S::K, lm = idx - tn * S::K;
             const int* np_ = sNp + (size_t)(tc * T + tn) * N1 * kNz;
             const float* nw = sNw + (size_t)(tc * T + tn) * N1 * kNz;
-            float* out = sGh + (size_t)idx * S::N1P;
+            float v[S::N1P];
 #pragma unroll
             for (int n = 0; n < S::N1P; ++n) {
-                float v = 0.f;
+                v[n] = 0.f;
                 if (n < N1) {
 #pragma unroll
                     for (int z = 0; z < kNz; ++z) {
                         const int pp = np_[n * kNz + z];
-                        if (pp >= 0) v += nw[n * kNz + z] * scr[lm * S::NPS + pp];
+                        if (pp >= 0) v[n] += nw[n * kNz + z] * scr[pp * S::K + lm];
                     }
                 }
-                out[n] = v;
             }
+            float4* out = reinterpret_cast<float4*>(sGh + (size_t)idx * S::N1P);
+#pragma unroll
+            for (int q = 0; q < S::N1P / 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
         }
         __syncwarp();
     }
