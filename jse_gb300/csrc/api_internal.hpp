@@ -107,6 +107,9 @@ struct Run {
     // has more than kNz nonzero rows or N1 >= NP (the backward then stays in NP space)
     std::vector<DevBuf<int>> nzp;
     std::vector<DevBuf<float>> nzw;
+    // per sub: alpha[tc][tn][p] of the radial-space forward ([T][kFwdTypes][NP]), empty
+    // unless every row p of W has its only nonzero in column p mod N1, N1 < NP, T <= kFwdTypes
+    std::vector<DevBuf<float>> falpha;
     // per sub: invariant-column terms (indices into A, -1 past the order; coefficients)
     // and each column's first term, [ninv + 1]
     std::vector<DevBuf<int4>> inv_idx;

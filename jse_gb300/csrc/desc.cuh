@@ -28,6 +28,9 @@ struct DescArgs {
     // their weights, or NULL (the kernel then works in the space of the NP channels)
     const int* nz_p;
     const float* nz_w;
+    // spherical forward: alpha[tc][tn][p] with W[tc][tn][p][n] = alpha delta(n, p mod N1),
+    // [T][kFwdTypes][NP], or NULL (the forward then accumulates the NP channels)
+    const float* fwd_alpha;
     // spherical: power-spectrum columns per channel (l < nl2) and descriptor columns per
     // channel (sl = nl2 + invariant columns); Gx, or NULL: the invariant columns' part of
     // dE/dA, [slot - range[t0]][NP][K] like A, added to the power-spectrum part
@@ -54,7 +57,8 @@ struct InvArgs {
 };
 cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st);
 
-constexpr int kNz = 4;  // nonzero rows per column of a fuse matrix kept in the sparse form
+constexpr int kNz = 4;        // nonzero rows per column (or columns per row) of a fuse matrix in sparse form
+constexpr int kFwdTypes = 3;  // most species for the radial-space forward (per-species accumulators)
 
 // Compiled shapes.  Radial: (NP, N1).  Spherical: (L, NP, N1).
 #define NNAP_RADIAL_SHAPES(X) X(11, 11) X(12, 6) X(4, 4) X(8, 4) X(12, 4) X(18, 9)

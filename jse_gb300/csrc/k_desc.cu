@@ -237,6 +237,144 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
     }
 }
 
+// Forward in the space of the radial functions, for at most kFwdTypes species and fuse
+// matrices whose row p has its only nonzero in column p mod N1 (every weight type but
+// rfuse): W[tc][tn][p][n] = alpha[tc][tn][p] delta(n, p mod N1).  Per neighbour species
+// tn the warp accumulates
+//   Ah[tn][n][lm] = sum_{j of species tn} fc_j T_n(r_j) Y_j[lm]
+// (N1 instead of NP products per neighbour and lm; the neighbour's species is uniform
+// across the warp in the accumulation loop, so the branch does not diverge), then
+//   A[p][lm] = sum_tn alpha[tc][tn][p] Ah[tn][p mod N1][lm]
+// straight from the accumulator registers.  fc Rnp is never formed.
+template <int L, int NP, int N1>
+struct SphFNShape {
+    static constexpr int K = (L + 1) * (L + 1);
+    static constexpr int COLS = (K + 31) / 32;
+    static constexpr int KS = K | 1;
+    static constexpr int N1P = (N1 + 3) & ~3;
+    static constexpr int H = (N1 + 1) / 2;
+    static constexpr int EVAL = 32 * KS + 32 * N1P + 32;   // Y, fc T, species
+    static constexpr int POST = NP * K;                     // A^2
+    static constexpr int WARP_FLOATS = ((EVAL > POST ? EVAL : POST) + 3) & ~3;
+};
+
+template <int L, int NP, int N1>
+__global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd_n(DescArgs a) {
+    using S = SphFNShape<L, NP, N1>;
+    extern __shared__ float smem[];
+    const int T = a.T;
+    const int ntab = T * kFwdTypes * NP;  // alpha[tc][tn][p], zero for tn >= T
+    float* sAl = smem;
+    for (int q = threadIdx.x; q < ntab; q += blockDim.x) sAl[q] = a.fwd_alpha[q];
+    __syncthreads();
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wl;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    float* base = smem + ((ntab + 3) & ~3) + (size_t)wl * S::WARP_FLOATS;
+    float* sY = base;                                       // [32][KS]
+    float* sF = sY + 32 * S::KS;                            // [32][N1P] fc T_n
+    int* sTn = reinterpret_cast<int*>(sF + 32 * S::N1P);    // [32]
+    const int at = a.perm[s0 + w];
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut, irc = 1.f / a.rcut;
+    float2 acc[kFwdTypes][S::H][S::COLS];
+#pragma unroll
+    for (int t = 0; t < kFwdTypes; ++t)
+#pragma unroll
+        for (int h = 0; h < S::H; ++h)
+#pragma unroll
+            for (int c = 0; c < S::COLS; ++c) acc[t][h][c] = make_float2(0.f, 0.f);
+    for (int b0 = 0; b0 < cnt; b0 += 32) {
+        const int k = b0 + lane;
+        float fT[S::N1P];
+#pragma unroll
+        for (int n = 0; n < S::N1P; ++n) fT[n] = 0.f;
+        float* y = sY + lane * S::KS;
+        int tn = 0;
+        bool valid = false;
+        if (k < cnt) {
+            const float4 d = a.P.dx[(size_t)at * M + k];
+            const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+            if (r < rc) {
+                valid = true;
+                tn = __float_as_int(d.w) - 1;
+                const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
+                cheby_f<N1>(1.f - 2.f * u, fT);
+#pragma unroll
+                for (int n = 0; n < N1; ++n) fT[n] *= fc;
+                const Angles an = angles_f(d.x, d.y, d.z, r);
+                sph_harm<L, false>(an, y, nullptr, 1);
+            }
+        }
+        if (!valid)
+#pragma unroll 7
+            for (int q = 0; q < S::K; ++q) y[q] = 0.f;
+        float4* frow = reinterpret_cast<float4*>(sF + lane * S::N1P);
+#pragma unroll
+        for (int q = 0; q < S::N1P / 4; ++q) frow[q] = make_float4(fT[4 * q], fT[4 * q + 1], fT[4 * q + 2], fT[4 * q + 3]);
+        sTn[lane] = tn;
+        __syncwarp();
+        const int nk = min(32, cnt - b0);
+        for (int kk = 0; kk < nk; ++kk) {
+            float2 f2[S::N1P / 2];
+            const float4* fr = reinterpret_cast<const float4*>(sF + kk * S::N1P);
+#pragma unroll
+            for (int q = 0; q < S::N1P / 4; ++q) {
+                const float4 v = fr[q];
+                f2[2 * q] = make_float2(v.x, v.y);
+                f2[2 * q + 1] = make_float2(v.z, v.w);
+            }
+            float2 yy[S::COLS];
+#pragma unroll
+            for (int col = 0; col < S::COLS; ++col) {
+                const int lm = lane + 32 * col;
+                const float yv = lm < S::K ? sY[kk * S::KS + lm] : 0.f;
+                yy[col] = make_float2(yv, yv);
+            }
+            const int t = sTn[kk];
+#pragma unroll
+            for (int tt = 0; tt < kFwdTypes; ++tt) {
+                if (t != tt) continue;  // uniform across the warp
+#pragma unroll
+                for (int h = 0; h < S::H; ++h)
+#pragma unroll
+                    for (int col = 0; col < S::COLS; ++col) acc[tt][h][col] = __ffma2_rn(f2[h], yy[col], acc[tt][h][col]);
+            }
+        }
+        __syncwarp();
+    }
+    // A from the accumulators and alpha; A to global memory, A^2 to shared memory
+    float* sA2 = base;
+    float* Aout = a.A + (size_t)w * NP * S::K;
+    const float* al = sAl + (size_t)tc * kFwdTypes * NP;
+#pragma unroll
+    for (int col = 0; col < S::COLS; ++col) {
+        const int lm = lane + 32 * col;
+        if (lm < S::K) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const int n = p % N1;  // a constant once the loop is unrolled
+                float v = 0.f;
+#pragma unroll
+                for (int t = 0; t < kFwdTypes; ++t)
+                    v += al[t * NP + p] * ((n & 1) ? acc[t][n >> 1][col].y : acc[t][n >> 1][col].x);
+                Aout[p * S::K + lm] = v;
+                sA2[p * S::K + lm] = v * v;
+            }
+        }
+    }
+    __syncwarp();
+    float* out = a.fp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    for (int e = lane; e < NP * a.nl2; e += 32) {
+        const int p = e / a.nl2, l = e - p * a.nl2;
+        float s = 0.f;
+        for (int m = 0; m <= 2 * l; ++m) s += sA2[p * S::K + l * l + m];
+        out[p * a.sl + l] = kPi4 / (float)(2 * l + 1) * s;
+    }
+}
+
 // Backward, one warp per atom slot, one neighbour per lane.  For each neighbour,
 //   dY_lm = sum_p c_p G[p][lm]        (chain into theta and phi),
 //   dc_p  = sum_lm G[p][lm] Y_lm      (chain into fc and the radial functions),
@@ -701,11 +839,30 @@ cudaError_t launch_sph_bwd_n(const DescArgs& a, cudaStream_t st) {
 }
 
 template <int L, int NP, int N1>
+cudaError_t launch_sph_fwd_n(const DescArgs& a, cudaStream_t st) {
+    using S = SphFNShape<L, NP, N1>;
+    const int wpc = a.warps;
+    const int grid = (a.nmax + wpc - 1) / wpc;
+    const size_t sm = sizeof(float) * (((size_t)a.T * kFwdTypes * NP + 3) / 4 * 4 + (size_t)wpc * S::WARP_FLOATS);
+    if (sm > 227 * 1024) return cudaErrorInvalidValue;
+    static int lim = 0;
+    if ((int)sm > lim) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_sph_fwd_n<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        lim = (int)sm;
+    }
+    k_sph_fwd_n<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L, int NP, int N1>
 cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     using S = SphShape<L, NP>;
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
     if (!fwd && a.nz_p && a.nz_w && N1 < NP) return launch_sph_bwd_n<L, NP, N1>(a, st);
+    if (fwd && a.fwd_alpha && N1 < NP && a.T <= kFwdTypes) return launch_sph_fwd_n<L, NP, N1>(a, st);
     const int wpc = a.warps;
     const int grid = (n + wpc - 1) / wpc;
     const size_t wbytes = sizeof(float) * ((size_t)a.T * a.T * NP * Fuse<N1>::N1P);

@@ -117,6 +117,24 @@ void upload_model(nnap_handle* h) {
                 CK(cudaMemcpy(r.inv_coef.back().p, tc.data(), tc.size() * sizeof(float), cudaMemcpyHostToDevice));
                 CK(cudaMemcpy(r.inv_start.back().p, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice));
             }
+            // per-row scales for the radial-space forward
+            {
+                std::vector<float> al((size_t)T * kFwdTypes * s.np, 0.f);
+                bool diag = s.kind == KIND_SPHERICAL && s.n1 < s.np && T <= kFwdTypes;
+                for (int tc = r.t0; tc < r.t1 && diag; ++tc)
+                    for (int tn = 0; tn < T && diag; ++tn)
+                        for (int p = 0; p < s.np && diag; ++p)
+                            for (int nn = 0; nn < s.n1; ++nn) {
+                                const float v = W[(((size_t)tc * T + tn) * s.np + p) * s.n1 + nn];
+                                if (nn == p % s.n1) al[((size_t)tc * kFwdTypes + tn) * s.np + p] = v;
+                                else if (v != 0.f) { diag = false; break; }
+                            }
+                r.falpha.emplace_back();
+                if (diag) {
+                    r.falpha.back().ensure(al.size());
+                    CK(cudaMemcpy(r.falpha.back().p, al.data(), al.size() * sizeof(float), cudaMemcpyHostToDevice));
+                }
+            }
             r.nzp.emplace_back();
             r.nzw.emplace_back();
             if (sparse) {
@@ -483,6 +501,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.warps = fwd ? h->tune.desc_fwd_warps : h->tune.desc_bwd_warps;
                 a.nz_p = r.nzp[k].p;
                 a.nz_w = r.nzw[k].p;
+                a.fwd_alpha = r.falpha[k].p;
                 a.nl2 = s.nl2;
                 a.sl = s.nl2 + s.ninv;
                 // invariant columns: forward after the expansion, their dE/dA before the backward
@@ -875,6 +894,7 @@ int nnap_destroy(nnap_handle* h) {
         for (auto& w : r.W) w.release();
         for (auto& b : r.nzp) b.release();
         for (auto& b : r.nzw) b.release();
+        for (auto& b : r.falpha) b.release();
         for (auto& b : r.inv_idx) b.release();
         for (auto& b : r.inv_coef) b.release();
         for (auto& b : r.inv_start) b.release();

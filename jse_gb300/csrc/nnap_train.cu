@@ -149,6 +149,7 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             a.warps = 4;
             a.nz_p = nullptr;
             a.nz_w = nullptr;
+            a.fwd_alpha = nullptr;
             a.nl2 = s.nl2;
             a.sl = s.nl2 + s.ninv;
             a.Gx = nullptr;
@@ -263,6 +264,7 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
                 a.warps = 4;
                 a.nz_p = nullptr;
                 a.nz_w = nullptr;
+                a.fwd_alpha = nullptr;
                 a.nl2 = sh.nl2;
                 a.sl = sh.nl2 + sh.ninv;
                 a.Gx = nullptr;
