@@ -269,6 +269,180 @@ __global__ void __launch_bounds__(32 * kJvpWarps) k_sph_jvp(JvpArgs ja) {
     }
 }
 
+// Directional derivative in the space of the radial functions (fuse matrices whose row p
+// has its only nonzero alpha[tc][tn][p] in column p mod N1, at most kFwdTypes species):
+//   dAh[tn][n][lm] = sum_{j of species tn} D_b(fc T_n) Y_lm + fc T_n D_b(Y_lm),
+//   dA[p][lm] = sum_tn alpha[tc][tn][p] dAh[tn][p mod N1][lm]
+// (2 N1 instead of 2 NP products per neighbour and lm, as the radial-space forward).
+template <int L, int NP, int N1>
+struct JvpNShape {
+    static constexpr int K = (L + 1) * (L + 1);
+    static constexpr int COLS = (K + 31) / 32;
+    static constexpr int KS = K | 1;
+    static constexpr int N1P = (N1 + 3) & ~3;
+    static constexpr int H = (N1 + 1) / 2;
+    static constexpr int EVAL = 2 * 32 * KS + 2 * 32 * N1P + 32;  // Y, D_b Y, fc T, D_b(fc T), species
+    static constexpr int POST = NP * K;
+    static constexpr int WARP_FLOATS = ((EVAL > POST ? EVAL : POST) + 3) & ~3;
+};
+
+template <int L, int NP, int N1>
+__global__ void __launch_bounds__(32 * kJvpWarps, 3) k_sph_jvp_n(JvpArgs ja) {
+    using S = JvpNShape<L, NP, N1>;
+    const DescArgs& a = ja.d;
+    extern __shared__ float smem[];
+    const int T = a.T;
+    const int ntab = T * kFwdTypes * NP;
+    float* sAl = smem;
+    for (int q = threadIdx.x; q < ntab; q += blockDim.x) sAl[q] = a.fwd_alpha[q];
+    __syncthreads();
+    const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * (blockDim.x >> 5) + wl;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    float* base = smem + ((ntab + 3) & ~3) + (size_t)wl * S::WARP_FLOATS;
+    float* sY = base;                       // [32][KS]
+    float* sD = sY + 32 * S::KS;            // [32][KS]
+    float* sF = sD + 32 * S::KS;            // [32][N1P] fc T_n
+    float* sV = sF + 32 * S::N1P;           // [32][N1P] D_b(fc T_n)
+    int* sTn = reinterpret_cast<int*>(sV + 32 * S::N1P);
+    const int at = a.perm[s0 + w];
+    const int tc = a.type[at] - 1;
+    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const float rc = a.rcut;
+    float2 acc[kFwdTypes][S::H][S::COLS];
+#pragma unroll
+    for (int t = 0; t < kFwdTypes; ++t)
+#pragma unroll
+        for (int h = 0; h < S::H; ++h)
+#pragma unroll
+            for (int c = 0; c < S::COLS; ++c) acc[t][h][c] = make_float2(0.f, 0.f);
+    for (int b0 = 0; b0 < cnt; b0 += 32) {
+        const int k = b0 + lane;
+        float* y = sY + lane * S::KS;
+        float* dy = sD + lane * S::KS;
+        int tn = 0;
+        bool valid = false;
+        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 b = make_float3(0.f, 0.f, 0.f);
+        float r = 1.f;
+        if (k < cnt) {
+            const size_t e = (size_t)at * M + k;
+            d = a.P.dx[e];
+            r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+            if (r < rc) {
+                valid = true;
+                tn = __float_as_int(d.w) - 1;
+                b = pair_upstream(ja, at, e, d);
+            }
+        }
+        {
+            // radial rows first, so they hold no registers during the harmonics
+            float fT[S::N1P], v[S::N1P];
+#pragma unroll
+            for (int n = 0; n < S::N1P; ++n) { fT[n] = 0.f; v[n] = 0.f; }
+            if (valid) radial_dir<N1>(r, rc, d.x * b.x + d.y * b.y + d.z * b.z, fT, v);
+            float4* fr = reinterpret_cast<float4*>(sF + lane * S::N1P);
+            float4* vr = reinterpret_cast<float4*>(sV + lane * S::N1P);
+#pragma unroll
+            for (int q = 0; q < S::N1P / 4; ++q) {
+                fr[q] = make_float4(fT[4 * q], fT[4 * q + 1], fT[4 * q + 2], fT[4 * q + 3]);
+                vr[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+        }
+        if (valid) {
+            {
+                const Angles an = angles_f(d.x, d.y, d.z, r);
+                sph_harm<L, true>(an, y, dy, 1);
+                const float ir = 1.f / r;
+                const float dth = an.ct * an.cp * ir * b.x + an.ct * an.sp * ir * b.y - an.st * ir * b.z;
+                const float dph = an.pole ? 0.f : (-an.sp * b.x + an.cp * b.y) / an.dxy;
+#pragma unroll
+                for (int l = 0; l <= L; ++l) {
+                    const int c0 = l * l + l;
+                    dy[c0] *= dth;
+#pragma unroll
+                    for (int m = 1; m <= l; ++m) {
+                        const float yp = y[c0 + m], ym = y[c0 - m];
+                        dy[c0 + m] = dy[c0 + m] * dth - (float)m * ym * dph;
+                        dy[c0 - m] = dy[c0 - m] * dth + (float)m * yp * dph;
+                    }
+                }
+            }
+        }
+        if (!valid)
+#pragma unroll 7
+            for (int q = 0; q < S::K; ++q) { y[q] = 0.f; dy[q] = 0.f; }
+        sTn[lane] = tn;
+        __syncwarp();
+        const int nk = min(32, cnt - b0);
+        for (int kk = 0; kk < nk; ++kk) {
+            float2 f2[S::N1P / 2], v2[S::N1P / 2];
+            const float4* fk = reinterpret_cast<const float4*>(sF + kk * S::N1P);
+            const float4* vk = reinterpret_cast<const float4*>(sV + kk * S::N1P);
+#pragma unroll
+            for (int q = 0; q < S::N1P / 4; ++q) {
+                const float4 x = fk[q], z = vk[q];
+                f2[2 * q] = make_float2(x.x, x.y);
+                f2[2 * q + 1] = make_float2(x.z, x.w);
+                v2[2 * q] = make_float2(z.x, z.y);
+                v2[2 * q + 1] = make_float2(z.z, z.w);
+            }
+            float2 yy[S::COLS], dd[S::COLS];
+#pragma unroll
+            for (int col = 0; col < S::COLS; ++col) {
+                const int lm = lane + 32 * col;
+                const float yv = lm < S::K ? sY[kk * S::KS + lm] : 0.f;
+                const float dv = lm < S::K ? sD[kk * S::KS + lm] : 0.f;
+                yy[col] = make_float2(yv, yv);
+                dd[col] = make_float2(dv, dv);
+            }
+            const int t = sTn[kk];
+#pragma unroll
+            for (int tt = 0; tt < kFwdTypes; ++tt) {
+                if (t != tt) continue;  // uniform across the warp
+#pragma unroll
+                for (int h = 0; h < S::H; ++h)
+#pragma unroll
+                    for (int col = 0; col < S::COLS; ++col) {
+                        acc[tt][h][col] = __ffma2_rn(v2[h], yy[col], acc[tt][h][col]);
+                        acc[tt][h][col] = __ffma2_rn(f2[h], dd[col], acc[tt][h][col]);
+                    }
+            }
+        }
+        __syncwarp();
+    }
+    // dA from the accumulators; A dA products into shared memory, then the l sums
+    const float* Ain = a.A + (size_t)w * NP * S::K;
+    float* dAout = ja.dA ? ja.dA + (size_t)w * NP * S::K : nullptr;
+    const float* al = sAl + (size_t)tc * kFwdTypes * NP;
+    float* sP = base;  // [NP][K]
+#pragma unroll
+    for (int col = 0; col < S::COLS; ++col) {
+        const int lm = lane + 32 * col;
+        if (lm < S::K) {
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const int n = p % N1;  // a constant once the loop is unrolled
+                float dv = 0.f;
+#pragma unroll
+                for (int t = 0; t < kFwdTypes; ++t)
+                    dv += al[t * NP + p] * ((n & 1) ? acc[t][n >> 1][col].y : acc[t][n >> 1][col].x);
+                sP[p * S::K + lm] = Ain[p * S::K + lm] * dv;
+                if (dAout) dAout[p * S::K + lm] = dv;
+            }
+        }
+    }
+    __syncwarp();
+    float* out = ja.u + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    for (int e = lane; e < NP * (L + 1); e += 32) {
+        const int p = e / (L + 1), l = e - p * (L + 1);
+        float s = 0.f;
+        for (int m = 0; m <= 2 * l; ++m) s += sP[p * S::K + l * l + m];
+        out[e] = -2.f * kPi4 / (float)(2 * l + 1) * s;
+    }
+}
+
 // =========================================================================== network
 namespace {
 
@@ -285,43 +459,66 @@ __device__ __forceinline__ float silu_gg(float z) {
     return s * (1.f - s) * (2.f + z * (1.f - 2.f * s));
 }
 
-// out[o][q] = sum_i WT[i][o] in[i][q] (+ bias[o]); lanes own outputs o.
+// out[o][q] = sum_i WT[i][o] in[i][q] (+ bias[o]); lanes own outputs o and o + 32, so each
+// pair of 8-atom input loads from shared memory feeds 16 FMAs per weight pair.
 __device__ __forceinline__ void mv_fwd(const float* __restrict__ WT, const float* __restrict__ bias, int in, int H,
                                        const float* vin, float* out, int lane) {
-    for (int o = lane; o < H; o += 32) {
-        float z[kTrainAtoms];
+    for (int o0 = 0; o0 < H; o0 += 64) {
+        const int oa = o0 + lane, ob = o0 + 32 + lane;
+        const bool ha = oa < H, hb = ob < H;
+        float za[kTrainAtoms], zb[kTrainAtoms];
 #pragma unroll
-        for (int q = 0; q < kTrainAtoms; ++q) z[q] = bias ? bias[o] : 0.f;
+        for (int q = 0; q < kTrainAtoms; ++q) {
+            za[q] = (bias && ha) ? bias[oa] : 0.f;
+            zb[q] = (bias && hb) ? bias[ob] : 0.f;
+        }
 #pragma unroll 4
         for (int i = 0; i < in; ++i) {
-            const float wv = WT[(size_t)i * H + o];
+            const float wa = ha ? WT[(size_t)i * H + oa] : 0.f;
+            const float wb = hb ? WT[(size_t)i * H + ob] : 0.f;
             const float4 x0 = *reinterpret_cast<const float4*>(vin + i * kTrainAtoms);
             const float4 x1 = *reinterpret_cast<const float4*>(vin + i * kTrainAtoms + 4);
-            z[0] += wv * x0.x; z[1] += wv * x0.y; z[2] += wv * x0.z; z[3] += wv * x0.w;
-            z[4] += wv * x1.x; z[5] += wv * x1.y; z[6] += wv * x1.z; z[7] += wv * x1.w;
+            za[0] += wa * x0.x; za[1] += wa * x0.y; za[2] += wa * x0.z; za[3] += wa * x0.w;
+            za[4] += wa * x1.x; za[5] += wa * x1.y; za[6] += wa * x1.z; za[7] += wa * x1.w;
+            zb[0] += wb * x0.x; zb[1] += wb * x0.y; zb[2] += wb * x0.z; zb[3] += wb * x0.w;
+            zb[4] += wb * x1.x; zb[5] += wb * x1.y; zb[6] += wb * x1.z; zb[7] += wb * x1.w;
         }
 #pragma unroll
-        for (int q = 0; q < kTrainAtoms; ++q) out[o * kTrainAtoms + q] = z[q];
+        for (int q = 0; q < kTrainAtoms; ++q) {
+            if (ha) out[oa * kTrainAtoms + q] = za[q];
+            if (hb) out[ob * kTrainAtoms + q] = zb[q];
+        }
     }
 }
 
-// out[i][q] = sum_o W[o][i] in[o][q]; lanes own inputs i.
+// out[i][q] = sum_o W[o][i] in[o][q]; lanes own inputs i, i + 32, i + 64 and i + 96.
 __device__ __forceinline__ void mv_bwd(const float* __restrict__ W, int in, int H, const float* vin, float* out,
                                        int lane) {
-    for (int i = lane; i < in; i += 32) {
-        float g[kTrainAtoms];
+    for (int i0 = 0; i0 < in; i0 += 128) {
+        float g[4][kTrainAtoms];
+        bool has[4];
 #pragma unroll
-        for (int q = 0; q < kTrainAtoms; ++q) g[q] = 0.f;
-#pragma unroll 4
+        for (int r = 0; r < 4; ++r) {
+            has[r] = i0 + 32 * r + lane < in;
+#pragma unroll
+            for (int q = 0; q < kTrainAtoms; ++q) g[r][q] = 0.f;
+        }
+#pragma unroll 2
         for (int o = 0; o < H; ++o) {
-            const float wv = W[(size_t)o * in + i];
             const float4 d0 = *reinterpret_cast<const float4*>(vin + o * kTrainAtoms);
             const float4 d1 = *reinterpret_cast<const float4*>(vin + o * kTrainAtoms + 4);
-            g[0] += wv * d0.x; g[1] += wv * d0.y; g[2] += wv * d0.z; g[3] += wv * d0.w;
-            g[4] += wv * d1.x; g[5] += wv * d1.y; g[6] += wv * d1.z; g[7] += wv * d1.w;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float wv = has[r] ? W[(size_t)o * in + i0 + 32 * r + lane] : 0.f;
+                g[r][0] += wv * d0.x; g[r][1] += wv * d0.y; g[r][2] += wv * d0.z; g[r][3] += wv * d0.w;
+                g[r][4] += wv * d1.x; g[r][5] += wv * d1.y; g[r][6] += wv * d1.z; g[r][7] += wv * d1.w;
+            }
         }
 #pragma unroll
-        for (int q = 0; q < kTrainAtoms; ++q) out[i * kTrainAtoms + q] = g[q];
+        for (int r = 0; r < 4; ++r)
+            if (has[r])
+#pragma unroll
+                for (int q = 0; q < kTrainAtoms; ++q) out[(i0 + 32 * r + lane) * kTrainAtoms + q] = g[r][q];
     }
 }
 
@@ -832,10 +1029,27 @@ cudaError_t launch_radial_jvp(const JvpArgs& a, cudaStream_t st) {
 }
 
 template <int L, int NP, int N1>
+cudaError_t launch_sph_jvp_n(const JvpArgs& a, cudaStream_t st) {
+    using S = JvpNShape<L, NP, N1>;
+    const size_t sm = sizeof(float) * (((size_t)a.d.T * kFwdTypes * NP + 3) / 4 * 4 + (size_t)kJvpWarps * S::WARP_FLOATS);
+    if (sm > 227 * 1024) return cudaErrorInvalidValue;
+    static int lim = 0;
+    if ((int)sm > lim) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_sph_jvp_n<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        lim = (int)sm;
+    }
+    k_sph_jvp_n<L, NP, N1><<<(a.d.nmax + kJvpWarps - 1) / kJvpWarps, 32 * kJvpWarps, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int L, int NP, int N1>
 cudaError_t launch_sph_jvp(const JvpArgs& a, cudaStream_t st) {
     using S = JvpShape<L, NP>;
     const int n = a.d.nmax;
     if (n <= 0) return cudaSuccess;
+    if (a.d.fwd_alpha && N1 < NP && a.d.T <= kFwdTypes) return launch_sph_jvp_n<L, NP, N1>(a, st);
     const size_t wf = ((size_t)a.d.T * a.d.T * NP * Fuse<N1>::N1P + 3) & ~(size_t)3;
     const size_t sm = sizeof(float) * (wf + (size_t)kJvpWarps * S::WARP_FLOATS);
     static int lim = 0;

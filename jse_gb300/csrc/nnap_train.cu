@@ -149,7 +149,7 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             a.warps = 4;
             a.nz_p = nullptr;
             a.nz_w = nullptr;
-            a.fwd_alpha = nullptr;
+            a.fwd_alpha = r.falpha[k].p;
             a.nl2 = s.nl2;
             a.sl = s.nl2 + s.ninv;
             a.Gx = nullptr;
