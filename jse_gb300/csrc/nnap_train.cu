@@ -16,7 +16,7 @@
 namespace nnapgb {
 namespace {
 
-constexpr int kTrainChunk = 1024;  // slots per partial sum
+constexpr int kTrainChunk = 256;  // slots per partial sum
 
 int net_params(const Species& sp) {
     int p = 0, in = sp.D;
