@@ -169,7 +169,7 @@ struct nnap_handle {
         lmp_tfill, lmp_tlist;
     // force-training gradients: directional derivatives, upstream gradients, per-slot
     // network records, chunk partials and the FP64 result
-    nnapgb::DevBuf<float> tu, trec, tpart, tbW, tdA, tgfp, tdfp, twpart;
+    nnapgb::DevBuf<float> tu, trec, tpart, tbW, tdA, tgfp, tdfp, twpart, tM1x, tM2x;
     nnapgb::DevBuf<float4> tbF;
     nnapgb::DevBuf<double> tbFd, tbE, tgrad, twgrad;
     nnapgb::DevBuf<nnapgb::GradTile> ttiles;

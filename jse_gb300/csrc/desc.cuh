@@ -54,8 +54,19 @@ struct InvArgs {
     const float* gfp;        // backward input: dE/dfp (by slot)
     int fp_stride, fp_off, nl2, sl;
     float* Gx;               // backward output, layout of A
+    // training: D_b A (layout of A), the directional derivatives u (descriptor layout),
+    // dL/dfp (descriptor layout) and the outputs M1x, M2x (layout of A)
+    const float* dA;
+    float* u;
+    const float* dfp;
+    float* M1x;
+    float* M2x;
 };
 cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st);
+// u of the invariant columns: -sum over terms of the column's derivative along D_b A.
+cudaError_t launch_invariants_jvp(const InvArgs& a, cudaStream_t st);
+// M1x = sum_c dfp_c dcol_c/dA - gfp_c (d2col_c/dA2) D_b A,  M2x = -sum_c gfp_c dcol_c/dA.
+cudaError_t launch_invariants_wgrad(const InvArgs& a, cudaStream_t st);
 
 constexpr int kNz = 4;        // nonzero rows per column (or columns per row) of a fuse matrix in sparse form
 constexpr int kFwdTypes = 3;  // most species for the radial-space forward (per-species accumulators)

@@ -787,6 +787,97 @@ __global__ void __launch_bounds__(128) k_inv_bwd(InvArgs a) {
     }
 }
 
+// u[p][nl2 + c] = -sum_terms coef sum_f (prod of the other factors) D_b A[factor f]
+__global__ void __launch_bounds__(128) k_inv_jvp(InvArgs a) {
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    float* out = a.u + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    for (int p = lane; p < a.NP; p += 32) {
+        const float* Ap = a.A + ((size_t)w * a.NP + p) * a.K;
+        const float* dAp = a.dA + ((size_t)w * a.NP + p) * a.K;
+        for (int c = 0; c < a.ncol; ++c) {
+            float s = 0.f;
+            for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
+                const int4 t = a.idx[q];
+                const float x = Ap[t.x], y = Ap[t.y], z = Ap[t.z];
+                const float dx = dAp[t.x], dy = dAp[t.y], dz = dAp[t.z];
+                float v;
+                if (t.w < 0) {
+                    v = dx * y * z + x * dy * z + x * y * dz;
+                } else {
+                    const float u = Ap[t.w], du = dAp[t.w];
+                    v = (dx * y * z + x * dy * z + x * y * dz) * u + x * y * z * du;
+                }
+                s += a.coef[q] * v;
+            }
+            out[p * a.sl + a.nl2 + c] = -s;
+        }
+    }
+}
+
+// Per channel: M1x and M2x of the radial-fuse gradient (the invariant columns' parts).
+__global__ void __launch_bounds__(128) k_inv_wgrad(InvArgs a) {
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
+    if (s0 + w >= s1) return;
+    const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    const float* df = a.dfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+    for (int p = lane; p < a.NP; p += 32) {
+        const size_t row = ((size_t)w * a.NP + p) * a.K;
+        const float* Ap = a.A + row;
+        const float* dAp = a.dA + row;
+        float* M1 = a.M1x + row;
+        float* M2 = a.M2x + row;
+        for (int k = 0; k < a.K; ++k) { M1[k] = 0.f; M2[k] = 0.f; }
+        for (int c = 0; c < a.ncol; ++c) {
+            const float gv = gf[p * a.sl + a.nl2 + c], dv = df[p * a.sl + a.nl2 + c];
+            for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
+                const int4 t = a.idx[q];
+                const float cf = a.coef[q];
+                const int ord = t.w < 0 ? 3 : 4;
+                const int id[4] = {t.x, t.y, t.z, t.w};
+                float v[4], dvv[4];
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    v[f] = f < ord ? Ap[id[f]] : 1.f;
+                    dvv[f] = f < ord ? dAp[id[f]] : 0.f;
+                }
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    if (f >= ord) continue;
+                    // d term / d A[f] and its derivative along D_b A
+                    float prod = 1.f, hd = 0.f;
+#pragma unroll
+                    for (int o = 0; o < 4; ++o) {
+                        if (o == f || o >= ord) continue;
+                        float pr = dvv[o];
+#pragma unroll
+                        for (int o2 = 0; o2 < 4; ++o2)
+                            if (o2 != f && o2 != o && o2 < ord) pr *= v[o2];
+                        hd += pr;
+                        prod *= v[o];
+                    }
+                    M1[id[f]] += cf * (dv * prod - gv * hd);
+                    M2[id[f]] -= cf * gv * prod;
+                }
+            }
+        }
+    }
+}
+
+cudaError_t launch_invariants_jvp(const InvArgs& a, cudaStream_t st) {
+    if (a.nmax <= 0 || a.ncol <= 0) return cudaSuccess;
+    k_inv_jvp<<<(a.nmax + 3) / 4, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_invariants_wgrad(const InvArgs& a, cudaStream_t st) {
+    if (a.nmax <= 0 || a.ncol <= 0) return cudaSuccess;
+    k_inv_wgrad<<<(a.nmax + 3) / 4, 128, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st) {
     if (a.nmax <= 0 || a.ncol <= 0) return cudaSuccess;
     const int grid = (a.nmax + 3) / 4;

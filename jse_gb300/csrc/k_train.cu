@@ -261,11 +261,11 @@ __global__ void __launch_bounds__(32 * kJvpWarps) k_sph_jvp(JvpArgs ja) {
     }
     __syncwarp();
     float* out = ja.u + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
-    for (int e = lane; e < NP * (L + 1); e += 32) {
-        const int p = e / (L + 1), l = e - p * (L + 1);
+    for (int e = lane; e < NP * a.nl2; e += 32) {
+        const int p = e / a.nl2, l = e - p * a.nl2;
         float s = 0.f;
         for (int m = 0; m <= 2 * l; ++m) s += sP[p * S::K + l * l + m];
-        out[e] = -2.f * kPi4 / (float)(2 * l + 1) * s;
+        out[p * a.sl + l] = -2.f * kPi4 / (float)(2 * l + 1) * s;
     }
 }
 
@@ -435,11 +435,11 @@ __global__ void __launch_bounds__(32 * kJvpWarps, 3) k_sph_jvp_n(JvpArgs ja) {
     }
     __syncwarp();
     float* out = ja.u + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
-    for (int e = lane; e < NP * (L + 1); e += 32) {
-        const int p = e / (L + 1), l = e - p * (L + 1);
+    for (int e = lane; e < NP * a.nl2; e += 32) {
+        const int p = e / a.nl2, l = e - p * a.nl2;
         float s = 0.f;
         for (int m = 0; m <= 2 * l; ++m) s += sP[p * S::K + l * l + m];
-        out[e] = -2.f * kPi4 / (float)(2 * l + 1) * s;
+        out[p * a.sl + l] = -2.f * kPi4 / (float)(2 * l + 1) * s;
     }
 }
 
@@ -890,17 +890,24 @@ __global__ void __launch_bounds__(32 * kWgWarps) k_wgrad(WgradArgs g) {
         if (SPH) {
             const float* Ain = a.A + (size_t)(slot - s0) * NP * S::K;
             const float* dAin = g.dA + (size_t)(slot - s0) * NP * S::K;
+            const float* M1x = g.M1x ? g.M1x + (size_t)(slot - s0) * NP * S::K : nullptr;
+            const float* M2x = g.M2x ? g.M2x + (size_t)(slot - s0) * NP * S::K : nullptr;
             for (int lm = lane; lm < S::K; lm += 32) {
                 int l = 0;
                 while ((l + 1) * (l + 1) <= lm) ++l;
-                const float k2 = 2.f * kPi4 / (float)(2 * l + 1);
+                const float k2 = l < a.nl2 ? 2.f * kPi4 / (float)(2 * l + 1) : 0.f;
+                const int lc = l < a.nl2 ? l : 0;
                 for (int p = 0; p < S::NPS; ++p) {
                     float m1 = 0.f, m2 = 0.f;
                     if (p < NP) {
                         const float av = Ain[p * S::K + lm], dav = dAin[p * S::K + lm];
-                        const float gv = gf[p * (L + 1) + l], dv = df[p * (L + 1) + l];
+                        const float gv = gf[p * a.sl + lc], dv = df[p * a.sl + lc];
                         m1 = k2 * (dv * av - gv * dav);
                         m2 = -k2 * gv * av;
+                        if (M1x) {  // the invariant columns' part
+                            m1 += M1x[p * S::K + lm];
+                            m2 += M2x[p * S::K + lm];
+                        }
                     }
                     sM1[lm * S::NPS + p] = m1;
                     sM2[lm * S::NPS + p] = m2;

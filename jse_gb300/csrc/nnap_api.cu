@@ -506,6 +506,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.sl = s.nl2 + s.ninv;
                 // invariant columns: forward after the expansion, their dE/dA before the backward
                 InvArgs ia;
+                std::memset(&ia, 0, sizeof ia);
                 if (s.ninv && n > 0) {
                     ia.perm = h->perm.p;
                     ia.range = h->type_start.p;
@@ -900,7 +901,8 @@ int nnap_destroy(nnap_handle* h) {
         for (auto& b : r.inv_start) b.release();
     }
     for (auto& nd : h->nets) { nd.w32.release(); net_tc_release(nd.tc); }
-    for (auto* b : {&h->tu, &h->trec, &h->tpart, &h->tbW, &h->tdA, &h->tgfp, &h->tdfp, &h->twpart}) b->release();
+    for (auto* b : {&h->tu, &h->trec, &h->tpart, &h->tbW, &h->tdA, &h->tgfp, &h->tdfp, &h->twpart, &h->tM1x, &h->tM2x})
+        b->release();
     for (auto* b : {&h->tbFd, &h->tbE, &h->tgrad, &h->twgrad}) b->release();
     h->tbF.release();
     h->ttiles.release();

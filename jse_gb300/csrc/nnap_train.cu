@@ -51,6 +51,31 @@ std::vector<GradTile> grad_tiles(const Species& sp) {
     return t;
 }
 
+// Invariant-column arguments of sub-basis k of run r (A: that sub's expansion arena).
+InvArgs inv_args(nnap_handle* h, const Run& r, size_t k, int n, const float* A, const SubShape& s) {
+    InvArgs ia;
+    std::memset(&ia, 0, sizeof ia);
+    ia.perm = h->perm.p;
+    ia.range = h->type_start.p;
+    ia.t0 = r.t0;
+    ia.t1 = r.t1;
+    ia.nmax = n;
+    ia.A = A;
+    ia.NP = s.np;
+    ia.K = (s.lmax + 1) * (s.lmax + 1);
+    ia.idx = r.inv_idx[k].p;
+    ia.coef = r.inv_coef[k].p;
+    ia.start = r.inv_start[k].p;
+    ia.ncol = s.ninv;
+    ia.fp = h->fp.p;
+    ia.gfp = h->gfp.p;
+    ia.fp_stride = h->fp_stride;
+    ia.fp_off = r.fp_off[k];
+    ia.nl2 = s.nl2;
+    ia.sl = s.nl2 + s.ninv;
+    return ia;
+}
+
 bool any_fused(const Model& m) {
     for (auto& sp : m.sp)
         for (auto& b : sp.subs)
@@ -110,6 +135,20 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
         dbE = h->tbE.p;
     }
     if (n) CK(cudaMemsetAsync(h->tu.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
+    bool inv = false;
+    for (auto& r : h->runs)
+        for (auto& sh : r.subs) inv = inv || sh.ninv > 0;
+    const bool want_dA = want_w || inv;  // D_b A: the fuse gradients and the invariant columns
+    if (want_dA) {
+        const size_t an = std::max<size_t>(a_arena_size(h, n), 1);
+        h->tdA.ensure(an);
+        CK(cudaMemsetAsync(h->tdA.p, 0, sizeof(float) * an, st));
+    }
+    if (want_w && inv) {
+        const size_t an = std::max<size_t>(a_arena_size(h, n), 1);
+        h->tM1x.ensure(an);
+        h->tM2x.ensure(an);
+    }
     if (want_w) {
         const size_t an = std::max<size_t>(a_arena_size(h, n), 1);
         h->tdA.ensure(an);
@@ -157,10 +196,17 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             ja.bW = dbW;
             ja.sid = h->sid.p;
             ja.u = h->tu.p;
-            ja.dA = (want_w && s.kind == KIND_SPHERICAL) ? h->tdA.p + (a.A - h->A.p) : nullptr;
+            ja.dA = (want_dA && s.kind == KIND_SPHERICAL) ? h->tdA.p + (a.A - h->A.p) : nullptr;
             if (n > 0 && (dbF || dbW)) {
                 CK(launch_jvp(s.kind, s.lmax, s.np, s.n1, ja, st));
                 ++h->launches;
+                if (s.ninv) {  // the invariant columns' directional derivatives
+                    InvArgs ia = inv_args(h, r, k, n, a.A, s);
+                    ia.dA = ja.dA;
+                    ia.u = h->tu.p;
+                    CK(launch_invariants_jvp(ia, st));
+                    ++h->launches;
+                }
             }
         }
     }
@@ -277,6 +323,20 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
                 g.dfp = h->tdfp.p;
                 g.partial = h->twpart.p;
                 g.G = G;
+                g.M1x = nullptr;
+                g.M2x = nullptr;
+                if (sh.ninv && n > 0) {  // the invariant columns' parts of M1 and M2
+                    InvArgs ia = inv_args(h, r, k, n, a.A, sh);
+                    ia.dA = g.dA;
+                    ia.gfp = h->tgfp.p;
+                    ia.dfp = h->tdfp.p;
+                    ia.M1x = h->tM1x.p + (a.A - h->A.p);
+                    ia.M2x = h->tM2x.p + (a.A - h->A.p);
+                    CK(launch_invariants_wgrad(ia, st));
+                    ++h->launches;
+                    g.M1x = ia.M1x;
+                    g.M2x = ia.M2x;
+                }
                 CK(cudaMemsetAsync(h->twpart.p, 0, sizeof(float) * (size_t)G * per, st));
                 if (n > 0) {
                     CK(launch_wgrad(sh.kind, sh.lmax, sh.np, sh.n1, g, st));
@@ -355,11 +415,6 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         const Model& m = h->model;
         const int T = m.ntypes();
         const bool want_w = grad_fp && any_fused(m);
-        for (auto& sp : m.sp)
-            for (auto& b : sp.subs)
-                if (!b.inv.empty())
-                    throw ApiFail(NNAP_ERR_UNSUPPORTED,
-                                  "training gradients of the l3max / l4max invariant columns are not implemented");
         h->launches = 0;
         Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");

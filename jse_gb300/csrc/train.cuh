@@ -58,6 +58,10 @@ struct WgradArgs {
     const float* dfp;
     float* partial;         // [G][t1 - t0][T][NP][N1], zeroed before the launch
     int G;                  // warps of the launch
+    // spherical with invariant columns, or NULL: their part of M1 (dL/dA at fixed D_b A)
+    // and M2 (dL/dD_b A), laid out like A
+    const float* M1x;
+    const float* M2x;
 };
 
 // One tile of a species' parameter gradient: a 64 x 64 block (o0, i0) of layer `layer`'s

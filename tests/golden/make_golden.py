@@ -151,6 +151,9 @@ def cases():
     out["sph_bispectrum"] = (_model(["A", "B"], _sph(3, 3, 5.0, "full", l3max=3, l4max=2), [8, 8], 45), s2)
     s1 = W.random_liquid(100, 0.06, [1.0], 2.0, 29)
     out["sph_bispectrum_high"] = (_model(["A"], _sph(4, 2, 5.0, "default", l3max=4, l4max=3), [8, 8], 46), s1)
+    fw2 = rng.uniform(-1, 1, 2 * 2).tolist()
+    out["sph_bispectrum_fuse"] = (_model(["A", "B"], _sph(3, 3, 5.0, "fuse", fuse_size=2, fuse_weight=fw2, l3max=3,
+                                                          l4max=2), [8, 8], 47), s2)
     return out
 
 

@@ -36,17 +36,10 @@ def _rel(a, b):
 
 
 def test_golden_gradients(golden):
-    from jse_gb300.nnap import NNAPError, NNAP_ERR_UNSUPPORTED
     pm = OM.load(golden.model)
     fused = any(sb.internal_wtype in (OM.WTYPE_FUSE, OM.WTYPE_RFUSE, OM.WTYPE_EXFUSE)
                 for b in pm.basis for sb in b.subs)
     s = W.Structure(golden.x, golden.types, golden.box, golden.box_kind)
-    if any(sb.l3max or sb.l4max for b in pm.basis for sb in b.subs):
-        # training through the three- and four-body invariant columns is not built
-        with _nnap(golden.model_json) as p, pytest.raises(NNAPError) as e:
-            p.backwardEnergyForceBatch([s], golden.train_be, golden.train_bf)
-        assert e.value.status == NNAP_ERR_UNSUPPORTED
-        return
     with _nnap(golden.model_json) as p:
         out = p.backwardEnergyForceBatch([s], golden.train_be, golden.train_bf, golden.train_bw[None, :],
                                          want_fp=False)
