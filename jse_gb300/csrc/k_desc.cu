@@ -23,6 +23,7 @@
 #include <math_constants.h>
 
 #include "common.cuh"
+#include "pdl.cuh"
 #include "desc.cuh"
 #include "sph_math.cuh"
 
@@ -41,6 +42,7 @@ __device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { re
 // =========================================================================== radial
 template <int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
+    pdl_enter();
     extern __shared__ float sW[];
     load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
@@ -78,6 +80,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
 
 template <int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_bwd(DescArgs a) {
+    pdl_enter();
     extern __shared__ float sW[];
     load_fuse<NP, N1>(a.W, sW, a.T);
     __syncthreads();
@@ -139,6 +142,7 @@ struct SphShape {
 
 template <int L, int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
+    pdl_enter();
     using S = SphShape<L, NP>;
     extern __shared__ float smem[];
     const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
@@ -260,6 +264,7 @@ struct SphFNShape {
 
 template <int L, int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd_n(DescArgs a) {
+    pdl_enter();
     using S = SphFNShape<L, NP, N1>;
     extern __shared__ float smem[];
     const int T = a.T;
@@ -385,6 +390,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd_n(DescArgs a) {
 // below 128 per thread (four CTAs of four warps per SM).
 template <int L, int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
+    pdl_enter();
     using S = SphShape<L, NP>;
     extern __shared__ float smem[];
     const int nW = a.T * a.T * NP * Fuse<N1>::N1P;
@@ -557,6 +563,7 @@ struct SphNShape {
 
 template <int L, int NP, int N1>
 __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a) {
+    pdl_enter();
     using S = SphNShape<L, NP, N1>;
     extern __shared__ float smem[];
     const int T = a.T;
@@ -737,6 +744,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
 // product, one factor at a time (calGradSphL3 / L4).  One lane owns one channel, so each
 // sum runs in term order and the results do not depend on scheduling.
 __global__ void __launch_bounds__(128) k_inv_fwd(InvArgs a) {
+    pdl_enter();
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
@@ -757,6 +765,7 @@ __global__ void __launch_bounds__(128) k_inv_fwd(InvArgs a) {
 }
 
 __global__ void __launch_bounds__(128) k_inv_bwd(InvArgs a) {
+    pdl_enter();
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
@@ -881,9 +890,8 @@ cudaError_t launch_invariants_wgrad(const InvArgs& a, cudaStream_t st) {
 cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st) {
     if (a.nmax <= 0 || a.ncol <= 0) return cudaSuccess;
     const int grid = (a.nmax + 3) / 4;
-    if (fwd) k_inv_fwd<<<grid, 128, 0, st>>>(a);
-    else k_inv_bwd<<<grid, 128, 0, st>>>(a);
-    return cudaGetLastError();
+    if (fwd) return launch_pdl(&k_inv_fwd, dim3(grid), dim3(128), 0, st, a);
+    return launch_pdl(&k_inv_bwd, dim3(grid), dim3(128), 0, st, a);
 }
 
 // =========================================================================== dispatch
@@ -905,9 +913,8 @@ cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    if (fwd) k_radial_fwd<NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
-    else k_radial_bwd<NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
-    return cudaGetLastError();
+    if (fwd) return launch_pdl(&k_radial_fwd<NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
+    return launch_pdl(&k_radial_bwd<NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
 template <int L, int NP, int N1>
@@ -925,8 +932,7 @@ cudaError_t launch_sph_bwd_n(const DescArgs& a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    k_sph_bwd_n<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(&k_sph_bwd_n<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
 template <int L, int NP, int N1>
@@ -943,8 +949,7 @@ cudaError_t launch_sph_fwd_n(const DescArgs& a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    k_sph_fwd_n<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(&k_sph_fwd_n<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
 template <int L, int NP, int N1>
@@ -969,9 +974,8 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    if (fwd) k_sph_fwd<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
-    else k_sph_bwd<L, NP, N1><<<grid, 32 * wpc, sm, st>>>(a);
-    return cudaGetLastError();
+    if (fwd) return launch_pdl(&k_sph_fwd<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
+    return launch_pdl(&k_sph_bwd<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
 }  // namespace

@@ -12,6 +12,7 @@
 // Packed FP32 parameters of a species (net_pack in nnap_api.cu):
 //   mu[D] | 1/sigma[D] | for each layer: W^T[in][H] | W[H][in] | b[H] | w_out[H_L] | b_out
 #include "desc.cuh"
+#include "pdl.cuh"
 
 namespace nnapgb {
 namespace {
@@ -26,6 +27,7 @@ __device__ __forceinline__ float silu_and_grad(float z, float* grad) {
 }
 
 __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp_floats) {
+    pdl_enter();
     extern __shared__ float smem[];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s0 = a.range[a.t], s1 = a.range[a.t + 1];
@@ -154,8 +156,7 @@ cudaError_t launch_net_fp32(const NetArgs& a, cudaStream_t st) {
         limit = (int)sm;
     }
     const int per_block = kNetAtoms * kNetWarps;
-    k_net_fp32<<<(n + per_block - 1) / per_block, 32 * kNetWarps, sm, st>>>(a, warp_floats);
-    return cudaGetLastError();
+    return launch_pdl(&k_net_fp32, dim3((n + per_block - 1) / per_block), dim3(32 * kNetWarps), sm, st, a, warp_floats);
 }
 
 }  // namespace nnapgb

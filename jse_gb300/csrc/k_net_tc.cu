@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "net_tc.cuh"
+#include "pdl.cuh"
 #include "tc_util.cuh"
 
 namespace nnapgb {
@@ -133,6 +134,7 @@ struct TcParams {
 
 template <int SPLIT>
 __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout L) {
+    pdl_enter();
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
@@ -428,9 +430,8 @@ cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int*
     p.err = err;
     const int ntiles = (n + 127) / 128 + nt;  // upper bound of the tiles over all species
     const int grid = ntiles < sm_count ? ntiles : sm_count;
-    if (split == 2) k_net_tc<2><<<grid, 256, sm, st>>>(p, L);
-    else k_net_tc<4><<<grid, 512, sm, st>>>(p, L);
-    return cudaGetLastError();
+    if (split == 2) return launch_pdl(&k_net_tc<2>, dim3(grid), dim3(256), sm, st, p, L);
+    return launch_pdl(&k_net_tc<4>, dim3(grid), dim3(512), sm, st, p, L);
 }
 
 }  // namespace nnapgb

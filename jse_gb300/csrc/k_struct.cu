@@ -18,6 +18,7 @@
 //                   gather over each atom's own row and the mirrored entries, without atomics.
 #include "box_math.cuh"
 #include "common.cuh"
+#include "pdl.cuh"
 
 namespace nnapgb {
 
@@ -28,6 +29,7 @@ __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restric
                            const int* __restrict__ type, int n, int ntypes, double* __restrict__ xw,
                            float4* __restrict__ xf, float4* __restrict__ xlo, int* __restrict__ cell_of,
                            int* __restrict__ cell_count, int* __restrict__ err) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const StructDev& st = S[sid[i]];
@@ -59,6 +61,7 @@ __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restric
 
 // Exclusive scan of n ints (one CTA of 1024 threads, sequential chunks); out has n+1 entries.
 __global__ void k_scan_excl(const int* __restrict__ in, int n, int* __restrict__ out) {
+    pdl_enter();
     __shared__ int warp_tot[32];
     __shared__ int carry;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -96,6 +99,7 @@ __global__ void k_scan_excl(const int* __restrict__ in, int n, int* __restrict__
 
 __global__ void k_fill_cells(const int* __restrict__ cell_of, int n, const int* __restrict__ cell_start,
                              int* __restrict__ cell_fill, int* __restrict__ cell_atoms) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int c = cell_of[i];
@@ -105,6 +109,7 @@ __global__ void k_fill_cells(const int* __restrict__ cell_of, int n, const int* 
 // Order each cell's atoms by index so that every neighbour row is deterministic.
 // One warp per cell: up to 32 atoms are placed by rank; larger cells are sorted by lane 0.
 __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int* __restrict__ cell_atoms) {
+    pdl_enter();
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (c >= ncells) return;
@@ -140,6 +145,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             const float4* __restrict__ xf, const float4* __restrict__ xlo, const int* __restrict__ cell_of,
             const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, int n, PairBufs P,
             int* __restrict__ err, int* __restrict__ max_count) {
+    pdl_enter();
     __shared__ int s_incl[kNbMaxWarps][32], s_start[kNbMaxWarps][32];
     __shared__ uint32_t s_img[kNbMaxWarps][32];
     __shared__ double s_sh[kNbMaxWarps][32][3];
@@ -320,6 +326,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
 // One warp per row.
 __global__ void k_mirror(const StructDev* __restrict__ S, const int* __restrict__ sid, PairBufs P, int n,
                          int* __restrict__ err) {
+    pdl_enter();
     const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
@@ -371,6 +378,7 @@ __global__ void k_mirror(const StructDev* __restrict__ S, const int* __restrict_
 constexpr int kSortBlock = 256;
 
 __global__ void k_type_hist(const int* __restrict__ type, int n, int T, int* __restrict__ block_counts) {
+    pdl_enter();
     __shared__ int h[kMaxTypes];
     if (threadIdx.x < kMaxTypes) h[threadIdx.x] = 0;
     __syncthreads();
@@ -385,6 +393,7 @@ __global__ void k_type_hist(const int* __restrict__ type, int n, int T, int* __r
 
 // In place: block_counts -> exclusive offsets in (type, block) order; type_start[T+1].
 __global__ void k_type_offsets(int* __restrict__ block_counts, int nb, int T, int* __restrict__ type_start) {
+    pdl_enter();
     __shared__ int warp_tot[32];
     __shared__ int carry;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -427,6 +436,7 @@ __global__ void k_type_offsets(int* __restrict__ block_counts, int nb, int T, in
 // Stable scatter: slot = offset(type, block) + rank of the atom among same-type atoms of its block.
 __global__ void k_type_scatter(const int* __restrict__ type, int n, int T, const int* __restrict__ block_offsets,
                                int* __restrict__ perm) {
+    pdl_enter();
     __shared__ int wc[kSortBlock / 32][kMaxTypes];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * kSortBlock + threadIdx.x;
@@ -463,6 +473,7 @@ __device__ __forceinline__ void ff_merge(float& h, float& l, unsigned mask, int 
 }
 
 __global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double* __restrict__ virials) {
+    pdl_enter();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int a = t / kGatherLanes, sub = t & (kGatherLanes - 1);
     if (a >= n) return;  // all eight lanes of an atom leave together
@@ -514,6 +525,7 @@ constexpr int kRedBlock = 256;
 __global__ void k_reduce_chunks(const int* __restrict__ cb, const int* __restrict__ ce,
                                 const double* __restrict__ e_atom, const double* __restrict__ virials,
                                 double* __restrict__ partial) {
+    pdl_enter();
     __shared__ double sm[10][kRedBlock / 32];
     const int c = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -541,6 +553,7 @@ __global__ void k_reduce_chunks(const int* __restrict__ cb, const int* __restric
 // structure s owns chunks [sc[s], sc[s+1]); one warp per structure, fixed summation order.
 __global__ void k_reduce_structs(const int* __restrict__ sc, int nstruct, const double* __restrict__ partial,
                                  double* __restrict__ energy, double* __restrict__ virial) {
+    pdl_enter();
     const int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (s >= nstruct) return;

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "api_internal.hpp"
+#include "pdl.cuh"
 
 using namespace nnapgb;
 
@@ -427,19 +428,19 @@ void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const 
     CK(cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * B.ncells, st));
     CK(cudaMemsetAsync(h->cell_fill.p, 0, sizeof(int) * B.ncells, st));
     if (n > 0) {
-        k_wrap_bin<<<(n + 255) / 256, 256, 0, st>>>(h->sdev.p, h->sid.p, d_x, d_type, n, T, h->xw.p, h->xf.p,
-                                                    h->xlo.p, h->cell_of.p, h->cell_count.p, h->status.p);
+        CK(launch_pdl(k_wrap_bin, dim3((n + 255) / 256), dim3(256), 0, st, h->sdev.p, h->sid.p, d_x, d_type, n, T, h->xw.p, h->xf.p,
+                                                    h->xlo.p, h->cell_of.p, h->cell_count.p, h->status.p));
         ++h->launches;
     }
-    k_scan_excl<<<1, 1024, 0, st>>>(h->cell_count.p, B.ncells, h->cell_start.p);
+    CK(launch_pdl(k_scan_excl, dim3(1), dim3(1024), 0, st, h->cell_count.p, B.ncells, h->cell_start.p));
     ++h->launches;
     if (n > 0) {
-        k_fill_cells<<<(n + 255) / 256, 256, 0, st>>>(h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p);
-        k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
+        CK(launch_pdl(k_fill_cells, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p));
+        CK(launch_pdl(k_sort_cells, dim3((B.ncells * 32 + 255) / 256), dim3(256), 0, st, h->cell_start.p, B.ncells, h->cell_atoms.p));
         const int nw = h->tune.nb_warps;
-        k_neighbors<<<(n + nw - 1) / nw, 32 * nw, 0, st>>>(
+        CK(launch_pdl(k_neighbors, dim3((n + nw - 1) / nw), dim3(32 * nw), 0, st, 
             h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
-            pair_bufs(h), h->status.p, h->status.p + 1);
+            pair_bufs(h), h->status.p, h->status.p + 1));
         h->launches += 3;
     }
 }
@@ -449,9 +450,9 @@ void enqueue_species(nnap_handle* h, int n, const int* d_type) {
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
     const int nb = (n + kSortBlock - 1) / kSortBlock;
-    k_type_hist<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p);
-    k_type_offsets<<<1, 1024, 0, st>>>(h->block_counts.p, nb, T, h->type_start.p);
-    k_type_scatter<<<nb, kSortBlock, 0, st>>>(d_type, n, T, h->block_counts.p, h->perm.p);
+    CK(launch_pdl(k_type_hist, dim3(nb), dim3(kSortBlock), 0, st, d_type, n, T, h->block_counts.p));
+    CK(launch_pdl(k_type_offsets, dim3(1), dim3(1024), 0, st, h->block_counts.p, nb, T, h->type_start.p));
+    CK(launch_pdl(k_type_scatter, dim3(nb), dim3(kSortBlock), 0, st, d_type, n, T, h->block_counts.p, h->perm.p));
     h->launches += 3;
 }
 
@@ -459,8 +460,8 @@ void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
     const int n = B.natoms;
     if (n <= 0) return;
     enqueue_species(h, n, d_type);
-    k_mirror<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, h->stream>>>(
-        h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p);
+    CK(launch_pdl(k_mirror, dim3((unsigned)(((size_t)n * 32 + 255) / 256)), dim3(256), 0, h->stream, 
+        h->sdev.p, h->sid.p, pair_bufs(h), n, h->status.p));
     ++h->launches;
 }
 
@@ -590,18 +591,18 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     if (!fp_only && gather) {
         if (n > 0) {
             const int gb = h->tune.gather_block;  // threads per CTA, eight per atom
-            k_gather<<<(unsigned)(((size_t)n * 8 + gb - 1) / gb), gb, 0, st>>>(pair_bufs(h), n, h->forces.p,
-                                                                               h->virials.p);
+            CK(launch_pdl(k_gather, dim3((unsigned)(((size_t)n * 8 + gb - 1) / gb)), dim3(gb), 0, st, pair_bufs(h), n, h->forces.p,
+                                                                               h->virials.p));
             ++h->launches;
         }
         const int nchunks = (int)B.cb.size();
         if (nchunks) {
-            k_reduce_chunks<<<nchunks, kRedBlock, 0, st>>>(h->chunk_b.p, h->chunk_e.p, h->e_atom.p, h->virials.p,
-                                                            h->partial.p);
+            CK(launch_pdl(k_reduce_chunks, dim3(nchunks), dim3(kRedBlock), 0, st, h->chunk_b.p, h->chunk_e.p, h->e_atom.p, h->virials.p,
+                                                            h->partial.p));
             ++h->launches;
         }
-        k_reduce_structs<<<(B.nstruct * 32 + 127) / 128, 128, 0, st>>>(h->struct_chunks.p, B.nstruct, h->partial.p,
-                                                                        h->energy.p, h->virial.p);
+        CK(launch_pdl(k_reduce_structs, dim3((B.nstruct * 32 + 127) / 128), dim3(128), 0, st, h->struct_chunks.p, B.nstruct, h->partial.p,
+                                                                        h->energy.p, h->virial.p));
         ++h->launches;
     }
     h->mark(5);
