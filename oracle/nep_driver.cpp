@@ -1,0 +1,61 @@
+// Driver around the reference's own per-atom NEP arithmetic.
+//
+// TEST INFRASTRUCTURE ONLY.  Compiled by oracle/nep_ref.py together with the reference's
+// nep_interface.cpp after oracle/nepgen.py has expanded it for one model into
+// oracle/_ref/<shape>/src (build output, never committed).  It restates the per-atom loop
+// of NEP.calEnergyForceVirial (NEP.java:160-212): jse_nep_calEnergyForce
+// (nep_interface.cpp:106-188) per atom over the caller's neighbour list, pair terms
+// scattered as F_i -= f_ij, F_j += f_ij and the per-atom virial dx (x) f_ij assigned to
+// the neighbour (the accumulators of IPairPotential.java:919-1006).  Species are 0-based
+// here, as the reference's arithmetic expects.
+#include <cstring>
+#include <vector>
+
+extern "C" int jse_nep_calEnergyForce(const double* nl_dx, const double* nl_dy, const double* nl_dz,
+                                      const int* nl_type, int num_neigh, int ctype, const int* atomic_numbers,
+                                      const double* q_scaler, const double** ann_w0, const double** ann_b0,
+                                      const double** ann_w1, const double* ann_b1, const double* ann_c,
+                                      const double* zbl_para, const double* gn_radial, const double* gn_angular,
+                                      const double* gnp_radial, const double* gnp_angular, double* eng, double* nl_fx,
+                                      double* nl_fy, double* nl_fz, double* fp, double* sum_fxyz);
+
+extern "C" int nep_ref_compute(int T, const int* atomic_numbers, const double* q_scaler, const double** w0,
+                               const double** b0, const double** w1, const double* b1, const double* c, int dim,
+                               int sum_size, int n, const int* type, const long* nei_off, const int* nei_j,
+                               const double* nei_dx, double* e_atom, double* force, double* virial) {
+    (void)T;
+    std::vector<double> dx, dy, dz, fx, fy, fz, fp(dim + 8), sf(sum_size + 8);
+    std::vector<int> ty;
+    std::memset(e_atom, 0, sizeof(double) * n);
+    std::memset(force, 0, sizeof(double) * 3 * n);
+    std::memset(virial, 0, sizeof(double) * 9 * n);
+    for (int i = 0; i < n; ++i) {
+        const long o = nei_off[i];
+        const int nn = (int)(nei_off[i + 1] - o);
+        dx.resize(nn + 1); dy.resize(nn + 1); dz.resize(nn + 1);
+        fx.resize(nn + 1); fy.resize(nn + 1); fz.resize(nn + 1); ty.resize(nn + 1);
+        for (int j = 0; j < nn; ++j) {
+            dx[j] = nei_dx[3 * (o + j)];
+            dy[j] = nei_dx[3 * (o + j) + 1];
+            dz[j] = nei_dx[3 * (o + j) + 2];
+            ty[j] = type[nei_j[o + j]];
+        }
+        double e = 0.0;
+        const int code = jse_nep_calEnergyForce(dx.data(), dy.data(), dz.data(), ty.data(), nn, type[i],
+                                                atomic_numbers, q_scaler, w0, b0, w1, b1, c, nullptr, nullptr,
+                                                nullptr, nullptr, nullptr, &e, fx.data(), fy.data(), fz.data(),
+                                                fp.data(), sf.data());
+        if (code) return code;
+        e_atom[i] += e;
+        for (int j = 0; j < nn; ++j) {
+            const int jj = nei_j[o + j];
+            force[3 * i] -= fx[j]; force[3 * i + 1] -= fy[j]; force[3 * i + 2] -= fz[j];
+            force[3 * jj] += fx[j]; force[3 * jj + 1] += fy[j]; force[3 * jj + 2] += fz[j];
+            double* v = virial + 9 * (size_t)jj;
+            v[0] += dx[j] * fx[j]; v[1] += dy[j] * fy[j]; v[2] += dz[j] * fz[j];
+            v[3] += dx[j] * fy[j]; v[4] += dx[j] * fz[j]; v[5] += dy[j] * fz[j];
+            v[6] += dy[j] * fx[j]; v[7] += dz[j] * fx[j]; v[8] += dz[j] * fy[j];
+        }
+    }
+    return 0;
+}

@@ -1,0 +1,143 @@
+"""NEP model files (nep.txt) for the oracle.
+
+TEST INFRASTRUCTURE ONLY.  Restates the subset of NEP.java's loader (NEP.java:786-1010)
+and of its parameter split (update_potential, NEP.java:1097-1140) that the GPU path
+supports: potential models of versions 3, 4 and 5 (``nep3``, ``nep4``, ``nep5``) without
+ZBL and without type-wise cutoffs.  Other variants raise ValueError.
+
+The file is whitespace-separated text:
+    nepV T sym_1 .. sym_T
+    cutoff rc_radial rc_angular MN_radial MN_angular
+    n_max n_max_radial n_max_angular
+    basis_size basis_size_radial basis_size_angular
+    l_max l_max_3body l_max_4body l_max_5body
+    ANN num_neurons 0
+followed by one number per line: the network parameters, the descriptor coefficients
+c and the dim descriptor scales q_scaler.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+
+
+@dataclass
+class NEPModel:
+    version: int
+    symbols: List[str]
+    rc_radial: float
+    rc_angular: float
+    n_max_radial: int
+    n_max_angular: int
+    basis_size_radial: int
+    basis_size_angular: int
+    l_max: int
+    l_max_4body: int
+    l_max_5body: int
+    num_neurons: int
+    params: np.ndarray = field(repr=False)     # network then descriptor parameters
+    q_scaler: np.ndarray = field(repr=False)
+
+    @property
+    def ntypes(self) -> int:
+        return len(self.symbols)
+
+    @property
+    def num_L(self) -> int:
+        return self.l_max + (1 if self.l_max_4body == 2 else 0) + (1 if self.l_max_5body == 1 else 0)
+
+    @property
+    def dim_angular(self) -> int:
+        return (self.n_max_angular + 1) * self.num_L
+
+    @property
+    def dim(self) -> int:
+        return (self.n_max_radial + 1) + self.dim_angular
+
+    @property
+    def num_para_ann(self) -> int:
+        T, d, h = self.ntypes, self.dim, self.num_neurons
+        if self.version == 3:
+            return (d + 2) * h + 1
+        if self.version == 4:
+            return (d + 2) * h * T + 1
+        return ((d + 2) * h + 1) * T + 1
+
+    @property
+    def num_c_radial(self) -> int:
+        return self.ntypes ** 2 * (self.n_max_radial + 1) * (self.basis_size_radial + 1)
+
+    @property
+    def num_para_descriptor(self) -> int:
+        return self.ntypes ** 2 * ((self.n_max_radial + 1) * (self.basis_size_radial + 1) +
+                                   (self.n_max_angular + 1) * (self.basis_size_angular + 1))
+
+    def ann(self, t: int):
+        """(w0 [h][dim], b0 [h], w1 [h], extra output bias) of species t (0-based)."""
+        d, h = self.dim, self.num_neurons
+        per = (d + 2) * h + (1 if self.version == 5 else 0)
+        off = 0 if self.version == 3 else t * per
+        p = self.params
+        w0 = p[off:off + h * d].reshape(h, d)
+        b0 = p[off + h * d:off + h * d + h]
+        w1 = p[off + h * d + h:off + h * d + 2 * h]
+        extra = float(p[off + h * d + 2 * h]) if self.version == 5 else 0.0
+        return w0, b0, w1, extra
+
+    @property
+    def b1(self) -> float:
+        return float(self.params[self.num_para_ann - 1])
+
+    @property
+    def c(self) -> np.ndarray:
+        return self.params[self.num_para_ann:self.num_para_ann + self.num_para_descriptor]
+
+
+def load(text: str) -> NEPModel:
+    lines = [ln.split() for ln in text.splitlines() if ln.split()]
+    head = lines[0]
+    versions = {"nep3": 3, "nep4": 4, "nep5": 5}
+    if head[0] not in versions:
+        raise ValueError("unsupported NEP variant %r (potential models nep3/nep4/nep5 without ZBL only)" % head[0])
+    T = int(head[1])
+    if len(head) != 2 + T:
+        raise ValueError("the first line must list %d symbols" % T)
+    cut = lines[1]
+    if cut[0] != "cutoff" or len(cut) not in (5, 8):
+        raise ValueError("expected: cutoff rc_radial rc_angular MN_radial MN_angular [factors]")
+    if len(cut) == 8 and (float(cut[5]) > 0 or float(cut[7]) > 0):
+        raise ValueError("type-wise cutoffs are not supported")
+    nmax, bsize, lmax, ann = lines[2], lines[3], lines[4], lines[5]
+    if nmax[0] != "n_max" or bsize[0] != "basis_size" or lmax[0] != "l_max" or ann[0] != "ANN":
+        raise ValueError("unexpected header line order")
+    m = NEPModel(version=versions[head[0]], symbols=head[2:], rc_radial=float(cut[1]), rc_angular=float(cut[2]),
+                 n_max_radial=int(nmax[1]), n_max_angular=int(nmax[2]), basis_size_radial=int(bsize[1]),
+                 basis_size_angular=int(bsize[2]), l_max=int(lmax[1]), l_max_4body=int(lmax[2]),
+                 l_max_5body=int(lmax[3]), num_neurons=int(ann[1]), params=np.zeros(0), q_scaler=np.zeros(0))
+    vals = np.array([float(x[0]) for x in lines[6:]], dtype=np.float64)
+    npar = m.num_para_ann + m.num_para_descriptor
+    if len(vals) != npar + m.dim:
+        raise ValueError("expected %d numbers after the header, found %d" % (npar + m.dim, len(vals)))
+    m.params = vals[:npar]
+    m.q_scaler = vals[npar:]
+    return m
+
+
+def write(symbols, version=4, rc=(5.0, 4.0), n_max=(4, 4), basis=(8, 8), l_max=(4, 2, 1), neurons=16, seed=0) -> str:
+    """A random model file (seeded), for tests and benchmarks."""
+    rng = np.random.default_rng(seed)
+    T = len(symbols)
+    m = NEPModel(version=version, symbols=list(symbols), rc_radial=rc[0], rc_angular=rc[1], n_max_radial=n_max[0],
+                 n_max_angular=n_max[1], basis_size_radial=basis[0], basis_size_angular=basis[1], l_max=l_max[0],
+                 l_max_4body=l_max[1], l_max_5body=l_max[2], num_neurons=neurons, params=np.zeros(0),
+                 q_scaler=np.zeros(0))
+    ann = rng.normal(0.0, 1.0 / np.sqrt(m.dim), m.num_para_ann)
+    c = rng.uniform(-1.0, 1.0, m.num_para_descriptor)
+    qs = rng.uniform(0.5, 2.0, m.dim)
+    out = ["nep%d %d %s" % (version, T, " ".join(symbols)),
+           "cutoff %g %g 100 100" % rc, "n_max %d %d" % n_max, "basis_size %d %d" % basis,
+           "l_max %d %d %d" % l_max, "ANN %d 0" % neurons]
+    out += ["%.17g" % v for v in np.concatenate([ann, c, qs])]
+    return "\n".join(out) + "\n"

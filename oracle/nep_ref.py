@@ -1,0 +1,95 @@
+"""The reference's NEP arithmetic for one model, compiled here (oracle).
+
+TEST INFRASTRUCTURE ONLY.  The model's shape expands the reference's NEP sources
+(``src/nep/resources/assets/nep/src``, read from the reference checkout at build time;
+nothing is committed) with oracle/nepgen.py into oracle/_ref/nep_<key>/src, which is
+compiled with oracle/nep_driver.cpp (g++ -O2, no fast-math) into libnepref.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import json
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+from . import nepgen
+from .build import REF_OUT
+from .nep_model import NEPModel
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def nep_src_dir() -> str:
+    root = os.environ.get("JSE_REFERENCE", "/root/reference")
+    return os.path.join(root, "src", "nep", "resources", "assets", "nep", "src")
+
+
+def shape_key(m: NEPModel) -> str:
+    blob = json.dumps({k: str(v) for k, v in nepgen.gen_map(m).items()}, sort_keys=True)
+    return "nep" + hashlib.sha1(blob.encode()).hexdigest()[:12]
+
+
+def build(m: NEPModel) -> str:
+    key = shape_key(m)
+    d = os.path.join(REF_OUT, key)
+    src = os.path.join(d, "src")
+    if not os.path.exists(os.path.join(src, "nep_interface.cpp")):
+        sd = nep_src_dir()
+        if not os.path.isdir(sd):
+            raise FileNotFoundError("reference NEP sources are not available")
+        nepgen.expand(sd, src, m)
+    out = os.path.join(d, "libnepref.so")
+    drv = os.path.join(HERE, "nep_driver.cpp")
+    deps = [os.path.join(src, "nep_interface.cpp"), os.path.join(src, "nep_core.hpp"), drv]
+    if not os.path.exists(out) or any(os.path.getmtime(p) > os.path.getmtime(out) for p in deps):
+        cmd = ["g++", "-std=c++14", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-I", src,
+               os.path.join(src, "nep_interface.cpp"), drv, "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError("building the reference NEP failed:\n" + r.stderr[-3000:])
+    return out
+
+
+class RefNEP:
+    def __init__(self, m: NEPModel):
+        self.m = m
+        self.lib = C.CDLL(build(m))
+        T = m.ntypes
+        self._keep = []
+        dp = C.POINTER(C.c_double)
+
+        def arr(a):
+            a = np.ascontiguousarray(a, dtype=np.float64).copy()
+            self._keep.append(a)
+            return a.ctypes.data_as(dp)
+        self.w0 = (dp * T)()
+        self.b0 = (dp * T)()
+        self.w1 = (dp * T)()
+        for t in range(T):
+            w0, b0, w1, extra = m.ann(t)
+            self.w0[t] = arr(w0.reshape(-1))
+            self.b0[t] = arr(b0)
+            self.w1[t] = arr(np.concatenate([w1, [extra]]) if m.version == 5 else w1)
+        self.b1 = arr(np.array([m.b1]))
+        self.c = arr(m.c)
+        self.qs = arr(m.q_scaler)
+        self.an = np.zeros(T, dtype=np.int32)
+
+    def compute(self, types0, nl):
+        types0 = np.ascontiguousarray(types0, dtype=np.int32)
+        n = len(types0)
+        e, f, v = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 9))
+        dx = np.ascontiguousarray(nl.dx, dtype=np.float64)
+        ip, lp, dp = C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_double)
+        code = self.lib.nep_ref_compute(self.m.ntypes, self.an.ctypes.data_as(ip), self.qs, self.w0, self.b0,
+                                        self.w1, self.b1, self.c, self.m.dim, (self.m.n_max_angular + 1) * 80, n,
+                                        types0.ctypes.data_as(ip), nl.offsets.ctypes.data_as(lp),
+                                        nl.j.ctypes.data_as(ip), dx.ctypes.data_as(dp), e.ctypes.data_as(dp),
+                                        f.ctypes.data_as(dp), v.ctypes.data_as(dp))
+        if code:
+            raise RuntimeError("reference NEP returned %d" % code)
+        return {"energies": e, "energy": float(e.sum()), "forces": f, "virials": v, "virial": v.sum(axis=0)}
