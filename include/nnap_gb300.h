@@ -76,6 +76,17 @@ enum {
 int nnap_create(const char* model_json, size_t len, int precision, int device, nnap_handle** out);
 /* Same, reading the JSON text from a file (NNAP(String), NNAP.java:407-411). */
 int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out);
+/* Create a handle from NEP potential text (nep.txt, the file read by NEP(String),
+ * NEP.java:98-100 and 786-1010): potential models nep3, nep4 and nep5 without ZBL and
+ * without type-wise cutoffs; other variants return NNAP_ERR_UNSUPPORTED.  Species are
+ * 1-based like every other call (NEP's 0-based species + 1).  The handle serves every
+ * evaluation entry point (compute, batch, device, LAMMPS, server); NNAP_PREC_MIXED is
+ * accepted and evaluates exactly like NNAP_PREC_FP32 (the tanh network runs in FP32);
+ * nnap_train_grad_batch returns NNAP_ERR_UNSUPPORTED.  Replaces the NEP constructor +
+ * JIT compile and NEP.calEnergyForceVirial (NEP.java:171-212). */
+int nnap_create_nep(const char* nep_txt, size_t len, int precision, int device, nnap_handle** out);
+/* Same, reading the nep.txt text from a file. */
+int nnap_create_nep_from_file(const char* path, int precision, int device, nnap_handle** out);
 /* Release the handle and its device memory (NNAP.close, NNAP.java:472-486). */
 int nnap_destroy(nnap_handle* h);
 

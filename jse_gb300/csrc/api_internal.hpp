@@ -91,9 +91,10 @@ struct SubShape {
     int kind, lmax, np, n1;
     double rcut;
     int nl2, l3, l4, ninv;  // power-spectrum columns, l3max, l4max, invariant columns
+    int basis;              // radial functions: kRbNNAP or kRbNEP
     bool operator==(const SubShape& o) const {
         return kind == o.kind && lmax == o.lmax && np == o.np && n1 == o.n1 && rcut == o.rcut && nl2 == o.nl2 &&
-               l3 == o.l3 && l4 == o.l4;
+               l3 == o.l3 && l4 == o.l4 && basis == o.basis;
     }
 };
 
@@ -123,6 +124,7 @@ struct NetDev {
     DevBuf<float> w32;
     double mu_e, sigma_e;
     NetTC tc;  // tensor-core parameters (mixed precision)
+    int act;   // kActSiLU or kActTanh
 };
 
 // One planned evaluation: the structures and the reduction chunks (chunk c covers atoms
@@ -142,6 +144,7 @@ struct Outputs {
 struct nnap_handle {
     nnapgb::Model model;
     int precision = NNAP_PREC_FP32;
+    bool net_tc = false;  // networks on the tensor cores (mixed precision, SiLU networks)
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;

@@ -77,9 +77,22 @@ constexpr int kFwdTypes = 3;  // most species for the radial-space forward (per-
     X(6, 18, 9) X(4, 18, 9) X(4, 5, 5) X(2, 4, 4) X(2, 8, 4) X(2, 12, 4) X(3, 5, 4) X(2, 16, 4) \
     X(3, 10, 5) X(6, 9, 9) X(4, 9, 9) X(3, 8, 4) X(4, 10, 5)
 
+// Radial functions of a sub-basis: the NNAP Chebyshev basis or the NEP basis (radial_f /
+// radial_g in sph_math.cuh).
+enum { kRbNNAP = 0, kRbNEP = 1 };
+// Hidden-layer activation of a species network.
+enum { kActSiLU = 0, kActTanh = 1 };
+
+// Shapes compiled for the NEP radial functions (basis kRbNEP of sph_math.cuh): radial
+// (n_max_R + 1, basis_size_R + 1) and angular (L, n_max_A + 1, basis_size_A + 1).
+#define NEP_RADIAL_SHAPES(X) X(5, 9) X(7, 9) X(9, 9)
+#define NEP_SPH_SHAPES(X) X(4, 5, 9) X(4, 7, 9) X(4, 9, 9)
+
 cudaError_t upload_sh_constants();
-bool desc_supported(int kind, int lmax, int np, int n1);
-cudaError_t launch_descriptor(int kind, int lmax, int np, int n1, const DescArgs& a, bool fwd, cudaStream_t st);
+// basis: kRbNNAP or kRbNEP (the radial functions of the sub-basis)
+bool desc_supported(int kind, int basis, int lmax, int np, int n1);
+cudaError_t launch_descriptor(int kind, int basis, int lmax, int np, int n1, const DescArgs& a, bool fwd,
+                              cudaStream_t st);
 
 // Network over the slots of one species.
 struct NetArgs {
@@ -95,6 +108,7 @@ struct NetArgs {
     double mu_e, sigma_e;
     double* e_atom;         // energy per atom (by atom index)
     float* gfp;             // dE/dfp by slot
+    int act;                // hidden activation: kActSiLU (NNAP) or kActTanh (NEP)
 };
 
 // FP32 SIMT network (plain precision).

@@ -40,7 +40,7 @@ __device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { re
 }  // namespace
 
 // =========================================================================== radial
-template <int NP, int N1>
+template <int NP, int N1, int RB>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
     pdl_enter();
     extern __shared__ float sW[];
@@ -61,9 +61,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
         const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         if (r >= rc) continue;
         const int tn = __float_as_int(d.w) - 1;
-        const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
         float T[N1], sv[NP];
-        cheby_f<N1>(1.f - 2.f * u, T);
+        const float fc = radial_f<RB, N1>(r, irc, T);
         fuse_apply<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, T, sv);
 #pragma unroll
         for (int p = 0; p < NP; ++p) acc[p] += fc * sv[p];
@@ -78,7 +77,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
         if (lane == (p & 31)) out[p] = acc[p];
 }
 
-template <int NP, int N1>
+template <int NP, int N1, int RB>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_bwd(DescArgs a) {
     pdl_enter();
     extern __shared__ float sW[];
@@ -102,12 +101,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_bwd(DescArgs a) {
         float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
         if (r < rc) {
             const int tn = __float_as_int(d.w) - 1;
-            const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
-            const float fcg = 8.f * fc1 * fc2 * irc * irc;
-            const float x = 1.f - 2.f * u;
-            float T[N1], TG[N1];
-            cheby_f<N1>(x, T);
-            cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+            float T[N1], TG[N1], fcg;
+            const float fc = radial_g<RB, N1>(r, rc, irc, T, TG, &fcg);
             float v[N1];
             fuse_apply_t<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, gfp, v);
             float dfc = 0.f, drn = 0.f;
@@ -140,7 +135,7 @@ struct SphShape {
     static constexpr int BWD_WARP_FLOATS = K * NPS + 2 * K * 32;
 };
 
-template <int L, int NP, int N1>
+template <int L, int NP, int N1, int RB>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
     pdl_enter();
     using S = SphShape<L, NP>;
@@ -179,9 +174,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
             if (r < rc) {
                 valid = true;
                 const int tn = __float_as_int(d.w) - 1;
-                const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
                 float T[N1], sv[NP];
-                cheby_f<N1>(1.f - 2.f * u, T);
+                const float fc = radial_f<RB, N1>(r, irc, T);
                 fuse_apply<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, T, sv);
 #pragma unroll
                 for (int p = 0; p < NP; ++p) c[p] = fc * sv[p];
@@ -388,7 +382,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd_n(DescArgs a) {
 // c and dc stay live through the lm loop: the radial sums are formed again afterwards
 // as v_n = sum_p dc_p W[p][n], so dfc = v . T and drn = v . dT.  Registers stay at or
 // below 128 per thread (four CTAs of four warps per SM).
-template <int L, int NP, int N1>
+template <int L, int NP, int N1, int RB>
 __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
     pdl_enter();
     using S = SphShape<L, NP>;
@@ -442,9 +436,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
         const int tn = valid ? __float_as_int(d.w) - 1 : 0;
         const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P;
         if (valid) {
-            const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
             float T[N1], sv[NP];
-            cheby_f<N1>(1.f - 2.f * u, T);
+            const float fc = radial_f<RB, N1>(r, irc, T);
             fuse_apply<NP, N1>(Wt, T, sv);
 #pragma unroll
             for (int p = 0; p < NP; ++p) c[p] = fc * sv[p];
@@ -504,12 +497,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
             const size_t e = (size_t)at * M + k;
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (valid) {
-                const float u = r * irc, fc1 = 1.f - u * u, fc2 = fc1 * fc1, fc = fc2 * fc2;
-                const float fcg = 8.f * fc1 * fc2 * irc * irc;
-                const float x = 1.f - 2.f * u;
-                float T[N1], TG[N1], v[N1];
-                cheby_f<N1>(x, T);
-                cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+                float T[N1], TG[N1], v[N1], fcg;
+                const float fc = radial_g<RB, N1>(r, rc, irc, T, TG, &fcg);
                 float dc[NP];
 #pragma unroll
                 for (int p = 0; p < NP; ++p) dc[p] = (p & 1) ? dc2[p >> 1].y : dc2[p >> 1].x;
@@ -897,7 +886,7 @@ cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st) {
 // =========================================================================== dispatch
 namespace {
 
-template <int NP, int N1>
+template <int NP, int N1, int RB>
 cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
@@ -908,13 +897,13 @@ cudaError_t launch_radial(const DescArgs& a, bool fwd, cudaStream_t st) {
     int& lim = fwd ? limit_fwd : limit_bwd;
     if ((int)sm > lim && sm > 48 * 1024) {
         const cudaError_t e =
-            fwd ? cudaFuncSetAttribute(k_radial_fwd<NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
-                : cudaFuncSetAttribute(k_radial_bwd<NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            fwd ? cudaFuncSetAttribute(k_radial_fwd<NP, N1, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                : cudaFuncSetAttribute(k_radial_bwd<NP, N1, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    if (fwd) return launch_pdl(&k_radial_fwd<NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
-    return launch_pdl(&k_radial_bwd<NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
+    if (fwd) return launch_pdl(&k_radial_fwd<NP, N1, RB>, dim3(grid), dim3(32 * wpc), sm, st, a);
+    return launch_pdl(&k_radial_bwd<NP, N1, RB>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
 template <int L, int NP, int N1>
@@ -952,13 +941,15 @@ cudaError_t launch_sph_fwd_n(const DescArgs& a, cudaStream_t st) {
     return launch_pdl(&k_sph_fwd_n<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
-template <int L, int NP, int N1>
+template <int L, int NP, int N1, int RB>
 cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     using S = SphShape<L, NP>;
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
-    if (!fwd && a.nz_p && a.nz_w && N1 < NP) return launch_sph_bwd_n<L, NP, N1>(a, st);
-    if (fwd && a.fwd_alpha && N1 < NP && a.T <= kFwdTypes) return launch_sph_fwd_n<L, NP, N1>(a, st);
+    if constexpr (RB == kRbNNAP) {   // the radial-space kernels are written for the NNAP radial functions
+        if (!fwd && a.nz_p && a.nz_w && N1 < NP) return launch_sph_bwd_n<L, NP, N1>(a, st);
+        if (fwd && a.fwd_alpha && N1 < NP && a.T <= kFwdTypes) return launch_sph_fwd_n<L, NP, N1>(a, st);
+    }
     const int wpc = a.warps;
     const int grid = (n + wpc - 1) / wpc;
     const size_t wbytes = sizeof(float) * ((size_t)a.T * a.T * NP * Fuse<N1>::N1P);
@@ -969,33 +960,47 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     int& lim = fwd ? limit_fwd : limit_bwd;
     if ((int)sm > lim) {
         const cudaError_t e =
-            fwd ? cudaFuncSetAttribute(k_sph_fwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
-                : cudaFuncSetAttribute(k_sph_bwd<L, NP, N1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            fwd ? cudaFuncSetAttribute(k_sph_fwd<L, NP, N1, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                : cudaFuncSetAttribute(k_sph_bwd<L, NP, N1, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         lim = (int)sm;
     }
-    if (fwd) return launch_pdl(&k_sph_fwd<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
-    return launch_pdl(&k_sph_bwd<L, NP, N1>, dim3(grid), dim3(32 * wpc), sm, st, a);
+    if (fwd) return launch_pdl(&k_sph_fwd<L, NP, N1, RB>, dim3(grid), dim3(32 * wpc), sm, st, a);
+    return launch_pdl(&k_sph_bwd<L, NP, N1, RB>, dim3(grid), dim3(32 * wpc), sm, st, a);
 }
 
 }  // namespace
 
 
-bool desc_supported(int kind, int lmax, int np, int n1) {
+bool desc_supported(int kind, int basis, int lmax, int np, int n1) {
 #define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return true;
 #define S_CASE(L_, P_, N_) if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return true;
-    NNAP_RADIAL_SHAPES(R_CASE)
-    NNAP_SPH_SHAPES(S_CASE)
+    if (basis == kRbNNAP) {
+        NNAP_RADIAL_SHAPES(R_CASE)
+        NNAP_SPH_SHAPES(S_CASE)
+    } else if (basis == kRbNEP) {
+        NEP_RADIAL_SHAPES(R_CASE)
+        NEP_SPH_SHAPES(S_CASE)
+    }
 #undef R_CASE
 #undef S_CASE
     return false;
 }
 
-cudaError_t launch_descriptor(int kind, int lmax, int np, int n1, const DescArgs& a, bool fwd, cudaStream_t st) {
-#define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return launch_radial<P_, N_>(a, fwd, st);
-#define S_CASE(L_, P_, N_) if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return launch_sph<L_, P_, N_>(a, fwd, st);
-    NNAP_RADIAL_SHAPES(R_CASE)
-    NNAP_SPH_SHAPES(S_CASE)
+cudaError_t launch_descriptor(int kind, int basis, int lmax, int np, int n1, const DescArgs& a, bool fwd,
+                              cudaStream_t st) {
+#define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return launch_radial<P_, N_, RB_>(a, fwd, st);
+#define S_CASE(L_, P_, N_) \
+    if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return launch_sph<L_, P_, N_, RB_>(a, fwd, st);
+    if (basis == kRbNNAP) {
+        constexpr int RB_ = kRbNNAP;
+        NNAP_RADIAL_SHAPES(R_CASE)
+        NNAP_SPH_SHAPES(S_CASE)
+    } else if (basis == kRbNEP) {
+        constexpr int RB_ = kRbNEP;
+        NEP_RADIAL_SHAPES(R_CASE)
+        NEP_SPH_SHAPES(S_CASE)
+    }
 #undef R_CASE
 #undef S_CASE
     return cudaErrorInvalidValue;

@@ -1,5 +1,5 @@
 // FP32 SIMT evaluation of the per-species SiLU feed-forward network and of its input
-// gradient (the plain-precision path).
+// gradient (the plain-precision path; also the tanh network of NEP models).
 //
 // Restates normedNnForward / normedNnBackward (nnap_main.hpp:267-323) and
 // nnForward / nnBackward (nn_FeedForward.hpp:8-21, 131-261):
@@ -24,6 +24,16 @@ __device__ __forceinline__ float silu_and_grad(float z, float* grad) {
     const float s = 1.f / (1.f + expf(-z));
     *grad = s * (1.f + z * (1.f - s));
     return z * s;
+}
+
+// tanh for NEP networks (apply_ann_one_layer, nep_core.hpp:267-305)
+__device__ __forceinline__ float act_and_grad(float z, float* grad, int act) {
+    if (act == kActTanh) {
+        const float t = tanhf(z);
+        *grad = 1.f - t * t;
+        return t;
+    }
+    return silu_and_grad(z, grad);
 }
 
 __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp_floats) {
@@ -72,7 +82,7 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
 #pragma unroll
             for (int q = 0; q < kNetAtoms; ++q) {
                 float gz;
-                nxt[o * kNetAtoms + q] = silu_and_grad(z[q], &gz);
+                nxt[o * kNetAtoms + q] = act_and_grad(z[q], &gz, a.act);
                 sd[((size_t)l * Hmax + o) * kNetAtoms + q] = gz;
             }
         }

@@ -2,6 +2,7 @@
 // into the per-species blocks the GPU kernels consume.
 #pragma once
 
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -46,10 +47,22 @@ struct Model {
     std::vector<Species> sp;
     std::string units;
     double rcut_max = 0.0;
+    int radial_fn = 0;  // radial functions of every sub-basis: 0 NNAP Chebyshev, 1 NEP
+    int act = 0;        // hidden activation of every network: 0 SiLU, 1 tanh (NEP)
     int ntypes() const { return (int)sp.size(); }
 };
 
 // Parse and pack; throws std::runtime_error with a message on invalid input.
 Model load_model(const char* text, size_t len);
+
+// A valid NEP file of a variant the GPU path does not evaluate (ZBL, dipole,
+// polarizability, type-wise cutoffs).
+struct NepUnsupported : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// Parse a NEP potential file (nep.txt) into the equivalent NNAP-pipeline model (see
+// nep_model.cpp); throws std::runtime_error on invalid input and NepUnsupported.
+Model load_nep_model(const char* text, size_t len);
 
 }  // namespace nnapgb

@@ -45,8 +45,9 @@ void upload_model(nnap_handle* h) {
     for (int t = 0; t < T;) {
         Run r;
         r.t0 = t;
-        auto shape = [](const SubBasis& b) {
-            return SubShape{b.kind, b.lmax, b.np, b.nmax + 1, b.rcut, b.nl2, b.l3max, b.l4max, (int)b.inv.size()};
+        auto shape = [&m](const SubBasis& b) {
+            return SubShape{b.kind, b.lmax, b.np, b.nmax + 1, b.rcut, b.nl2, b.l3max, b.l4max, (int)b.inv.size(),
+                            m.radial_fn ? kRbNEP : kRbNNAP};
         };
         for (auto& b : m.sp[t].subs) {
             r.subs.push_back(shape(b));
@@ -64,10 +65,10 @@ void upload_model(nnap_handle* h) {
         r.t1 = u;
         for (size_t k = 0; k < r.subs.size(); ++k) {
             const SubShape& s = r.subs[k];
-            if (!desc_supported(s.kind, s.lmax, s.np, s.n1)) {
+            if (!desc_supported(s.kind, s.basis, s.lmax, s.np, s.n1)) {
                 char buf[160];
-                std::snprintf(buf, sizeof buf, "no compiled descriptor kernel for kind=%d lmax=%d np=%d nmax=%d",
-                              s.kind, s.lmax, s.np, s.n1 - 1);
+                std::snprintf(buf, sizeof buf, "no compiled descriptor kernel for %s kind=%d lmax=%d np=%d nmax=%d",
+                              s.basis == kRbNEP ? "NEP" : "NNAP", s.kind, s.lmax, s.np, s.n1 - 1);
                 throw ApiFail(NNAP_ERR_UNSUPPORTED, buf);
             }
             std::vector<float> W((size_t)T * T * s.np * s.n1, 0.f);
@@ -81,7 +82,7 @@ void upload_model(nnap_handle* h) {
             // sparse columns for the radial-space backward
             std::vector<int> zp((size_t)T * T * s.n1 * kNz, -1);
             std::vector<float> zw(zp.size(), 0.f);
-            bool sparse = s.kind == KIND_SPHERICAL && s.n1 < s.np;
+            bool sparse = s.kind == KIND_SPHERICAL && s.n1 < s.np && s.basis == kRbNNAP;
             for (int tc = r.t0; tc < r.t1 && sparse; ++tc)
                 for (int tn = 0; tn < T && sparse; ++tn)
                     for (int n = 0; n < s.n1 && sparse; ++n) {
@@ -121,7 +122,7 @@ void upload_model(nnap_handle* h) {
             // per-row scales for the radial-space forward
             {
                 std::vector<float> al((size_t)T * kFwdTypes * s.np, 0.f);
-                bool diag = s.kind == KIND_SPHERICAL && s.n1 < s.np && T <= kFwdTypes;
+                bool diag = s.kind == KIND_SPHERICAL && s.n1 < s.np && T <= kFwdTypes && s.basis == kRbNNAP;
                 for (int tc = r.t0; tc < r.t1 && diag; ++tc)
                     for (int tn = 0; tn < T && diag; ++tn)
                         for (int p = 0; p < s.np && diag; ++p)
@@ -162,6 +163,7 @@ void upload_model(nnap_handle* h) {
         }
         nd.mu_e = sp.mu_e;
         nd.sigma_e = sp.sigma_e;
+        nd.act = m.act ? kActTanh : kActSiLU;
         std::vector<float> w;
         for (int i = 0; i < sp.D; ++i) w.push_back((float)sp.mu[i]);
         for (int i = 0; i < sp.D; ++i) w.push_back((float)(1.0 / sp.sigma[i]));
@@ -178,7 +180,7 @@ void upload_model(nnap_handle* h) {
         w.push_back((float)sp.bo);
         nd.w32.ensure(w.size());
         CK(cudaMemcpy(nd.w32.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
-        if (h->precision == NNAP_PREC_MIXED) {
+        if (h->net_tc) {
             std::string why;
             if (!net_tc_prepare(sp, nd.tc, why)) throw ApiFail(NNAP_ERR_UNSUPPORTED, why);
         }
@@ -535,7 +537,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                     }
                 }
                 if (n > 0) {
-                    CK(launch_descriptor(s.kind, s.lmax, s.np, s.n1, a, fwd, st));
+                    CK(launch_descriptor(s.kind, s.basis, s.lmax, s.np, s.n1, a, fwd, st));
                     ++h->launches;
                     if (fwd && s.ninv) {
                         CK(launch_invariants(ia, true, st));
@@ -566,12 +568,13 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
             a.sigma_e = nd.sigma_e;
             a.e_atom = h->e_atom.p;
             a.gfp = h->gfp.p;
-            if (h->precision != NNAP_PREC_MIXED) {
+            a.act = nd.act;
+            if (!h->net_tc) {
                 CK(launch_net_fp32(a, st));
                 ++h->launches;
             }
         }
-        if (h->precision == NNAP_PREC_MIXED) {
+        if (h->net_tc) {
             // one launch per run of consecutive species with the same network shape
             for (int t = 0; t < T;) {
                 int u = t + 1;
@@ -701,7 +704,7 @@ Tuning tune_launches(nnap_handle* h, const Batch& B, const double* d_x, const in
                                  {&Tuning::desc_fwd_warps, 1, {2, 4, 8}},
                                  {&Tuning::desc_bwd_warps, 3, {2, 4, 8}},
                                  {&Tuning::gather_block, 4, {64, 128, 256}}};
-    if (h->precision == NNAP_PREC_MIXED) params.push_back({&Tuning::net_split, 2, {2, 4}});
+    if (h->net_tc) params.push_back({&Tuning::net_split, 2, {2, 4}});
     try {
         for (auto& p : params) {
             int bv = best.*(p.field);
@@ -840,21 +843,14 @@ void upload_inputs(nnap_handle* h, int n, const double* x, const int* type) {
 }  // namespace nnapgb
 
 // =================================================================== C ABI
-extern "C" {
-
-int nnap_create(const char* model_json, size_t len, int precision, int device, nnap_handle** out) {
-    if (!model_json || !out) return NNAP_ERR_ARG;
-    *out = nullptr;
-    if (precision != NNAP_PREC_FP32 && precision != NNAP_PREC_MIXED) return NNAP_ERR_ARG;
+// Handle creation shared by the NNAP and NEP loaders.  NEP's tanh networks always run
+// on the FP32 network kernel; NNAP_PREC_MIXED then changes nothing for them.
+static int create_handle(Model&& model, int precision, int device, nnap_handle** out) {
     std::unique_ptr<nnap_handle> h(new (std::nothrow) nnap_handle());
     if (!h) return NNAP_ERR_CAPACITY;
-    try {
-        h->model = load_model(model_json, len);
-    } catch (const std::exception& e) {
-        std::fprintf(stderr, "nnap_create: %s\n", e.what());
-        return NNAP_ERR_BAD_MODEL;
-    }
+    h->model = std::move(model);
     h->precision = precision;
+    h->net_tc = precision == NNAP_PREC_MIXED && h->model.act == 0;
     h->device = device;
     try {
         CK(cudaSetDevice(device));
@@ -877,14 +873,58 @@ int nnap_create(const char* model_json, size_t len, int precision, int device, n
     return NNAP_OK;
 }
 
-int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out) {
-    if (!path || !out) return NNAP_ERR_ARG;
+static bool read_file(const char* path, std::string& s) {
     std::ifstream f(path, std::ios::binary);
-    if (!f) return NNAP_ERR_ARG;
+    if (!f) return false;
     std::stringstream ss;
     ss << f.rdbuf();
-    const std::string s = ss.str();
+    s = ss.str();
+    return true;
+}
+
+extern "C" {
+
+int nnap_create(const char* model_json, size_t len, int precision, int device, nnap_handle** out) {
+    if (!model_json || !out) return NNAP_ERR_ARG;
+    *out = nullptr;
+    if (precision != NNAP_PREC_FP32 && precision != NNAP_PREC_MIXED) return NNAP_ERR_ARG;
+    Model m;
+    try {
+        m = load_model(model_json, len);
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "nnap_create: %s\n", e.what());
+        return NNAP_ERR_BAD_MODEL;
+    }
+    return create_handle(std::move(m), precision, device, out);
+}
+
+int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out) {
+    std::string s;
+    if (!path || !out || !read_file(path, s)) return NNAP_ERR_ARG;
     return nnap_create(s.data(), s.size(), precision, device, out);
+}
+
+int nnap_create_nep(const char* nep_txt, size_t len, int precision, int device, nnap_handle** out) {
+    if (!nep_txt || !out) return NNAP_ERR_ARG;
+    *out = nullptr;
+    if (precision != NNAP_PREC_FP32 && precision != NNAP_PREC_MIXED) return NNAP_ERR_ARG;
+    Model m;
+    try {
+        m = load_nep_model(nep_txt, len);
+    } catch (const NepUnsupported& e) {
+        std::fprintf(stderr, "nnap_create_nep: %s\n", e.what());
+        return NNAP_ERR_UNSUPPORTED;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "nnap_create_nep: %s\n", e.what());
+        return NNAP_ERR_BAD_MODEL;
+    }
+    return create_handle(std::move(m), precision, device, out);
+}
+
+int nnap_create_nep_from_file(const char* path, int precision, int device, nnap_handle** out) {
+    std::string s;
+    if (!path || !out || !read_file(path, s)) return NNAP_ERR_ARG;
+    return nnap_create_nep(s.data(), s.size(), precision, device, out);
 }
 
 int nnap_destroy(nnap_handle* h) {

@@ -413,6 +413,7 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         if (nstruct < 1 || !natoms || !box_kind || !boxes) throw ApiFail(NNAP_ERR_ARG, "invalid batch description");
         if (!grad_nn) throw ApiFail(NNAP_ERR_ARG, "grad_nn is NULL");
         const Model& m = h->model;
+        if (m.radial_fn || m.act) throw ApiFail(NNAP_ERR_UNSUPPORTED, "training gradients are computed for NNAP models only");
         const int T = m.ntypes();
         const bool want_w = grad_fp && any_fused(m);
         h->launches = 0;

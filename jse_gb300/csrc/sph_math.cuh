@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+#include "desc.cuh"
+
 #include <cmath>
 
 namespace nnapgb {
@@ -63,6 +65,49 @@ __device__ __forceinline__ void cheby_grad_f(float x, float mul, float* G) {
         if (n >= 2) { um2 = um1; um1 = u; }
         G[n] = (float)n * u;
     }
+}
+
+// Radial functions of the two bases the p-space descriptor kernels serve (template
+// parameter RB); a neighbour's channel value is c_p = fc sum_n W[p][n] R_n.
+//   kRbNNAP (nnap_util.hpp:226-271):            u = r/rc, fc = (1 - u^2)^4, R_n = T_n(1 - 2u)
+//   kRbNEP  (find_fc / find_fn, nep_core.hpp):  fc = (cos(pi u) + 1)/2,
+//                                               R_n = (T_n(2(u - 1)^2 - 1) + 1)/2
+// radial_f returns fc and fills R; radial_g also fills RG_n = -(1/r) dR_n/dr and sets
+// fcg = -(1/r) dfc/dr.
+template <int RB, int N1>
+__device__ __forceinline__ float radial_f(float r, float irc, float* R) {
+    const float u = r * irc;
+    if (RB == kRbNEP) {
+        cheby_f<N1>(2.f * (u - 1.f) * (u - 1.f) - 1.f, R);
+#pragma unroll
+        for (int n = 0; n < N1; ++n) R[n] = 0.5f * (R[n] + 1.f);
+        return 0.5f * cospif(u) + 0.5f;
+    }
+    const float fc1 = 1.f - u * u, fc2 = fc1 * fc1;
+    cheby_f<N1>(1.f - 2.f * u, R);
+    return fc2 * fc2;
+}
+
+template <int RB, int N1>
+__device__ __forceinline__ float radial_g(float r, float rc, float irc, float* R, float* RG, float* fcg) {
+    const float u = r * irc;
+    if (RB == kRbNEP) {
+        const float x = 2.f * (u - 1.f) * (u - 1.f) - 1.f;
+        cheby_f<N1>(x, R);
+        cheby_grad_f<N1>(x, 2.f * (1.f - u) / (r * rc), RG);   // dx/dr = 4 (u - 1)/rc
+#pragma unroll
+        for (int n = 0; n < N1; ++n) R[n] = 0.5f * (R[n] + 1.f);
+        float sn, cs;
+        sincospif(u, &sn, &cs);
+        *fcg = 0.5f * 3.14159265358979f * sn * irc / r;
+        return 0.5f * cs + 0.5f;
+    }
+    const float fc1 = 1.f - u * u, fc2 = fc1 * fc1;
+    *fcg = 8.f * fc1 * fc2 * irc * irc;
+    const float x = 1.f - 2.f * u;
+    cheby_f<N1>(x, R);
+    cheby_grad_f<N1>(x, 2.f / (r * rc), RG);
+    return fc2 * fc2;
 }
 
 // Normalised associated Legendre functions P[tri(l,m)], Condon-Shortley phase included.

@@ -41,7 +41,8 @@ EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes"
            "nnap_stage_times", "nnap_compute_batch_device", "nnap_set_graphs", "nnap_neighbor_counts_noalloc",
            "nnap_server_create", "nnap_server_destroy", "nnap_server_admit", "nnap_server_release",
            "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats", "nnap_set_autotune",
-           "nnap_get_tuning", "nnap_set_tuning", "nnap_compute_lammps"]
+           "nnap_get_tuning", "nnap_set_tuning", "nnap_compute_lammps", "nnap_param_sizes", "nnap_train_grad_batch",
+           "nnap_create_nep", "nnap_create_nep_from_file"]
 
 
 class IllegalStateError(RuntimeError):
@@ -100,6 +101,8 @@ def load_library(path: str = LIB_PATH):
     L.nnap_server_stats.argtypes = [P, C.POINTER(C.c_longlong)]
     L.nnap_param_sizes.argtypes = [P, I, ip, ip]
     L.nnap_train_grad_batch.argtypes = [P, I, ip, dp, ip, ip, dp, dp, dp, dp, dp, dp]
+    L.nnap_create_nep.argtypes = [C.c_char_p, S, I, I, C.POINTER(P)]
+    L.nnap_create_nep_from_file.argtypes = [C.c_char_p, I, I, C.POINTER(P)]
     _lib = L
     return L
 

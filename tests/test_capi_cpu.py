@@ -124,3 +124,50 @@ def test_valid_mirror_and_shared_model_passes_the_loader():
     if rc == 0:
         L.nnap_destroy(h)
     assert rc != 1
+
+
+def _nep_text(**kw):
+    from oracle import nep_model as NM
+    return NM.write(["Si", "O"], neurons=4, seed=2, **kw)
+
+
+def _nep_lines(mut):
+    lines = _nep_text().splitlines()
+    mut(lines)
+    return "\n".join(lines) + "\n"
+
+
+NEP_BAD = [
+    ("", 1), ("nep4 2 Si\n", 1), ("lj 1 Ar\n", 1),
+    (_nep_lines(lambda ls: ls.__setitem__(0, "nep4_zbl 2 Si O")), 5),            # ZBL variant
+    (_nep_lines(lambda ls: ls.__setitem__(0, "nep3_dipole 2 Si O")), 5),
+    (_nep_lines(lambda ls: ls.__setitem__(1, "cutoff 5 4 100 100 1.5 1.5 0")), 5),  # type-wise cutoffs
+    (_nep_lines(lambda ls: ls.__setitem__(2, "n_max 4")), 1),
+    (_nep_lines(lambda ls: ls.__setitem__(4, "l_max 4 2")), 1),
+    (_nep_lines(lambda ls: ls.pop()), 1),                                        # one scale short
+    (_nep_lines(lambda ls: ls.append("0.5")), 1),                                # one number too many
+    (_nep_lines(lambda ls: ls.__setitem__(9, "abc")), 1),
+]
+
+
+@pytest.mark.parametrize("text,status", NEP_BAD)
+def test_invalid_nep_files_are_rejected(text, status):
+    """nnap_create_nep parses before any device work: malformed files return
+    NNAP_ERR_BAD_MODEL (the reference loader throws IllegalArgumentException, NEP.java:795-981)
+    and valid files of variants the GPU path does not evaluate NNAP_ERR_UNSUPPORTED."""
+    L = _lib()
+    h = C.c_void_p()
+    b = text.encode()
+    assert L.nnap_create_nep(b, len(b), 0, 0, C.byref(h)) == status
+    assert not h.value
+    assert L.nnap_create_nep(None, 0, 0, 0, None) == 6
+
+
+def test_valid_nep_file_passes_the_loader():
+    L = _lib()
+    h = C.c_void_p()
+    b = _nep_text().encode()
+    rc = L.nnap_create_nep(b, len(b), 0, 0, C.byref(h))
+    if rc == 0:
+        L.nnap_destroy(h)
+    assert rc not in (1, 5, 6)
