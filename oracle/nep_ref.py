@@ -3,7 +3,9 @@
 TEST INFRASTRUCTURE ONLY.  The model's shape expands the reference's NEP sources
 (``src/nep/resources/assets/nep/src``, read from the reference checkout at build time;
 nothing is committed) with oracle/nepgen.py into oracle/_ref/nep_<key>/src, which is
-compiled with oracle/nep_driver.cpp (g++ -O2, no fast-math) into libnepref.so.
+compiled with oracle/nep_driver.cpp into libnepref.so (g++ -O2, no fast-math: the oracle
+values) or libnepref_fast.so (-O3 -ffast-math: the CPU baseline).  An expansion made where a
+reference checkout exists is compiled wherever the repository is copied.
 """
 from __future__ import annotations
 
@@ -33,20 +35,30 @@ def shape_key(m: NEPModel) -> str:
     return "nep" + hashlib.sha1(blob.encode()).hexdigest()[:12]
 
 
-def build(m: NEPModel) -> str:
-    key = shape_key(m)
-    d = os.path.join(REF_OUT, key)
-    src = os.path.join(d, "src")
+def expand(m: NEPModel) -> str:
+    """Expand the reference's NEP sources for the model's shape (needs a reference checkout,
+    unless an earlier expansion is present); returns the source directory."""
+    src = os.path.join(REF_OUT, shape_key(m), "src")
     if not os.path.exists(os.path.join(src, "nep_interface.cpp")):
         sd = nep_src_dir()
         if not os.path.isdir(sd):
             raise FileNotFoundError("reference NEP sources are not available")
         nepgen.expand(sd, src, m)
-    out = os.path.join(d, "libnepref.so")
+    return src
+
+
+def build(m: NEPModel, fast: bool = False) -> str:
+    """Compile the expanded sources: exact (-O2, no contraction; oracle values) or fast
+    (-O3 -ffast-math, the reference's default JIT optimisation without -march=native; the
+    CPU baseline)."""
+    src = expand(m)
+    d = os.path.dirname(src)
+    out = os.path.join(d, "libnepref_fast.so" if fast else "libnepref.so")
     drv = os.path.join(HERE, "nep_driver.cpp")
     deps = [os.path.join(src, "nep_interface.cpp"), os.path.join(src, "nep_core.hpp"), drv]
     if not os.path.exists(out) or any(os.path.getmtime(p) > os.path.getmtime(out) for p in deps):
-        cmd = ["g++", "-std=c++14", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-I", src,
+        opt = ["-O3", "-ffast-math"] if fast else ["-O2", "-ffp-contract=off"]
+        cmd = ["g++", "-std=c++14"] + opt + ["-fPIC", "-shared", "-w", "-pthread", "-I", src,
                os.path.join(src, "nep_interface.cpp"), drv, "-o", out]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
@@ -55,9 +67,9 @@ def build(m: NEPModel) -> str:
 
 
 class RefNEP:
-    def __init__(self, m: NEPModel):
+    def __init__(self, m: NEPModel, fast: bool = False):
         self.m = m
-        self.lib = C.CDLL(build(m))
+        self.lib = C.CDLL(build(m, fast))
         T = m.ntypes
         self._keep = []
         dp = C.POINTER(C.c_double)
@@ -79,15 +91,16 @@ class RefNEP:
         self.qs = arr(m.q_scaler)
         self.an = np.zeros(T, dtype=np.int32)
 
-    def compute(self, types0, nl):
+    def compute(self, types0, nl, nthreads: int = 1, n_eval: Optional[int] = None):
         types0 = np.ascontiguousarray(types0, dtype=np.int32)
         n = len(types0)
+        n_eval = n if n_eval is None else int(n_eval)
         e, f, v = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 9))
         dx = np.ascontiguousarray(nl.dx, dtype=np.float64)
         ip, lp, dp = C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_double)
         code = self.lib.nep_ref_compute(self.m.ntypes, self.an.ctypes.data_as(ip), self.qs, self.w0, self.b0,
-                                        self.w1, self.b1, self.c, self.m.dim, (self.m.n_max_angular + 1) * 80, n,
-                                        types0.ctypes.data_as(ip), nl.offsets.ctypes.data_as(lp),
+                                        self.w1, self.b1, self.c, self.m.dim, (self.m.n_max_angular + 1) * 80, n, n_eval,
+                                        int(nthreads), types0.ctypes.data_as(ip), nl.offsets.ctypes.data_as(lp),
                                         nl.j.ctypes.data_as(ip), dx.ctypes.data_as(dp), e.ctypes.data_as(dp),
                                         f.ctypes.data_as(dp), v.ctypes.data_as(dp))
         if code:
