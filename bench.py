@@ -314,6 +314,104 @@ def train_measurement(device: int, s, model: dict, steps: int = 5, cpu: bool = T
     return out
 
 
+# ----------------------------------------------------------------------------- NEP
+def nep_measurement(device: int, steps: int = 10, cpu: bool = True) -> dict:
+    """NEP potential through nnap_create_nep on the NEP benchmark: a 32000-atom binary liquid
+    (0.060 /A^3) under a seeded nep4 potential of GPUMD's default hyperparameters (cutoff
+    8 / 4 A, n_max 4 4, basis_size 8 8, l_max 4 2 1, 30 neurons), FP32.  ``value`` is
+    device-resident (CUDA events on the launching stream, L2 flushed between steps); ``e2e``
+    goes through nnap_compute with pinned host buffers.  The CPU baseline is the reference's
+    NEP arithmetic (oracle/_ref, -O3 -ffast-math) with all host threads on a sample of the
+    same structure's atoms (full neighbour rows)."""
+    import torch
+    from jse_gb300.nep import NEP
+    from jse_gb300.nnap import WANT_ENERGY, WANT_FORCES, WANT_VIRIAL, _dptr, _iptr
+    text, s = W.nep_bench()
+    n = s.natoms
+    dev = torch.device("cuda", device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    x_d = torch.from_numpy(np.ascontiguousarray(s.x)).to(dev)
+    t_d = torch.from_numpy(np.ascontiguousarray(s.types, dtype=np.int32)).to(dev)
+    e_d = torch.zeros(1, dtype=torch.float64, device=dev)
+    f_d = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+    v_d = torch.zeros(9, dtype=torch.float64, device=dev)
+    flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
+    out = {"unit": "atom-evals/s", "atoms": n, "model": "nep4, 2 species, cutoff 8/4 A, n_max 4 4, basis_size 8 8, "
+           "l_max 4 2 1, 30 neurons (seeded random weights)", "precision": "FP32"}
+    with NEP(text, device=device) as p:
+        def dstep():
+            p.computeDevice(n, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
+                            f_d.data_ptr(), v_d.data_ptr(), 0, stream=torch.cuda.current_stream(dev).cuda_stream)
+        p.setProfiling(True)
+        for _ in range(3):
+            flush.zero_()
+            dstep()
+        torch.cuda.synchronize(dev)
+        ms, stages, launches = [], np.zeros(5), 0
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dstep()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            stages += p.stageTimes()
+            launches += p.lastLaunchCount()
+        out["value"] = n * steps / (sum(ms) / 1e3)
+        out["ms_per_step"] = sum(ms) / steps
+        out["gpu_launches"] = launches
+        out["stage_ms"] = dict(zip(["neighbours", "descriptors_fwd", "network", "descriptors_bwd", "scatter"],
+                                   [round(float(v), 5) for v in stages / steps]))
+        xh = torch.from_numpy(np.ascontiguousarray(s.x)).pin_memory().numpy()
+        th = torch.from_numpy(np.ascontiguousarray(s.types, dtype=np.int32)).pin_memory().numpy()
+        fh = torch.zeros((n, 3), dtype=torch.float64).pin_memory().numpy()
+        eh = torch.zeros(1, dtype=torch.float64).pin_memory().numpy()
+        vh = torch.zeros(9, dtype=torch.float64).pin_memory().numpy()
+        box = np.ascontiguousarray(s.box, dtype=np.float64).reshape(9)
+
+        def hstep():
+            p._check(p._L.nnap_compute(p._handle(), n, _dptr(xh), _iptr(th), int(s.box_kind), _dptr(box), flags,
+                                       _dptr(eh), None, _dptr(fh), _dptr(vh), None))
+        for _ in range(3):
+            hstep()
+        dts = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            hstep()
+            dts.append(time.perf_counter() - t0)
+        out["e2e"] = {"value": n * steps / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": n * 28,
+                      "d2h_bytes_per_step": 8 + n * 24 + 72}
+    if cpu:
+        try:
+            from oracle import native as ON, nep_model as NM, nep_ref as NR
+            m = NM.load(text)
+            ref = NR.RefNEP(m, fast=True)
+            nl = ON.neighbors(ON.wrap(s.x, s.box_kind, s.box), s.box_kind, s.box, max(m.rc_radial, m.rc_angular))
+            threads = os.cpu_count() or 1
+            t0s = s.types - 1
+            k = 256
+            while True:
+                t0 = time.perf_counter()
+                ref.compute(t0s, nl, nthreads=threads, n_eval=k)
+                dt = time.perf_counter() - t0
+                if dt > 1.0 or k >= n:
+                    break
+                k = min(n, k * 4)
+            k = int(min(n, max(k, k / dt * 10.0)))
+            t0 = time.perf_counter()
+            ref.compute(t0s, nl, nthreads=threads, n_eval=k)
+            v = k / (time.perf_counter() - t0)
+            out["cpu_baseline"] = {"value": v, "unit": "atom-evals/s", "kind": "reference", "cores": threads,
+                                   "sample": "%d of %d atoms, full neighbour rows, reference NEP per-atom C++ "
+                                             "(-O3 -ffast-math)" % (k, n)}
+        except Exception as ex:  # the baseline is reported, never required
+            out["cpu_baseline"] = {"value": None, "error": str(ex)[:200]}
+    return out
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -326,6 +424,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-train", action="store_true", help="skip the training-gradient measurement")
+    ap.add_argument("--no-nep", action="store_true", help="skip the NEP measurement")
+    ap.add_argument("--only-nep", action="store_true", help="run only the NEP measurement (profiling runs)")
     ap.add_argument("--only-train", action="store_true", help="run only the training-gradient measurement "
                     "(profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=5000)
@@ -338,6 +438,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     dist, rank, world = init_from_env("gloo")
 
+    if args.only_nep:
+        if rank == 0:
+            print(json.dumps({"nep": nep_measurement(local, steps=args.steps, cpu=not args.no_cpu_baseline)}))
+        return
     structures, cfg = make_workload(args.workload, args.atoms)
     natoms_step = sum(s.natoms for s in structures)
     config = {"workload": args.workload, "structures": len(structures), "atoms_per_step": natoms_step,
@@ -496,6 +600,9 @@ def main():
     training = None
     if rank == 0 and not args.no_train and args.workload == "liquid32k":
         training = train_measurement(local, s, model, cpu=not args.no_cpu_baseline)
+    nep = None
+    if rank == 0 and not args.no_nep and args.workload == "liquid32k":
+        nep = nep_measurement(local, cpu=not args.no_cpu_baseline)
 
     # roofline of the dominant stage
     peak, peak_kind, sm_max = load_peaks()
@@ -538,6 +645,8 @@ def main():
             line["serving"] = serving
         if training is not None:
             line["training"] = training
+        if nep is not None:
+            line["nep"] = nep
         print(json.dumps(line))
     pot.close()
     if dist:

@@ -116,6 +116,8 @@ struct Run {
     std::vector<DevBuf<int4>> inv_idx;
     std::vector<DevBuf<float>> inv_coef;
     std::vector<DevBuf<int>> inv_start;
+    // per sub: the spherical kernels scan the compact rows of the handle's sub_rc cutoff
+    std::vector<char> use_sub;
 };
 
 struct NetDev {
@@ -165,6 +167,11 @@ struct nnap_handle {
     nnapgb::DevBuf<float4> pdx, pg;
     nnapgb::DevBuf<int> prev, pcount;
     nnapgb::DevBuf<float> fp, gfp, A, Gx;  // Gx: invariant-column part of dE/dA (when present)
+    // compact rows of the entries within sub_rc (0: none) for spherical sub-bases whose
+    // cutoff is well inside the neighbour cutoff: dx and row position [n][M], count [n]
+    double sub_rc = 0.0;
+    nnapgb::DevBuf<float4> sdx;
+    nnapgb::DevBuf<int> spos, scount;
     int M = 0;
     // LAMMPS-style boundary: caller's atoms (local + ghost), list, targets of the scatter
     nnapgb::DevBuf<double> lmp_x, lmp_forces, lmp_virials;

@@ -36,6 +36,12 @@ struct DescArgs {
     // dE/dA, [slot - range[t0]][NP][K] like A, added to the power-spectrum part
     int nl2, sl;
     const float* Gx;
+    // spherical p-space kernels of an accumulating call: compact rows of the entries within
+    // rcut (dx, position in the full row; capacity P.M per atom) and their count per atom,
+    // or NULL: the kernels then scan the full rows
+    const float4* sub_dx;
+    const int* sub_pos;
+    const int* sub_count;
 };
 
 // Invariant (l3max / l4max) columns of one spherical sub-basis over a run of species:
@@ -89,6 +95,9 @@ enum { kActSiLU = 0, kActTanh = 1 };
 #define NEP_SPH_SHAPES(X) X(4, 5, 9) X(4, 7, 9) X(4, 9, 9)
 
 cudaError_t upload_sh_constants();
+// Compact rows of the entries within rc (k_subrows): sdx / spos [n][P.M], scount [n].
+cudaError_t launch_subrows(const PairBufs& P, int n, float rc, float4* sdx, int* spos, int* scount,
+                           cudaStream_t st);
 // basis: kRbNNAP or kRbNEP (the radial functions of the sub-basis)
 bool desc_supported(int kind, int basis, int lmax, int np, int n1);
 cudaError_t launch_descriptor(int kind, int basis, int lmax, int np, int n1, const DescArgs& a, bool fwd,

@@ -152,7 +152,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
     float* sC = sY + 32 * S::KS;                                       // [32][NPS]
     const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
-    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const int M = a.P.M, cnt = a.sub_dx ? a.sub_count[at] : min(a.P.count[at], M);
+    const float4* rdx = (a.sub_dx ? a.sub_dx : a.P.dx) + (size_t)at * M;
     const float rc = a.rcut, irc = 1.f / a.rcut;
     // accumulators in packed pairs of channels (p = 2h, 2h + 1) for paired FP32 FMAs
     constexpr int NH = (NP + 1) / 2;
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
         float* y = sY + lane * S::KS;
         bool valid = false;
         if (k < cnt) {
-            const float4 d = a.P.dx[(size_t)at * M + k];
+            const float4 d = rdx[k];
             const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
             if (r < rc) {
                 valid = true;
@@ -400,7 +401,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
     float* sYt = sY + S::K * 32;                     // [K][32]
     const int at = atom_of(a, s0, w);
     const int tc = a.type[at] - 1;
-    const int M = a.P.M, cnt = min(a.P.count[at], M);
+    const int M = a.P.M, cnt = a.sub_dx ? a.sub_count[at] : min(a.P.count[at], M);
+    const float4* rdx = (a.sub_dx ? a.sub_dx : a.P.dx) + (size_t)at * M;
     const float rc = a.rcut, irc = 1.f / a.rcut;
     // G[p][lm] = 2 * 4pi/(2l+1) * dE/dfp[p][l] * A[p][lm], stored transposed
     {
@@ -429,7 +431,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
         float r = 1.f;
         bool valid = false;
         if (k < cnt) {
-            d = a.P.dx[(size_t)at * M + k];
+            d = rdx[k];
             r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
             valid = r < rc;
         }
@@ -494,7 +496,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
             }
         }
         if (k < cnt) {
-            const size_t e = (size_t)at * M + k;
+            const size_t e = (size_t)at * M + (a.sub_dx ? a.sub_pos[(size_t)at * M + k] : k);
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (valid) {
                 float T[N1], TG[N1], v[N1], fcg;
@@ -727,44 +729,112 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
     }
 }
 
+// =========================================================================== sub-rows
+// Compact copy of the entries of each row within cutoff rc (same FP32 test as the
+// descriptor kernels), with their positions in the full row: the spherical kernels of a
+// sub-basis whose cutoff is well inside the neighbour cutoff scan these instead of the
+// full rows.  One warp per atom; entries keep their row order.
+__global__ void __launch_bounds__(256) k_subrows(PairBufs P, int n, float rc, float4* __restrict__ sdx,
+                                                 int* __restrict__ spos, int* __restrict__ scount) {
+    pdl_enter();
+    const int at = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (at >= n) return;
+    const int M = P.M, cnt = min(P.count[at], M);
+    int c = 0;
+    for (int base = 0; base < cnt; base += 32) {
+        const int k = base + lane;
+        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        bool in = false;
+        if (k < cnt) {
+            d = P.dx[(size_t)at * M + k];
+            in = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z) < rc;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, in);
+        if (in) {
+            const size_t q = (size_t)at * M + c + __popc(m & ((1u << lane) - 1u));
+            sdx[q] = d;
+            spos[q] = k;
+        }
+        c += __popc(m);
+    }
+    if (lane == 0) scount[at] = c;
+}
+
+cudaError_t launch_subrows(const PairBufs& P, int n, float rc, float4* sdx, int* spos, int* scount,
+                           cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    return launch_pdl(&k_subrows, dim3((unsigned)(((size_t)n * 32 + 255) / 256)), dim3(256), 0, st, P, n, rc, sdx,
+                      spos, scount);
+}
+
 // =========================================================================== invariants
 // Columns: sum over the column's terms of coefficient x product of a channel's A entries
 // (calSphL3 / calSphL4, basis_SphericalUtil.hpp:395-467).  Backward: dE/dA of each
-// product, one factor at a time (calGradSphL3 / L4).  One lane owns one channel, so each
-// sum runs in term order and the results do not depend on scheduling.
-__global__ void __launch_bounds__(128) k_inv_fwd(InvArgs a) {
+// product, one factor at a time (calGradSphL3 / L4).  One thread owns one (atom slot,
+// channel) row of A, so each sum runs in term order and the results do not depend on
+// scheduling.  The rows of a block are contiguous in A; the block stages them in shared
+// memory with an odd row stride: the lanes of a warp apply the same term at the same time,
+// so their reads of one index fall in distinct banks.
+constexpr int kInvThreads = 128;
+
+__device__ __forceinline__ int inv_stage(const InvArgs& a, float* sA, long long& r0) {
+    const long long nrows = (long long)(a.range[a.t1] - a.range[a.t0]) * a.NP;
+    r0 = (long long)blockIdx.x * kInvThreads;
+    if (r0 >= nrows) return 0;
+    const int nr = (int)min((long long)kInvThreads, nrows - r0);
+    const int KS = a.K | 1;
+    const float* Ab = a.A + r0 * a.K;
+    for (int e = threadIdx.x; e < nr * a.K; e += kInvThreads) {
+        const int r = e / a.K;
+        sA[r * KS + (e - r * a.K)] = Ab[e];
+    }
+    return nr;
+}
+
+__global__ void __launch_bounds__(kInvThreads) k_inv_fwd(InvArgs a) {
     pdl_enter();
-    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
-    if (s0 + w >= s1) return;
-    float* out = a.fp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
-    for (int p = lane; p < a.NP; p += 32) {
-        const float* Ap = a.A + ((size_t)w * a.NP + p) * a.K;
-        for (int c = 0; c < a.ncol; ++c) {
-            float s = 0.f;
-            for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
-                const int4 t = a.idx[q];
-                float v = a.coef[q] * Ap[t.x] * Ap[t.y] * Ap[t.z];
-                if (t.w >= 0) v *= Ap[t.w];
-                s += v;
-            }
-            out[p * a.sl + a.nl2 + c] = s;
+    extern __shared__ float sA[];  // [kInvThreads][K | 1]
+    long long r0;
+    const int nr = inv_stage(a, sA, r0);
+    if (!nr) return;
+    __syncthreads();
+    const int r = threadIdx.x;
+    if (r >= nr) return;
+    const long long row = r0 + r;
+    const int w = (int)(row / a.NP), p = (int)(row - (long long)w * a.NP);
+    const float* Ap = sA + r * (a.K | 1);
+    float* out = a.fp + (size_t)(a.range[a.t0] + w) * a.fp_stride + a.fp_off + p * a.sl + a.nl2;
+    for (int c = 0; c < a.ncol; ++c) {
+        float s = 0.f;
+        for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
+            const int4 t = a.idx[q];
+            float v = a.coef[q] * Ap[t.x] * Ap[t.y] * Ap[t.z];
+            if (t.w >= 0) v *= Ap[t.w];
+            s += v;
         }
+        out[c] = s;
     }
 }
 
-__global__ void __launch_bounds__(128) k_inv_bwd(InvArgs a) {
+__global__ void __launch_bounds__(kInvThreads) k_inv_bwd(InvArgs a) {
     pdl_enter();
-    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    const int s0 = a.range[a.t0], s1 = a.range[a.t1];
-    if (s0 + w >= s1) return;
-    const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
-    for (int p = lane; p < a.NP; p += 32) {
-        const float* Ap = a.A + ((size_t)w * a.NP + p) * a.K;
-        float* Gp = a.Gx + ((size_t)w * a.NP + p) * a.K;
-        for (int k = 0; k < a.K; ++k) Gp[k] = 0.f;
+    extern __shared__ float sA[];  // [kInvThreads][K | 1] A rows, then as many dE/dA rows
+    const int KS = a.K | 1;
+    float* sG = sA + kInvThreads * KS;
+    long long r0;
+    const int nr = inv_stage(a, sA, r0);
+    if (!nr) return;
+    for (int e = threadIdx.x; e < kInvThreads * KS; e += kInvThreads) sG[e] = 0.f;
+    __syncthreads();
+    const int r = threadIdx.x;
+    if (r < nr) {
+        const long long row = r0 + r;
+        const int w = (int)(row / a.NP), p = (int)(row - (long long)w * a.NP);
+        const float* Ap = sA + r * KS;
+        float* Gp = sG + r * KS;
+        const float* gf = a.gfp + (size_t)(a.range[a.t0] + w) * a.fp_stride + a.fp_off + p * a.sl + a.nl2;
         for (int c = 0; c < a.ncol; ++c) {
-            const float g = gf[p * a.sl + a.nl2 + c];
+            const float g = gf[c];
             for (int q = a.start[c]; q < a.start[c + 1]; ++q) {
                 const int4 t = a.idx[q];
                 const float cg = g * a.coef[q];
@@ -782,6 +852,12 @@ __global__ void __launch_bounds__(128) k_inv_bwd(InvArgs a) {
                 }
             }
         }
+    }
+    __syncthreads();
+    float* Gb = a.Gx + r0 * a.K;
+    for (int e = threadIdx.x; e < nr * a.K; e += kInvThreads) {
+        const int rr = e / a.K;
+        Gb[e] = sG[rr * KS + (e - rr * a.K)];
     }
 }
 
@@ -878,9 +954,18 @@ cudaError_t launch_invariants_wgrad(const InvArgs& a, cudaStream_t st) {
 
 cudaError_t launch_invariants(const InvArgs& a, bool fwd, cudaStream_t st) {
     if (a.nmax <= 0 || a.ncol <= 0) return cudaSuccess;
-    const int grid = (a.nmax + 3) / 4;
-    if (fwd) return launch_pdl(&k_inv_fwd, dim3(grid), dim3(128), 0, st, a);
-    return launch_pdl(&k_inv_bwd, dim3(grid), dim3(128), 0, st, a);
+    const int grid = (int)(((long long)a.nmax * a.NP + kInvThreads - 1) / kInvThreads);
+    const size_t sm = sizeof(float) * kInvThreads * (a.K | 1) * (fwd ? 1 : 2);
+    static int limit_fwd = 0, limit_bwd = 0;  // raised once, before any graph capture
+    int& lim = fwd ? limit_fwd : limit_bwd;
+    if ((int)sm > lim && sm > 48 * 1024) {
+        const cudaError_t e = fwd ? cudaFuncSetAttribute(k_inv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
+                                  : cudaFuncSetAttribute(k_inv_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        lim = (int)sm;
+    }
+    if (fwd) return launch_pdl(&k_inv_fwd, dim3(grid), dim3(kInvThreads), sm, st, a);
+    return launch_pdl(&k_inv_bwd, dim3(grid), dim3(kInvThreads), sm, st, a);
 }
 
 // =========================================================================== dispatch

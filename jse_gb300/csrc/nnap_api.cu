@@ -137,6 +137,14 @@ void upload_model(nnap_handle* h) {
                     CK(cudaMemcpy(r.falpha.back().p, al.data(), al.size() * sizeof(float), cudaMemcpyHostToDevice));
                 }
             }
+            // a spherical sub-basis after the first, on the channel-space kernels, with a cutoff
+            // well inside the neighbour cutoff scans compact rows (one such cutoff per model)
+            {
+                const bool pspace = !sparse && !r.falpha.back().p;
+                bool use = s.kind == KIND_SPHERICAL && k > 0 && pspace && s.rcut <= 0.85 * m.rcut_max;
+                if (use && h->sub_rc == 0.0) h->sub_rc = s.rcut;
+                r.use_sub.push_back(use && s.rcut == h->sub_rc);
+            }
             r.nzp.emplace_back();
             r.nzw.emplace_back();
             if (sparse) {
@@ -236,6 +244,8 @@ float screen_bound(const StructDev& s, double rc, int Rm) {
     return (float)(rc * rc + margin) * (1.0f + 1e-6f);
 }
 
+constexpr double kHalfCellAtoms = 20.0;  // atoms per rc^3 from which cells are rc/2 wide
+
 StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0) {
     if (kind < 0 || kind > 2) throw ApiFail(NNAP_ERR_ARG, "box_kind must be 0, 1 or 2");
     StructDev s;
@@ -255,8 +265,12 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
     if (!(s.vol > 0.0) || !std::isfinite(s.vol)) throw ApiFail(NNAP_ERR_ARG, "box must be right-handed with positive volume");
     auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
     const double h[3] = {s.vol / nrm(s.bc), s.vol / nrm(s.ca), s.vol / nrm(s.ab)};
+    // cells at least rc wide, or rc/2 wide where an rc^3 volume holds many atoms: the
+    // 5^3-cell stencil, trimmed by each cell's distance bound, visits about half the
+    // candidates of the 3^3 stencil
+    const int div = (double)n / s.vol * rc * rc * rc >= kHalfCellAtoms ? 2 : 1;
     for (int d = 0; d < 3; ++d) {
-        s.nc[d] = std::max(1, (int)std::floor(h[d] / rc));
+        s.nc[d] = std::max(1, (int)std::floor(h[d] * div / rc));
         s.nc[d] = std::min(s.nc[d], 1024);
         s.R[d] = (int)std::floor(rc * s.nc[d] / h[d] + 1e-6) + 1;
         if (s.R[d] > 64) throw ApiFail(NNAP_ERR_ARG, "box too thin for the cutoff");
@@ -315,6 +329,11 @@ void grow_pairs(nnap_handle* h, int n, int M) {
     h->pg.ensure(np);
     h->prev.ensure(np);
     h->pgrp.ensure(np);
+    if (h->sub_rc > 0.0) {
+        h->sdx.ensure(np);
+        h->spos.ensure(np);
+        h->scount.ensure(std::max(n, 1));
+    }
 }
 
 PairBufs pair_bufs(nnap_handle* h) {
@@ -473,6 +492,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     cudaStream_t st = h->stream;
     if (n > 0) CK(cudaMemsetAsync(h->fp.p, 0, sizeof(float) * (size_t)n * h->fp_stride, st));
     // descriptors, per run of species sharing a basis shape and per sub-basis
+    // compact rows for the sub-bases that scan them (once per evaluation)
+    bool sub_built = false;
     auto descriptors = [&](bool fwd) {
         size_t a_off = 0;
         for (auto& r : h->runs) {
@@ -507,6 +528,19 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.fwd_alpha = r.falpha[k].p;
                 a.nl2 = s.nl2;
                 a.sl = s.nl2 + s.ninv;
+                a.sub_dx = nullptr;
+                a.sub_pos = nullptr;
+                a.sub_count = nullptr;
+                if (r.use_sub[k] && n > 0) {
+                    if (!sub_built) {
+                        CK(launch_subrows(a.P, n, (float)h->sub_rc, h->sdx.p, h->spos.p, h->scount.p, st));
+                        ++h->launches;
+                        sub_built = true;
+                    }
+                    a.sub_dx = h->sdx.p;
+                    a.sub_pos = h->spos.p;
+                    a.sub_count = h->scount.p;
+                }
                 // invariant columns: forward after the expansion, their dE/dA before the backward
                 InvArgs ia;
                 std::memset(&ia, 0, sizeof ia);
@@ -954,6 +988,7 @@ int nnap_destroy(nnap_handle* h) {
     h->type_start.release(); h->chunk_b.release(); h->chunk_e.release(); h->struct_chunks.release();
     h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->Gx.release(); h->gstart.release();
+    h->sdx.release(); h->spos.release(); h->scount.release();
     for (auto* b : {&h->lmp_x, &h->lmp_forces, &h->lmp_virials}) b->release();
     for (auto* b : {&h->lmp_type, &h->lmp_ilist, &h->lmp_off, &h->lmp_idx, &h->lmp_rowtype, &h->lmp_rowof,
                     &h->lmp_tcount, &h->lmp_tstart, &h->lmp_tfill, &h->lmp_tlist})

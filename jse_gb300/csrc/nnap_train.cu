@@ -192,6 +192,9 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
             a.nl2 = s.nl2;
             a.sl = s.nl2 + s.ninv;
             a.Gx = nullptr;
+            a.sub_dx = nullptr;
+            a.sub_pos = nullptr;
+            a.sub_count = nullptr;
             ja.bF = dbF;
             ja.bW = dbW;
             ja.sid = h->sid.p;

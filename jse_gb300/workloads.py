@@ -213,3 +213,37 @@ def c5_pool(count: int = 512, seed: int = 5, sigma: float = 1.0) -> List[Structu
         n = int(min(20000, max(50, round(math.exp(math.log(500.0) + sigma * rng.standard_normal())))))
         out.append(random_liquid(n, 0.060, [0.46, 0.46, 0.08], 2.0, seed * 100003 + k))
     return out
+
+
+def random_nep_text(symbols: Sequence[str], version: int = 4, rc=(8.0, 4.0), n_max=(4, 4), basis=(8, 8),
+                    l_max=(4, 2, 1), neurons: int = 30, seed: int = 0) -> str:
+    """A seeded random NEP potential file (nep.txt) of the given hyperparameters (defaults:
+    GPUMD's nep.in defaults, cutoff 8 / 4 A, n_max 4 4, basis_size 8 8, l_max 4 2 1, 30
+    neurons).  Network weights ~ N(0, 1/dim), descriptor coefficients ~ U(-1, 1), descriptor
+    scales ~ U(0.5, 2)."""
+    rng = np.random.default_rng(seed)
+    T = len(symbols)
+    numL = l_max[0] + (1 if l_max[1] == 2 else 0) + (1 if l_max[2] == 1 else 0)
+    dim = (n_max[0] + 1) + (n_max[1] + 1) * numL
+    if version == 3:
+        nann = (dim + 2) * neurons + 1
+    elif version == 4:
+        nann = (dim + 2) * neurons * T + 1
+    else:
+        nann = ((dim + 2) * neurons + 1) * T + 1
+    ndesc = T * T * ((n_max[0] + 1) * (basis[0] + 1) + (n_max[1] + 1) * (basis[1] + 1))
+    vals = np.concatenate([rng.normal(0.0, 1.0 / math.sqrt(dim), nann), rng.uniform(-1.0, 1.0, ndesc),
+                           rng.uniform(0.5, 2.0, dim)])
+    head = ["nep%d %d %s" % (version, T, " ".join(symbols)), "cutoff %g %g 100 100" % tuple(rc),
+            "n_max %d %d" % tuple(n_max), "basis_size %d %d" % tuple(basis), "l_max %d %d %d" % tuple(l_max),
+            "ANN %d 0" % neurons]
+    return "\n".join(head + ["%.17g" % v for v in vals]) + "\n"
+
+
+# NEP benchmark: a binary liquid at 0.060 /A^3 under a nep4 potential of GPUMD's default
+# hyperparameters.
+NEP_BENCH_ATOMS = 32000
+
+
+def nep_bench(n: int = NEP_BENCH_ATOMS, seed: int = 21):
+    return random_nep_text(["Si", "O"], seed=seed), random_liquid(n, 0.060, [0.5, 0.5], 2.0, seed)
