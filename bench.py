@@ -23,6 +23,7 @@ has no collective); value = atoms of all ranks / max-over-ranks time.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import os
@@ -314,6 +315,94 @@ def train_measurement(device: int, s, model: dict, steps: int = 5, cpu: bool = T
     return out
 
 
+# ----------------------------------------------------------------------------- reference GPU kernels
+def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int = 10) -> dict:
+    """The reference's own CUDA kernels (nnap_interface_cuda.cu, FP32, one thread per atom;
+    oracle/ref_cuda.py) beside this build's, on the LAMMPS form of the same structure (local
+    atoms, ghost atoms, full neighbour lists from nnap_neighbor_list).
+    ``lammps_e2e``: one call of each LAMMPS boundary per step with host arrays in and out
+    (reference: jse_nnap_lammps2cuda + jse_nnap_computeLammpsCuda + jse_nnap_cuda2lammps,
+    lists sent every step; this build: nnap_compute_lammps).  ``kernels``: the reference's
+    jse_nnap_computeLammpsCuda with its inputs on the device (its memsets, three kernels and
+    closing synchronisation) against this build's device-resident nnap_compute_device on the
+    periodic structure, which also builds its own neighbour list.  L2 flushed between steps."""
+    import torch
+    from jse_gb300.nnap import NNAP, WANT_ENERGY, WANT_FORCES, WANT_VIRIAL, _dptr, _iptr
+    from oracle import ref_cuda as RC
+    dev = torch.device("cuda", device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    n = s.natoms
+    out = {"unit": "atom-evals/s", "atoms": n, "reference": "nnap_interface_cuda.cu kernels compiled for sm_103a "
+           "(-O3), FP32, driven through their own host functions", "precision_ours": precision}
+
+    def timed(fn, k):
+        for _ in range(2):
+            fn()
+        dts = []
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize(dev)
+            dts.append(time.perf_counter() - t0)
+        return n * k / sum(dts), 1e3 * sum(dts) / k
+    with NNAP(model, precision=precision, device=device) as p:
+        off, j, img = p.neighborList(s)
+        x, t, lists, owner = W.lammps_form(s, off, j, img)
+        nall = len(x)
+        out["ghosts"] = nall - n
+        out["mean_neighbours"] = float(len(j)) / n
+        il = np.arange(n, dtype=np.int32)
+        rows = [np.ascontiguousarray(l, dtype=np.int32) for l in lists] + [np.zeros(0, np.int32)] * (nall - n)
+        num = np.array([len(r) for r in rows], dtype=np.int32)
+        ptrs = (C.POINTER(C.c_int) * nall)(*[_iptr(r) for r in rows])
+        xh = np.ascontiguousarray(x)
+        f, eng, eatom, vir = np.zeros((nall, 3)), np.zeros(1), np.zeros(nall), np.zeros(6)
+
+        def ours_lmp():
+            p._check(p._L.nnap_compute_lammps(p._handle(), n, nall, _iptr(il), _iptr(num), ptrs, _dptr(xh), _iptr(t),
+                                              None, 1, 1, 1, 0, 0, _dptr(f), _dptr(eng), _dptr(eatom), _dptr(vir),
+                                              None, None))
+        v, ms = timed(ours_lmp, steps)
+        out["ours_lammps_e2e"] = {"value": v, "ms_per_step": ms}
+        x_d = torch.from_numpy(np.ascontiguousarray(s.x)).to(dev)
+        t_d = torch.from_numpy(np.ascontiguousarray(s.types, dtype=np.int32)).to(dev)
+        e_d = torch.zeros(1, dtype=torch.float64, device=dev)
+        f_d = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+        v_d = torch.zeros(9, dtype=torch.float64, device=dev)
+
+        def ours_dev():
+            p.computeDevice(n, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, WANT_ENERGY | WANT_FORCES | WANT_VIRIAL,
+                            e_d.data_ptr(), 0, f_d.data_ptr(), v_d.data_ptr(), 0,
+                            stream=torch.cuda.current_stream(dev).cuda_stream)
+        v, ms = timed(ours_dev, steps)
+        out["ours_kernels"] = {"value": v, "ms_per_step": ms}
+        for a in (f, eng, eatom, vir):  # the LAMMPS boundary accumulates, like a pair style
+            a[...] = 0.0
+        ours_lmp()
+        f_ours = f[:n].copy()
+        np.add.at(f_ours, owner, f[n:])
+    try:
+        ref = RC.RefCudaNNAP(model, device)
+    except (FileNotFoundError, RuntimeError, OSError, ValueError) as ex:
+        out["reference_error"] = str(ex)[:200]
+        return out
+    ref.setup(x, t, n, lists)
+    v, ms = timed(ref.step, steps)
+    out["ref_lammps_e2e"] = {"value": v, "ms_per_step": ms}
+    ref.to_device(True)
+    v, ms = timed(ref.compute, steps)
+    out["ref_kernels"] = {"value": v, "ms_per_step": ms}
+    r = ref.step()
+    f_ref = r["forces"][:n].copy()
+    np.add.at(f_ref, owner, r["forces"][n:])
+    out["max_abs_force_difference"] = float(np.abs(f_ref - f_ours).max())
+    out["speedup_lammps_e2e"] = out["ours_lammps_e2e"]["value"] / out["ref_lammps_e2e"]["value"]
+    out["speedup_kernels"] = out["ours_kernels"]["value"] / out["ref_kernels"]["value"]
+    return out
+
+
 # ----------------------------------------------------------------------------- NEP
 def nep_measurement(device: int, steps: int = 10, cpu: bool = True) -> dict:
     """NEP potential through nnap_create_nep on the NEP benchmark: a 32000-atom binary liquid
@@ -425,6 +514,8 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-train", action="store_true", help="skip the training-gradient measurement")
     ap.add_argument("--no-nep", action="store_true", help="skip the NEP measurement")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="skip the reference-CUDA-kernel comparison")
+    ap.add_argument("--only-ref-gpu", action="store_true", help="run only the reference-CUDA-kernel comparison")
     ap.add_argument("--only-nep", action="store_true", help="run only the NEP measurement (profiling runs)")
     ap.add_argument("--only-train", action="store_true", help="run only the training-gradient measurement "
                     "(profiling runs)")
@@ -473,6 +564,11 @@ def main():
     from jse_gb300.nnap import NNAP, WANT_ENERGY, WANT_FORCES, WANT_VIRIAL
     torch.cuda.set_device(local)
     model = normalised_model(cfg, structures, args.precision)
+    if args.only_ref_gpu:
+        if rank == 0:
+            print(json.dumps({"reference_gpu": ref_gpu_measurement(local, structures[0], model, args.precision,
+                                                                   steps=args.steps)}))
+        return
     if args.only_train:
         if rank == 0:
             print(json.dumps({"training": train_measurement(local, structures[0], model, steps=args.steps,
@@ -600,6 +696,9 @@ def main():
     training = None
     if rank == 0 and not args.no_train and args.workload == "liquid32k":
         training = train_measurement(local, s, model, cpu=not args.no_cpu_baseline)
+    ref_gpu = None
+    if rank == 0 and not args.no_ref_gpu and args.workload == "liquid32k":
+        ref_gpu = ref_gpu_measurement(local, s, model, args.precision)
     nep = None
     if rank == 0 and not args.no_nep and args.workload == "liquid32k":
         nep = nep_measurement(local, cpu=not args.no_cpu_baseline)
@@ -647,6 +746,8 @@ def main():
             line["training"] = training
         if nep is not None:
             line["nep"] = nep
+        if ref_gpu is not None:
+            line["reference_gpu"] = ref_gpu
         print(json.dumps(line))
     pot.close()
     if dist:

@@ -87,6 +87,26 @@ struct DevBuf {
     }
 };
 
+// Pinned host staging grown on demand.
+struct Pinned {
+    void* p = nullptr;
+    size_t cap = 0;
+    void* ensure(size_t n) {
+        if (n <= cap) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        CK(cudaMallocHost(&p, std::max<size_t>(n, 256)));
+        cap = std::max<size_t>(n, 256);
+        return p;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
 struct SubShape {
     int kind, lmax, np, n1;
     double rcut;
@@ -175,6 +195,7 @@ struct nnap_handle {
     int M = 0;
     // LAMMPS-style boundary: caller's atoms (local + ghost), list, targets of the scatter
     nnapgb::DevBuf<double> lmp_x, lmp_forces, lmp_virials;
+    nnapgb::Pinned lmp_pin_in, lmp_pin_out;  // per-call layout arrays in, results out
     nnapgb::DevBuf<int> lmp_type, lmp_ilist, lmp_off, lmp_idx, lmp_rowtype, lmp_rowof, lmp_tcount, lmp_tstart,
         lmp_tfill, lmp_tlist;
     // force-training gradients: directional derivatives, upstream gradients, per-slot

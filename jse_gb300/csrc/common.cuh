@@ -47,6 +47,8 @@ __host__ __device__ inline void unpack_img(uint32_t p, int& na, int& nb, int& nc
 __host__ __device__ inline uint64_t pair_key(int j, uint32_t img) { return ((uint64_t)(uint32_t)j << 32) | img; }
 
 // Device buffers of one evaluation (all owned by the handle; see nnap_api.cu).
+constexpr int kLmpSumThreads = 256;  // threads of the LAMMPS global-virial sum
+
 struct PairBufs {
     int M;                 // neighbour capacity per atom (row stride)
     uint64_t* key;         // [n*M] (j << 32) | packed image

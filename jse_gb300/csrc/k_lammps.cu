@@ -143,3 +143,29 @@ __global__ void k_lmp_gather(PairBufs P, int nall, const int* __restrict__ row_o
 }
 
 }  // namespace nnapgb
+
+namespace nnapgb {
+
+// Global virial: the first six components of every atom's virial summed in double in a
+// fixed order (thread t takes atoms t, t + blockDim, ...; then a tree over the threads).
+__global__ void __launch_bounds__(kLmpSumThreads) k_lmp_virial_sum(const double* __restrict__ virials, int nall,
+                                                                   double* __restrict__ out) {
+    __shared__ double s[6][kLmpSumThreads];
+    const int t = threadIdx.x;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int a = t; a < nall; a += kLmpSumThreads)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] += virials[9 * (size_t)a + c];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s[c][t] = acc[c];
+    __syncthreads();
+    for (int w = kLmpSumThreads / 2; w > 0; w >>= 1) {
+        if (t < w)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s[c][t] += s[c][t + w];
+        __syncthreads();
+    }
+    if (t < 6) out[t] = s[t][0];
+}
+
+}  // namespace nnapgb

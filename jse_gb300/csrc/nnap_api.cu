@@ -990,6 +990,8 @@ int nnap_destroy(nnap_handle* h) {
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->Gx.release(); h->gstart.release();
     h->sdx.release(); h->spos.release(); h->scount.release();
     for (auto* b : {&h->lmp_x, &h->lmp_forces, &h->lmp_virials}) b->release();
+    h->lmp_pin_in.release();
+    h->lmp_pin_out.release();
     for (auto* b : {&h->lmp_type, &h->lmp_ilist, &h->lmp_off, &h->lmp_idx, &h->lmp_rowtype, &h->lmp_rowof,
                     &h->lmp_tcount, &h->lmp_tstart, &h->lmp_tfill, &h->lmp_tlist})
         b->release();

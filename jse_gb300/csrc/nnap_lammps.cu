@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "api_internal.hpp"
@@ -17,12 +18,15 @@ __global__ void k_lmp_rows(int, int, const int*, const int*, const int*, const d
 __global__ void k_lmp_count(PairBufs, int, int*);
 __global__ void k_lmp_fill(PairBufs, int, const int*, int*, int*);
 __global__ void k_lmp_gather(PairBufs, int, const int*, const int*, const int*, double*, double*);
+__global__ void k_lmp_virial_sum(const double*, int, double*);
 }  // namespace nnapgb
 
 using namespace nnapgb;
 
 namespace {
 constexpr int kLmpNeighMask = 0x1FFFFFFF;  // LAMMPS keeps special-bond bits above this mask
+constexpr size_t kLmpThreadedEntries = 1 << 18;  // list entries from which the copy is threaded
+constexpr unsigned kLmpMaxThreads = 8;
 }
 
 extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int* ilist, const int* numneigh,
@@ -41,23 +45,57 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         if (cvflag_atom && !cvatom) throw ApiFail(NNAP_ERR_ARG, "centroid per-atom virials are NULL");
         h->launches = 0;
         if (nall == 0) return NNAP_OK;
-        // host-side layout: species through the type map, the list in ilist order
-        std::vector<int> ty((size_t)nall), row_of((size_t)nall, -1), off((size_t)inum + 1, 0);
-        for (int a = 0; a < nall; ++a) ty[a] = type_map ? type_map[type[a]] : type[a];
+        // host-side layout, written straight into pinned staging: species through the type
+        // map, the row of each local atom, the list in ilist order
+        size_t total = 0;
         int deg_max = 0;
         for (int ii = 0; ii < inum; ++ii) {
             const int i = ilist[ii];
-            if (i < 0 || i >= nall || row_of[i] >= 0) throw ApiFail(NNAP_ERR_ARG, "ilist entries must be distinct atoms");
-            row_of[i] = ii;
+            if (i < 0 || i >= nall) throw ApiFail(NNAP_ERR_ARG, "ilist entries must be distinct atoms");
             if (numneigh[i] < 0) throw ApiFail(NNAP_ERR_ARG, "negative neighbour count");
-            off[ii + 1] = off[ii] + numneigh[i];
+            total += (size_t)numneigh[i];
             deg_max = std::max(deg_max, numneigh[i]);
         }
-        const size_t total = (size_t)off[inum];
-        std::vector<int> nidx(std::max<size_t>(total, 1));
+        if (total > (size_t)INT32_MAX) throw ApiFail(NNAP_ERR_CAPACITY, "more than 2^31 neighbour entries");
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        const size_t in_bytes = 2 * al(sizeof(int) * nall) + al(sizeof(int) * ((size_t)inum + 1)) +
+                                al(sizeof(int) * std::max<size_t>(total, 1));
+        char* pin = static_cast<char*>(h->lmp_pin_in.ensure(in_bytes));
+        int* ty = reinterpret_cast<int*>(pin);
+        int* row_of = reinterpret_cast<int*>(pin + al(sizeof(int) * nall));
+        int* off = reinterpret_cast<int*>(pin + 2 * al(sizeof(int) * nall));
+        int* nidx = reinterpret_cast<int*>(pin + 2 * al(sizeof(int) * nall) + al(sizeof(int) * ((size_t)inum + 1)));
+        for (int a = 0; a < nall; ++a) {
+            ty[a] = type_map ? type_map[type[a]] : type[a];
+            row_of[a] = -1;
+        }
+        off[0] = 0;
         for (int ii = 0; ii < inum; ++ii) {
             const int i = ilist[ii];
-            for (int jj = 0; jj < numneigh[i]; ++jj) nidx[off[ii] + jj] = firstneigh[i][jj] & kLmpNeighMask;
+            if (row_of[i] >= 0) throw ApiFail(NNAP_ERR_ARG, "ilist entries must be distinct atoms");
+            row_of[i] = ii;
+            off[ii + 1] = off[ii] + numneigh[i];
+        }
+        // the list copy (the bulk of the host work) in contiguous ranges of ilist, one per thread
+        auto copy_rows = [&](int a, int b) {
+            for (int ii = a; ii < b; ++ii) {
+                const int i = ilist[ii];
+                const int* src = firstneigh[i];
+                int* dst = nidx + off[ii];
+                for (int jj = 0, c = numneigh[i]; jj < c; ++jj) dst[jj] = src[jj] & kLmpNeighMask;
+            }
+        };
+        const int nth = total >= kLmpThreadedEntries
+                            ? (int)std::min<unsigned>(kLmpMaxThreads, std::max(1u, std::thread::hardware_concurrency()))
+                            : 1;
+        if (nth > 1) {
+            std::vector<std::thread> th;
+            for (int k = 1; k < nth; ++k)
+                th.emplace_back(copy_rows, (int)((long long)inum * k / nth), (int)((long long)inum * (k + 1) / nth));
+            copy_rows(0, inum / nth);
+            for (auto& t : th) t.join();
+        } else {
+            copy_rows(0, inum);
         }
         // device buffers: rows for the local atoms at capacity = longest list
         const int n1 = std::max(inum, 1);
@@ -82,13 +120,13 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         cudaStream_t st = h->stream;
         const int T = h->model.ntypes();
         CK(cudaMemcpyAsync(h->lmp_x.p, x, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(h->lmp_type.p, ty.data(), sizeof(int) * nall, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(h->lmp_rowof.p, row_of.data(), sizeof(int) * nall, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->lmp_type.p, ty, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->lmp_rowof.p, row_of, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
         if (inum) {
             CK(cudaMemcpyAsync(h->lmp_ilist.p, ilist, sizeof(int) * inum, cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(h->lmp_off.p, off.data(), sizeof(int) * (inum + 1), cudaMemcpyHostToDevice, st));
+            CK(cudaMemcpyAsync(h->lmp_off.p, off, sizeof(int) * (inum + 1), cudaMemcpyHostToDevice, st));
         }
-        if (total) CK(cudaMemcpyAsync(h->lmp_idx.p, nidx.data(), sizeof(int) * total, cudaMemcpyHostToDevice, st));
+        if (total) CK(cudaMemcpyAsync(h->lmp_idx.p, nidx, sizeof(int) * total, cudaMemcpyHostToDevice, st));
         CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
         CK(cudaMemsetAsync(h->lmp_tcount.p, 0, sizeof(int) * nall, st));
         CK(cudaMemsetAsync(h->lmp_tfill.p, 0, sizeof(int) * nall, st));
@@ -121,17 +159,28 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
                                                          h->lmp_tlist.p, h->lmp_forces.p, h->lmp_virials.p);
         h->launches += 3;
         CK(cudaGetLastError());
-        // results back and into LAMMPS's accumulators
-        std::vector<double> fo(3 * (size_t)nall), eo((size_t)n1), vo;
-        const bool want_v = vflag || vflag_atom || cvflag_atom;
-        CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
-        CK(cudaMemcpyAsync(fo.data(), h->lmp_forces.p, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, st));
-        if ((eflag || eflag_atom) && inum)
-            CK(cudaMemcpyAsync(eo.data(), h->e_atom.p, sizeof(double) * inum, cudaMemcpyDeviceToHost, st));
-        if (want_v) {
-            vo.resize(9 * (size_t)nall);
-            CK(cudaMemcpyAsync(vo.data(), h->lmp_virials.p, sizeof(double) * 9 * nall, cudaMemcpyDeviceToHost, st));
+        // results back (pinned) and into LAMMPS's accumulators; a global virial alone is
+        // summed on the device in a fixed order
+        const bool per_atom_v = vflag_atom || cvflag_atom;
+        if (vflag && !per_atom_v) {
+            k_lmp_virial_sum<<<1, kLmpSumThreads, 0, st>>>(h->lmp_virials.p, nall, h->virial.p);
+            ++h->launches;
+            CK(cudaGetLastError());
         }
+        const size_t out_bytes = al(sizeof(double) * 3 * nall) + al(sizeof(double) * n1) +
+                                 al(sizeof(double) * (per_atom_v ? 9 * (size_t)nall : 9));
+        char* pout = static_cast<char*>(h->lmp_pin_out.ensure(out_bytes));
+        double* fo = reinterpret_cast<double*>(pout);
+        double* eo = reinterpret_cast<double*>(pout + al(sizeof(double) * 3 * nall));
+        double* vo = reinterpret_cast<double*>(pout + al(sizeof(double) * 3 * nall) + al(sizeof(double) * n1));
+        CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(fo, h->lmp_forces.p, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, st));
+        if ((eflag || eflag_atom) && inum)
+            CK(cudaMemcpyAsync(eo, h->e_atom.p, sizeof(double) * inum, cudaMemcpyDeviceToHost, st));
+        if (per_atom_v)
+            CK(cudaMemcpyAsync(vo, h->lmp_virials.p, sizeof(double) * 9 * nall, cudaMemcpyDeviceToHost, st));
+        else if (vflag)
+            CK(cudaMemcpyAsync(vo, h->virial.p, sizeof(double) * 6, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         const int bits = h->h_status[0];
         if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
@@ -143,9 +192,9 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
             for (int ii = 0; ii < inum; ++ii) *eng_vdwl += eo[ii];
         if (eflag_atom)
             for (int ii = 0; ii < inum; ++ii) eatom[ilist[ii]] += eo[ii];
-        if (want_v) {
+        if (per_atom_v) {
             for (int a = 0; a < nall; ++a) {
-                const double* w = vo.data() + 9 * (size_t)a;
+                const double* w = vo + 9 * (size_t)a;
                 if (vflag)
                     for (int c = 0; c < 6; ++c) virial[c] += w[c];
                 if (vflag_atom)
@@ -153,6 +202,8 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
                 if (cvflag_atom)
                     for (int c = 0; c < 9; ++c) cvatom[9 * (size_t)a + c] += w[c];
             }
+        } else if (vflag) {
+            for (int c = 0; c < 6; ++c) virial[c] += vo[c];
         }
         return NNAP_OK;
     });

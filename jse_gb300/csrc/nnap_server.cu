@@ -60,26 +60,6 @@ struct ServerSlot {
     long long last_stamp = -1;  // last step call that listed it
 };
 
-// Pinned host staging grown on demand.
-struct Pinned {
-    void* p = nullptr;
-    size_t cap = 0;
-    void* ensure(size_t n) {
-        if (n <= cap) return p;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-        CK(cudaMallocHost(&p, std::max<size_t>(n, 256)));
-        cap = std::max<size_t>(n, 256);
-        return p;
-    }
-    void release() {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
 }  // namespace
 
 struct nnap_server {

@@ -247,3 +247,30 @@ NEP_BENCH_ATOMS = 32000
 
 def nep_bench(n: int = NEP_BENCH_ATOMS, seed: int = 21):
     return random_nep_text(["Si", "O"], seed=seed), random_liquid(n, 0.060, [0.5, 0.5], 2.0, seed)
+
+
+def lammps_form(s: Structure, offsets, j, img):
+    """A structure in the form LAMMPS hands a pair style: the local atoms, then one ghost
+    atom per (atom, periodic image) that appears in a full neighbour list, and per local
+    atom the list of its neighbours as indices into local + ghost atoms.  ``offsets, j,
+    img`` is a full neighbour list of ``s`` with image offsets (``NNAP.neighborList``);
+    the positions must lie inside the box (direct coordinates in [0, 1)), as the list's
+    images refer to wrapped positions.  Returns (x_all, types_all, lists, owner) with
+    owner[g] the local atom of ghost n + g."""
+    x = np.asarray(s.x, dtype=np.float64).reshape(-1, 3)
+    box = np.asarray(s.box, dtype=np.float64).reshape(3, 3)
+    frac = x @ np.linalg.inv(box)
+    if (frac < 0.0).any() or (frac >= 1.0).any():
+        raise ValueError("positions must lie inside the box")
+    n = len(x)
+    j = np.asarray(j, dtype=np.int64)
+    img = np.asarray(img, dtype=np.int64).reshape(-1, 3)
+    shifted = img.any(axis=1)
+    keys, inv = np.unique(np.column_stack([j[shifted], img[shifted]]), axis=0, return_inverse=True)
+    idx = j.copy()
+    idx[shifted] = n + inv.reshape(-1)
+    x_all = np.concatenate([x, x[keys[:, 0]] + keys[:, 1:] @ box]) if len(keys) else x.copy()
+    types = np.asarray(s.types, dtype=np.int32)
+    t_all = np.concatenate([types, types[keys[:, 0]]]) if len(keys) else types.copy()
+    lists = np.split(idx.astype(np.int32), np.asarray(offsets[1:-1], dtype=np.int64))
+    return x_all, t_all.astype(np.int32), lists, keys[:, 0].astype(np.int64) if len(keys) else np.zeros(0, np.int64)

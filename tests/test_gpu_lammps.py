@@ -93,3 +93,22 @@ def test_lammps_rejects_bad_indices():
             p.computeLammps(np.arange(s.natoms), lists, s.x, s.types)
         with pytest.raises(NNAPError):
             p.computeLammps(np.array([0, 0]), lists, s.x, s.types)  # duplicate ilist entry
+
+
+def test_lammps_large_list_global_virial_only():
+    """A list of more than 2^18 entries (the host copy runs on several threads) with only
+    the global virial requested (summed on the device)."""
+    from jse_gb300.nnap import NNAP
+    s = W.random_liquid(6000, 0.060, [0.46, 0.46, 0.08], 2.0, 74, tilt=0.1)
+    model = W.model_for("c2")
+    with NNAP(model, precision="mixed") as p:
+        x, types, lists, owner, xw = _lammps_form(s, p.rcutMax() + 0.4)
+        n = s.natoms
+        assert sum(len(l) for l in lists) > (1 << 18)
+        out = p.computeLammps(np.arange(n), lists, x, types, cvflag_atom=False)
+        full = p.computeLammps(np.arange(n), lists, x, types, cvflag_atom=True)
+        ref = p.calEnergyForceVirials(W.Structure(xw, s.types, s.box, s.box_kind))
+    assert np.array_equal(out["forces"], full["forces"]) and out["eng"] == full["eng"]
+    assert np.max(np.abs(out["virial"] - full["virial"])) <= 1e-9 * max(1.0, np.abs(full["virial"]).max())
+    assert np.max(np.abs(out["virial"] - ref["virial"][:6])) <= V_TOL * n ** 0.5
+    assert np.max(np.abs(_reverse(out["forces"], n, owner) - ref["forces"])) <= F_TOL
