@@ -322,7 +322,9 @@ def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int 
     atoms, ghost atoms, full neighbour lists from nnap_neighbor_list).
     ``lammps_e2e``: one call of each LAMMPS boundary per step with host arrays in and out
     (reference: jse_nnap_lammps2cuda + jse_nnap_computeLammpsCuda + jse_nnap_cuda2lammps,
-    lists sent every step; this build: nnap_compute_lammps).  ``kernels``: the reference's
+    lists sent every step; this build: nnap_compute_lammps); ``_list_reused``: the same with
+    the list of the previous step kept on the device (nlflag = 0, as between LAMMPS
+    neighbour-list rebuilds).  ``kernels``: the reference's
     jse_nnap_computeLammpsCuda with its inputs on the device (its memsets, three kernels and
     closing synchronisation) against this build's device-resident nnap_compute_device on the
     periodic structure, which also builds its own neighbour list.  L2 flushed between steps."""
@@ -366,6 +368,13 @@ def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int 
                                               None, None))
         v, ms = timed(ours_lmp, steps)
         out["ours_lammps_e2e"] = {"value": v, "ms_per_step": ms}
+
+        def ours_lmp_reuse():
+            p._check(p._L.nnap_compute_lammps_nl(p._handle(), 0, n, nall, _iptr(il), _iptr(num), ptrs, _dptr(xh),
+                                                 _iptr(t), None, 1, 1, 1, 0, 0, _dptr(f), _dptr(eng), _dptr(eatom),
+                                                 _dptr(vir), None, None))
+        v, ms = timed(ours_lmp_reuse, steps)
+        out["ours_lammps_e2e_list_reused"] = {"value": v, "ms_per_step": ms}
         x_d = torch.from_numpy(np.ascontiguousarray(s.x)).to(dev)
         t_d = torch.from_numpy(np.ascontiguousarray(s.types, dtype=np.int32)).to(dev)
         e_d = torch.zeros(1, dtype=torch.float64, device=dev)
@@ -391,6 +400,13 @@ def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int 
     ref.setup(x, t, n, lists)
     v, ms = timed(ref.step, steps)
     out["ref_lammps_e2e"] = {"value": v, "ms_per_step": ms}
+
+    def ref_step_reuse():
+        ref.to_device(False)
+        ref.compute()
+        ref.to_host()
+    v, ms = timed(ref_step_reuse, steps)
+    out["ref_lammps_e2e_list_reused"] = {"value": v, "ms_per_step": ms}
     ref.to_device(True)
     v, ms = timed(ref.compute, steps)
     out["ref_kernels"] = {"value": v, "ms_per_step": ms}

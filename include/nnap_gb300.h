@@ -166,6 +166,16 @@ int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int* ilist, co
                         const int* const* firstneigh, const double* x, const int* type, const int* type_map,
                         int eflag, int vflag, int eflag_atom, int vflag_atom, int cvflag_atom, double* f,
                         double* eng_vdwl, double* eatom, double* virial, double* vatom, double* cvatom);
+/* Same, with the reference's nlflag (jse_nnap_lammps2cuda, NNAP.java:948-1000: nlflag =
+ * neighbor->ago == 0).  nlflag = 0 reuses the device copy of the list sent by the last
+ * call on this handle that had nlflag = 1 (nnap_compute_lammps counts as one): ilist,
+ * numneigh and firstneigh must be unchanged and are not read; inum and nall must match
+ * (NNAP_ERR_ARG otherwise, or when no such call precedes).  Positions and types are sent
+ * every call; pairs are re-filtered by the cutoff every call. */
+int nnap_compute_lammps_nl(nnap_handle* h, int nlflag, int inum, int nall, const int* ilist, const int* numneigh,
+                           const int* const* firstneigh, const double* x, const int* type, const int* type_map,
+                           int eflag, int vflag, int eflag_atom, int vflag_atom, int cvflag_atom, double* f,
+                           double* eng_vdwl, double* eatom, double* virial, double* vatom, double* cvatom);
 
 /* Parameter counts of species `type` (1-based): *fp_size entries of its basis's C-level
  * parameters (the internal radial-fuse matrices of its sub-bases, [t_nei][np][n] each,

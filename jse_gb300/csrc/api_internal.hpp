@@ -196,6 +196,10 @@ struct nnap_handle {
     // LAMMPS-style boundary: caller's atoms (local + ghost), list, targets of the scatter
     nnapgb::DevBuf<double> lmp_x, lmp_forces, lmp_virials;
     nnapgb::Pinned lmp_pin_in, lmp_pin_out;  // per-call layout arrays in, results out
+    // the list on the device from the last LAMMPS call (reused with nlflag = 0)
+    bool lmp_cached = false;
+    int lmp_inum = 0, lmp_nall = 0, lmp_deg = 0;
+    size_t lmp_total = 0;
     nnapgb::DevBuf<int> lmp_type, lmp_ilist, lmp_off, lmp_idx, lmp_rowtype, lmp_rowof, lmp_tcount, lmp_tstart,
         lmp_tfill, lmp_tlist;
     // force-training gradients: directional derivatives, upstream gradients, per-slot

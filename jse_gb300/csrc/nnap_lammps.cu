@@ -29,11 +29,16 @@ constexpr size_t kLmpThreadedEntries = 1 << 18;  // list entries from which the 
 constexpr unsigned kLmpMaxThreads = 8;
 }
 
-extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int* ilist, const int* numneigh,
-                                   const int* const* firstneigh, const double* x, const int* type,
-                                   const int* type_map, int eflag, int vflag, int eflag_atom, int vflag_atom,
-                                   int cvflag_atom, double* f, double* eng_vdwl, double* eatom, double* virial,
-                                   double* vatom, double* cvatom) {
+namespace {
+
+// nlflag = 0: the list (inum, nall, ilist, numneigh, firstneigh) is the one of the last
+// call with nlflag = 1 on this handle; its device copy is reused and only positions and
+// types are sent (NNAP.computeLammpsCuda passes nlflag = neighbor->ago == 0 to
+// jse_nnap_lammps2cuda, NNAP.java:948-1000).
+int compute_lammps(nnap_handle* h, int nlflag, int inum, int nall, const int* ilist, const int* numneigh,
+                   const int* const* firstneigh, const double* x, const int* type, const int* type_map, int eflag,
+                   int vflag, int eflag_atom, int vflag_atom, int cvflag_atom, double* f, double* eng_vdwl,
+                   double* eatom, double* virial, double* vatom, double* cvatom) {
     return guarded(h, [&]() -> int {
         if (inum < 0 || nall < inum) throw ApiFail(NNAP_ERR_ARG, "need 0 <= inum <= nall");
         if (inum > 0 && (!ilist || !numneigh || !firstneigh)) throw ApiFail(NNAP_ERR_ARG, "neighbour list is NULL");
@@ -45,11 +50,15 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         if (cvflag_atom && !cvatom) throw ApiFail(NNAP_ERR_ARG, "centroid per-atom virials are NULL");
         h->launches = 0;
         if (nall == 0) return NNAP_OK;
+        const bool reuse = !nlflag;
+        if (reuse && !(h->lmp_cached && h->lmp_inum == inum && h->lmp_nall == nall))
+            throw ApiFail(NNAP_ERR_ARG, "nlflag = 0 needs the list of an earlier call with the same inum and nall");
+        h->lmp_cached = false;  // set again once this call's list is on the device
         // host-side layout, written straight into pinned staging: species through the type
         // map, the row of each local atom, the list in ilist order
-        size_t total = 0;
-        int deg_max = 0;
-        for (int ii = 0; ii < inum; ++ii) {
+        size_t total = reuse ? h->lmp_total : 0;
+        int deg_max = reuse ? h->lmp_deg : 0;
+        for (int ii = 0; ii < inum && !reuse; ++ii) {
             const int i = ilist[ii];
             if (i < 0 || i >= nall) throw ApiFail(NNAP_ERR_ARG, "ilist entries must be distinct atoms");
             if (numneigh[i] < 0) throw ApiFail(NNAP_ERR_ARG, "negative neighbour count");
@@ -65,11 +74,10 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         int* row_of = reinterpret_cast<int*>(pin + al(sizeof(int) * nall));
         int* off = reinterpret_cast<int*>(pin + 2 * al(sizeof(int) * nall));
         int* nidx = reinterpret_cast<int*>(pin + 2 * al(sizeof(int) * nall) + al(sizeof(int) * ((size_t)inum + 1)));
-        for (int a = 0; a < nall; ++a) {
-            ty[a] = type_map ? type_map[type[a]] : type[a];
-            row_of[a] = -1;
-        }
+        for (int a = 0; a < nall; ++a) ty[a] = type_map ? type_map[type[a]] : type[a];
+        for (int a = 0; a < nall && !reuse; ++a) row_of[a] = -1;
         off[0] = 0;
+        if (!reuse) {
         for (int ii = 0; ii < inum; ++ii) {
             const int i = ilist[ii];
             if (row_of[i] >= 0) throw ApiFail(NNAP_ERR_ARG, "ilist entries must be distinct atoms");
@@ -97,6 +105,7 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         } else {
             copy_rows(0, inum);
         }
+        }
         // device buffers: rows for the local atoms at capacity = longest list
         const int n1 = std::max(inum, 1);
         h->M = std::max(8, (deg_max + 7) & ~7);
@@ -121,12 +130,14 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         const int T = h->model.ntypes();
         CK(cudaMemcpyAsync(h->lmp_x.p, x, sizeof(double) * 3 * nall, cudaMemcpyHostToDevice, st));
         CK(cudaMemcpyAsync(h->lmp_type.p, ty, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(h->lmp_rowof.p, row_of, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
-        if (inum) {
-            CK(cudaMemcpyAsync(h->lmp_ilist.p, ilist, sizeof(int) * inum, cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(h->lmp_off.p, off, sizeof(int) * (inum + 1), cudaMemcpyHostToDevice, st));
+        if (!reuse) {
+            CK(cudaMemcpyAsync(h->lmp_rowof.p, row_of, sizeof(int) * nall, cudaMemcpyHostToDevice, st));
+            if (inum) {
+                CK(cudaMemcpyAsync(h->lmp_ilist.p, ilist, sizeof(int) * inum, cudaMemcpyHostToDevice, st));
+                CK(cudaMemcpyAsync(h->lmp_off.p, off, sizeof(int) * (inum + 1), cudaMemcpyHostToDevice, st));
+            }
+            if (total) CK(cudaMemcpyAsync(h->lmp_idx.p, nidx, sizeof(int) * total, cudaMemcpyHostToDevice, st));
         }
-        if (total) CK(cudaMemcpyAsync(h->lmp_idx.p, nidx, sizeof(int) * total, cudaMemcpyHostToDevice, st));
         CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
         CK(cudaMemsetAsync(h->lmp_tcount.p, 0, sizeof(int) * nall, st));
         CK(cudaMemsetAsync(h->lmp_tfill.p, 0, sizeof(int) * nall, st));
@@ -205,6 +216,31 @@ extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int
         } else if (vflag) {
             for (int c = 0; c < 6; ++c) virial[c] += vo[c];
         }
+        h->lmp_cached = true;
+        h->lmp_inum = inum;
+        h->lmp_nall = nall;
+        h->lmp_total = total;
+        h->lmp_deg = deg_max;
         return NNAP_OK;
     });
+}
+
+}  // namespace
+
+extern "C" int nnap_compute_lammps(nnap_handle* h, int inum, int nall, const int* ilist, const int* numneigh,
+                                   const int* const* firstneigh, const double* x, const int* type,
+                                   const int* type_map, int eflag, int vflag, int eflag_atom, int vflag_atom,
+                                   int cvflag_atom, double* f, double* eng_vdwl, double* eatom, double* virial,
+                                   double* vatom, double* cvatom) {
+    return compute_lammps(h, 1, inum, nall, ilist, numneigh, firstneigh, x, type, type_map, eflag, vflag, eflag_atom,
+                          vflag_atom, cvflag_atom, f, eng_vdwl, eatom, virial, vatom, cvatom);
+}
+
+extern "C" int nnap_compute_lammps_nl(nnap_handle* h, int nlflag, int inum, int nall, const int* ilist,
+                                      const int* numneigh, const int* const* firstneigh, const double* x,
+                                      const int* type, const int* type_map, int eflag, int vflag, int eflag_atom,
+                                      int vflag_atom, int cvflag_atom, double* f, double* eng_vdwl, double* eatom,
+                                      double* virial, double* vatom, double* cvatom) {
+    return compute_lammps(h, nlflag, inum, nall, ilist, numneigh, firstneigh, x, type, type_map, eflag, vflag,
+                          eflag_atom, vflag_atom, cvflag_atom, f, eng_vdwl, eatom, virial, vatom, cvatom);
 }

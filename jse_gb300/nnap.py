@@ -42,7 +42,7 @@ EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes"
            "nnap_server_create", "nnap_server_destroy", "nnap_server_admit", "nnap_server_release",
            "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats", "nnap_set_autotune",
            "nnap_get_tuning", "nnap_set_tuning", "nnap_compute_lammps", "nnap_param_sizes", "nnap_train_grad_batch",
-           "nnap_create_nep", "nnap_create_nep_from_file"]
+           "nnap_create_nep", "nnap_create_nep_from_file", "nnap_compute_lammps_nl"]
 
 
 class IllegalStateError(RuntimeError):
@@ -101,6 +101,8 @@ def load_library(path: str = LIB_PATH):
     L.nnap_server_stats.argtypes = [P, C.POINTER(C.c_longlong)]
     L.nnap_param_sizes.argtypes = [P, I, ip, ip]
     L.nnap_train_grad_batch.argtypes = [P, I, ip, dp, ip, ip, dp, dp, dp, dp, dp, dp]
+    L.nnap_compute_lammps_nl.argtypes = [P, I, I, I, ip, ip, C.POINTER(ip), dp, ip, ip, I, I, I, I, I, dp, dp, dp,
+                                         dp, dp, dp]
     L.nnap_create_nep.argtypes = [C.c_char_p, S, I, I, C.POINTER(P)]
     L.nnap_create_nep_from_file.argtypes = [C.c_char_p, I, I, C.POINTER(P)]
     _lib = L
@@ -395,12 +397,13 @@ class NNAP:
         return out
 
     def computeLammps(self, ilist, neighbors, x, types, type_map=None, eflag=True, vflag=True, eflag_atom=True,
-                      vflag_atom=False, cvflag_atom=True) -> dict:
+                      vflag_atom=False, cvflag_atom=True, nlflag=True) -> dict:
         """LAMMPS-style evaluation (``PairNNAP_gpu``): ``ilist`` local atoms, ``neighbors[i]``
         the full list of local atom i (indices into the nall = len(x) local + ghost atoms),
-        ``types`` LAMMPS types (mapped through ``type_map`` when given).  Returns fresh
-        accumulators: forces on every atom (ghosts included), eng, eatom, virial[6],
-        vatom (nall x 6), cvatom (nall x 9)."""
+        ``types`` LAMMPS types (mapped through ``type_map`` when given).  ``nlflag=False``
+        reuses the list sent by the last call with ``nlflag=True`` (``neighbors`` is then not
+        read).  Returns fresh accumulators: forces on every atom (ghosts included), eng,
+        eatom, virial[6], vatom (nall x 6), cvatom (nall x 9)."""
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
         t = np.ascontiguousarray(types, dtype=np.int32)
         il = np.ascontiguousarray(ilist, dtype=np.int32)
@@ -416,10 +419,11 @@ class NNAP:
         vir = np.zeros(6)
         vatom = np.zeros((nall, 6))
         cvatom = np.zeros((nall, 9))
-        self._check(self._L.nnap_compute_lammps(self._handle(), len(il), nall, _iptr(il), _iptr(num), ptrs, _dptr(x),
-                                                _iptr(t), _iptr(tm), int(eflag), int(vflag), int(eflag_atom),
-                                                int(vflag_atom), int(cvflag_atom), _dptr(f), _dptr(eng), _dptr(eatom),
-                                                _dptr(vir), _dptr(vatom), _dptr(cvatom)))
+        self._check(self._L.nnap_compute_lammps_nl(self._handle(), int(bool(nlflag)), len(il), nall, _iptr(il),
+                                                   _iptr(num), ptrs, _dptr(x), _iptr(t), _iptr(tm), int(eflag),
+                                                   int(vflag), int(eflag_atom), int(vflag_atom), int(cvflag_atom),
+                                                   _dptr(f), _dptr(eng), _dptr(eatom), _dptr(vir), _dptr(vatom),
+                                                   _dptr(cvatom)))
         return {"forces": f, "eng": float(eng[0]), "eatom": eatom, "virial": vir, "vatom": vatom, "cvatom": cvatom}
 
     def computeBatchDevice(self, natoms, x_ptr: int, type_ptr: int, box_kinds, boxes, flags: int,

@@ -112,3 +112,26 @@ def test_lammps_large_list_global_virial_only():
     assert np.max(np.abs(out["virial"] - full["virial"])) <= 1e-9 * max(1.0, np.abs(full["virial"]).max())
     assert np.max(np.abs(out["virial"] - ref["virial"][:6])) <= V_TOL * n ** 0.5
     assert np.max(np.abs(_reverse(out["forces"], n, owner) - ref["forces"])) <= F_TOL
+
+
+def test_lammps_list_reuse_equals_resend():
+    """nlflag = 0 (the list of the previous call, new positions) gives exactly what sending
+    the same list again gives; without a previous list, or with another inum, it is refused."""
+    from jse_gb300.nnap import NNAP, NNAPError
+    s = W.random_liquid(1500, 0.060, [0.46, 0.46, 0.08], 2.0, 75)
+    rng = np.random.default_rng(3)
+    with NNAP(W.model_for("c2"), precision="mixed") as p:
+        x, types, lists, owner, xw = _lammps_form(s, p.rcutMax() + 0.4)
+        n = s.natoms
+        with pytest.raises(NNAPError):
+            p.computeLammps(np.arange(n), lists, x, types, nlflag=False)
+        p.computeLammps(np.arange(n), lists, x, types)
+        x2 = x + rng.normal(0.0, 0.02, size=x.shape)
+        sent = p.computeLammps(np.arange(n), lists, x2, types)
+        reused = p.computeLammps(np.arange(n), lists, x2, types, nlflag=False)
+        assert np.array_equal(sent["forces"], reused["forces"]) and sent["eng"] == reused["eng"]
+        assert np.array_equal(sent["cvatom"], reused["cvatom"])
+        with pytest.raises(NNAPError):
+            p.computeLammps(np.arange(n - 1), lists, x2, types, nlflag=False)
+        again = p.computeLammps(np.arange(n), lists, x2, types, nlflag=False)  # a refusal keeps the list
+        assert np.array_equal(sent["forces"], again["forces"])
