@@ -170,12 +170,11 @@ def load_peaks():
 
 
 def load_traffic():
-    """DRAM bytes per atom per stage from a committed ncu summary, if present."""
-    p = os.path.join(ROOT, "profiles", "dram_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f)
-    return {}
+    """DRAM bytes per atom of a stage's dominant kernel, from one ncu capture
+    (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided by its atoms):
+    liquid32k / descriptors_bwd is k_sph_bwd_n<6,18,9> on the 32000-atom liquid, 159.2 MB
+    read + 16.9 MB written (profiles/k_sph_liquid32k.md)."""
+    return {"liquid32k/descriptors_bwd": (159.2e6 + 16.9e6) / 32000}
 
 
 # ----------------------------------------------------------------------------- reference arm
