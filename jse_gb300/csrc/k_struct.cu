@@ -151,6 +151,8 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     __shared__ double s_sh[kNbMaxWarps][32][3];
     __shared__ float s_fsh[kNbMaxWarps][32][3], s_flo[kNbMaxWarps][32][3];
     __shared__ int s_acc[kNbMaxWarps][32];  // accepted entries per cell-offset group of the batch
+    __shared__ int s_qj[kNbMaxWarps][64];   // candidates passing the FP32 screen: atom, cell slot
+    __shared__ int s_qs[kNbMaxWarps][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + w;
     if (i >= n) return;
@@ -230,60 +232,49 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         s_incl[w][lane] = incl;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
         __syncwarp();
-        for (int cb = 0; cb < total; cb += 32) {
-            const int cidx = cb + lane;
+        // Candidates are screened 32 at a time in FP32; the ones that pass (about one in four
+        // or five) queue in candidate order in shared memory and take the exact test 32 at a
+        // time, so its lanes stay busy.  Accepted entries keep candidate order.
+        int qn = 0;  // queued candidates (warp-uniform)
+        auto exact_batch = [&](int k) {  // the first k queued candidates
             bool acc = false;
             int j = 0, slot = 0;
             float ox = 0.f, oy = 0.f, oz = 0.f;
-            if (cidx < total) {
-                int lo = 0, hi = 31;  // first slot with incl > cidx
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_incl[w][mid] > cidx) hi = mid; else lo = mid + 1;
-                }
-                slot = lo;
-                const int before = slot ? s_incl[w][slot - 1] : 0;
-                j = cell_atoms[s_start[w][slot] + (cidx - before)];
-                const uint32_t img = s_img[w][slot];
-                if (!(j == i && img == pack_img(0, 0, 0))) {
-                    const float4 fj = xf[j];
-                    const float fx = (fj.x + s_fsh[w][slot][0]) - fi.x;
-                    const float fy = (fj.y + s_fsh[w][slot][1]) - fi.y;
-                    const float fz = (fj.z + s_fsh[w][slot][2]) - fi.z;
-                    if (fx * fx + fy * fy + fz * fz < st.rc2_hi) {
-                        // (x_j + shift) - x_i in float-float, then d^2 in float-float
-                        const float4 lj = xlo[j];
-                        float dh[3], dl[3];
-                        const float ajh[3] = {fj.x, fj.y, fj.z}, ajl[3] = {lj.x, lj.y, lj.z};
-                        const float aih[3] = {fi.x, fi.y, fi.z}, ail[3] = {li.x, li.y, li.z};
+            if (lane < k) {
+                j = s_qj[w][lane];
+                slot = s_qs[w][lane];
+                const float4 fj = xf[j];
+                const float4 lj = xlo[j];
+                // (x_j + shift) - x_i in float-float, then d^2 in float-float
+                float dh[3], dl[3];
+                const float ajh[3] = {fj.x, fj.y, fj.z}, ajl[3] = {lj.x, lj.y, lj.z};
+                const float aih[3] = {fi.x, fi.y, fi.z}, ail[3] = {li.x, li.y, li.z};
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            float s1, e1, s2, e2;
-                            two_sum(ajh[d], s_fsh[w][slot][d], s1, e1);
-                            two_sum(s1, -aih[d], s2, e2);
-                            const float lo = ((ajl[d] + s_flo[w][slot][d]) - ail[d]) + (e1 + e2);
-                            two_sum(s2, lo, dh[d], dl[d]);
-                        }
-                        float d2h = 0.f, d2l = 0.f;
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            ff_acc_prod(d2h, d2l, dh[d], dh[d]);
-                            d2l += 2.f * dh[d] * dl[d];
-                        }
-                        const float diff = (d2h - rc2h) + (d2l - rc2l);
-                        if (fabsf(diff) > tol) {
-                            acc = diff < 0.f;
-                        } else {  // within 1e-10 of the cutoff: the exact FP64 test
-                            const double dxv = ds(da(xw[3 * j], s_sh[w][slot][0]), xi);
-                            const double dyv = ds(da(xw[3 * j + 1], s_sh[w][slot][1]), yi);
-                            const double dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
-                            acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
-                        }
-                        ox = dh[0] + dl[0];
-                        oy = dh[1] + dl[1];
-                        oz = dh[2] + dl[2];
-                    }
+                for (int d = 0; d < 3; ++d) {
+                    float s1, e1, s2, e2;
+                    two_sum(ajh[d], s_fsh[w][slot][d], s1, e1);
+                    two_sum(s1, -aih[d], s2, e2);
+                    const float lo = ((ajl[d] + s_flo[w][slot][d]) - ail[d]) + (e1 + e2);
+                    two_sum(s2, lo, dh[d], dl[d]);
                 }
+                float d2h = 0.f, d2l = 0.f;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    ff_acc_prod(d2h, d2l, dh[d], dh[d]);
+                    d2l += 2.f * dh[d] * dl[d];
+                }
+                const float diff = (d2h - rc2h) + (d2l - rc2l);
+                if (fabsf(diff) > tol) {
+                    acc = diff < 0.f;
+                } else {  // within 1e-10 of the cutoff: the exact FP64 test
+                    const double dxv = ds(da(xw[3 * j], s_sh[w][slot][0]), xi);
+                    const double dyv = ds(da(xw[3 * j + 1], s_sh[w][slot][1]), yi);
+                    const double dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
+                    acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
+                }
+                ox = dh[0] + dl[0];
+                oy = dh[1] + dl[1];
+                oz = dh[2] + dl[2];
             }
             const unsigned m = __ballot_sync(0xffffffffu, acc);
             if (acc) {
@@ -297,7 +288,54 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 if (keep_groups) atomicAdd(&s_acc[w][slot], 1);
             }
             cnt += __popc(m);
+        };
+        for (int cb = 0; cb < total; cb += 32) {
+            const int cidx = cb + lane;
+            bool pass = false;
+            int j = 0, slot = 0;
+            if (cidx < total) {
+                int lo = 0, hi = 31;  // first slot with incl > cidx
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (s_incl[w][mid] > cidx) hi = mid; else lo = mid + 1;
+                }
+                slot = lo;
+                const int before = slot ? s_incl[w][slot - 1] : 0;
+                j = cell_atoms[s_start[w][slot] + (cidx - before)];
+                if (!(j == i && s_img[w][slot] == pack_img(0, 0, 0))) {
+                    const float4 fj = xf[j];
+                    const float fx = (fj.x + s_fsh[w][slot][0]) - fi.x;
+                    const float fy = (fj.y + s_fsh[w][slot][1]) - fi.y;
+                    const float fz = (fj.z + s_fsh[w][slot][2]) - fi.z;
+                    pass = fx * fx + fy * fy + fz * fz < st.rc2_hi;
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (pass) {
+                const int q = qn + __popc(m & ((1u << lane) - 1u));
+                s_qj[w][q] = j;
+                s_qs[w][q] = slot;
+            }
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                exact_batch(32);
+                // move the overflow (at most 31 entries) to the front of the queue
+                int rj = 0, rs = 0;
+                if (lane < qn - 32) {
+                    rj = s_qj[w][32 + lane];
+                    rs = s_qs[w][32 + lane];
+                }
+                __syncwarp();
+                if (lane < qn - 32) {
+                    s_qj[w][lane] = rj;
+                    s_qs[w][lane] = rs;
+                }
+                qn -= 32;
+                __syncwarp();
+            }
         }
+        if (qn > 0) exact_batch(qn);
         __syncwarp();
         if (keep_groups) {  // start of each group of this batch: cnt0 + accepted entries of earlier groups
             const int a = s_acc[w][lane];
