@@ -316,8 +316,9 @@ def train_measurement(device: int, s, model: dict, steps: int = 5, cpu: bool = T
 
 # ----------------------------------------------------------------------------- reference GPU kernels
 def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int = 10) -> dict:
-    """The reference's own CUDA kernels (nnap_interface_cuda.cu, FP32, one thread per atom;
-    oracle/ref_cuda.py) beside this build's, on the LAMMPS form of the same structure (local
+    """A baseline leg: the reference's own CUDA kernels (nnap_interface_cuda.cu, FP32, one
+    thread per atom, compiled by oracle/ref_cuda.py; the reference is what is measured,
+    never this build) beside this build's, on the LAMMPS form of the same structure (local
     atoms, ghost atoms, full neighbour lists from nnap_neighbor_list).
     ``lammps_e2e``: one call of each LAMMPS boundary per step with host arrays in and out
     (reference: jse_nnap_lammps2cuda + jse_nnap_computeLammpsCuda + jse_nnap_cuda2lammps,
@@ -711,8 +712,8 @@ def main():
     training = None
     if rank == 0 and not args.no_train and args.workload == "liquid32k":
         training = train_measurement(local, s, model, cpu=not args.no_cpu_baseline)
-    ref_gpu = None
-    if rank == 0 and not args.no_ref_gpu and args.workload == "liquid32k":
+    ref_gpu = None  # a baseline leg: runs with the other baselines
+    if rank == 0 and not args.no_ref_gpu and not args.no_cpu_baseline and args.workload == "liquid32k":
         ref_gpu = ref_gpu_measurement(local, s, model, args.precision)
     nep = None
     if rank == 0 and not args.no_nep and args.workload == "liquid32k":
