@@ -420,6 +420,68 @@ def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int 
 
 
 # ----------------------------------------------------------------------------- NEP
+def nep_ref_gpu(device: int, p, s, text: str, flush, steps: int) -> dict:
+    """The reference's CUDA NEP kernels (nep_interface_cuda.cu, FP32, one thread per atom,
+    compiled by oracle/nep_ref_cuda.py; the reference is what is measured) beside this
+    build's LAMMPS boundary on the LAMMPS form of the NEP benchmark structure: host arrays
+    in and out, lists sent every step; and the reference's kernels alone with their inputs
+    on the device."""
+    import torch
+    from jse_gb300.nnap import _dptr, _iptr
+    dev = torch.device("cuda", device)
+    n = s.natoms
+    off, j, img = p.neighborList(s)
+    x, t, lists, owner = W.lammps_form(s, off, j, img)
+    nall = len(x)
+    out = {"unit": "atom-evals/s", "ghosts": nall - n}
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        dts = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize(dev)
+            dts.append(time.perf_counter() - t0)
+        return {"value": n * steps / sum(dts), "ms_per_step": 1e3 * sum(dts) / steps}
+    il = np.arange(n, dtype=np.int32)
+    rows = [np.ascontiguousarray(l, dtype=np.int32) for l in lists] + [np.zeros(0, np.int32)] * (nall - n)
+    num = np.array([len(r) for r in rows], dtype=np.int32)
+    ptrs = (C.POINTER(C.c_int) * nall)(*[_iptr(r) for r in rows])
+    xh = np.ascontiguousarray(x)
+    f, eng, eatom, vir = np.zeros((nall, 3)), np.zeros(1), np.zeros(nall), np.zeros(6)
+
+    def ours():
+        p._check(p._L.nnap_compute_lammps(p._handle(), n, nall, _iptr(il), _iptr(num), ptrs, _dptr(xh), _iptr(t),
+                                          None, 1, 1, 1, 0, 0, _dptr(f), _dptr(eng), _dptr(eatom), _dptr(vir),
+                                          None, None))
+    out["ours_lammps_e2e"] = timed(ours)
+    for a in (f, eng, eatom, vir):
+        a[...] = 0.0
+    ours()
+    f_ours = f[:n].copy()
+    np.add.at(f_ours, owner, f[n:])
+    try:
+        from oracle import nep_model as NM, nep_ref_cuda as NRC
+        ref = NRC.RefCudaNEP(NM.load(text), device)
+    except (FileNotFoundError, RuntimeError, OSError, ValueError) as ex:
+        out["reference_error"] = str(ex)[:200]
+        return out
+    ref.setup(x, t, n, lists)
+    out["ref_lammps_e2e"] = timed(ref.step)
+    ref.to_device(True)
+    out["ref_kernels"] = timed(ref.compute)
+    r = ref.step()
+    f_ref = r["forces"][:n].copy()
+    np.add.at(f_ref, owner, r["forces"][n:])
+    out["max_abs_force_difference"] = float(np.abs(f_ref - f_ours).max())
+    out["speedup_lammps_e2e"] = out["ours_lammps_e2e"]["value"] / out["ref_lammps_e2e"]["value"]
+    return out
+
+
 def nep_measurement(device: int, steps: int = 10, cpu: bool = True) -> dict:
     """NEP potential through nnap_create_nep on the NEP benchmark: a 32000-atom binary liquid
     (0.060 /A^3) under a seeded nep4 potential of GPUMD's default hyperparameters (cutoff
@@ -489,6 +551,8 @@ def nep_measurement(device: int, steps: int = 10, cpu: bool = True) -> dict:
             dts.append(time.perf_counter() - t0)
         out["e2e"] = {"value": n * steps / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": n * 28,
                       "d2h_bytes_per_step": 8 + n * 24 + 72}
+        if cpu:  # a baseline leg: the reference's own CUDA NEP on the LAMMPS form of the structure
+            out["reference_gpu"] = nep_ref_gpu(device, p, s, text, flush, steps)
     if cpu:
         try:
             from oracle import native as ON, nep_model as NM, nep_ref as NR

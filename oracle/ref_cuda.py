@@ -82,8 +82,104 @@ def lammps_arrays(x_all, types_all, inum: int, lists):
     return x_all, types_all, rows
 
 
-class RefCudaNNAP:
+class LammpsRef:
+    """LAMMPS-side plumbing of a reference CUDA path: the host arrays LAMMPS holds (row
+    pointers), the device buffers NNAP / NEP keep, and the reference's own lammps2cuda /
+    cuda2lammps host functions (``<prefix>lammps2cuda``, ``<prefix>cuda2lammps``).
+    Subclasses add their parameter tables, their work buffers and ``compute``."""
+    prefix = ""
+
+    def _bind_io(self):
+        P, I = C.c_void_p, C.c_int
+        getattr(self.lib, self.prefix + "lammps2cuda").argtypes = [I, I, I, I] + [P] * 12
+        getattr(self.lib, self.prefix + "cuda2lammps").argtypes = [I] * 7 + [P] * 12
+
+    def _work_buffers(self, nb: int, inum: int, nall: int) -> dict:
+        return {}
+
+    def setup(self, x_all, types_all, inum: int, lists, cvflag_atom: bool = False):
+        """Size every buffer for one LAMMPS-form configuration (NNAP.java:953-992,
+        NEP.java:262-311)."""
+        torch = self.torch
+        x, t, rows = lammps_arrays(x_all, types_all, inum, lists)
+        if t.min() < 1 or t.max() > self.T:
+            raise ValueError("species outside 1..ntypes")
+        nall = len(x)
+        self.inum, self.nall = inum, nall
+        self.maxn = max(1, max((len(r) for r in rows), default=1))
+        if any(((r < 0) | (r >= nall)).any() for r in rows):
+            raise ValueError("neighbour index outside the local + ghost atoms")
+        self.cv = bool(cvflag_atom)
+        # host side: row pointers, as LAMMPS holds them
+        self.h_x = x
+        self.h_xrows = (C.c_void_p * nall)(*[x[i:].ctypes.data for i in range(nall)])
+        self.h_type = t
+        self.h_ilist = np.arange(inum, dtype=np.int32)
+        self.h_num = np.array([len(r) for r in rows], dtype=np.int32)
+        self.h_rows = rows
+        self.h_first = (C.c_void_p * inum)(*[r.ctypes.data if len(r) else 0 for r in rows])
+        self.h_flt = np.zeros(max(9 * nall, 6 * inum, 1), dtype=np.float32)
+        self.h_int = np.zeros(max(inum * self.maxn, inum, 1), dtype=np.int32)
+        self.h_f = np.zeros((nall, 3))
+        self.h_frows = (C.c_void_p * nall)(*[self.h_f[i:].ctypes.data for i in range(nall)])
+        self.h_eng = np.zeros(1)
+        self.h_eatom = np.zeros(nall)
+        self.h_vir = np.zeros(6)
+        self.h_cv = np.zeros((nall, 9))
+        self.h_cvrows = (C.c_void_p * nall)(*[self.h_cv[i:].ctypes.data for i in range(nall)])
+        d = self.dev
+        f32, i32 = torch.float32, torch.int32
+        nb = inum * self.maxn
+        self.d = {
+            "x": torch.zeros(3 * nall, dtype=f32, device=d), "type": torch.zeros(nall, dtype=i32, device=d),
+            "ilist": torch.zeros(inum, dtype=i32, device=d), "num": torch.zeros(inum, dtype=i32, device=d),
+            "first": torch.zeros(nb, dtype=i32, device=d), "f": torch.zeros(3 * nall, dtype=f32, device=d),
+            "eatom0": torch.zeros(inum, dtype=f32, device=d), "vatom0": torch.zeros(6 * inum, dtype=f32, device=d),
+            "vatom1": torch.zeros((9 if self.cv else 6) * nall, dtype=f32, device=d),
+        }
+        self.d.update(self._work_buffers(nb, inum, nall))
+        torch.cuda.synchronize(d)
+
+    def to_device(self, nlflag: bool = True):
+        """<prefix>lammps2cuda: positions and types (and the lists when nlflag)."""
+        D = self.d
+        code = getattr(self.lib, self.prefix + "lammps2cuda")(
+            self.inum, self.nall, 1 if nlflag else 0, self.maxn, C.cast(self.h_xrows, C.c_void_p),
+            self.h_type.ctypes.data, self.h_ilist.ctypes.data, self.h_num.ctypes.data,
+            C.cast(self.h_first, C.c_void_p), self.h_flt.ctypes.data, self.h_int.ctypes.data, D["x"].data_ptr(),
+            D["type"].data_ptr(), D["ilist"].data_ptr(), D["num"].data_ptr(), D["first"].data_ptr())
+        if code:
+            raise RuntimeError(self.prefix + "lammps2cuda returned %d" % code)
+
+    def to_host(self, eflag: bool = True, vflag: bool = True, eflag_atom: bool = True) -> dict:
+        """<prefix>cuda2lammps into fresh accumulators."""
+        D = self.d
+        self.h_f[:] = 0.0
+        self.h_eng[:] = 0.0
+        self.h_eatom[:] = 0.0
+        self.h_vir[:] = 0.0
+        self.h_cv[:] = 0.0
+        code = getattr(self.lib, self.prefix + "cuda2lammps")(
+            self.inum, self.nall, int(eflag), int(vflag), int(eflag_atom), 0, int(self.cv),
+            C.cast(self.h_frows, C.c_void_p), self.h_eng.ctypes.data, self.h_eatom.ctypes.data,
+            self.h_vir.ctypes.data, None, C.cast(self.h_cvrows, C.c_void_p), self.h_flt.ctypes.data,
+            self.h_ilist.ctypes.data, D["f"].data_ptr(), D["eatom0"].data_ptr(), D["vatom0"].data_ptr(),
+            D["vatom1"].data_ptr())
+        if code:
+            raise RuntimeError(self.prefix + "cuda2lammps returned %d" % code)
+        return {"forces": self.h_f.copy(), "eng": float(self.h_eng[0]), "eatom": self.h_eatom.copy(),
+                "virial": self.h_vir.copy(), "cvatom": self.h_cv.copy() if self.cv else None}
+
+    def step(self) -> dict:
+        """One LAMMPS step as the reference runs it (lists sent every call)."""
+        self.to_device(True)
+        self.compute()
+        return self.to_host()
+
+
+class RefCudaNNAP(LammpsRef):
     """The reference's CUDA NNAP for one model on one device (FP32, one thread per atom)."""
+    prefix = "jse_nnap_"
 
     def __init__(self, model, device: int = 0):
         import torch
@@ -127,66 +223,17 @@ class RefCudaNNAP:
         self.type_map = torch.arange(T + 1, dtype=torch.int32, device=self.dev)
         L = self.lib
         P, I = C.c_void_p, C.c_int
-        L.jse_nnap_lammps2cuda.argtypes = [I, I, I, I, P, P, P, P, P, P, P, P, P, P, P, P]
         L.jse_nnap_computeLammpsCuda.argtypes = [I] * 7 + [P] * 27
-        L.jse_nnap_cuda2lammps.argtypes = [I] * 7 + [P] * 12
+        self._bind_io()
 
-    def setup(self, x_all, types_all, inum: int, lists, cvflag_atom: bool = False):
-        """Size every buffer for one LAMMPS-form configuration (NNAP.java:953-992)."""
-        torch = self.torch
-        x, t, rows = lammps_arrays(x_all, types_all, inum, lists)
-        if t.min() < 1 or t.max() > self.T:
-            raise ValueError("species outside 1..ntypes")
-        nall = len(x)
-        self.inum, self.nall = inum, nall
-        self.maxn = max(1, max((len(r) for r in rows), default=1))
-        if any(((r < 0) | (r >= nall)).any() for r in rows):
-            raise ValueError("neighbour index outside the local + ghost atoms")
-        self.cv = bool(cvflag_atom)
-        # host side: row pointers, as LAMMPS holds them
-        self.h_x = x
-        self.h_xrows = (C.c_void_p * nall)(*[x[i:].ctypes.data for i in range(nall)])
-        self.h_type = t
-        self.h_ilist = np.arange(inum, dtype=np.int32)
-        self.h_num = np.array([len(r) for r in rows], dtype=np.int32)
-        self.h_rows = rows
-        self.h_first = (C.c_void_p * inum)(*[r.ctypes.data if len(r) else 0 for r in rows])
-        self.h_flt = np.zeros(max(9 * nall, 6 * inum, 1), dtype=np.float32)
-        self.h_int = np.zeros(max(inum * self.maxn, inum, 1), dtype=np.int32)
-        self.h_f = np.zeros((nall, 3))
-        self.h_frows = (C.c_void_p * nall)(*[self.h_f[i:].ctypes.data for i in range(nall)])
-        self.h_eng = np.zeros(1)
-        self.h_eatom = np.zeros(nall)
-        self.h_vir = np.zeros(6)
-        self.h_cv = np.zeros((nall, 9))
-        self.h_cvrows = (C.c_void_p * nall)(*[self.h_cv[i:].ctypes.data for i in range(nall)])
-        d = self.dev
+    def _work_buffers(self, nb: int, inum: int, nall: int) -> dict:
+        torch, d = self.torch, self.dev
         f32, i32 = torch.float32, torch.int32
-        nb = inum * self.maxn
-        self.d = {
-            "x": torch.zeros(3 * nall, dtype=f32, device=d), "type": torch.zeros(nall, dtype=i32, device=d),
-            "ilist": torch.zeros(inum, dtype=i32, device=d), "num": torch.zeros(inum, dtype=i32, device=d),
-            "first": torch.zeros(nb, dtype=i32, device=d), "f": torch.zeros(3 * nall, dtype=f32, device=d),
-            "eatom0": torch.zeros(inum, dtype=f32, device=d), "vatom0": torch.zeros(6 * inum, dtype=f32, device=d),
-            "vatom1": torch.zeros((9 if self.cv else 6) * nall, dtype=f32, device=d),
-            "nldx": torch.zeros(nb, dtype=f32, device=d), "nldy": torch.zeros(nb, dtype=f32, device=d),
-            "nldz": torch.zeros(nb, dtype=f32, device=d), "nltype": torch.zeros(nb, dtype=i32, device=d),
-            "nlidx": torch.zeros(nb, dtype=i32, device=d), "neinum": torch.zeros(2 * inum, dtype=i32, device=d),
-            "ctype": torch.zeros(inum, dtype=i32, device=d), "gdx": torch.zeros(nb, dtype=f32, device=d),
-            "gdy": torch.zeros(nb, dtype=f32, device=d), "gdz": torch.zeros(nb, dtype=f32, device=d),
-        }
-        torch.cuda.synchronize(d)
-
-    def to_device(self, nlflag: bool = True):
-        """jse_nnap_lammps2cuda: positions and types (and the lists when nlflag)."""
-        D = self.d
-        code = self.lib.jse_nnap_lammps2cuda(
-            self.inum, self.nall, 1 if nlflag else 0, self.maxn, C.cast(self.h_xrows, C.c_void_p),
-            self.h_type.ctypes.data, self.h_ilist.ctypes.data, self.h_num.ctypes.data,
-            C.cast(self.h_first, C.c_void_p), self.h_flt.ctypes.data, self.h_int.ctypes.data, D["x"].data_ptr(),
-            D["type"].data_ptr(), D["ilist"].data_ptr(), D["num"].data_ptr(), D["first"].data_ptr())
-        if code:
-            raise RuntimeError("jse_nnap_lammps2cuda returned %d" % code)
+        return {"nldx": torch.zeros(nb, dtype=f32, device=d), "nldy": torch.zeros(nb, dtype=f32, device=d),
+                "nldz": torch.zeros(nb, dtype=f32, device=d), "nltype": torch.zeros(nb, dtype=i32, device=d),
+                "nlidx": torch.zeros(nb, dtype=i32, device=d), "neinum": torch.zeros(2 * inum, dtype=i32, device=d),
+                "ctype": torch.zeros(inum, dtype=i32, device=d), "gdx": torch.zeros(nb, dtype=f32, device=d),
+                "gdy": torch.zeros(nb, dtype=f32, device=d), "gdz": torch.zeros(nb, dtype=f32, device=d)}
 
     def compute(self, eflag: bool = True, vflag: bool = True, eflag_atom: bool = True):
         """jse_nnap_computeLammpsCuda (three kernels, then cudaDeviceSynchronize)."""
@@ -202,28 +249,3 @@ class RefCudaNNAP:
             D["gdx"].data_ptr(), D["gdy"].data_ptr(), D["gdz"].data_ptr())
         if code:
             raise RuntimeError("jse_nnap_computeLammpsCuda returned %d" % code)
-
-    def to_host(self, eflag: bool = True, vflag: bool = True, eflag_atom: bool = True) -> dict:
-        """jse_nnap_cuda2lammps into fresh accumulators."""
-        D = self.d
-        self.h_f[:] = 0.0
-        self.h_eng[:] = 0.0
-        self.h_eatom[:] = 0.0
-        self.h_vir[:] = 0.0
-        self.h_cv[:] = 0.0
-        code = self.lib.jse_nnap_cuda2lammps(
-            self.inum, self.nall, int(eflag), int(vflag), int(eflag_atom), 0, int(self.cv),
-            C.cast(self.h_frows, C.c_void_p), self.h_eng.ctypes.data, self.h_eatom.ctypes.data,
-            self.h_vir.ctypes.data, None, C.cast(self.h_cvrows, C.c_void_p), self.h_flt.ctypes.data,
-            self.h_ilist.ctypes.data, D["f"].data_ptr(), D["eatom0"].data_ptr(), D["vatom0"].data_ptr(),
-            D["vatom1"].data_ptr())
-        if code:
-            raise RuntimeError("jse_nnap_cuda2lammps returned %d" % code)
-        return {"forces": self.h_f.copy(), "eng": float(self.h_eng[0]), "eatom": self.h_eatom.copy(),
-                "virial": self.h_vir.copy(), "cvatom": self.h_cv.copy() if self.cv else None}
-
-    def step(self) -> dict:
-        """One LAMMPS step as NNAP.computeLammpsCuda runs it (lists sent every call)."""
-        self.to_device(True)
-        self.compute()
-        return self.to_host()

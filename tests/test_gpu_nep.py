@@ -114,3 +114,32 @@ def test_nep_uncompiled_shape_is_unsupported():
     with pytest.raises(NNAPError) as e:
         NEP(text)
     assert e.value.status == NNAP_ERR_UNSUPPORTED
+
+
+def test_reference_cuda_nep_matches():
+    """The reference's own CUDA NEP (nep_interface_cuda.cu, oracle/nep_ref_cuda.py) on the
+    LAMMPS form of a fixture structure: it and this build's LAMMPS boundary both agree with
+    the reference's FP64 CPU outputs."""
+    from jse_gb300.nep import NEP
+    from oracle import nep_model as NM, nep_ref_cuda as NRC
+    text, s, z = _case(CASES[1])
+    try:
+        ref = NRC.RefCudaNEP(NM.load(text))
+    except (FileNotFoundError, RuntimeError) as e:
+        pytest.skip(str(e))
+    with NEP(text) as p:
+        off, j, img = p.neighborList(s)
+        x, t, lists, owner = W.lammps_form(s, off, j, img)
+        n = s.natoms
+        ours = p.computeLammps(np.arange(n), lists, x, t, cvflag_atom=False)
+    ref.setup(x, t, n, lists)
+    r = ref.step()
+
+    def rev(v):
+        out = v[:n].copy()
+        np.add.at(out, owner, v[n:])
+        return out
+    assert np.max(np.abs(r["eatom"][:n] - z["energies"])) <= 1e-4
+    assert np.max(np.abs(rev(r["forces"]) - z["forces"])) <= 2e-3
+    assert np.max(np.abs(ours["eatom"][:n] - z["energies"])) <= E_TOL
+    assert np.max(np.abs(rev(ours["forces"]) - z["forces"])) <= F_MAX
