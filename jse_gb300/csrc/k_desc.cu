@@ -652,19 +652,37 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
             v2[h] = make_float2(0.f, 0.f);
         }
         const float* gh = sGh + (size_t)tn * S::K * S::N1P;
-        // one Gh row: returns dY_lm and adds Gh[lm][n] * y into v
+        // one Gh row: returns dY_lm and adds Gh[lm][n] * y into v.  Whole float4 groups of
+        // the N1 radial functions, then the remainder (the row's padding is never multiplied)
         auto row = [&](int lm, float y) -> float {
             const float4* gr = reinterpret_cast<const float4*>(gh + lm * S::N1P);
             const float2 yy = make_float2(y, y);
             float2 da = make_float2(0.f, 0.f), db = make_float2(0.f, 0.f);
+            constexpr int NQ = N1 / 4, NR = N1 - 4 * (N1 / 4);
 #pragma unroll
-            for (int q = 0; q < S::N1P / 4; ++q) {
+            for (int q = 0; q < NQ; ++q) {
                 const float4 g = gr[q];
                 const float2 ga = make_float2(g.x, g.y), gb = make_float2(g.z, g.w);
                 da = __ffma2_rn(T2[2 * q], ga, da);
                 db = __ffma2_rn(T2[2 * q + 1], gb, db);
                 v2[2 * q] = __ffma2_rn(ga, yy, v2[2 * q]);
                 v2[2 * q + 1] = __ffma2_rn(gb, yy, v2[2 * q + 1]);
+            }
+            if (NR >= 2) {
+                const float2 ga = reinterpret_cast<const float2*>(gr + NQ)[0];
+                da = __ffma2_rn(T2[2 * NQ], ga, da);
+                v2[2 * NQ] = __ffma2_rn(ga, yy, v2[2 * NQ]);
+            }
+            if (NR & 1) {
+                constexpr int n = N1 - 1;
+                const float g = gh[lm * S::N1P + n];
+                if (n & 1) {
+                    db.y = fmaf(T2[n >> 1].y, g, db.y);
+                    v2[n >> 1].y = fmaf(g, y, v2[n >> 1].y);
+                } else {
+                    db.x = fmaf(T2[n >> 1].x, g, db.x);
+                    v2[n >> 1].x = fmaf(g, y, v2[n >> 1].x);
+                }
             }
             return fc * ((da.x + db.x) + (da.y + db.y));
         };
