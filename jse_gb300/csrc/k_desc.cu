@@ -317,6 +317,8 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd_n(DescArgs a) {
         sTn[lane] = tn;
         __syncwarp();
         const int nk = min(32, cnt - b0);
+        // unrolled so the loads of the next neighbours overlap the FMAs of this one
+#pragma unroll 4
         for (int kk = 0; kk < nk; ++kk) {
             float2 f2[S::N1P / 2];
             const float4* fr = reinterpret_cast<const float4*>(sF + kk * S::N1P);
