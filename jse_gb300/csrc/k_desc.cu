@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
         for (int p = 0; p < S::NPS; ++p) sC[lane * S::NPS + p] = p < NP ? c[p] : 0.f;
         __syncwarp();
         const int nk = min(32, cnt - base);
+#pragma unroll 4
         for (int kk = 0; kk < nk; ++kk) {
             float2 cv[NH];
             const float4* crow = reinterpret_cast<const float4*>(sC + kk * S::NPS);
