@@ -35,6 +35,7 @@ CASES = {
     "nep3_single": (["C"], 3, (4.5, 4.5), (4, 4), (8, 8), (4, 0, 0), 8, ("liquid", 90, None)),
     "nep5_ternary": (["A", "B", "C"], 5, (5.5, 4.2), (4, 4), (8, 8), (4, 2, 0), 12, ("liquid", 200, 0.05)),
     "nep4_wide": (["Ga", "N"], 4, (5.2, 4.6), (6, 6), (8, 8), (4, 2, 1), 20, ("liquid", 120, None)),
+    "nep4_5body": (["Li", "P", "S"], 4, (6.0, 4.0), (4, 4), (8, 8), (4, 0, 1), 10, ("liquid", 160, 0.08)),
 }
 
 
