@@ -95,11 +95,15 @@ Model load_nep_model(const char* text, size_t len) {
     const int bR = to_int(bs[1]), bA = to_int(bs[2]);
     const auto& lm = next(4, "l_max l_max_3body l_max_4body l_max_5body");
     const int L = to_int(lm[1]);
-    const bool b4 = to_int(lm[2]) == 2, b5 = to_int(lm[3]) == 1;
+    // the flags only count columns; the reference keys the terms on the count (find_q,
+    // nep_core.hpp:943-955): the 4-body column when there is one extra, the 5-body column
+    // when there are two
+    const int nextra = (to_int(lm[2]) == 2 ? 1 : 0) + (to_int(lm[3]) == 1 ? 1 : 0);
+    const bool b4 = nextra >= 1, b5 = nextra >= 2;
     const auto& ann = next(3, "ANN num_neurons 0");
     const int H = to_int(ann[1]);
     if (nR < 0 || nA < 0 || bR < 0 || bA < 0 || L < 1 || H < 1) bad("invalid sizes");
-    const int numL = L + (b4 ? 1 : 0) + (b5 ? 1 : 0);
+    const int numL = L + nextra;
     const int dim = (nR + 1) + (nA + 1) * numL;
     const int per = (dim + 2) * H + (version == 5 ? 1 : 0);
     const int npa = version == 3 ? (dim + 2) * H + 1 : per * T + 1;

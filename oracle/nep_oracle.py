@@ -11,8 +11,10 @@ nep5 without ZBL or type-wise cutoffs, written in the quantities of the NNAP pip
   radial columns     q_n = sum_j g_n(r_ij)                            (n = 0 .. n_max_R)
   expansion          A[n][lm] = sum_j g_n(r_ij) Y_lm(r_ij)            (r_ij < rc_A)
   angular columns    q[(l-1)(n_max_A+1) + n] = sum_m A[n][lm]^2        (l = 1 .. l_max)
-  4-body column      L3(2 2 2)(A[n])   when l_max_4body == 2
-  5-body column      L4(1 1 1 1)(A[n]) when l_max_5body == 1
+  4-body column      L3(2 2 2)(A[n])   when num_L >= l_max + 1
+  5-body column      L4(1 1 1 1)(A[n]) when num_L >= l_max + 2
+                     (num_L = l_max + [l_max_4body == 2] + [l_max_5body == 1], so a file with
+                     the 5-body flag alone gets the 4-body column, as the reference computes)
   network            E_i = sum_h w1[h] tanh(sum_d w0[h][d] q_d s_d - b0[h]) - b1
                      (nep5 also subtracts the species' own output bias)
 
@@ -90,8 +92,10 @@ def descriptors(m: NEPModel, types0: np.ndarray, nl) -> np.ndarray:
     n = len(types0)
     L, nA = m.l_max, m.n_max_angular
     q = np.zeros((n, m.dim))
-    t222 = BS.l3_terms(2, 2, 2) if m.l_max_4body == 2 else []
-    t1111 = BS.l4_terms(1, 1, 1, 1) if m.l_max_5body == 1 else []
+    # the reference keys both terms on the column count alone (find_q, nep_core.hpp:943-955):
+    # num_L >= l_max + 1 gives the 4-body column, num_L >= l_max + 2 the 5-body column
+    t222 = BS.l3_terms(2, 2, 2) if m.num_L >= L + 1 else []
+    t1111 = BS.l4_terms(1, 1, 1, 1) if m.num_L >= L + 2 else []
     Lx = max(L, 2 if t222 else 0, 1 if t1111 else 0)
     for i in range(n):
         o0, o1 = nl.offsets[i], nl.offsets[i + 1]

@@ -21,6 +21,7 @@ from tests.conftest import GOLDEN_DIR
 pytestmark = pytest.mark.gpu
 
 CASES = sorted(glob.glob(os.path.join(GOLDEN_DIR, "nep_*.npz")))
+BINARY = os.path.join(GOLDEN_DIR, "nep_nep4_binary.npz")   # two species, 4- and 5-body terms
 E_TOL, F_MAX, F_RMS, V_TOL = 1e-5, 1e-3, 1e-4, 2e-3
 
 
@@ -73,7 +74,7 @@ def test_nep_batch_lammps_server_agree():
     from jse_gb300.nep import NEP
     from jse_gb300.serve import NNAPServer
     from tests.test_gpu_lammps import _lammps_form, _reverse
-    text, _, _ = _case(CASES[1])
+    text, _, _ = _case(BINARY)
     T = int(text.split()[1])
     structs = _structs(T)
     with NEP(text) as p:
@@ -122,7 +123,7 @@ def test_reference_cuda_nep_matches():
     the reference's FP64 CPU outputs."""
     from jse_gb300.nep import NEP
     from oracle import nep_model as NM, nep_ref_cuda as NRC
-    text, s, z = _case(CASES[1])
+    text, s, z = _case(BINARY)
     try:
         ref = NRC.RefCudaNEP(NM.load(text))
     except (FileNotFoundError, RuntimeError) as e:
