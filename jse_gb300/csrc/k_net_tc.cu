@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int s_tstart[kMaxTypes + 1];
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int part = tid >> 7;  // column share of this thread in the epilogues
     __shared__ float s_e[SPLIT][128];
     const int Dp = L.Dp, H1 = L.H1, H2 = L.H2;
@@ -203,16 +203,39 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
         const int row = tid & 127;
         const int slot = s0 + tile * 128 + row;
         const bool valid = slot < s1;
-        // ---- X = (fp - mu) / sigma, split into hi / lo
-        const float* frow = p.fp + (size_t)(valid ? slot : s0) * p.fp_stride;
-        for (int k0 = 8 * part; k0 < Dp; k0 += 8 * SPLIT) {
-            float v[8];
+        // ---- X = (fp - mu) / sigma, split into hi / lo.  Warp-cooperative: the lanes of a
+        // warp take 8 rows (one core-matrix block) x 4 chunks of 8 columns, so the global
+        // reads are 128-byte row segments and the shared stores fill 512 contiguous bytes
+        {
+            const int nch = Dp >> 3, ngr = (nch + 3) >> 2;
+            const int r8 = lane & 7, cq = lane >> 3;
+            for (int it = warp; it < 16 * ngr; it += 4 * SPLIT) {
+                const int rb = it / ngr, c = 4 * (it - rb * ngr) + cq;
+                if (c >= nch) continue;
+                const int r = rb * 8 + r8, k0 = 8 * c;
+                const int sl = s0 + tile * 128 + r;
+                float v[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int k = k0 + q;
-                v[q] = (valid && k < p.D) ? (frow[k] - fv[L.fmu + k]) * fv[L.fisig + k] : 0.f;
+                for (int q = 0; q < 8; ++q) v[q] = 0.f;
+                if (sl < s1) {
+                    const float* fr = p.fp + (size_t)sl * p.fp_stride + k0;
+                    if (k0 + 8 <= p.D) {
+                        const float4 a = reinterpret_cast<const float4*>(fr)[0];
+                        const float4 b = reinterpret_cast<const float4*>(fr)[1];
+                        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+                        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) v[q] = k0 + q < p.D ? fr[q] : 0.f;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int k = k0 + q;
+                        v[q] = k < p.D ? (v[q] - fv[L.fmu + k]) * fv[L.fisig + k] : 0.f;
+                    }
+                }
+                store_split8(sx, sx_lo, r, k0, Dp, v);
             }
-            store_split8(sx, sx_lo, row, k0, Dp, v);
         }
         fence_async_smem();
         __syncthreads();
@@ -316,10 +339,20 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
         for (int c0 = 16 * part; c0 < Dp; c0 += 16 * SPLIT) {
             float g[16];
             tmem_ld16(tlane + L.dx + c0, g);
+            if (!valid) continue;
+            if (c0 + 16 <= p.D) {  // whole 16-column chunk inside the descriptor: float4 stores
+                float4* o = reinterpret_cast<float4*>(grow + c0);
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int k = c0 + q;
-                if (valid && k < p.D) grow[k] = g[q] * fv[L.fisig + k];
+                for (int q = 0; q < 4; ++q)
+                    o[q] = make_float4(g[4 * q] * fv[L.fisig + c0 + 4 * q], g[4 * q + 1] * fv[L.fisig + c0 + 4 * q + 1],
+                                       g[4 * q + 2] * fv[L.fisig + c0 + 4 * q + 2],
+                                       g[4 * q + 3] * fv[L.fisig + c0 + 4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const int k = c0 + q;
+                    if (k < p.D) grow[k] = g[q] * fv[L.fisig + k];
+                }
             }
         }
         fence_before();
