@@ -334,24 +334,36 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
         phase ^= 1;
         if (!ok) break;
         fence_after();
-        // ---- dE/dfp = dX / sigma
-        float* grow = p.gfp + (size_t)(valid ? slot : s0) * p.fp_stride;
-        for (int c0 = 16 * part; c0 < Dp; c0 += 16 * SPLIT) {
-            float g[16];
-            tmem_ld16(tlane + L.dx + c0, g);
-            if (!valid) continue;
-            if (c0 + 16 <= p.D) {  // whole 16-column chunk inside the descriptor: float4 stores
-                float4* o = reinterpret_cast<float4*>(grow + c0);
+        // ---- dE/dfp = dX / sigma.  Staged in shared memory over the X and A operand areas
+        // (free once GEMM 4 has completed; rows padded to Dp + 4 floats against bank
+        // conflicts), then written row by row with coalesced float4 stores
+        {
+            const int Dps = Dp + 4;
+            float* sg = reinterpret_cast<float*>(sx);  // [128][Dps]
+            for (int c0 = 16 * part; c0 < Dp; c0 += 16 * SPLIT) {
+                float g[16];
+                tmem_ld16(tlane + L.dx + c0, g);
+                float4* o = reinterpret_cast<float4*>(sg + (size_t)row * Dps + c0);
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     o[q] = make_float4(g[4 * q] * fv[L.fisig + c0 + 4 * q], g[4 * q + 1] * fv[L.fisig + c0 + 4 * q + 1],
                                        g[4 * q + 2] * fv[L.fisig + c0 + 4 * q + 2],
                                        g[4 * q + 3] * fv[L.fisig + c0 + 4 * q + 3]);
-            } else {
-#pragma unroll
-                for (int q = 0; q < 16; ++q) {
-                    const int k = c0 + q;
-                    if (k < p.D) grow[k] = g[q] * fv[L.fisig + k];
+            }
+            __syncthreads();
+            for (int r = warp; r < 128; r += 4 * SPLIT) {
+                const int sl = s0 + tile * 128 + r;
+                if (sl >= s1) continue;  // uniform across the warp
+                float* gr = p.gfp + (size_t)sl * p.fp_stride;
+                const float* src = sg + (size_t)r * Dps;
+                for (int k = 4 * lane; k < p.D; k += 128) {
+                    const float4 v = *reinterpret_cast<const float4*>(src + k);
+                    if (k + 4 <= p.D) {
+                        *reinterpret_cast<float4*>(gr + k) = v;
+                    } else {
+                        const float w[4] = {v.x, v.y, v.z, v.w};
+                        for (int q = 0; k + q < p.D; ++q) gr[k + q] = w[q];
+                    }
                 }
             }
         }
