@@ -25,13 +25,11 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
-import math
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
