@@ -1,0 +1,92 @@
+// NEP's ZBL short-range term over the pair rows (find_force_ZBL, nep_core.hpp:1321-1386).
+//
+// For every row entry (i -> j) with r < 2.5 A:
+//   f(r)  = k Z_i Z_j / r * phi(r / a) * fc(r),   1/a = 2.134563 (Z_i^0.23 + Z_j^0.23),
+//   phi(x) = sum_k a_k exp(-b_k x)   (the universal ZBL screening coefficients, or the
+//                                     file's per-pair a_k, b_k in the flexible form),
+//   fc = 1 below rc_inner, (cos(pi (r - rc_inner)/(rc_outer - rc_inner)) + 1)/2 up to
+//        rc_outer, 0 beyond,
+// atom i takes f/2 of its energy and the entry's pair gradient gets -dx f'(r) / (2 r): the
+// full rows hold each pair in both directions, as the reference's neighbour lists do.
+// One warp per atom row; the row's energy is summed in a fixed order and added once.
+#include "common.cuh"
+#include "pdl.cuh"
+#include "zbl.cuh"
+
+namespace nnapgb {
+
+namespace {
+
+__device__ __forceinline__ void zbl_term(float a, float b, float x, float& phi, float& dphi) {
+    const float t = a * expf(-b * x);
+    phi += t;
+    dphi -= b * t;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_nep_zbl(PairBufs P, int n, const int* __restrict__ type, ZblArgs z,
+                                                 double* __restrict__ e_atom) {
+    pdl_enter();
+    const int at = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (at >= n) return;
+    const int M = P.M, cnt = min(P.count[at], M);
+    const int ti = type[at] - 1;
+    double esum = 0.0;
+    for (int k = lane; k < cnt; k += 32) {
+        const size_t e = (size_t)at * M + k;
+        const float4 d = P.dx[e];
+        const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+        if (r2 >= kZblMaxR * kZblMaxR) continue;
+        const int tj = __float_as_int(d.w) - 1;
+        const float r = sqrtf(r2), rinv = 1.f / r;
+        const float a_inv = (z.zp[ti] + z.zp[tj]) * 2.134563f;
+        const float zizj = 14.399645f * z.z[ti] * z.z[tj];
+        const float x = r * a_inv;
+        float phi = 0.f, dphi = 0.f, rin = z.rc_inner, rout = z.rc_outer;
+        if (z.flexible) {
+            const int t1 = min(ti, tj), t2 = max(ti, tj);
+            const float* p = z.para + 10 * (t1 * z.T - t1 * (t1 - 1) / 2 + (t2 - t1));
+            rin = p[0];
+            rout = p[1];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) zbl_term(p[2 + 2 * q], p[3 + 2 * q], x, phi, dphi);
+        } else {
+            zbl_term(0.18175f, 3.1998f, x, phi, dphi);
+            zbl_term(0.50986f, 0.94229f, x, phi, dphi);
+            zbl_term(0.28022f, 0.4029f, x, phi, dphi);
+            zbl_term(0.02817f, 0.20162f, x, phi, dphi);
+        }
+        // f = zizj phi / r and its r-derivative, then the switch
+        float f = zizj * phi * rinv;
+        float fp = zizj * a_inv * dphi * rinv - f * rinv;
+        float fc = 0.f, fcp = 0.f;
+        if (r < rin) {
+            fc = 1.f;
+        } else if (r < rout) {
+            const float w = 3.14159265358979f / (rout - rin);
+            float sn, cs;
+            sincosf(w * (r - rin), &sn, &cs);
+            fc = 0.5f * cs + 0.5f;
+            fcp = -0.5f * w * sn;
+        }
+        fp = fp * fc + f * fcp;
+        f *= fc;
+        const float s = 0.5f * fp * rinv;
+        const float4 g = P.g[e];
+        P.g[e] = make_float4(g.x - s * d.x, g.y - s * d.y, g.z - s * d.z, g.w);
+        esum += 0.5 * (double)f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, o);
+    if (lane == 0) e_atom[at] += esum;
+}
+
+cudaError_t launch_nep_zbl(const PairBufs& P, int n, const int* type, const ZblArgs& z, double* e_atom,
+                           cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    return launch_pdl(&k_nep_zbl, dim3((unsigned)(((size_t)n * 32 + 255) / 256)), dim3(256), 0, st, P, n, type, z,
+                      e_atom);
+}
+
+}  // namespace nnapgb

@@ -43,10 +43,22 @@ struct Species {
     bool basis_mirror = false;               // the basis is a mirror of basis_src's
 };
 
+// NEP's ZBL short-range term (nepV_zbl): per pair r < 2.5 A, the screened Coulomb
+// repulsion with the universal screening function and a cosine switch from rc_inner to
+// rc_outer (fixed form), or ten per-species-pair parameters [rc_inner, rc_outer, a1, b1,
+// .., a4, b4] (flexible form); see k_zbl.cu.
+struct ZblModel {
+    bool on = false, flexible = false;
+    double rc_inner = 0.0, rc_outer = 0.0;
+    std::vector<int> z;        // atomic number of each species
+    std::vector<double> para;  // flexible: 10 per pair (t1 <= t2, row-major upper triangle)
+};
+
 struct Model {
     std::vector<Species> sp;
     std::string units;
     double rcut_max = 0.0;
+    ZblModel zbl;
     int radial_fn = 0;  // radial functions of every sub-basis: 0 NNAP Chebyshev, 1 NEP
     int act = 0;        // hidden activation of every network: 0 SiLU, 1 tanh (NEP)
     int ntypes() const { return (int)sp.size(); }
@@ -55,8 +67,8 @@ struct Model {
 // Parse and pack; throws std::runtime_error with a message on invalid input.
 Model load_model(const char* text, size_t len);
 
-// A valid NEP file of a variant the GPU path does not evaluate (ZBL, dipole,
-// polarizability, type-wise cutoffs).
+// A valid NEP file of a variant the GPU path does not evaluate (dipole, polarizability,
+// type-wise cutoffs).
 struct NepUnsupported : std::runtime_error {
     using std::runtime_error::runtime_error;
 };

@@ -2,9 +2,9 @@
 //
 // The loader follows NEP(String) (NEP.java:786-1010): a header of whitespace-separated
 // lines, then one number per line (the network parameters, the descriptor coefficients
-// c and the dim descriptor scales q_scaler).  Potential models nep3, nep4 and nep5
-// without ZBL and without type-wise cutoffs are mapped; the other variants (ZBL, dipole,
-// polarizability, type-wise cutoffs) throw NepUnsupported.
+// c and the dim descriptor scales q_scaler).  Potential models nep3, nep4 and nep5,
+// with or without ZBL (fixed or flexible), without type-wise cutoffs, are mapped; the
+// other variants (dipole, polarizability, type-wise cutoffs) throw NepUnsupported.
 //
 // NEP's per-atom arithmetic (nep_core.hpp, find_q / find_q_with_4body / _5body and
 // apply_ann_one_layer) is, in the quantities of the NNAP pipeline:
@@ -32,6 +32,16 @@ namespace nnapgb {
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
+
+// Element symbols in periodic-table order (H .. Pu); a species' atomic number is its index + 1
+constexpr int kNumElements = 94;
+const char* const kElements[kNumElements] = {
+    "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",  "Ne", "Na", "Mg", "Al", "Si", "P",  "S",
+    "Cl", "Ar", "K",  "Ca", "Sc", "Ti", "V",  "Cr", "Mn", "Fe", "Co", "Ni", "Cu", "Zn", "Ga", "Ge",
+    "As", "Se", "Br", "Kr", "Rb", "Sr", "Y",  "Zr", "Nb", "Mo", "Tc", "Ru", "Rh", "Pd", "Ag", "Cd",
+    "In", "Sn", "Sb", "Te", "I",  "Xe", "Cs", "Ba", "La", "Ce", "Pr", "Nd", "Pm", "Sm", "Eu", "Gd",
+    "Tb", "Dy", "Ho", "Er", "Tm", "Yb", "Lu", "Hf", "Ta", "W",  "Re", "Os", "Ir", "Pt", "Au", "Hg",
+    "Tl", "Pb", "Bi", "Po", "At", "Rn", "Fr", "Ra", "Ac", "Th", "Pa", "U",  "Np", "Pu"};
 
 void bad(const std::string& m) { throw std::runtime_error("nep.txt: " + m); }
 
@@ -75,13 +85,25 @@ Model load_nep_model(const char* text, size_t len) {
     const auto& head = next(0, "the model line");
     if (head.size() < 3) bad("the first line should have at least 3 items");
     int version = 0;
-    if (head[0] == "nep3") version = 3;
-    else if (head[0] == "nep4") version = 4;
-    else if (head[0] == "nep5") version = 5;
-    else if (head[0].rfind("nep", 0) == 0) throw NepUnsupported("NEP variant " + head[0] + " is not supported (potential models nep3, nep4 and nep5 without ZBL)");
+    const bool zbl = head[0].size() > 4 && head[0].compare(head[0].size() - 4, 4, "_zbl") == 0;
+    const std::string kind = zbl ? head[0].substr(0, head[0].size() - 4) : head[0];
+    if (kind == "nep3") version = 3;
+    else if (kind == "nep4") version = 4;
+    else if (kind == "nep5") version = 5;
+    else if (head[0].rfind("nep", 0) == 0)
+        throw NepUnsupported("NEP variant " + head[0] + " is not supported (potential models nep3, nep4, nep5, with or without ZBL)");
     else bad("unknown model type " + head[0]);
     const int T = to_int(head[1]);
     if (T < 1 || (int)head.size() != 2 + T) bad("the first line should list the atom symbols");
+    // zbl rc_inner rc_outer (both zero: flexible per-pair parameters after the scales)
+    double zin = 0.0, zout = 0.0;
+    if (zbl) {
+        const auto& z = next(3, "zbl rc_inner rc_outer");
+        if (z[0] != "zbl") bad("this line should be zbl rc_inner rc_outer");
+        zin = to_double(z[1]);
+        zout = to_double(z[2]);
+    }
+    const bool zflex = zbl && zin == 0.0 && zout == 0.0;
     // cutoff rc_R rc_A MN_R MN_A [factors]
     const auto& cut = next(0, "cutoff");
     if (cut.size() != 5 && cut.size() != 8) bad("this line should be cutoff rc_radial rc_angular MN_radial MN_angular");
@@ -111,7 +133,8 @@ Model load_nep_model(const char* text, size_t len) {
     const int npd = ncR + T * T * (nA + 1) * (bA + 1);
     std::vector<double> v;
     while (at < lines.size()) v.push_back(to_double(lines[at++][0]));
-    if ((int)v.size() != npa + npd + dim) bad("wrong number of parameters");
+    const int nz = zflex ? 10 * T * (T + 1) / 2 : 0;
+    if ((int)v.size() != npa + npd + dim + nz) bad("wrong number of parameters");
     const double* c = v.data() + npa;
     const double* qs = v.data() + npa + npd;
     const double b1 = v[npa - 1];
@@ -121,6 +144,22 @@ Model load_nep_model(const char* text, size_t len) {
     m.rcut_max = std::max(rcR, rcA);
     m.radial_fn = 1;
     m.act = 1;
+    if (zbl) {
+        m.zbl.on = true;
+        m.zbl.flexible = zflex;
+        m.zbl.rc_inner = zin;
+        m.zbl.rc_outer = zout;
+        for (int t = 0; t < T; ++t) {
+            int zi = 0;  // index in the periodic table, 0 (hydrogen) when the symbol is not an element
+            for (int e = 0; e < kNumElements; ++e)
+                if (head[2 + t] == kElements[e]) {
+                    zi = e;
+                    break;
+                }
+            m.zbl.z.push_back(zi + 1);
+        }
+        m.zbl.para.assign(v.begin() + npa + npd + dim, v.end());
+    }
     const int l3 = b4 ? 2 : 0, l4 = b5 ? 1 : 0;
     const auto inv = invariant_columns(l3, l4);
     const int nl2 = L + 1, sl = nl2 + (int)inv.size();

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "api_internal.hpp"
+#include "zbl.cuh"
 #include "pdl.cuh"
 
 using namespace nnapgb;
@@ -156,6 +157,21 @@ void upload_model(nnap_handle* h) {
         }
         h->runs.push_back(std::move(r));
         t = u;
+    }
+    // NEP's ZBL term
+    if (m.zbl.on) {
+        std::vector<float> z(T), zp(T), par(m.zbl.para.begin(), m.zbl.para.end());
+        for (int t = 0; t < T; ++t) {
+            z[t] = (float)m.zbl.z[t];
+            zp[t] = (float)std::pow((double)m.zbl.z[t], 0.23);
+        }
+        h->zbl_z.ensure(T);
+        h->zbl_zp.ensure(T);
+        h->zbl_para.ensure(std::max<size_t>(par.size(), 1));
+        CK(cudaMemcpy(h->zbl_z.p, z.data(), sizeof(float) * T, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->zbl_zp.p, zp.data(), sizeof(float) * T, cudaMemcpyHostToDevice));
+        if (!par.empty())
+            CK(cudaMemcpy(h->zbl_para.p, par.data(), sizeof(float) * par.size(), cudaMemcpyHostToDevice));
     }
     // networks
     h->nets.resize(T);
@@ -624,6 +640,19 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     }
     h->mark(3);
     if (!fp_only) descriptors(false);
+    if (!fp_only && n > 0 && h->model.zbl.on) {  // NEP's ZBL term: energies and pair gradients
+        const ZblModel& zm = h->model.zbl;
+        ZblArgs za;
+        za.flexible = zm.flexible ? 1 : 0;
+        za.T = T;
+        za.rc_inner = (float)zm.rc_inner;
+        za.rc_outer = (float)zm.rc_outer;
+        za.z = h->zbl_z.p;
+        za.zp = h->zbl_zp.p;
+        za.para = h->zbl_para.p;
+        CK(launch_nep_zbl(pair_bufs(h), n, d_type, za, h->e_atom.p, st));
+        ++h->launches;
+    }
     h->mark(4);
     if (!fp_only && gather) {
         if (n > 0) {
@@ -989,6 +1018,7 @@ int nnap_destroy(nnap_handle* h) {
     h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->Gx.release(); h->gstart.release();
     h->sdx.release(); h->spos.release(); h->scount.release();
+    h->zbl_z.release(); h->zbl_zp.release(); h->zbl_para.release();
     for (auto* b : {&h->lmp_x, &h->lmp_forces, &h->lmp_virials}) b->release();
     h->lmp_pin_in.release();
     h->lmp_pin_out.release();

@@ -25,6 +25,7 @@ namespace {
 
 struct Args {
     const int* atomic_numbers;
+    const double* zbl_para;
     const double* q_scaler;
     const double** w0;
     const double** b0;
@@ -56,7 +57,7 @@ int run_atoms(const Args& a, int tid, int nthreads, double* e_atom, double* forc
         }
         double e = 0.0;
         const int code = jse_nep_calEnergyForce(dx.data(), dy.data(), dz.data(), ty.data(), nn, a.type[i],
-                                                a.atomic_numbers, a.q_scaler, a.w0, a.b0, a.w1, a.b1, a.c, nullptr,
+                                                a.atomic_numbers, a.q_scaler, a.w0, a.b0, a.w1, a.b1, a.c, a.zbl_para,
                                                 nullptr, nullptr, nullptr, nullptr, &e, fx.data(), fy.data(),
                                                 fz.data(), fp.data(), sf.data());
         if (code) return code;
@@ -78,14 +79,16 @@ int run_atoms(const Args& a, int tid, int nthreads, double* e_atom, double* forc
 
 // Evaluates atoms [0, n_eval) over the caller's full neighbour rows with nthreads threads;
 // outputs cover all n atoms (a neighbour's force and virial shares included).
-extern "C" int nep_ref_compute(int T, const int* atomic_numbers, const double* q_scaler, const double** w0,
+extern "C" int nep_ref_compute(int T, const int* atomic_numbers, const double* zbl_para, const double* q_scaler,
+                               const double** w0,
                                const double** b0, const double** w1, const double* b1, const double* c, int dim,
                                int sum_size, int n, int n_eval, int nthreads, const int* type, const long* nei_off,
                                const int* nei_j, const double* nei_dx, double* e_atom, double* force,
                                double* virial) {
     (void)T;
     if (nthreads < 1) nthreads = 1;
-    const Args a{atomic_numbers, q_scaler, w0, b0, w1, b1, c, dim, sum_size, n_eval, type, nei_off, nei_j, nei_dx};
+    const Args a{atomic_numbers, zbl_para, q_scaler, w0, b0, w1, b1, c, dim, sum_size, n_eval, type, nei_off, nei_j,
+                 nei_dx};
     std::vector<std::vector<double>> acc(nthreads);
     std::vector<int> codes(nthreads, 0);
     for (auto& v : acc) v.assign((size_t)13 * n, 0.0);

@@ -2,8 +2,10 @@
 
 TEST INFRASTRUCTURE ONLY.  Restates the subset of NEP.java's loader (NEP.java:786-1010)
 and of its parameter split (update_potential, NEP.java:1097-1140) that the GPU path
-supports: potential models of versions 3, 4 and 5 (``nep3``, ``nep4``, ``nep5``) without
-ZBL and without type-wise cutoffs.  Other variants raise ValueError.
+supports: potential models of versions 3, 4 and 5 (``nep3``, ``nep4``, ``nep5``), with or
+without ZBL (``nepV_zbl``: a ``zbl rc_inner rc_outer`` line after the first; both zero
+select the flexible form, whose 10 parameters per species pair follow the descriptor
+scales), without type-wise cutoffs.  Other variants raise ValueError.
 
 The file is whitespace-separated text:
     nepV T sym_1 .. sym_T
@@ -23,6 +25,13 @@ from typing import List
 import numpy as np
 
 
+# Element symbols in periodic-table order (H .. Pu): a species' atomic number is its index + 1
+ELEMENTS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge "
+            "As Se Br Kr Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm "
+            "Eu Gd Tb Dy Ho Er Tm Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn Fr Ra Ac Th Pa U "
+            "Np Pu").split()
+
+
 @dataclass
 class NEPModel:
     version: int
@@ -39,6 +48,19 @@ class NEPModel:
     num_neurons: int
     params: np.ndarray = field(repr=False)     # network then descriptor parameters
     q_scaler: np.ndarray = field(repr=False)
+    zbl: bool = False                          # ZBL short-range term (nepV_zbl)
+    zbl_rc_inner: float = 0.0
+    zbl_rc_outer: float = 0.0
+    zbl_para: np.ndarray = field(default_factory=lambda: np.zeros(0), repr=False)  # flexible: 10 per pair
+
+    @property
+    def zbl_flexible(self) -> bool:
+        return self.zbl and self.zbl_rc_inner == 0.0 and self.zbl_rc_outer == 0.0
+
+    @property
+    def atomic_numbers0(self) -> np.ndarray:
+        """0-based element index of each species (0 for a symbol outside the table)."""
+        return np.array([ELEMENTS.index(x) if x in ELEMENTS else 0 for x in self.symbols], dtype=np.int32)
 
     @property
     def ntypes(self) -> int:
@@ -99,11 +121,18 @@ def load(text: str) -> NEPModel:
     lines = [ln.split() for ln in text.splitlines() if ln.split()]
     head = lines[0]
     versions = {"nep3": 3, "nep4": 4, "nep5": 5}
-    if head[0] not in versions:
-        raise ValueError("unsupported NEP variant %r (potential models nep3/nep4/nep5 without ZBL only)" % head[0])
+    name = head[0][:-4] if head[0].endswith("_zbl") else head[0]
+    if name not in versions:
+        raise ValueError("unsupported NEP variant %r (potential models nep3/nep4/nep5, with or without ZBL)" % head[0])
+    zbl = head[0].endswith("_zbl")
     T = int(head[1])
     if len(head) != 2 + T:
         raise ValueError("the first line must list %d symbols" % T)
+    if zbl:
+        z = lines.pop(1)
+        if z[0] != "zbl" or len(z) != 3:
+            raise ValueError("expected: zbl rc_inner rc_outer")
+        zin, zout = float(z[1]), float(z[2])
     cut = lines[1]
     if cut[0] != "cutoff" or len(cut) not in (5, 8):
         raise ValueError("expected: cutoff rc_radial rc_angular MN_radial MN_angular [factors]")
@@ -112,21 +141,27 @@ def load(text: str) -> NEPModel:
     nmax, bsize, lmax, ann = lines[2], lines[3], lines[4], lines[5]
     if nmax[0] != "n_max" or bsize[0] != "basis_size" or lmax[0] != "l_max" or ann[0] != "ANN":
         raise ValueError("unexpected header line order")
-    m = NEPModel(version=versions[head[0]], symbols=head[2:], rc_radial=float(cut[1]), rc_angular=float(cut[2]),
+    m = NEPModel(version=versions[name], symbols=head[2:], rc_radial=float(cut[1]), rc_angular=float(cut[2]),
                  n_max_radial=int(nmax[1]), n_max_angular=int(nmax[2]), basis_size_radial=int(bsize[1]),
                  basis_size_angular=int(bsize[2]), l_max=int(lmax[1]), l_max_4body=int(lmax[2]),
                  l_max_5body=int(lmax[3]), num_neurons=int(ann[1]), params=np.zeros(0), q_scaler=np.zeros(0))
     vals = np.array([float(x[0]) for x in lines[6:]], dtype=np.float64)
     npar = m.num_para_ann + m.num_para_descriptor
-    if len(vals) != npar + m.dim:
-        raise ValueError("expected %d numbers after the header, found %d" % (npar + m.dim, len(vals)))
+    if zbl:
+        m.zbl, m.zbl_rc_inner, m.zbl_rc_outer = True, zin, zout
+    nz = 10 * T * (T + 1) // 2 if m.zbl_flexible else 0
+    if len(vals) != npar + m.dim + nz:
+        raise ValueError("expected %d numbers after the header, found %d" % (npar + m.dim + nz, len(vals)))
     m.params = vals[:npar]
-    m.q_scaler = vals[npar:]
+    m.q_scaler = vals[npar:npar + m.dim]
+    m.zbl_para = vals[npar + m.dim:]
     return m
 
 
-def write(symbols, version=4, rc=(5.0, 4.0), n_max=(4, 4), basis=(8, 8), l_max=(4, 2, 1), neurons=16, seed=0) -> str:
-    """A random model file (seeded), for tests and benchmarks."""
+def write(symbols, version=4, rc=(5.0, 4.0), n_max=(4, 4), basis=(8, 8), l_max=(4, 2, 1), neurons=16, seed=0,
+          zbl=None) -> str:
+    """A random model file (seeded), for tests and benchmarks.  ``zbl``: None, (rc_inner,
+    rc_outer) for the fixed ZBL form, or "flexible" for per-pair parameters."""
     rng = np.random.default_rng(seed)
     T = len(symbols)
     m = NEPModel(version=version, symbols=list(symbols), rc_radial=rc[0], rc_angular=rc[1], n_max_radial=n_max[0],
@@ -136,8 +171,18 @@ def write(symbols, version=4, rc=(5.0, 4.0), n_max=(4, 4), basis=(8, 8), l_max=(
     ann = rng.normal(0.0, 1.0 / np.sqrt(m.dim), m.num_para_ann)
     c = rng.uniform(-1.0, 1.0, m.num_para_descriptor)
     qs = rng.uniform(0.5, 2.0, m.dim)
-    out = ["nep%d %d %s" % (version, T, " ".join(symbols)),
-           "cutoff %g %g 100 100" % rc, "n_max %d %d" % n_max, "basis_size %d %d" % basis,
-           "l_max %d %d %d" % l_max, "ANN %d 0" % neurons]
-    out += ["%.17g" % v for v in np.concatenate([ann, c, qs])]
+    out = ["nep%d%s %d %s" % (version, "_zbl" if zbl else "", T, " ".join(symbols))]
+    extra = np.zeros(0)
+    if zbl == "flexible":
+        out.append("zbl 0 0")
+        pairs = T * (T + 1) // 2
+        extra = np.concatenate([[rng.uniform(1.0, 1.4), rng.uniform(2.0, 2.4), rng.uniform(0.1, 0.3),
+                                 rng.uniform(2.5, 3.5), rng.uniform(0.4, 0.6), rng.uniform(0.8, 1.0),
+                                 rng.uniform(0.2, 0.3), rng.uniform(0.3, 0.5), rng.uniform(0.02, 0.04),
+                                 rng.uniform(0.15, 0.25)] for _ in range(pairs)])
+    elif zbl:
+        out.append("zbl %g %g" % tuple(zbl))
+    out += ["cutoff %g %g 100 100" % rc, "n_max %d %d" % n_max, "basis_size %d %d" % basis,
+            "l_max %d %d %d" % l_max, "ANN %d 0" % neurons]
+    out += ["%.17g" % v for v in np.concatenate([ann, c, qs, extra])]
     return "\n".join(out) + "\n"

@@ -122,10 +122,48 @@ def descriptors(m: NEPModel, types0: np.ndarray, nl) -> np.ndarray:
     return q
 
 
+# Universal ZBL screening function (Ziegler, Biersack and Littmark): phi(x) = sum a_k exp(-b_k x)
+ZBL_UNIVERSAL = ((0.18175, 3.1998), (0.50986, 0.94229), (0.28022, 0.4029), (0.02817, 0.20162))
+K_COULOMB = 14.399645   # e^2 / (4 pi eps0) in eV A
+ZBL_MAX_R = 2.5         # pairs at or beyond this distance carry no ZBL term (find_force_ZBL)
+
+
+def zbl_pair_energy(m: NEPModel, ti: int, tj: int, r: float) -> float:
+    """The ZBL energy of one pair (find_force_ZBL, nep_core.hpp:1321-1386): the screened
+    Coulomb repulsion Z_i Z_j k / r phi(r / a), 1/a = 2.134563 (Z_i^0.23 + Z_j^0.23), times a
+    cosine switch from 1 at rc_inner to 0 at rc_outer.  Fixed form: the universal phi and the
+    file's two radii; flexible form: per species pair [rc_inner, rc_outer, a1, b1, .., a4, b4]."""
+    if r >= ZBL_MAX_R:
+        return 0.0
+    zi, zj = m.atomic_numbers0[ti] + 1, m.atomic_numbers0[tj] + 1
+    a_inv = (zi ** 0.23 + zj ** 0.23) * 2.134563   # 1 / a in 1/A
+    x = r * a_inv
+    if m.zbl_flexible:
+        t1, t2 = min(ti, tj), max(ti, tj)
+        k = t1 * m.ntypes - t1 * (t1 - 1) // 2 + (t2 - t1)
+        p = m.zbl_para[10 * k:10 * k + 10]
+        rin, rout, coefs = p[0], p[1], [(p[2 + 2 * q], p[3 + 2 * q]) for q in range(4)]
+    else:
+        rin, rout, coefs = m.zbl_rc_inner, m.zbl_rc_outer, ZBL_UNIVERSAL
+    phi = sum(a * np.exp(-b * x) for a, b in coefs)
+    if r < rin:
+        fc = 1.0
+    elif r < rout:
+        fc = 0.5 * np.cos(np.pi / (rout - rin) * (r - rin)) + 0.5
+    else:
+        fc = 0.0
+    return K_COULOMB * zi * zj * phi / r * fc
+
+
 def energies(m: NEPModel, types0: np.ndarray, nl) -> np.ndarray:
     q = descriptors(m, types0, nl) * m.q_scaler[None, :]
     e = np.zeros(len(types0))
     for i, t in enumerate(types0):
         w0, b0, w1, extra = m.ann(int(t))
         e[i] = float(w1 @ np.tanh(w0 @ q[i] - b0)) - m.b1 - extra
+    if m.zbl:  # each atom holds half of each of its pairs' ZBL energies
+        r = np.linalg.norm(np.asarray(nl.dx, dtype=np.float64), axis=1)
+        owner = np.repeat(np.arange(len(types0)), np.diff(nl.offsets))
+        for q in np.nonzero(r < ZBL_MAX_R)[0]:
+            e[owner[q]] += 0.5 * zbl_pair_energy(m, int(types0[owner[q]]), int(types0[nl.j[q]]), float(r[q]))
     return e

@@ -89,7 +89,8 @@ class RefNEP:
         self.b1 = arr(np.array([m.b1]))
         self.c = arr(m.c)
         self.qs = arr(m.q_scaler)
-        self.an = np.zeros(T, dtype=np.int32)
+        self.zp = arr(m.zbl_para if len(m.zbl_para) else np.zeros(1))
+        self.an = np.ascontiguousarray(m.atomic_numbers0, dtype=np.int32)
 
     def compute(self, types0, nl, nthreads: int = 1, n_eval: Optional[int] = None):
         types0 = np.ascontiguousarray(types0, dtype=np.int32)
@@ -98,7 +99,7 @@ class RefNEP:
         e, f, v = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 9))
         dx = np.ascontiguousarray(nl.dx, dtype=np.float64)
         ip, lp, dp = C.POINTER(C.c_int), C.POINTER(C.c_long), C.POINTER(C.c_double)
-        code = self.lib.nep_ref_compute(self.m.ntypes, self.an.ctypes.data_as(ip), self.qs, self.w0, self.b0,
+        code = self.lib.nep_ref_compute(self.m.ntypes, self.an.ctypes.data_as(ip), self.zp, self.qs, self.w0, self.b0,
                                         self.w1, self.b1, self.c, self.m.dim, (self.m.n_max_angular + 1) * 80, n, n_eval,
                                         int(nthreads), types0.ctypes.data_as(ip), nl.offsets.ctypes.data_as(lp),
                                         nl.j.ctypes.data_as(ip), dx.ctypes.data_as(dp), e.ctypes.data_as(dp),

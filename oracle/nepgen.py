@@ -25,13 +25,14 @@ def gen_map(m: NEPModel) -> Dict[str, object]:
         "NEPGEN_TYPEWISE_CUTOFF_FACTOR_R": 2.5, "NEPGEN_TYPEWISE_CUTOFF_FACTOR_A": 2.0,
         "NEPGEN_TYPEWISE_CUTOFF_FACTOR_ZBL": 0.65,
         "NEPGEN_RCUT_R": repr(float(m.rc_radial)), "NEPGEN_RCUT_A": repr(float(m.rc_angular)),
-        "NEPGEN_RCUT_INNER_ZBL": "1.0", "NEPGEN_RCUT_OUTER_ZBL": "2.0",
+        "NEPGEN_RCUT_INNER_ZBL": repr(float(m.zbl_rc_inner)) if m.zbl else "1.0",
+        "NEPGEN_RCUT_OUTER_ZBL": repr(float(m.zbl_rc_outer)) if m.zbl else "2.0",
         "NEPGEN_NMAX_R": m.n_max_radial, "NEPGEN_NMAX_A": m.n_max_angular,
         "NEPGEN_BSIZE_R": m.basis_size_radial, "NEPGEN_BSIZE_A": m.basis_size_angular,
         "NEPGEN_NUMC_R": m.num_c_radial, "NEPGEN_LMAX": m.l_max, "NEPGEN_NUML": m.num_L,
         "NEPGEN_ANN_DIM_A": m.dim_angular, "NEPGEN_ANN_DIM": m.dim, "NEPGEN_NUM_NEURONS1": m.num_neurons,
         "NEPGEN_NUM_PARA": m.num_para_ann + m.num_para_descriptor, "NEPGEN_NUM_PARA_ANN": m.num_para_ann,
-        "NEPGEN_ZBL": 0, "NEPGEN_ZBL_FLEXIBLED": 0,
+        "NEPGEN_ZBL": 1 if m.zbl else 0, "NEPGEN_ZBL_FLEXIBLED": 1 if m.zbl_flexible else 0,
         "[PRECISION]": "double", "[ARCH]": "cpu",
     }
 

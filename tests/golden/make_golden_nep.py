@@ -29,26 +29,35 @@ from oracle import native as ON, nep_model as NM, nep_ref as NR  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
-# name: (symbols, version, rc (R, A), n_max, basis, l_max (3-, 4-, 5-body), neurons, structure)
+# name: (symbols, version, rc (R, A), n_max, basis, l_max (3-, 4-, 5-body), neurons, structure
+#        (kind, atoms, tilt[, minimum separation]) [, ZBL: (rc_inner, rc_outer) or "flexible"])
 CASES = {
     "nep4_binary": (["Si", "O"], 4, (5.0, 4.0), (4, 4), (8, 8), (4, 2, 1), 16, ("liquid", 150, 0.1)),
     "nep3_single": (["C"], 3, (4.5, 4.5), (4, 4), (8, 8), (4, 0, 0), 8, ("liquid", 90, None)),
     "nep5_ternary": (["A", "B", "C"], 5, (5.5, 4.2), (4, 4), (8, 8), (4, 2, 0), 12, ("liquid", 200, 0.05)),
     "nep4_wide": (["Ga", "N"], 4, (5.2, 4.6), (6, 6), (8, 8), (4, 2, 1), 20, ("liquid", 120, None)),
     "nep4_5body": (["Li", "P", "S"], 4, (6.0, 4.0), (4, 4), (8, 8), (4, 0, 1), 10, ("liquid", 160, 0.08)),
+    # ZBL: the fixed universal form with its two radii, and the flexible per-pair form; a 1.3 A
+    # minimum separation puts pairs inside rc_inner as well as in the switching range
+    "nep4_zbl": (["Si", "O"], 4, (5.0, 4.0), (4, 4), (8, 8), (4, 2, 1), 12, ("liquid", 150, 0.1, 1.3),
+                 (1.6, 2.3)),
+    "nep3_zbl_flex": (["W", "Be"], 3, (5.0, 4.0), (4, 4), (8, 8), (4, 2, 0), 8, ("liquid", 120, None, 1.3),
+                      "flexible"),
 }
 
 
 def structure(spec, T, seed):
-    kind, n, tilt = spec
-    return W.random_liquid(n, 0.06, [1.0 / T] * T, 2.0, seed, tilt=tilt)
+    kind, n, tilt = spec[:3]
+    rmin = spec[3] if len(spec) > 3 else 2.0
+    return W.random_liquid(n, 0.06, [1.0 / T] * T, rmin, seed, tilt=tilt)
 
 
 def make(name):
-    symbols, version, rc, n_max, basis, l_max, neurons, spec = CASES[name]
+    symbols, version, rc, n_max, basis, l_max, neurons, spec = CASES[name][:8]
+    zbl = CASES[name][8] if len(CASES[name]) > 8 else None
     seed = 1000 + sum(map(ord, name))
     text = NM.write(symbols, version=version, rc=rc, n_max=n_max, basis=basis, l_max=l_max, neurons=neurons,
-                    seed=seed)
+                    seed=seed, zbl=zbl)
     m = NM.load(text)
     s = structure(spec, len(symbols), seed)
     xw = ON.wrap(s.x, s.box_kind, s.box)
