@@ -138,6 +138,8 @@ struct Run {
     std::vector<DevBuf<int>> inv_start;
     // per sub: the spherical kernels scan the compact rows of the handle's sub_rc cutoff
     std::vector<char> use_sub;
+    // per sub: NEP type-wise cutoffs, [T][T] (rc, 1/rc), empty when the pairs share rcut
+    std::vector<DevBuf<float2>> prc;
 };
 
 struct NetDev {
@@ -187,7 +189,7 @@ struct nnap_handle {
     nnapgb::DevBuf<float4> pdx, pg;
     nnapgb::DevBuf<int> prev, pcount;
     nnapgb::DevBuf<float> fp, gfp, A, Gx;  // Gx: invariant-column part of dE/dA (when present)
-    nnapgb::DevBuf<float> zbl_z, zbl_zp, zbl_para;  // NEP ZBL: per species Z, Z^0.23; flexible parameters
+    nnapgb::DevBuf<float> zbl_z, zbl_zp, zbl_para, zbl_rc;  // NEP ZBL: per species Z, Z^0.23; flexible parameters
     // compact rows of the entries within sub_rc (0: none) for spherical sub-bases whose
     // cutoff is well inside the neighbour cutoff: dx and row position [n][M], count [n]
     double sub_rc = 0.0;

@@ -42,6 +42,9 @@ struct DescArgs {
     const float4* sub_dx;
     const int* sub_pos;
     const int* sub_count;
+    // NEP type-wise cutoffs: (rc, 1/rc) of each species pair, [T][T] centre species major,
+    // or NULL: every pair uses rcut
+    const float2* pair_rc = nullptr;
 };
 
 // Invariant (l3max / l4max) columns of one spherical sub-basis over a run of species:

@@ -39,6 +39,22 @@ __device__ __forceinline__ int atom_of(const DescArgs& a, int s0, int warp) { re
 
 }  // namespace
 
+// NEP type-wise cutoffs (find_descriptor, nep_core.hpp:1074-1082 and 1117-1125): a pair's
+// radial functions use its own cutoff min(rc, (R_cov,i + R_cov,j) factor), and a pair at or
+// beyond it adds nothing. Sets rc / irc to the pair's values; false when r is beyond them.
+template <int RB>
+__device__ __forceinline__ bool pair_cut(const DescArgs& a, int tc, int tn, float r, float& rc, float& irc) {
+    if constexpr (RB == kRbNEP) {
+        if (a.pair_rc) {
+            const float2 q = a.pair_rc[tc * a.T + tn];
+            rc = q.x;
+            irc = q.y;
+            return r < rc;
+        }
+    }
+    return true;
+}
+
 // =========================================================================== radial
 template <int NP, int N1, int RB>
 __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
@@ -61,8 +77,10 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_fwd(DescArgs a) {
         const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         if (r >= rc) continue;
         const int tn = __float_as_int(d.w) - 1;
+        float rcp = rc, ircp = irc;
+        if (!pair_cut<RB>(a, tc, tn, r, rcp, ircp)) continue;
         float T[N1], sv[NP];
-        const float fc = radial_f<RB, N1>(r, irc, T);
+        const float fc = radial_f<RB, N1>(r, ircp, T);
         fuse_apply<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, T, sv);
 #pragma unroll
         for (int p = 0; p < NP; ++p) acc[p] += fc * sv[p];
@@ -99,10 +117,11 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_radial_bwd(DescArgs a) {
         const float4 d = a.P.dx[e];
         const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
         float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (r < rc) {
-            const int tn = __float_as_int(d.w) - 1;
+        const int tn = __float_as_int(d.w) - 1;
+        float rcp = rc, ircp = irc;
+        if (r < rc && pair_cut<RB>(a, tc, tn, r, rcp, ircp)) {
             float T[N1], TG[N1], fcg;
-            const float fc = radial_g<RB, N1>(r, rc, irc, T, TG, &fcg);
+            const float fc = radial_g<RB, N1>(r, rcp, ircp, T, TG, &fcg);
             float v[N1];
             fuse_apply_t<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, gfp, v);
             float dfc = 0.f, drn = 0.f;
@@ -172,11 +191,12 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps) k_sph_fwd(DescArgs a) {
         if (k < cnt) {
             const float4 d = rdx[k];
             const float r = sqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
-            if (r < rc) {
+            const int tn = __float_as_int(d.w) - 1;
+            float rcp = rc, ircp = irc;
+            if (r < rc && pair_cut<RB>(a, tc, tn, r, rcp, ircp)) {
                 valid = true;
-                const int tn = __float_as_int(d.w) - 1;
                 float T[N1], sv[NP];
-                const float fc = radial_f<RB, N1>(r, irc, T);
+                const float fc = radial_f<RB, N1>(r, ircp, T);
                 fuse_apply<NP, N1>(sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P, T, sv);
 #pragma unroll
                 for (int p = 0; p < NP; ++p) c[p] = fc * sv[p];
@@ -431,7 +451,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
         const int k = base + lane;
         float c[NP];
         float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
-        float r = 1.f;
+        float r = 1.f, rcp = rc, ircp = irc;
         bool valid = false;
         if (k < cnt) {
             d = rdx[k];
@@ -439,10 +459,11 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
             valid = r < rc;
         }
         const int tn = valid ? __float_as_int(d.w) - 1 : 0;
+        if (valid) valid = pair_cut<RB>(a, tc, tn, r, rcp, ircp);
         const float* Wt = sW + (size_t)(tc * a.T + tn) * NP * Fuse<N1>::N1P;
         if (valid) {
             float T[N1], sv[NP];
-            const float fc = radial_f<RB, N1>(r, irc, T);
+            const float fc = radial_f<RB, N1>(r, ircp, T);
             fuse_apply<NP, N1>(Wt, T, sv);
 #pragma unroll
             for (int p = 0; p < NP; ++p) c[p] = fc * sv[p];
@@ -503,7 +524,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (valid) {
                 float T[N1], TG[N1], v[N1], fcg;
-                const float fc = radial_g<RB, N1>(r, rc, irc, T, TG, &fcg);
+                const float fc = radial_g<RB, N1>(r, rcp, ircp, T, TG, &fcg);
                 float dc[NP];
 #pragma unroll
                 for (int p = 0; p < NP; ++p) dc[p] = (p & 1) ? dc2[p >> 1].y : dc2[p >> 1].x;

@@ -52,6 +52,10 @@ __global__ void __launch_bounds__(256) k_nep_zbl(PairBufs P, int n, const int* _
 #pragma unroll
             for (int q = 0; q < 4; ++q) zbl_term(p[2 + 2 * q], p[3 + 2 * q], x, phi, dphi);
         } else {
+            if (z.rc_pair) {
+                rin = z.rc_pair[2 * (ti * z.T + tj)];
+                rout = z.rc_pair[2 * (ti * z.T + tj) + 1];
+            }
             zbl_term(0.18175f, 3.1998f, x, phi, dphi);
             zbl_term(0.50986f, 0.94229f, x, phi, dphi);
             zbl_term(0.28022f, 0.4029f, x, phi, dphi);

@@ -24,6 +24,7 @@ struct SubBasis {
     std::vector<std::vector<InvTerm>> inv;
     int fp_off = 0, size = 0;
     double rcut = 6.0;
+    std::vector<double> pair_rc;  // NEP type-wise cutoffs: per neighbour species (<= rcut), or empty
     bool fused = false;     // wtype fuse / rfuse / exfuse: the matrix is a trainable parameter
     std::vector<double> W;  // T * np * (nmax+1)
 };
@@ -52,6 +53,7 @@ struct ZblModel {
     double rc_inner = 0.0, rc_outer = 0.0;
     std::vector<int> z;        // atomic number of each species
     std::vector<double> para;  // flexible: 10 per pair (t1 <= t2, row-major upper triangle)
+    std::vector<double> pair_rc;  // fixed form, type-wise radii: [T][T][2] (rc_inner, rc_outer), or empty
 };
 
 struct Model {
@@ -67,8 +69,7 @@ struct Model {
 // Parse and pack; throws std::runtime_error with a message on invalid input.
 Model load_model(const char* text, size_t len);
 
-// A valid NEP file of a variant the GPU path does not evaluate (dipole, polarizability,
-// type-wise cutoffs).
+// A valid NEP file of a variant the GPU path does not evaluate (dipole, polarizability).
 struct NepUnsupported : std::runtime_error {
     using std::runtime_error::runtime_error;
 };

@@ -3,8 +3,8 @@
 // The loader follows NEP(String) (NEP.java:786-1010): a header of whitespace-separated
 // lines, then one number per line (the network parameters, the descriptor coefficients
 // c and the dim descriptor scales q_scaler).  Potential models nep3, nep4 and nep5,
-// with or without ZBL (fixed or flexible), without type-wise cutoffs, are mapped; the
-// other variants (dipole, polarizability, type-wise cutoffs) throw NepUnsupported.
+// with or without ZBL (fixed or flexible) and type-wise cutoffs, are mapped; the other
+// variants (dipole, polarizability) throw NepUnsupported.
 //
 // NEP's per-atom arithmetic (nep_core.hpp, find_q / find_q_with_4body / _5body and
 // apply_ann_one_layer) is, in the quantities of the NNAP pipeline:
@@ -42,6 +42,22 @@ const char* const kElements[kNumElements] = {
     "In", "Sn", "Sb", "Te", "I",  "Xe", "Cs", "Ba", "La", "Ce", "Pr", "Nd", "Pm", "Sm", "Eu", "Gd",
     "Tb", "Dy", "Ho", "Er", "Tm", "Yb", "Lu", "Hf", "Ta", "W",  "Re", "Os", "Ir", "Pt", "Au", "Hg",
     "Tl", "Pb", "Bi", "Po", "At", "Rn", "Fr", "Ra", "Ac", "Th", "Pa", "U",  "Np", "Pu"};
+
+// Covalent radii (A) by periodic-table index, the table NEP's type-wise cutoffs scale
+// (COVALENT_RADIUS, nep_core.hpp:247-258)
+const double kCovalentRadius[kNumElements] = {
+    0.426667, 0.613333, 1.6, 1.25333, 1.02667, 1.0, 0.946667, 0.84,
+    0.853333, 0.893333, 1.86667, 1.66667, 1.50667, 1.38667, 1.46667, 1.36,
+    1.32, 1.28, 2.34667, 2.05333, 1.77333, 1.62667, 1.61333, 1.46667,
+    1.42667, 1.38667, 1.33333, 1.32, 1.34667, 1.45333, 1.49333, 1.45333,
+    1.53333, 1.46667, 1.52, 1.56, 2.52, 2.22667, 1.96, 1.85333,
+    1.76, 1.65333, 1.53333, 1.50667, 1.50667, 1.44, 1.53333, 1.64,
+    1.70667, 1.68, 1.68, 1.64, 1.76, 1.74667, 2.78667, 2.34667,
+    2.16, 1.96, 2.10667, 2.09333, 2.08, 2.06667, 2.01333, 2.02667,
+    2.01333, 2.0, 1.98667, 1.98667, 1.97333, 2.04, 1.94667, 1.82667,
+    1.74667, 1.64, 1.57333, 1.54667, 1.48, 1.49333, 1.50667, 1.76,
+    1.73333, 1.73333, 1.81333, 1.74667, 1.84, 1.89333, 2.68, 2.41333,
+    2.22667, 2.10667, 2.02667, 2.04, 2.05333, 2.06667};
 
 void bad(const std::string& m) { throw std::runtime_error("nep.txt: " + m); }
 
@@ -108,8 +124,13 @@ Model load_nep_model(const char* text, size_t len) {
     const auto& cut = next(0, "cutoff");
     if (cut.size() != 5 && cut.size() != 8) bad("this line should be cutoff rc_radial rc_angular MN_radial MN_angular");
     const double rcR = to_double(cut[1]), rcA = to_double(cut[2]);
-    if (cut.size() == 8 && (to_double(cut[5]) > 0.0 || to_double(cut[7]) > 0.0))
-        throw NepUnsupported("type-wise cutoffs are not supported");
+    // type-wise cutoff factors (radial, angular, ZBL): a radial factor > 0 gives every
+    // species pair of the descriptors its own cutoffs, a ZBL factor > 0 the fixed-form ZBL
+    // its own radii (NEP.java:905-916)
+    const double fR = cut.size() == 8 ? to_double(cut[5]) : 0.0;
+    const double fA = cut.size() == 8 ? to_double(cut[6]) : 0.0;
+    const double fZ = cut.size() == 8 ? to_double(cut[7]) : 0.0;
+    const bool tw = fR > 0.0, twz = fZ > 0.0;
     if (!(rcR > 0.0) || !(rcA > 0.0)) bad("cutoffs must be positive");
     const auto& nm = next(3, "n_max n_max_radial n_max_angular");
     const int nR = to_int(nm[1]), nA = to_int(nm[2]);
@@ -139,6 +160,19 @@ Model load_nep_model(const char* text, size_t len) {
     const double* qs = v.data() + npa + npd;
     const double b1 = v[npa - 1];
 
+    // periodic-table index of each species, 0 (hydrogen) when the symbol is not an element
+    std::vector<int> anum(T, 0);
+    for (int t = 0; t < T; ++t)
+        for (int e = 0; e < kNumElements; ++e)
+            if (head[2 + t] == kElements[e]) {
+                anum[t] = e;
+                break;
+            }
+    // a pair's type-wise cutoff: min(rc, (R_cov,i + R_cov,j) factor) (nep_core.hpp:1078, 1121, 1371)
+    auto pair_cut = [&](double rc, double f, int ti, int tj) {
+        return std::min(rc, (kCovalentRadius[anum[ti]] + kCovalentRadius[anum[tj]]) * f);
+    };
+
     Model m;
     m.units = "metal";
     m.rcut_max = std::max(rcR, rcA);
@@ -149,16 +183,15 @@ Model load_nep_model(const char* text, size_t len) {
         m.zbl.flexible = zflex;
         m.zbl.rc_inner = zin;
         m.zbl.rc_outer = zout;
-        for (int t = 0; t < T; ++t) {
-            int zi = 0;  // index in the periodic table, 0 (hydrogen) when the symbol is not an element
-            for (int e = 0; e < kNumElements; ++e)
-                if (head[2 + t] == kElements[e]) {
-                    zi = e;
-                    break;
-                }
-            m.zbl.z.push_back(zi + 1);
-        }
+        for (int t = 0; t < T; ++t) m.zbl.z.push_back(anum[t] + 1);
         m.zbl.para.assign(v.begin() + npa + npd + dim, v.end());
+        if (twz && !zflex)  // rc_outer shrunk to the pair's covalent size, rc_inner its half
+            for (int ti = 0; ti < T; ++ti)
+                for (int tj = 0; tj < T; ++tj) {
+                    const double ro = pair_cut(zout, fZ, ti, tj);
+                    m.zbl.pair_rc.push_back(0.5 * ro);
+                    m.zbl.pair_rc.push_back(ro);
+                }
     }
     const int l3 = b4 ? 2 : 0, l4 = b5 ? 1 : 0;
     const auto inv = invariant_columns(l3, l4);
@@ -213,6 +246,11 @@ Model load_nep_model(const char* text, size_t len) {
             for (int n = 0; n <= nA; ++n)
                 for (int k = 0; k <= bA; ++k)
                     s.W[((size_t)tn * s.np + n) * (bA + 1) + k] = c[ncR + (n * (bA + 1) + k) * T * T + t * T + tn];
+        if (tw)
+            for (int tn = 0; tn < T; ++tn) {
+                r.pair_rc.push_back(pair_cut(rcR, fR, t, tn));
+                s.pair_rc.push_back(pair_cut(rcA, fA, t, tn));
+            }
         sp.subs = {r, s};
         sp.D = D;
         // network: one tanh layer of H units

@@ -146,6 +146,18 @@ void upload_model(nnap_handle* h) {
                 if (use && h->sub_rc == 0.0) h->sub_rc = s.rcut;
                 r.use_sub.push_back(use && s.rcut == h->sub_rc);
             }
+            // NEP type-wise cutoffs of the run's species pairs
+            r.prc.emplace_back();
+            if (!m.sp[r.t0].subs[k].pair_rc.empty()) {
+                std::vector<float2> q((size_t)T * T, make_float2((float)s.rcut, (float)(1.0 / s.rcut)));
+                for (int tc = r.t0; tc < r.t1; ++tc)
+                    for (int tn = 0; tn < T; ++tn) {
+                        const double rc = m.sp[tc].subs[k].pair_rc[tn];
+                        q[(size_t)tc * T + tn] = make_float2((float)rc, (float)(1.0 / rc));
+                    }
+                r.prc.back().ensure(q.size());
+                CK(cudaMemcpy(r.prc.back().p, q.data(), q.size() * sizeof(float2), cudaMemcpyHostToDevice));
+            }
             r.nzp.emplace_back();
             r.nzw.emplace_back();
             if (sparse) {
@@ -172,6 +184,11 @@ void upload_model(nnap_handle* h) {
         CK(cudaMemcpy(h->zbl_zp.p, zp.data(), sizeof(float) * T, cudaMemcpyHostToDevice));
         if (!par.empty())
             CK(cudaMemcpy(h->zbl_para.p, par.data(), sizeof(float) * par.size(), cudaMemcpyHostToDevice));
+        if (!m.zbl.pair_rc.empty()) {
+            std::vector<float> rcp(m.zbl.pair_rc.begin(), m.zbl.pair_rc.end());
+            h->zbl_rc.ensure(rcp.size());
+            CK(cudaMemcpy(h->zbl_rc.p, rcp.data(), sizeof(float) * rcp.size(), cudaMemcpyHostToDevice));
+        }
     }
     // networks
     h->nets.resize(T);
@@ -529,6 +546,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.fp = h->fp.p;
                 a.fp_stride = h->fp_stride;
                 a.fp_off = r.fp_off[k];
+                a.pair_rc = r.prc[k].p;
                 a.A = nullptr;
                 a.Gx = nullptr;
                 size_t this_off = a_off;
@@ -650,6 +668,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
         za.z = h->zbl_z.p;
         za.zp = h->zbl_zp.p;
         za.para = h->zbl_para.p;
+        za.rc_pair = h->zbl_rc.p;
         CK(launch_nep_zbl(pair_bufs(h), n, d_type, za, h->e_atom.p, st));
         ++h->launches;
     }
@@ -1018,7 +1037,7 @@ int nnap_destroy(nnap_handle* h) {
     h->status.release(); h->xf.release(); h->xlo.release(); h->pgrp.release(); h->sdev.release(); h->pkey.release(); h->pdx.release(); h->pg.release();
     h->prev.release(); h->pcount.release(); h->fp.release(); h->gfp.release(); h->A.release(); h->Gx.release(); h->gstart.release();
     h->sdx.release(); h->spos.release(); h->scount.release();
-    h->zbl_z.release(); h->zbl_zp.release(); h->zbl_para.release();
+    h->zbl_z.release(); h->zbl_zp.release(); h->zbl_para.release(); h->zbl_rc.release();
     for (auto* b : {&h->lmp_x, &h->lmp_forces, &h->lmp_virials}) b->release();
     h->lmp_pin_in.release();
     h->lmp_pin_out.release();

@@ -15,6 +15,7 @@ struct ZblArgs {
     const float* z;            // [T] atomic numbers
     const float* zp;           // [T] Z^0.23
     const float* para;         // flexible: [T (T + 1) / 2][10]
+    const float* rc_pair;      // fixed form with type-wise radii: [T][T][2] (rc_inner, rc_outer), or NULL
 };
 
 // Adds each atom's half of its pairs' ZBL energies to e_atom and the ZBL part of each

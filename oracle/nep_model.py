@@ -5,11 +5,12 @@ and of its parameter split (update_potential, NEP.java:1097-1140) that the GPU p
 supports: potential models of versions 3, 4 and 5 (``nep3``, ``nep4``, ``nep5``), with or
 without ZBL (``nepV_zbl``: a ``zbl rc_inner rc_outer`` line after the first; both zero
 select the flexible form, whose 10 parameters per species pair follow the descriptor
-scales), without type-wise cutoffs.  Other variants raise ValueError.
+scales), with or without type-wise cutoffs (three factors after the cutoff line's
+neighbour counts: radial, angular, ZBL).  Other variants raise ValueError.
 
 The file is whitespace-separated text:
     nepV T sym_1 .. sym_T
-    cutoff rc_radial rc_angular MN_radial MN_angular
+    cutoff rc_radial rc_angular MN_radial MN_angular [radial_factor angular_factor zbl_factor]
     n_max n_max_radial n_max_angular
     basis_size basis_size_radial basis_size_angular
     l_max l_max_3body l_max_4body l_max_5body
@@ -32,6 +33,21 @@ ELEMENTS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe
             "Np Pu").split()
 
 
+# Covalent radii (A) by periodic-table index, scaled by the type-wise cutoffs
+# (COVALENT_RADIUS, nep_core.hpp:247-258)
+COVALENT_RADIUS = (
+    0.426667, 0.613333, 1.6, 1.25333, 1.02667, 1.0, 0.946667, 0.84, 0.853333, 0.893333,
+    1.86667, 1.66667, 1.50667, 1.38667, 1.46667, 1.36, 1.32, 1.28, 2.34667, 2.05333,
+    1.77333, 1.62667, 1.61333, 1.46667, 1.42667, 1.38667, 1.33333, 1.32, 1.34667, 1.45333,
+    1.49333, 1.45333, 1.53333, 1.46667, 1.52, 1.56, 2.52, 2.22667, 1.96, 1.85333,
+    1.76, 1.65333, 1.53333, 1.50667, 1.50667, 1.44, 1.53333, 1.64, 1.70667, 1.68,
+    1.68, 1.64, 1.76, 1.74667, 2.78667, 2.34667, 2.16, 1.96, 2.10667, 2.09333,
+    2.08, 2.06667, 2.01333, 2.02667, 2.01333, 2.0, 1.98667, 1.98667, 1.97333, 2.04,
+    1.94667, 1.82667, 1.74667, 1.64, 1.57333, 1.54667, 1.48, 1.49333, 1.50667, 1.76,
+    1.73333, 1.73333, 1.81333, 1.74667, 1.84, 1.89333, 2.68, 2.41333, 2.22667, 2.10667,
+    2.02667, 2.04, 2.05333, 2.06667,
+)
+
 @dataclass
 class NEPModel:
     version: int
@@ -52,6 +68,21 @@ class NEPModel:
     zbl_rc_inner: float = 0.0
     zbl_rc_outer: float = 0.0
     zbl_para: np.ndarray = field(default_factory=lambda: np.zeros(0), repr=False)  # flexible: 10 per pair
+    typewise: tuple = (0.0, 0.0, 0.0)          # type-wise cutoff factors: radial, angular, ZBL
+
+    def pair_cutoff(self, rc: float, factor: float, ti, tj):
+        """A species pair's type-wise cutoff min(rc, (R_cov,i + R_cov,j) factor)
+        (find_descriptor / find_force_ZBL, nep_core.hpp:1078, 1121, 1371); ti, tj may be arrays."""
+        R = np.asarray(COVALENT_RADIUS)[self.atomic_numbers0]
+        return np.minimum(rc, (R[ti] + R[tj]) * factor)
+
+    @property
+    def typewise_descriptors(self) -> bool:
+        return self.typewise[0] > 0.0
+
+    @property
+    def typewise_zbl(self) -> bool:
+        return self.typewise[2] > 0.0
 
     @property
     def zbl_flexible(self) -> bool:
@@ -136,8 +167,6 @@ def load(text: str) -> NEPModel:
     cut = lines[1]
     if cut[0] != "cutoff" or len(cut) not in (5, 8):
         raise ValueError("expected: cutoff rc_radial rc_angular MN_radial MN_angular [factors]")
-    if len(cut) == 8 and (float(cut[5]) > 0 or float(cut[7]) > 0):
-        raise ValueError("type-wise cutoffs are not supported")
     nmax, bsize, lmax, ann = lines[2], lines[3], lines[4], lines[5]
     if nmax[0] != "n_max" or bsize[0] != "basis_size" or lmax[0] != "l_max" or ann[0] != "ANN":
         raise ValueError("unexpected header line order")
@@ -145,6 +174,8 @@ def load(text: str) -> NEPModel:
                  n_max_radial=int(nmax[1]), n_max_angular=int(nmax[2]), basis_size_radial=int(bsize[1]),
                  basis_size_angular=int(bsize[2]), l_max=int(lmax[1]), l_max_4body=int(lmax[2]),
                  l_max_5body=int(lmax[3]), num_neurons=int(ann[1]), params=np.zeros(0), q_scaler=np.zeros(0))
+    if len(cut) == 8:
+        m.typewise = (float(cut[5]), float(cut[6]), float(cut[7]))
     vals = np.array([float(x[0]) for x in lines[6:]], dtype=np.float64)
     npar = m.num_para_ann + m.num_para_descriptor
     if zbl:
@@ -159,9 +190,10 @@ def load(text: str) -> NEPModel:
 
 
 def write(symbols, version=4, rc=(5.0, 4.0), n_max=(4, 4), basis=(8, 8), l_max=(4, 2, 1), neurons=16, seed=0,
-          zbl=None) -> str:
+          zbl=None, typewise=None) -> str:
     """A random model file (seeded), for tests and benchmarks.  ``zbl``: None, (rc_inner,
-    rc_outer) for the fixed ZBL form, or "flexible" for per-pair parameters."""
+    rc_outer) for the fixed ZBL form, or "flexible" for per-pair parameters; ``typewise``:
+    None or the three type-wise cutoff factors (radial, angular, ZBL)."""
     rng = np.random.default_rng(seed)
     T = len(symbols)
     m = NEPModel(version=version, symbols=list(symbols), rc_radial=rc[0], rc_angular=rc[1], n_max_radial=n_max[0],
@@ -182,7 +214,8 @@ def write(symbols, version=4, rc=(5.0, 4.0), n_max=(4, 4), basis=(8, 8), l_max=(
                                  rng.uniform(0.15, 0.25)] for _ in range(pairs)])
     elif zbl:
         out.append("zbl %g %g" % tuple(zbl))
-    out += ["cutoff %g %g 100 100" % rc, "n_max %d %d" % n_max, "basis_size %d %d" % basis,
+    cutline = "cutoff %g %g 100 100" % rc + ("" if typewise is None else " %g %g %g" % tuple(typewise))
+    out += [cutline, "n_max %d %d" % n_max, "basis_size %d %d" % basis,
             "l_max %d %d %d" % l_max, "ANN %d 0" % neurons]
     out += ["%.17g" % v for v in np.concatenate([ann, c, qs, extra])]
     return "\n".join(out) + "\n"

@@ -81,7 +81,11 @@ def _channels(m: NEPModel, r: np.ndarray, ti: int, tj: np.ndarray, angular: bool
         rc, nmax, b, off = m.rc_angular, m.n_max_angular, m.basis_size_angular, m.num_c_radial
     else:
         rc, nmax, b, off = m.rc_radial, m.n_max_radial, m.basis_size_radial, 0
-    f = radial_functions(r, rc, b)                                        # [b+1, nj]
+    if m.typewise_descriptors:   # each pair's own cutoff; pairs beyond it add nothing
+        rc = m.pair_cutoff(rc, m.typewise[1 if angular else 0], ti, np.asarray(tj))
+        f = radial_functions(r, rc, b) * (r < rc)
+    else:
+        f = radial_functions(r, rc, b)                                    # [b+1, nj]
     nk = (np.arange(nmax + 1)[:, None] * (b + 1) + np.arange(b + 1)[None, :]) * T * T
     C = m.c[off + nk[None, :, :] + ti * T + np.asarray(tj)[:, None, None]]  # [nj, nmax+1, b+1]
     return np.einsum("jnk,kj->nj", C, f)
@@ -145,6 +149,9 @@ def zbl_pair_energy(m: NEPModel, ti: int, tj: int, r: float) -> float:
         rin, rout, coefs = p[0], p[1], [(p[2 + 2 * q], p[3 + 2 * q]) for q in range(4)]
     else:
         rin, rout, coefs = m.zbl_rc_inner, m.zbl_rc_outer, ZBL_UNIVERSAL
+        if m.typewise_zbl:   # rc_outer shrunk to the pair's covalent size, rc_inner its half
+            rout = float(m.pair_cutoff(rout, m.typewise[2], ti, tj))
+            rin = 0.5 * rout
     phi = sum(a * np.exp(-b * x) for a, b in coefs)
     if r < rin:
         fc = 1.0

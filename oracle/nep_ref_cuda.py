@@ -89,7 +89,9 @@ class RefCudaNEP(LammpsRef):
         qs = np.zeros(max(140, m.dim), dtype=np.float32)
         qs[:m.dim] = m.q_scaler
         self.q_scaler = dev(qs, np.float32)
-        self.atomic_numbers = dev(np.zeros(NUM_ELEMENTS), np.int32)
+        an = np.zeros(NUM_ELEMENTS)
+        an[:m.ntypes] = m.atomic_numbers0
+        self.atomic_numbers = dev(an, np.int32)
         w0, b0, w1 = [], [], []
         for t in range(m.ntypes):
             a, b, c, extra = m.ann(t)

@@ -21,9 +21,12 @@ PICK_START, PICK_CASE, PICK_END = "// >>> NEPGEN PICK", "// --- NEPGEN PICK:", "
 def gen_map(m: NEPModel) -> Dict[str, object]:
     return {
         "NEPGEN_USE_TABLE": 0, "NEPGEN_VERSION": m.version, "NEPGEN_NTYPES": m.ntypes,
-        "NEPGEN_USE_TYPEWISE_CUTOFF": 0, "NEPGEN_USE_TYPEWISE_CUTOFF_ZBL": 0,
-        "NEPGEN_TYPEWISE_CUTOFF_FACTOR_R": 2.5, "NEPGEN_TYPEWISE_CUTOFF_FACTOR_A": 2.0,
-        "NEPGEN_TYPEWISE_CUTOFF_FACTOR_ZBL": 0.65,
+        # type-wise cutoffs (NEP.java:650-654): the file's factors, else NEP's defaults
+        "NEPGEN_USE_TYPEWISE_CUTOFF": 1 if m.typewise_descriptors else 0,
+        "NEPGEN_USE_TYPEWISE_CUTOFF_ZBL": 1 if m.typewise_zbl else 0,
+        "NEPGEN_TYPEWISE_CUTOFF_FACTOR_R": repr(float(m.typewise[0])) if any(m.typewise) else 2.5,
+        "NEPGEN_TYPEWISE_CUTOFF_FACTOR_A": repr(float(m.typewise[1])) if any(m.typewise) else 2.0,
+        "NEPGEN_TYPEWISE_CUTOFF_FACTOR_ZBL": repr(float(m.typewise[2])) if any(m.typewise) else 0.65,
         "NEPGEN_RCUT_R": repr(float(m.rc_radial)), "NEPGEN_RCUT_A": repr(float(m.rc_angular)),
         "NEPGEN_RCUT_INNER_ZBL": repr(float(m.zbl_rc_inner)) if m.zbl else "1.0",
         "NEPGEN_RCUT_OUTER_ZBL": repr(float(m.zbl_rc_outer)) if m.zbl else "2.0",

@@ -30,7 +30,8 @@ from oracle import native as ON, nep_model as NM, nep_ref as NR  # noqa: E402
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 # name: (symbols, version, rc (R, A), n_max, basis, l_max (3-, 4-, 5-body), neurons, structure
-#        (kind, atoms, tilt[, minimum separation]) [, ZBL: (rc_inner, rc_outer) or "flexible"])
+#        (kind, atoms, tilt[, minimum separation]) [, ZBL: (rc_inner, rc_outer) or "flexible"
+#        [, type-wise cutoff factors (radial, angular, ZBL)]])
 CASES = {
     "nep4_binary": (["Si", "O"], 4, (5.0, 4.0), (4, 4), (8, 8), (4, 2, 1), 16, ("liquid", 150, 0.1)),
     "nep3_single": (["C"], 3, (4.5, 4.5), (4, 4), (8, 8), (4, 0, 0), 8, ("liquid", 90, None)),
@@ -43,6 +44,12 @@ CASES = {
                  (1.6, 2.3)),
     "nep3_zbl_flex": (["W", "Be"], 3, (5.0, 4.0), (4, 4), (8, 8), (4, 2, 0), 8, ("liquid", 120, None, 1.3),
                       "flexible"),
+    # type-wise cutoffs: Si-Si, Si-O and O-O pairs each get their own radial and angular
+    # cutoffs inside the global ones; the second case also shrinks the fixed ZBL radii per pair
+    "nep4_typewise": (["Si", "O"], 4, (6.0, 5.0), (4, 4), (8, 8), (4, 2, 1), 12, ("liquid", 160, 0.07),
+                      None, (2.0, 1.6, 0.0)),
+    "nep5_typewise_zbl": (["Ga", "N", "O"], 5, (6.0, 4.5), (4, 4), (8, 8), (4, 2, 0), 10,
+                          ("liquid", 150, None, 1.3), (1.0, 2.2), (1.9, 1.5, 0.7)),
 }
 
 
@@ -55,9 +62,10 @@ def structure(spec, T, seed):
 def make(name):
     symbols, version, rc, n_max, basis, l_max, neurons, spec = CASES[name][:8]
     zbl = CASES[name][8] if len(CASES[name]) > 8 else None
+    typewise = CASES[name][9] if len(CASES[name]) > 9 else None
     seed = 1000 + sum(map(ord, name))
     text = NM.write(symbols, version=version, rc=rc, n_max=n_max, basis=basis, l_max=l_max, neurons=neurons,
-                    seed=seed, zbl=zbl)
+                    seed=seed, zbl=zbl, typewise=typewise)
     m = NM.load(text)
     s = structure(spec, len(symbols), seed)
     xw = ON.wrap(s.x, s.box_kind, s.box)

@@ -142,7 +142,7 @@ NEP_BAD = [
     (_nep_lines(lambda ls: ls.__setitem__(0, "nep4_zbl 2 Si O")), 1),            # ZBL without its zbl line
     (_nep_lines(lambda ls: ls.__setitem__(0, "nep4_polarizability 2 Si O")), 5),
     (_nep_lines(lambda ls: ls.__setitem__(0, "nep3_dipole 2 Si O")), 5),
-    (_nep_lines(lambda ls: ls.__setitem__(1, "cutoff 5 4 100 100 1.5 1.5 0")), 5),  # type-wise cutoffs
+    (_nep_lines(lambda ls: ls.__setitem__(1, "cutoff 5 4 100 100 1.5 1.5")), 1),    # two of three factors
     (_nep_lines(lambda ls: ls.__setitem__(2, "n_max 4")), 1),
     (_nep_lines(lambda ls: ls.__setitem__(4, "l_max 4 2")), 1),
     (_nep_lines(lambda ls: ls.pop()), 1),                                        # one scale short
@@ -164,11 +164,12 @@ def test_invalid_nep_files_are_rejected(text, status):
     assert L.nnap_create_nep(None, 0, 0, 0, None) == 6
 
 
-@pytest.mark.parametrize("zbl", [None, (1.6, 2.3), "flexible"])
-def test_valid_nep_file_passes_the_loader(zbl):
+@pytest.mark.parametrize("zbl,typewise", [(None, None), ((1.6, 2.3), None), ("flexible", None),
+                                          (None, (1.5, 1.5, 0.0)), ((1.6, 2.3), (2.0, 1.6, 0.6))])
+def test_valid_nep_file_passes_the_loader(zbl, typewise):
     L = _lib()
     h = C.c_void_p()
-    b = _nep_text(zbl=zbl).encode()
+    b = _nep_text(zbl=zbl, typewise=typewise).encode()
     rc = L.nnap_create_nep(b, len(b), 0, 0, C.byref(h))
     if rc == 0:
         L.nnap_destroy(h)

@@ -39,7 +39,8 @@ def test_energies_match_reference(path):
     assert np.max(np.abs(e - z["energies"])) <= 1e-11
 
 
-FD_CASES = [os.path.join(GOLDEN_DIR, "nep_%s.npz" % k) for k in ("nep3_single", "nep4_binary", "nep4_zbl")]
+FD_CASES = [os.path.join(GOLDEN_DIR, "nep_%s.npz" % k) for k in ("nep3_single", "nep4_binary", "nep4_zbl",
+                                                                   "nep5_typewise_zbl")]
 
 
 @pytest.mark.parametrize("path", FD_CASES, ids=lambda p: os.path.basename(p)[:-4])
@@ -85,6 +86,17 @@ def test_loader_round_trip_and_rejections():
     with pytest.raises(ValueError):
         NM.load("\n".join(["nep4_zbl 2 A B"] + lines[1:]))
     with pytest.raises(ValueError):
-        NM.load("\n".join(lines[:1] + ["cutoff 5 4 100 100 1 1 1"] + lines[2:]))
+        NM.load("\n".join(lines[:1] + ["cutoff 5 4 100 100 1 1"] + lines[2:]))
+    assert NM.load("\n".join(lines[:1] + ["cutoff 5 4 100 100 2 1.5 0"] + lines[2:])).typewise == (2.0, 1.5, 0.0)
     with pytest.raises(ValueError):
         NM.load("\n".join(lines[:-1]))
+
+
+def test_typewise_cutoffs_change_the_energies():
+    """The type-wise fixture's pair cutoffs sit inside the global ones: evaluating the same
+    model with the factors removed gives other energies, so the fixture pins them."""
+    m, z = _load(os.path.join(GOLDEN_DIR, "nep_nep5_typewise_zbl.npz"))
+    nl = _nl(m, z["x"], z)
+    e_tw = NO.energies(m, z["types"] - 1, nl)
+    m.typewise = (0.0, 0.0, 0.0)
+    assert np.max(np.abs(NO.energies(m, z["types"] - 1, nl) - e_tw)) > 1e-3
