@@ -78,8 +78,8 @@ int nnap_create(const char* model_json, size_t len, int precision, int device, n
 int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out);
 /* Create a handle from NEP potential text (nep.txt, the file read by NEP(String),
  * NEP.java:98-100 and 786-1010): potential models nep3, nep4 and nep5, with or without
- * ZBL (nepV_zbl, fixed or flexible), without type-wise cutoffs; other variants (dipole,
- * polarizability, type-wise cutoffs) return NNAP_ERR_UNSUPPORTED.  Species are
+ * ZBL (nepV_zbl, fixed or flexible) and with or without type-wise cutoffs; other
+ * variants (dipole, polarizability) return NNAP_ERR_UNSUPPORTED.  Species are
  * 1-based like every other call (NEP's 0-based species + 1).  The handle serves every
  * evaluation entry point (compute, batch, device, LAMMPS, server); NNAP_PREC_MIXED is
  * accepted and evaluates exactly like NNAP_PREC_FP32 (the tanh network runs in FP32);

@@ -189,7 +189,7 @@ struct nnap_handle {
     nnapgb::DevBuf<float4> pdx, pg;
     nnapgb::DevBuf<int> prev, pcount;
     nnapgb::DevBuf<float> fp, gfp, A, Gx;  // Gx: invariant-column part of dE/dA (when present)
-    nnapgb::DevBuf<float> zbl_z, zbl_zp, zbl_para, zbl_rc;  // NEP ZBL: per species Z, Z^0.23; flexible parameters
+    nnapgb::DevBuf<double> zbl_z, zbl_zp, zbl_para, zbl_rc;  // NEP ZBL: per species Z, Z^0.23; flexible parameters
     // compact rows of the entries within sub_rc (0: none) for spherical sub-bases whose
     // cutoff is well inside the neighbour cutoff: dx and row position [n][M], count [n]
     double sub_rc = 0.0;

@@ -9,6 +9,8 @@
 // atom i takes f/2 of its energy and the entry's pair gradient gets -dx f'(r) / (2 r): the
 // full rows hold each pair in both directions, as the reference's neighbour lists do.
 // One warp per atom row; the row's energy is summed in a fixed order and added once.
+// The pair terms are evaluated in FP64 from the FP32 displacement: an atom's ZBL energy
+// reaches tens of eV at short range, where FP32 arithmetic alone would cost 1e-5 eV.
 #include "common.cuh"
 #include "pdl.cuh"
 #include "zbl.cuh"
@@ -17,8 +19,8 @@ namespace nnapgb {
 
 namespace {
 
-__device__ __forceinline__ void zbl_term(float a, float b, float x, float& phi, float& dphi) {
-    const float t = a * expf(-b * x);
+__device__ __forceinline__ void zbl_term(double a, double b, double x, double& phi, double& dphi) {
+    const double t = a * exp(-b * x);
     phi += t;
     dphi -= b * t;
 }
@@ -39,14 +41,14 @@ __global__ void __launch_bounds__(256) k_nep_zbl(PairBufs P, int n, const int* _
         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
         if (r2 >= kZblMaxR * kZblMaxR) continue;
         const int tj = __float_as_int(d.w) - 1;
-        const float r = sqrtf(r2), rinv = 1.f / r;
-        const float a_inv = (z.zp[ti] + z.zp[tj]) * 2.134563f;
-        const float zizj = 14.399645f * z.z[ti] * z.z[tj];
-        const float x = r * a_inv;
-        float phi = 0.f, dphi = 0.f, rin = z.rc_inner, rout = z.rc_outer;
+        const double r = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z), rinv = 1.0 / r;
+        const double a_inv = (z.zp[ti] + z.zp[tj]) * 2.134563;
+        const double zizj = 14.399645 * z.z[ti] * z.z[tj];
+        const double x = r * a_inv;
+        double phi = 0.0, dphi = 0.0, rin = z.rc_inner, rout = z.rc_outer;
         if (z.flexible) {
             const int t1 = min(ti, tj), t2 = max(ti, tj);
-            const float* p = z.para + 10 * (t1 * z.T - t1 * (t1 - 1) / 2 + (t2 - t1));
+            const double* p = z.para + 10 * (t1 * z.T - t1 * (t1 - 1) / 2 + (t2 - t1));
             rin = p[0];
             rout = p[1];
 #pragma unroll
@@ -56,30 +58,29 @@ __global__ void __launch_bounds__(256) k_nep_zbl(PairBufs P, int n, const int* _
                 rin = z.rc_pair[2 * (ti * z.T + tj)];
                 rout = z.rc_pair[2 * (ti * z.T + tj) + 1];
             }
-            zbl_term(0.18175f, 3.1998f, x, phi, dphi);
-            zbl_term(0.50986f, 0.94229f, x, phi, dphi);
-            zbl_term(0.28022f, 0.4029f, x, phi, dphi);
-            zbl_term(0.02817f, 0.20162f, x, phi, dphi);
+            zbl_term(0.18175, 3.1998, x, phi, dphi);
+            zbl_term(0.50986, 0.94229, x, phi, dphi);
+            zbl_term(0.28022, 0.4029, x, phi, dphi);
+            zbl_term(0.02817, 0.20162, x, phi, dphi);
         }
         // f = zizj phi / r and its r-derivative, then the switch
-        float f = zizj * phi * rinv;
-        float fp = zizj * a_inv * dphi * rinv - f * rinv;
-        float fc = 0.f, fcp = 0.f;
+        double f = zizj * phi * rinv;
+        double fp = zizj * a_inv * dphi * rinv - f * rinv;
+        double fc = 0.0, fcp = 0.0;
         if (r < rin) {
-            fc = 1.f;
+            fc = 1.0;
         } else if (r < rout) {
-            const float w = 3.14159265358979f / (rout - rin);
-            float sn, cs;
-            sincosf(w * (r - rin), &sn, &cs);
-            fc = 0.5f * cs + 0.5f;
-            fcp = -0.5f * w * sn;
+            double sn, cs;
+            sincospi((r - rin) / (rout - rin), &sn, &cs);
+            fc = 0.5 * cs + 0.5;
+            fcp = -0.5 * (3.141592653589793 / (rout - rin)) * sn;
         }
         fp = fp * fc + f * fcp;
         f *= fc;
-        const float s = 0.5f * fp * rinv;
+        const float s = (float)(0.5 * fp * rinv);
         const float4 g = P.g[e];
         P.g[e] = make_float4(g.x - s * d.x, g.y - s * d.y, g.z - s * d.z, g.w);
-        esum += 0.5 * (double)f;
+        esum += 0.5 * f;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, o);

@@ -172,22 +172,22 @@ void upload_model(nnap_handle* h) {
     }
     // NEP's ZBL term
     if (m.zbl.on) {
-        std::vector<float> z(T), zp(T), par(m.zbl.para.begin(), m.zbl.para.end());
+        std::vector<double> z(T), zp(T), par(m.zbl.para.begin(), m.zbl.para.end());
         for (int t = 0; t < T; ++t) {
-            z[t] = (float)m.zbl.z[t];
-            zp[t] = (float)std::pow((double)m.zbl.z[t], 0.23);
+            z[t] = (double)m.zbl.z[t];
+            zp[t] = std::pow((double)m.zbl.z[t], 0.23);
         }
         h->zbl_z.ensure(T);
         h->zbl_zp.ensure(T);
         h->zbl_para.ensure(std::max<size_t>(par.size(), 1));
-        CK(cudaMemcpy(h->zbl_z.p, z.data(), sizeof(float) * T, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(h->zbl_zp.p, zp.data(), sizeof(float) * T, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->zbl_z.p, z.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->zbl_zp.p, zp.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
         if (!par.empty())
-            CK(cudaMemcpy(h->zbl_para.p, par.data(), sizeof(float) * par.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(h->zbl_para.p, par.data(), sizeof(double) * par.size(), cudaMemcpyHostToDevice));
         if (!m.zbl.pair_rc.empty()) {
-            std::vector<float> rcp(m.zbl.pair_rc.begin(), m.zbl.pair_rc.end());
+            const std::vector<double>& rcp = m.zbl.pair_rc;
             h->zbl_rc.ensure(rcp.size());
-            CK(cudaMemcpy(h->zbl_rc.p, rcp.data(), sizeof(float) * rcp.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(h->zbl_rc.p, rcp.data(), sizeof(double) * rcp.size(), cudaMemcpyHostToDevice));
         }
     }
     // networks
@@ -663,8 +663,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
         ZblArgs za;
         za.flexible = zm.flexible ? 1 : 0;
         za.T = T;
-        za.rc_inner = (float)zm.rc_inner;
-        za.rc_outer = (float)zm.rc_outer;
+        za.rc_inner = zm.rc_inner;
+        za.rc_outer = zm.rc_outer;
         za.z = h->zbl_z.p;
         za.zp = h->zbl_zp.p;
         za.para = h->zbl_para.p;

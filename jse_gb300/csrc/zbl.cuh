@@ -11,11 +11,11 @@ constexpr float kZblMaxR = 2.5f;  // pairs at or beyond this distance carry no Z
 
 struct ZblArgs {
     int flexible, T;
-    float rc_inner, rc_outer;  // fixed form
-    const float* z;            // [T] atomic numbers
-    const float* zp;           // [T] Z^0.23
-    const float* para;         // flexible: [T (T + 1) / 2][10]
-    const float* rc_pair;      // fixed form with type-wise radii: [T][T][2] (rc_inner, rc_outer), or NULL
+    double rc_inner, rc_outer;  // fixed form
+    const double* z;            // [T] atomic numbers
+    const double* zp;           // [T] Z^0.23
+    const double* para;         // flexible: [T (T + 1) / 2][10]
+    const double* rc_pair;      // fixed form with type-wise radii: [T][T][2] (rc_inner, rc_outer), or NULL
 };
 
 // Adds each atom's half of its pairs' ZBL energies to e_atom and the ZBL part of each

@@ -1,7 +1,7 @@
 """GB300 NEP potential: the reference's ``jsex.nep.NEP`` over the NNAP descriptor pipeline.
 
 ``NEP(path_or_text)`` loads a nep.txt potential (NEP.java:98-100, loader NEP.java:786-1010;
-nep3 / nep4 / nep5 potential models, with or without ZBL, without type-wise cutoffs) through
+nep3 / nep4 / nep5 potential models, with or without ZBL and type-wise cutoffs) through
 ``nnap_create_nep``; every evaluation method of :class:`jse_gb300.nnap.NNAP` applies
 (energies, forces and virials of single structures, batches, device buffers, the
 LAMMPS-style boundary and the serving loop).  Species are 1-based, as the reference's
