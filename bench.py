@@ -480,7 +480,7 @@ def nep_ref_gpu(device: int, p, s, text: str, flush, steps: int) -> dict:
     return out
 
 
-def nep_measurement(device: int, steps: int = 10, cpu: bool = True) -> dict:
+def nep_measurement(device: int, steps: int = 10, cpu: bool = True, autotune: bool = True) -> dict:
     """NEP potential through nnap_create_nep on the NEP benchmark: a 32000-atom binary liquid
     (0.060 /A^3) under a seeded nep4 potential of GPUMD's default hyperparameters (cutoff
     8 / 4 A, n_max 4 4, basis_size 8 8, l_max 4 2 1, 30 neurons), FP32.  ``value`` is
@@ -508,6 +508,7 @@ def nep_measurement(device: int, steps: int = 10, cpu: bool = True) -> dict:
             p.computeDevice(n, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
                             f_d.data_ptr(), v_d.data_ptr(), 0, stream=torch.cuda.current_stream(dev).cuda_stream)
         p.setProfiling(True)
+        p.setAutotune(autotune)  # shapes picked on the first warm-up step, as for the NNAP liquid
         for _ in range(3):
             flush.zero_()
             dstep()
@@ -609,7 +610,8 @@ def main():
 
     if args.only_nep:
         if rank == 0:
-            print(json.dumps({"nep": nep_measurement(local, steps=args.steps, cpu=not args.no_cpu_baseline)}))
+            print(json.dumps({"nep": nep_measurement(local, steps=args.steps, cpu=not args.no_cpu_baseline,
+                                                        autotune=not args.no_autotune)}))
         return
     structures, cfg = make_workload(args.workload, args.atoms)
     natoms_step = sum(s.natoms for s in structures)
@@ -779,7 +781,7 @@ def main():
         ref_gpu = ref_gpu_measurement(local, s, model, args.precision)
     nep = None
     if rank == 0 and not args.no_nep and args.workload == "liquid32k":
-        nep = nep_measurement(local, cpu=not args.no_cpu_baseline)
+        nep = nep_measurement(local, cpu=not args.no_cpu_baseline, autotune=not args.no_autotune)
 
     # roofline of the dominant stage
     peak, peak_kind, sm_max = load_peaks()
