@@ -1,24 +1,30 @@
 """Benchmark: NNAP energy+force+virial evaluation, atom-evals/s, on one GB300 per rank.
 
-A step evaluates energies, forces and virials of one structure (or one batch of
-structures) of the chosen workload.  ``value`` is the device-resident throughput
-(inputs already in HBM, outputs left in HBM), timed per step with CUDA events on the
-caller's stream with an L2 flush (a 256 MiB write) between steps outside the events.
-``e2e`` is the same metric through the host-buffer C-ABI call ``nnap_compute`` with
-pinned host inputs and outputs: host->device copies of positions and species and the
-device->host read of energy, forces and virial are inside the timed region.
+A step evaluates energies, forces and virials of one batch of structures (or one
+structure) of the chosen workload.  ``value`` is the device-resident throughput (inputs
+already in HBM, outputs left in HBM), timed per step with CUDA events on the caller's
+stream with an L2 flush (a 256 MiB write) between steps outside the events.  ``e2e`` is
+the same metric through the host-buffer C-ABI call ``nnap_compute_batch`` with pinned host
+inputs and outputs: host->device copies of positions and species and the device->host
+read of energies, forces and virials are inside the timed region.  ``plain_gpu`` is the
+plain FP32 drop-in: one synchronous single-structure ``nnap_compute`` per structure.
 
 Workloads (seeded synthetic inputs; the reference publishes none):
+  batch1024   1024 structures, 32..2048 atoms log-uniform, half triclinic, the liquid's model (default)
   liquid32k   ternary liquid, 32000 atoms, spherical Chebyshev nmax 8 lmax 6 rc 6.0, 126->64->64->1
   fcc4000     perturbed FCC Cu, 4000 atoms, radial Chebyshev nmax 10 rc 6.0, 11->32->32->1
   glass1m     binary glass, 1048576 atoms, LAMMPS triclinic, nmax 8 lmax 4 rc 5.5, 90->64->64->1
-  batch1024   1024 structures, 32..2048 atoms log-uniform, half triclinic, liquid32k model
+Every model carries the descriptor normalisation committed in tests/golden/bench_norm.json,
+so both arms evaluate the same model file.  The default run also measures the liquid
+(``liquid32k`` object), serving, training gradients, NEP and the reference's own CUDA
+kernels.
 
 ``--impl reference`` times the reference's own per-atom C++ arithmetic (expanded from its
-headers, compiled -O3 -ffast-math into oracle/_ref) driven over the oracle's neighbour
-list on all host cores, or the oracle port when that build is absent; only rank 0 runs it.
-With torchrun and N > 1 every rank evaluates its own replica of the workload (the path
-has no collective); value = atoms of all ranks / max-over-ranks time.
+headers, compiled -O3 -ffast-math into oracle/_ref) on all host cores over a bounded
+sample of the same workload, driven over neighbour lists built outside the timed region
+(the reference's neighbour search is not timed; this build's ``value`` includes its own);
+only rank 0 runs it.  With torchrun and N > 1 every rank evaluates its own replica of the
+workload (the path has no collective); value = atoms of all ranks / max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -57,24 +63,13 @@ def make_workload(name: str, atoms: int = 0):
     raise SystemExit("unknown workload " + name)
 
 
-def normalised_model(cfg: str, structures, precision: str):
-    """Model with norm_mu/norm_sigma set to descriptor statistics of the first structure,
-    computed with the GPU descriptors (as a trainer would set them)."""
-    from jse_gb300.nnap import NNAP
-    raw = W.model_for(cfg)
-    s = structures[0]
-    with NNAP(raw, precision="fp32") as p:
-        fp = p.calFp(s)
-    T = len(raw["models"])
-    mu, sg = [], []
-    for t in range(T):
-        D = raw["models"][t]["nn"]["input_dim"]
-        sel = fp[s.types == t + 1, :D]
-        if len(sel) == 0:
-            sel = fp[:, :D]
-        mu.append(sel.mean(0))
-        sg.append(sel.std(0) + 1e-3)
-    return W.model_for(cfg, norm_mu=mu, norm_sigma=sg)
+def bench_model(cfg: str) -> dict:
+    """The workload's model with the committed descriptor normalisation (per species mean
+    and standard deviation of the descriptors of one seeded structure of the workload,
+    tests/golden/make_bench_norm.py): the same model file for both arms."""
+    with open(os.path.join(ROOT, "tests", "golden", "bench_norm.json")) as f:
+        st = json.load(f)["c2" if cfg in ("c4", "c5") else cfg]
+    return W.model_for(cfg, norm_mu=[np.asarray(v) for v in st["mu"]], norm_sigma=[np.asarray(v) for v in st["sigma"]])
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -176,44 +171,96 @@ def load_traffic():
 
 
 # ----------------------------------------------------------------------------- reference arm
-def cpu_reference(structures, model: dict, budget_s: float = 12.0, threads: int = 0):
+class _RefSample:
+    """A prefix of the workload's structures as one list of independent atoms for the
+    reference's per-atom arithmetic: wrapped positions, neighbour lists (built here, outside
+    any timed region) and species, concatenated with shifted atom indices.  Structures are
+    independent, so one call over the concatenation does the work of one call per
+    structure without the per-call thread start-up of the driver."""
+
+    def __init__(self, structures, rcut: float, max_atoms: int):
+        from oracle import native as ON
+        offs, js, dxs, types, imgs = [np.zeros(1, dtype=np.int64)], [], [], [], []
+        n = 0
+        self.nstruct = 0
+        for s in structures:
+            if n and n + s.natoms > max_atoms:
+                break
+            xw = ON.wrap(s.x, s.box_kind, s.box)
+            nl = ON.neighbors(xw, s.box_kind, s.box, rcut)
+            offs.append(nl.offsets[1:] + offs[-1][-1])
+            js.append(nl.j + n)
+            dxs.append(nl.dx)
+            imgs.append(nl.img)
+            types.append(np.asarray(s.types, dtype=np.int32))
+            n += s.natoms
+            self.nstruct += 1
+        self.natoms = n
+        self.types = np.concatenate(types)
+        self.nl = ON.NeighborList(np.concatenate(offs), np.concatenate(js).astype(np.int32),
+                                  np.concatenate(imgs), np.ascontiguousarray(np.concatenate(dxs)))
+
+
+def cpu_reference(structures, model: dict, budget_s: float = 12.0, threads: int = 0, single_thread_s: float = 0.0):
     """Time the reference's per-atom arithmetic (oracle/_ref, -O3 -ffast-math) or, when that
-    build is absent, the oracle port, on a bounded sample of atoms.  Returns (atoms/s, info)."""
+    build is absent, the oracle port, on a bounded sample of the workload: the first
+    structures up to about ``budget_s`` seconds of work (for a single large structure, its
+    first atoms).  Neighbour lists are built before the timed region.  Returns (atoms/s,
+    info); with ``single_thread_s`` > 0 info also holds a one-thread rate on a smaller
+    sample of the same kind."""
     from oracle import model as OM, native as ON
     threads = threads or os.cpu_count() or 1
     pm = OM.load(model)
-    s = structures[0]
-    xw = ON.wrap(s.x, s.box_kind, s.box)
-    nl_full = ON.neighbors(xw, s.box_kind, s.box, pm.rcut_max)
     kind = "reference"
     try:
         ref = ON.RefLib(pm, fast=True)
     except (FileNotFoundError, OSError, RuntimeError):
         ref = None
         kind = "port"
-    n = len(s.types)
+    many = len(structures) > 1
 
-    def run(m):
-        # evaluate the first m atoms (full neighbour rows, scatter into full-size outputs)
+    def sample(atoms):
+        if many:
+            return _RefSample(structures, pm.rcut_max, atoms)
+        return _RefSample(structures[:1], pm.rcut_max, structures[0].natoms)
+
+    def run(smp, m, nth):
         t0 = time.perf_counter()
         if ref is not None:
-            ref.compute(s.types, nl_full, nthreads=threads, n_eval=m)
+            ref.compute(smp.types, smp.nl, nthreads=nth, n_eval=m)
         else:
-            ON.compute(pm, s.x, s.types, s.box_kind, s.box, nl=nl_full, n_eval=m)
+            ON.compute(pm, np.zeros((smp.natoms, 3)), smp.types, 0, np.eye(3), nl=smp.nl, n_eval=m)
         return time.perf_counter() - t0
 
-    m = min(n, 256)
-    dt = run(m)
-    while dt < 0.5 and m < n:
-        m = min(n, m * 4)
-        dt = run(m)
-    rate = m / dt
-    m_final = int(min(n, max(m, rate * budget_s)))
-    dt = run(m_final)
-    return m_final / dt, {"kind": kind, "cores": threads if ref is not None else 1,
-                          "sample": "%d of %d atoms of the first structure, full neighbour rows, %s" % (
-                              m_final, n, "reference per-atom C++ (-O3 -ffast-math), %d threads" % threads
-                              if ref is not None else "FP64 oracle port, 1 thread")}
+    def measure(budget, nth):
+        atoms = 2048
+        while True:
+            smp = sample(atoms)
+            m = smp.natoms if many else min(smp.natoms, atoms)
+            dt = run(smp, m, nth)
+            if dt >= 0.25 * budget or (many and smp.nstruct == len(structures)) or (not many and m == smp.natoms):
+                break
+            atoms = int(atoms * min(16.0, max(2.0, 0.5 * budget / max(dt, 1e-3))))
+        rate = m / dt
+        want = int(rate * budget)
+        if want > m:
+            smp = sample(want)
+            m = smp.natoms if many else min(smp.natoms, want)
+            dt = run(smp, m, nth)
+        what = ("%d structures (%d atoms) of %d" % (smp.nstruct, m, len(structures)) if many
+                else "%d of %d atoms of the structure" % (m, smp.natoms))
+        return m / dt, what
+
+    nth = threads if ref is not None else 1
+    rate, what = measure(budget_s, nth)
+    info = {"kind": kind, "cores": nth,
+            "sample": "%s, full neighbour rows built outside the timed region (neighbour search not timed), %s" % (
+                what, "reference per-atom C++ (-O3 -ffast-math), %d threads" % nth if ref is not None
+                else "FP64 oracle port, 1 thread")}
+    if single_thread_s > 0 and ref is not None:
+        r1, what1 = measure(single_thread_s, 1)
+        info["single_thread"] = {"value": r1, "unit": "atom-evals/s", "cores": 1, "sample": what1}
+    return rate, info
 
 
 # ----------------------------------------------------------------------------- serving
@@ -230,7 +277,7 @@ def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2))
     from jse_gb300.nnap import NNAP
     from jse_gb300.serve import GaussianMoves, NNAPServer, RequestLoop, poisson_requests
     pool = W.c5_pool(256)
-    model = normalised_model("c5", [max(pool, key=lambda q: q.natoms)], "mixed")
+    model = bench_model("c5")
     moves = GaussianMoves(sigma=0.01, seed=7)
     out = {"requests": nreq, "evaluations_per_request": 20, "skin_A": 0.5, "memory_budget_GB": 120,
            "max_resident": 1024, "pool": "256 structures, n ~ lognormal(median 500, sd 1.0) in [50, 20000]",
@@ -390,6 +437,21 @@ def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int 
         ours_lmp()
         f_ours = f[:n].copy()
         np.add.at(f_ours, owner, f[n:])
+    if precision != "fp32":  # this build in FP32 too, for an FP32-against-FP32 comparison
+        with NNAP(model, precision="fp32", device=device) as p32:
+            def ours_lmp32():
+                p32._check(p32._L.nnap_compute_lammps(p32._handle(), n, nall, _iptr(il), _iptr(num), ptrs, _dptr(xh),
+                                                      _iptr(t), None, 1, 1, 1, 0, 0, _dptr(f), _dptr(eng),
+                                                      _dptr(eatom), _dptr(vir), None, None))
+            v, ms = timed(ours_lmp32, steps)
+            out["ours_lammps_e2e_fp32"] = {"value": v, "ms_per_step": ms}
+
+            def ours_dev32():
+                p32.computeDevice(n, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind,
+                                  WANT_ENERGY | WANT_FORCES | WANT_VIRIAL, e_d.data_ptr(), 0, f_d.data_ptr(),
+                                  v_d.data_ptr(), 0, stream=torch.cuda.current_stream(dev).cuda_stream)
+            v, ms = timed(ours_dev32, steps)
+            out["ours_kernels_fp32"] = {"value": v, "ms_per_step": ms}
     try:
         ref = RC.RefCudaNNAP(model, device)
     except (FileNotFoundError, RuntimeError, OSError, ValueError) as ex:
@@ -414,6 +476,9 @@ def ref_gpu_measurement(device: int, s, model: dict, precision: str, steps: int 
     out["max_abs_force_difference"] = float(np.abs(f_ref - f_ours).max())
     out["speedup_lammps_e2e"] = out["ours_lammps_e2e"]["value"] / out["ref_lammps_e2e"]["value"]
     out["speedup_kernels"] = out["ours_kernels"]["value"] / out["ref_kernels"]["value"]
+    if "ours_kernels_fp32" in out:  # FP32 against the reference's FP32 kernels
+        out["speedup_lammps_e2e_fp32"] = out["ours_lammps_e2e_fp32"]["value"] / out["ref_lammps_e2e"]["value"]
+        out["speedup_kernels_fp32"] = out["ours_kernels_fp32"]["value"] / out["ref_kernels"]["value"]
     return out
 
 
@@ -580,6 +645,179 @@ def nep_measurement(device: int, steps: int = 10, cpu: bool = True, autotune: bo
     return out
 
 
+# ----------------------------------------------------------------------------- device runs
+def _sm_count(dev) -> int:
+    import torch
+    return int(torch.cuda.get_device_properties(dev).multi_processor_count)
+
+
+def device_run(pot, structures, dev, flush, steps: int, warmup: int, clocks=None, dist=None):
+    """Warm-up then ``steps`` timed evaluations of the whole workload with inputs and outputs
+    resident on the device (CUDA events on the launching stream, L2 flushed between steps
+    outside the events).  Returns timing, per-stage times, kernel launches and the
+    device arrays."""
+    import torch
+    from jse_gb300.nnap import WANT_ENERGY, WANT_FORCES, WANT_VIRIAL
+    from jse_gb300.replicas import barrier
+    single = len(structures) == 1
+    s = structures[0]
+    nat = np.array([st.natoms for st in structures], dtype=np.int32)
+    kinds = np.array([st.box_kind for st in structures], dtype=np.int32)
+    boxes = np.ascontiguousarray(np.concatenate([np.asarray(st.box, dtype=np.float64).reshape(9) for st in structures]))
+    x_all = np.ascontiguousarray(np.concatenate([st.x for st in structures]))
+    t_all = np.ascontiguousarray(np.concatenate([st.types for st in structures]).astype(np.int32))
+    N, S = int(nat.sum()), len(structures)
+    x_d = torch.from_numpy(x_all).to(dev)
+    t_d = torch.from_numpy(t_all).to(dev)
+    e_d = torch.zeros(S, dtype=torch.float64, device=dev)
+    f_d = torch.zeros((N, 3), dtype=torch.float64, device=dev)
+    v_d = torch.zeros((S, 9), dtype=torch.float64, device=dev)
+    flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
+
+    def step():
+        st_ = torch.cuda.current_stream(dev).cuda_stream
+        if single:
+            pot.computeDevice(N, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
+                              f_d.data_ptr(), v_d.data_ptr(), 0, stream=st_)
+        else:
+            pot.computeBatchDevice(nat, x_d.data_ptr(), t_d.data_ptr(), kinds, boxes, flags, e_d.data_ptr(), 0,
+                                   f_d.data_ptr(), v_d.data_ptr(), 0, stream=st_)
+
+    pot.setProfiling(True)
+    for _ in range(warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize(dev)
+    if clocks is not None:
+        clocks.start()
+        time.sleep(0.2)
+    barrier(dist)
+    torch.cuda.synchronize(dev)
+    ms, stages, launches, stage_ok = [], np.zeros(5), 0, True
+    t_wall = time.perf_counter()
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        if stage_ok:
+            try:
+                stages += pot.stageTimes()
+            except Exception:
+                stage_ok = False
+        launches += pot.lastLaunchCount()
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t_wall
+    barrier(dist)
+    clk = clocks.stop() if clocks is not None else None
+    return {"ms": ms, "stages": stages / steps, "launches": launches, "wall": wall, "clocks": clk, "N": N, "S": S,
+            "nat": nat, "kinds": kinds, "boxes": boxes, "x_all": x_all, "t_all": t_all}
+
+
+def e2e_run(pot, run, dev, flush, steps: int) -> dict:
+    """The same evaluations through nnap_compute_batch with pinned host buffers: the copies of
+    inputs and outputs are inside the timed region."""
+    import torch
+    from jse_gb300.nnap import WANT_ENERGY, WANT_FORCES, WANT_VIRIAL, _dptr, _iptr
+    N, S = run["N"], run["S"]
+    nat, kinds, boxes = run["nat"], run["kinds"], run["boxes"]
+    xh = torch.from_numpy(run["x_all"]).pin_memory().numpy()
+    th = torch.from_numpy(run["t_all"]).pin_memory().numpy()
+    fh = torch.zeros((N, 3), dtype=torch.float64).pin_memory().numpy()
+    eh = torch.zeros(S, dtype=torch.float64).pin_memory().numpy()
+    vh = torch.zeros((S, 9), dtype=torch.float64).pin_memory().numpy()
+    flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
+
+    def host_step():
+        pot._check(pot._L.nnap_compute_batch(pot._handle(), S, _iptr(nat), _dptr(xh), _iptr(th), _iptr(kinds),
+                                             _dptr(boxes), flags, _dptr(eh), None, _dptr(fh), _dptr(vh), None))
+    for _ in range(3):
+        host_step()
+    dts = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        host_step()
+        dts.append(time.perf_counter() - t0)
+    return {"value": N * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": N * 28,
+            "d2h_bytes_per_step": S * 8 + N * 24 + S * 72, "path": "nnap_compute_batch, pinned host buffers"}
+
+
+def plain_run(model, run, local, dev, flush, steps: int) -> dict:
+    """The plain FP32 drop-in: one synchronous single-structure nnap_compute per structure
+    on an FP32 handle, host buffers (graphs off for a batch: every structure has its own
+    layout)."""
+    import torch
+    from jse_gb300.nnap import NNAP, WANT_ENERGY, WANT_FORCES, WANT_VIRIAL, _dptr, _iptr
+    N, S = run["N"], run["S"]
+    nat, kinds, boxes = run["nat"], run["kinds"], run["boxes"]
+    xh, th = run["x_all"], run["t_all"]
+    fh, eh, vh = np.zeros((N, 3)), np.zeros(S), np.zeros((S, 9))
+    flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
+    with NNAP(model, precision="fp32", device=local) as pp:
+        if S > 1:
+            pp.setGraphs(False)
+        offs = np.concatenate([[0], np.cumsum(nat)])
+
+        def plain_step():
+            for k in range(S):
+                a, b = offs[k], offs[k + 1]
+                pp._check(pp._L.nnap_compute(pp._handle(), int(nat[k]), _dptr(xh[a:b]), _iptr(th[a:b]),
+                                             int(kinds[k]), _dptr(boxes[9 * k:9 * k + 9]), flags, _dptr(eh[k:k + 1]),
+                                             None, _dptr(fh[a:b]), _dptr(vh[k]), None))
+        for _ in range(3):
+            plain_step()
+        pts = []
+        for _ in range(max(1, min(steps, 5) if S > 1 else steps)):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            plain_step()
+            pts.append(time.perf_counter() - t0)
+    pv = N * len(pts) / sum(pts)
+    return {"value": pv, "unit": "atom-evals/s", "ms_per_step": 1e3 * sum(pts) / len(pts),
+            "path": "plain FP32, one synchronous nnap_compute per structure, host buffers"}
+
+
+def mean_neighbours(pot, structures) -> float:
+    pairs, atoms = 0, 0
+    for s in structures:
+        off, j, img = pot.neighborList(s)
+        pairs += len(j)
+        atoms += s.natoms
+    return pairs / max(1, atoms)
+
+
+def roofline(model, mean_nei: float, stages, natoms_step: int, workload: str, sm_count: int) -> dict:
+    """HBM roofline of the dominant stage (algorithmic bytes / stage time against the measured
+    copy bandwidth) and its FP32 fraction against this GPU's FP32 peak (SMs x 128 lanes x 2
+    x maximum clock)."""
+    peak, peak_kind, sm_max = load_peaks()
+    costs = stage_costs(model, mean_nei)
+    names = list(costs.keys())
+    dom = int(np.argmax(stages))
+    dname = names[dom]
+    t_dom = stages[dom] / 1e3
+    achieved = costs[dname]["bytes"] * natoms_step / t_dom / 1e9
+    fp32_peak = sm_count * 128 * 2 * sm_max * 1e6 / 1e12
+    traffic = load_traffic().get("%s/%s" % (workload, dname))
+    return {"bound": "hbm", "kernel_stage": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": traffic * natoms_step if traffic else None,
+            "algorithmic_bytes_per_atom": costs[dname]["bytes"],
+            "fp32": {"achieved_tflops": costs[dname]["flops"] * natoms_step / t_dom / 1e12,
+                     "peak_tflops": fp32_peak,
+                     "peak_source": "%d SMs (cudaDeviceProp) x 128 lanes x 2 x max clock %.0f MHz" % (sm_count, sm_max),
+                     "frac": costs[dname]["flops"] * natoms_step / t_dom / 1e12 / fp32_peak},
+            "stage_ms": dict(zip(names, [round(float(x), 5) for x in stages])),
+            "mean_neighbours": mean_nei}
+
+
 # ----------------------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -587,9 +825,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="liquid32k", choices=["liquid32k", "fcc4000", "glass1m", "batch1024"])
+    ap.add_argument("--workload", default="batch1024", choices=["batch1024", "liquid32k", "fcc4000", "glass1m"])
     ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="only the headline workload (no liquid, serving, "
+                    "training, NEP or reference-GPU legs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-train", action="store_true", help="skip the training-gradient measurement")
     ap.add_argument("--no-nep", action="store_true", help="skip the NEP measurement")
@@ -599,6 +839,8 @@ def main():
     ap.add_argument("--only-train", action="store_true", help="run only the training-gradient measurement "
                     "(profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=5000)
+    ap.add_argument("--ref-seconds", type=float, default=20.0, help="host seconds of the reference arm's timed "
+                    "samples over all steps (plus a 5 s single-thread sample)")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes (profiling runs)")
     ap.add_argument("--atoms", type=int, default=0, help="resize the liquid / glass workload (profiling runs)")
     args = ap.parse_args()
@@ -617,33 +859,34 @@ def main():
     natoms_step = sum(s.natoms for s in structures)
     config = {"workload": args.workload, "structures": len(structures), "atoms_per_step": natoms_step,
               "precision": args.precision, "l2": "flushed between steps (256 MiB write)",
-              "parallelism": "replicas x%d" % world}
+              "parallelism": "replicas x%d" % world,
+              "model": "normalisation from tests/golden/bench_norm.json (same model file in both arms)"}
+    model = bench_model(cfg)
 
     if args.impl == "reference":
         if rank != 0:
             return
-        model = W.model_for(cfg)
         rates = []
         info = None
-        for _ in range(args.warmup):
-            pass
-        for _ in range(args.steps):
-            r, info = cpu_reference(structures, model, budget_s=max(1.0, 20.0 / max(args.steps, 1)))
+        for k in range(args.steps):
+            r, info = cpu_reference(structures, model, budget_s=max(0.5, args.ref_seconds / max(args.steps, 1)),
+                                    single_thread_s=min(5.0, args.ref_seconds / 4) if k == args.steps - 1 else 0.0)
             rates.append(r)
         v = statistics.median(rates)
         line = {"metric": METRIC, "value": v, "unit": "atom-evals/s", "n_gpus": 0, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": natoms_step / v * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
                 "config": config, "impl": "reference",
+                "timed": "the reference's per-atom energy/force arithmetic and its force/virial scatter; its "
+                         "neighbour search is built before the timed region (this build's value includes its own)",
                 "cpu_baseline": dict(info, value=v, unit="atom-evals/s"),
                 "e2e": {"value": v, "unit": "atom-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
 
     import torch
-    from jse_gb300.nnap import NNAP, WANT_ENERGY, WANT_FORCES, WANT_VIRIAL
+    from jse_gb300.nnap import NNAP
     torch.cuda.set_device(local)
-    model = normalised_model(cfg, structures, args.precision)
     if args.only_ref_gpu:
         if rank == 0:
             print(json.dumps({"reference_gpu": ref_gpu_measurement(local, structures[0], model, args.precision,
@@ -654,180 +897,70 @@ def main():
             print(json.dumps({"training": train_measurement(local, structures[0], model, steps=args.steps,
                                                              cpu=not args.no_cpu_baseline)}))
         return
-    pot = NNAP(model, precision=args.precision, device=local)
-    pot.setAutotune(not args.no_autotune)  # shapes picked on the first warm-up step of the size bucket
     dev = torch.device("cuda", local)
-    s = structures[0]
-    single = len(structures) == 1
+    sm_count = _sm_count(dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    nat = np.array([st.natoms for st in structures], dtype=np.int32)
-    kinds = np.array([st.box_kind for st in structures], dtype=np.int32)
-    boxes = np.ascontiguousarray(np.concatenate([np.asarray(st.box, dtype=np.float64).reshape(9) for st in structures]))
-    x_all = np.ascontiguousarray(np.concatenate([st.x for st in structures]))
-    t_all = np.ascontiguousarray(np.concatenate([st.types for st in structures]).astype(np.int32))
-    N = int(nat.sum())
-    S = len(structures)
-    x_d = torch.from_numpy(x_all).to(dev)
-    t_d = torch.from_numpy(t_all).to(dev)
-    e_d = torch.zeros(S, dtype=torch.float64, device=dev)
-    f_d = torch.zeros((N, 3), dtype=torch.float64, device=dev)
-    v_d = torch.zeros((S, 9), dtype=torch.float64, device=dev)
-    flags = WANT_ENERGY | WANT_FORCES | WANT_VIRIAL
-
-    def device_step():
-        st_ = torch.cuda.current_stream(dev).cuda_stream
-        if single:
-            pot.computeDevice(N, x_d.data_ptr(), t_d.data_ptr(), s.box, s.box_kind, flags, e_d.data_ptr(), 0,
-                              f_d.data_ptr(), v_d.data_ptr(), 0, stream=st_)
-        else:
-            pot.computeBatchDevice(nat, x_d.data_ptr(), t_d.data_ptr(), kinds, boxes, flags, e_d.data_ptr(), 0,
-                                   f_d.data_ptr(), v_d.data_ptr(), 0, stream=st_)
-
     bench_stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(bench_stream)
-    pot.setProfiling(True)
-    for _ in range(args.warmup):
-        flush.zero_()
-        device_step()
-    torch.cuda.synchronize(dev)
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.2)
-    barrier(dist)
-    torch.cuda.synchronize(dev)
-    ms, stages, launches, stage_ok = [], np.zeros(5), 0, True
-    t_wall = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        device_step()
-        e1.record()
-        e1.synchronize()
-        ms.append(e0.elapsed_time(e1))
-        if stage_ok:
-            try:
-                stages += pot.stageTimes()
-            except Exception:
-                stage_ok = False
-        launches += pot.lastLaunchCount()
-    torch.cuda.synchronize(dev)
-    wall = time.perf_counter() - t_wall
-    barrier(dist)
-    clk = clocks.stop()
-    t_dev = max_over_ranks(sum(ms) / 1e3, dist)
+    pot = NNAP(model, precision=args.precision, device=local)
+    pot.setAutotune(not args.no_autotune)  # shapes picked on the first warm-up step of each size bucket
+    run = device_run(pot, structures, dev, flush, args.steps, args.warmup, clocks=ClockSampler(local), dist=dist)
+    t_dev = max_over_ranks(sum(run["ms"]) / 1e3, dist)
     value = whole_job_rate(natoms_step, args.steps, world, t_dev)
-    stages /= args.steps
+    e2e = e2e_run(pot, run, dev, flush, args.steps)
+    plain = plain_run(model, run, local, dev, flush, args.steps)
+    plain["tuned_e2e_over_plain"] = e2e["value"] / plain["value"]
+    plain["tuned_value_over_plain"] = value / plain["value"]
+    mean_nei = mean_neighbours(pot, structures)
+    roof = roofline(model, mean_nei, run["stages"], natoms_step, args.workload, sm_count)
+    config["launch_shapes"] = pot.tuning(max(s.natoms for s in structures))
 
-    # end to end through host buffers (pinned)
-    from jse_gb300.nnap import _dptr, _iptr
-    xh = torch.from_numpy(x_all).pin_memory().numpy()
-    th = torch.from_numpy(t_all).pin_memory().numpy()
-    fh = torch.zeros((N, 3), dtype=torch.float64).pin_memory().numpy()
-    eh = torch.zeros(S, dtype=torch.float64).pin_memory().numpy()
-    vh = torch.zeros((S, 9), dtype=torch.float64).pin_memory().numpy()
-
-    def host_step(p_):
-        p_._check(p_._L.nnap_compute_batch(p_._handle(), S, _iptr(nat), _dptr(xh), _iptr(th), _iptr(kinds),
-                                           _dptr(boxes), flags, _dptr(eh), None, _dptr(fh), _dptr(vh), None))
-
-    for _ in range(3):
-        host_step(pot)
-    dts = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        host_step(pot)
-        dts.append(time.perf_counter() - t0)
-    e2e = {"value": N * len(dts) / sum(dts), "unit": "atom-evals/s", "h2d_bytes_per_step": N * 28,
-           "d2h_bytes_per_step": S * 8 + N * 24 + S * 72}
-
-    # the plain GPU path: one FP32 single-structure nnap_compute per structure
-    with NNAP(model, precision="fp32", device=local) as pp:
-        if not single:
-            pp.setGraphs(False)
-        offs = np.concatenate([[0], np.cumsum(nat)])
-
-        def plain_step():
-            for k in range(S):
-                a, b = offs[k], offs[k + 1]
-                pp._check(pp._L.nnap_compute(pp._handle(), int(nat[k]), _dptr(xh[a:b]), _iptr(th[a:b]),
-                                             int(kinds[k]), _dptr(boxes[9 * k:9 * k + 9]), flags, _dptr(eh[k:k + 1]),
-                                             None, _dptr(fh[a:b]), _dptr(vh[k]), None))
-        for _ in range(3):
-            plain_step()
-        pts = []
-        for _ in range(max(1, min(args.steps, 5) if not single else args.steps)):
-            flush.zero_()
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            plain_step()
-            pts.append(time.perf_counter() - t0)
-        pv = N * len(pts) / sum(pts)
-        plain = {"value": pv, "unit": "atom-evals/s", "ms_per_step": 1e3 * sum(pts) / len(pts),
-                 "path": "plain FP32, one nnap_compute per structure, host buffers",
-                 "tuned_e2e_over_plain": e2e["value"] / pv}
-
-    serving = None
-    if rank == 0 and not args.no_serve and args.workload == "liquid32k":
+    extras = rank == 0 and not args.no_extras
+    liquid = None
+    if extras and args.workload == "batch1024":  # the 32000-atom liquid of the same model, as an extra object
+        ls, _ = make_workload("liquid32k")
+        lm = bench_model("c2")
+        with NNAP(lm, precision=args.precision, device=local) as lp:
+            lp.setAutotune(not args.no_autotune)
+            lr = device_run(lp, ls, dev, flush, args.steps, args.warmup)
+            lv = ls[0].natoms * args.steps / (sum(lr["ms"]) / 1e3)
+            le2e = e2e_run(lp, lr, dev, flush, args.steps)
+            lroof = roofline(lm, mean_neighbours(lp, ls), lr["stages"], ls[0].natoms, "liquid32k", sm_count)
+            liquid = {"value": lv, "unit": "atom-evals/s", "ms_per_step": sum(lr["ms"]) / args.steps,
+                      "atoms": ls[0].natoms, "gpu_launches": lr["launches"], "e2e": le2e, "roofline": lroof,
+                      "plain_gpu": plain_run(lm, lr, local, dev, flush, args.steps),
+                      "launch_shapes": lp.tuning(ls[0].natoms)}
+    else:
+        ls = structures
+    serving = training = ref_gpu = nep = None
+    if extras and not args.no_serve and args.workload in ("batch1024", "liquid32k"):
         serving = serve_measurement(local, args.serve_requests)
-    training = None
-    if rank == 0 and not args.no_train and args.workload == "liquid32k":
-        training = train_measurement(local, s, model, cpu=not args.no_cpu_baseline)
-    ref_gpu = None  # a baseline leg: runs with the other baselines
-    if rank == 0 and not args.no_ref_gpu and not args.no_cpu_baseline and args.workload == "liquid32k":
-        ref_gpu = ref_gpu_measurement(local, s, model, args.precision)
-    nep = None
-    if rank == 0 and not args.no_nep and args.workload == "liquid32k":
+    if extras and not args.no_train and args.workload in ("batch1024", "liquid32k"):
+        training = train_measurement(local, ls[0], bench_model("c2"), cpu=not args.no_cpu_baseline)
+    if extras and not args.no_ref_gpu and not args.no_cpu_baseline and args.workload in ("batch1024", "liquid32k"):
+        ref_gpu = ref_gpu_measurement(local, ls[0], bench_model("c2"), args.precision)
+    if extras and not args.no_nep and args.workload in ("batch1024", "liquid32k"):
         nep = nep_measurement(local, cpu=not args.no_cpu_baseline, autotune=not args.no_autotune)
-
-    # roofline of the dominant stage
-    peak, peak_kind, sm_max = load_peaks()
-    off, j, img = pot.neighborList(s)
-    mean_nei = float(len(j)) / max(1, s.natoms)
-    costs = stage_costs(model, mean_nei)
-    names = list(costs.keys())
-    dom = int(np.argmax(stages))
-    dname = names[dom]
-    t_dom = stages[dom] / 1e3
-    achieved = costs[dname]["bytes"] * natoms_step / t_dom / 1e9
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-    traffic = load_traffic().get("%s/%s" % (args.workload, dname))
-    roof = {"bound": "hbm", "kernel_stage": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind,
-            "traffic": traffic * natoms_step if traffic else None,
-            "fp32": {"achieved_tflops": costs[dname]["flops"] * natoms_step / t_dom / 1e12,
-                     "peak_tflops": fp32_peak, "peak_source": "nominal 152 SM x 128 lanes x 2 x max clock",
-                     "frac": costs[dname]["flops"] * natoms_step / t_dom / 1e12 / fp32_peak},
-            "stage_ms": dict(zip(names, [round(float(x), 5) for x in stages])),
-            "mean_neighbours": mean_nei}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            v_cpu, info = cpu_reference(structures, W.model_for(cfg), budget_s=10.0)
+            v_cpu, info = cpu_reference(structures, model, budget_s=10.0)
             cpu = dict(info, value=v_cpu, unit="atom-evals/s")
         except Exception as ex:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "atom-evals/s", "error": str(ex)[:200]}
 
-    config["launch_shapes"] = pot.tuning(N)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "atom-evals/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "bf16+f32",
                 "data": "synthetic (seeded)", "config": config, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-                "clocks": clk, "gpu_launches": launches, "wall_s_timed": wall}
-        line["plain_gpu"] = plain
-        if serving is not None:
-            line["serving"] = serving
-        if training is not None:
-            line["training"] = training
-        if nep is not None:
-            line["nep"] = nep
-        if ref_gpu is not None:
-            line["reference_gpu"] = ref_gpu
+                "clocks": run["clocks"], "gpu_launches": run["launches"], "wall_s_timed": run["wall"],
+                "plain_gpu": plain}
+        for k, v in (("liquid32k", liquid), ("serving", serving), ("training", training), ("nep", nep),
+                     ("reference_gpu", ref_gpu)):
+            if v is not None:
+                line[k] = v
         print(json.dumps(line))
     pot.close()
     if dist:

@@ -239,16 +239,18 @@ int nnap_stage_times(nnap_handle* h, double* ms5);
 
 /* Per-atom neighbour counts of one structure without allocating any memory.  This entry
  * point has no counterpart in the reference.  It is for callers that cannot call
- * cudaMalloc when they need the answer: a program capturing a CUDA graph in global
- * capture mode, or an engine that pre-reserves all device memory and forbids later
- * allocations.  No handle is needed; rcut is the cutoff.  d_x (3n doubles), d_type
- * (n ints) and d_counts (n ints) are device pointers; box is a host array.
+ * cudaMalloc when they need the answer: an engine (or a framework's caching allocator)
+ * that reserves all device memory for its own pool up front, so a later cudaMalloc
+ * fails, or code in a latency-critical loop where cudaMalloc/cudaFree would synchronise
+ * the device.  No handle is needed; rcut is the cutoff.  d_x (3n doubles), d_type
+ * (n ints) and d_counts (n ints) are device pointers; box is a host array.  The box
+ * and cutoff pass the same checks as every other entry point (NNAP_ERR_ARG otherwise).
  * Its scratch is one fixed 2 MiB device array compiled into the library (held by every
- * GPU that loads it): at most 16384 atoms and 16384 cells, larger inputs return
- * NNAP_ERR_CAPACITY.  The first call on each device looks up that array's address and
- * should come before any stream capture.  All calls share the array, so calls whose
- * work overlaps on the GPU race.  Work is queued on `stream` (NULL: CUDA's default
- * stream) and the call waits for it. */
+ * GPU that loads it): at most 16384 atoms and 16384 cells of the cell list, larger
+ * inputs return NNAP_ERR_CAPACITY before any device work.  The first call on each
+ * device looks up that array's address and should come before any stream capture.
+ * All calls share the array, so calls whose work overlaps on the GPU race.  Work is
+ * queued on `stream` (NULL: CUDA's default stream) and the call waits for it. */
 int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const int* d_type, int box_kind, const double* box,
                                  double rcut, int* d_counts, void* stream);
 

@@ -264,7 +264,13 @@ int guarded(nnap_handle* h, F&& f) {
     }
 }
 
-// Structure descriptor for cutoff rc: box rows, cell grid, float screen bound.
+// Box geometry of one structure of n atoms for cutoff rc: box rows, cell grid, float
+// screen bound (a0 and c0 left at zero).  Shared by every entry point; never throws:
+// returns NNAP_OK, or NNAP_ERR_ARG with *why (may be NULL) set for a bad box kind, a
+// box that is not right-handed with finite positive volume, a non-finite or
+// non-positive cutoff, or a box too thin for the cutoff.
+int struct_geometry(int kind, const double* box, double rc, int n, StructDev& s, const char** why);
+// Structure descriptor for cutoff rc (struct_geometry, throwing ApiFail on failure).
 StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0);
 // Float screen bound for cutoff rc when image shifts reach Rm cells.
 float screen_bound(const StructDev& s, double rc, int Rm);

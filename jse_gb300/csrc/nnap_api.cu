@@ -279,10 +279,22 @@ float screen_bound(const StructDev& s, double rc, int Rm) {
 
 constexpr double kHalfCellAtoms = 20.0;  // atoms per rc^3 from which cells are rc/2 wide
 
-StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0) {
-    if (kind < 0 || kind > 2) throw ApiFail(NNAP_ERR_ARG, "box_kind must be 0, 1 or 2");
-    StructDev s;
+int struct_geometry(int kind, const double* box, double rc, int n, StructDev& s, const char** why) {
     std::memset(&s, 0, sizeof s);
+    const char* dummy = nullptr;
+    const char*& msg = why ? *why : dummy;
+    if (kind < 0 || kind > 2) {
+        msg = "box_kind must be 0, 1 or 2";
+        return NNAP_ERR_ARG;
+    }
+    if (!box) {
+        msg = "box is NULL";
+        return NNAP_ERR_ARG;
+    }
+    if (!(rc > 0.0) || !std::isfinite(rc)) {
+        msg = "the cutoff must be positive and finite";
+        return NNAP_ERR_ARG;
+    }
     s.kind = kind;
     for (int d = 0; d < 3; ++d) { s.a[d] = box[d]; s.b[d] = box[3 + d]; s.c[d] = box[6 + d]; }
     if (kind == 0) {
@@ -295,7 +307,10 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
     cross3(s.a, s.b, s.ab);
     s.vol = (s.a[1] * s.b[2] - s.b[1] * s.a[2]) * s.c[0] + (s.a[2] * s.b[0] - s.b[2] * s.a[0]) * s.c[1] +
             (s.a[0] * s.b[1] - s.b[0] * s.a[1]) * s.c[2];
-    if (!(s.vol > 0.0) || !std::isfinite(s.vol)) throw ApiFail(NNAP_ERR_ARG, "box must be right-handed with positive volume");
+    if (!(s.vol > 0.0) || !std::isfinite(s.vol)) {
+        msg = "box must be right-handed with positive volume";
+        return NNAP_ERR_ARG;
+    }
     auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
     const double h[3] = {s.vol / nrm(s.bc), s.vol / nrm(s.ca), s.vol / nrm(s.ab)};
     // cells at least rc wide, or rc/2 wide where an rc^3 volume holds many atoms: the
@@ -303,13 +318,24 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
     // candidates of the 3^3 stencil
     const int div = (double)n / s.vol * rc * rc * rc >= kHalfCellAtoms ? 2 : 1;
     for (int d = 0; d < 3; ++d) {
-        s.nc[d] = std::max(1, (int)std::floor(h[d] * div / rc));
-        s.nc[d] = std::min(s.nc[d], 1024);
-        s.R[d] = (int)std::floor(rc * s.nc[d] / h[d] + 1e-6) + 1;
-        if (s.R[d] > 64) throw ApiFail(NNAP_ERR_ARG, "box too thin for the cutoff");
+        if (!std::isfinite(h[d]) || !(h[d] > 0.0)) {
+            msg = "box must be right-handed with positive volume";
+            return NNAP_ERR_ARG;
+        }
+        // bounded in double before any conversion to int
+        const double ncd = std::min(1024.0, std::max(1.0, std::floor(h[d] * div / rc)));
+        s.nc[d] = (int)ncd;
+        const double Rd = std::floor(rc * ncd / h[d] + 1e-6) + 1.0;
+        if (!(Rd <= 64.0)) {
+            msg = "box too thin for the cutoff";
+            return NNAP_ERR_ARG;
+        }
+        s.R[d] = (int)Rd;
     }
-    if ((2 * s.R[0] + 1) * (2 * s.R[1] + 1) * (2 * s.R[2] + 1) > 65535)
-        throw ApiFail(NNAP_ERR_ARG, "box too thin for the cutoff");
+    if ((2 * s.R[0] + 1) * (2 * s.R[1] + 1) * (2 * s.R[2] + 1) > 65535) {
+        msg = "box too thin for the cutoff";
+        return NNAP_ERR_ARG;
+    }
     for (int d = 0; d < 3; ++d) {
         s.fa[d] = (float)s.a[d]; s.fb[d] = (float)s.b[d]; s.fc[d] = (float)s.c[d];
         s.la[d] = (float)(s.a[d] - (double)s.fa[d]);
@@ -324,8 +350,16 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
         s.iv[2][d] = (float)(s.ab[d] / s.vol);
     }
     s.smin2 = (float)(smallest_sq_singular(s) * (1.0 - 1e-5));
-    s.a0 = a0;
     s.n = n;
+    return NNAP_OK;
+}
+
+StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int c0) {
+    StructDev s;
+    const char* why = "";
+    const int st = struct_geometry(kind, box, rc, n, s, &why);
+    if (st != NNAP_OK) throw ApiFail(st, why);
+    s.a0 = a0;
     s.c0 = c0;
     return s;
 }

@@ -1,17 +1,19 @@
 // Neighbour counting that allocates nothing.
 //
-// Some callers cannot call cudaMalloc at the moment they need an answer.  Examples:
-// - a host program capturing a CUDA graph in global capture mode, where allocation
-//   calls are prohibited until the capture ends;
-// - a simulation engine that reserves all device memory from its own pool at start-up
-//   and forbids allocations afterwards.
+// Some callers cannot call cudaMalloc at the moment they need an answer:
+// - a simulation engine, or a framework's caching allocator, that reserves all device
+//   memory for its own pool at start-up, so that a later cudaMalloc fails or takes
+//   memory the engine has already promised elsewhere;
+// - code in a latency-critical loop, where cudaMalloc and cudaFree synchronise the
+//   device and stall the work of every other stream.
 // nnap_neighbor_counts_noalloc serves them.  It runs the same wrap, cell-binning and
-// neighbour kernels as the handle-based path, but every scratch buffer lives in the
-// fixed array below.  That array is part of the library image: every GPU that loads the
-// library holds it until the process exits.
+// neighbour kernels as the handle-based path, with the same box geometry and checks
+// (struct_geometry), but every scratch buffer lives in the fixed array below.  That
+// array is part of the library image: every GPU that loads the library holds it until
+// the process exits.
 //
 // The array is shared by all calls.  The first call on each device looks up the
-// array's device address (cudaGetSymbolAddress) with that device current.  Make that
+// array's device address (cudaGetSymbolAddress) with that device current; make that
 // first call before any stream capture.  Calls whose work overlaps on the GPU race on
 // the array.  Each call clears the parts that must start at zero.
 #include <cuda_runtime.h>
@@ -21,18 +23,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "../../include/nnap_gb300.h"
-#include "common.cuh"
-
-namespace nnapgb {
-__global__ void k_wrap_bin(const StructDev*, const int*, const double*, const int*, int, int, double*, float4*,
-                           float4*, int*, int*, int*);
-__global__ void k_scan_excl(const int*, int, int*);
-__global__ void k_fill_cells(const int*, int, const int*, int*, int*);
-__global__ void k_sort_cells(const int*, int, int*);
-__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const int*,
-                            const int*, const int*, int, PairBufs, int*, int*);
-}  // namespace nnapgb
+#include "api_internal.hpp"
 
 using namespace nnapgb;
 
@@ -72,19 +63,20 @@ static_assert(carve(kNoAllocMaxAtoms, kNoAllocMaxCells).end <= kNoAllocBytes, "s
 constexpr int kMaxDevices = 64;
 unsigned char* g_scratch_ptr[kMaxDevices] = {nullptr};
 
-void cross3(const double* u, const double* v, double* r) {
-    r[0] = u[1] * v[2] - v[1] * u[2];
-    r[1] = u[2] * v[0] - v[2] * u[0];
-    r[2] = u[0] * v[1] - v[0] * u[1];
-}
-
 }  // namespace
 
 extern "C" int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const int* d_type, int box_kind,
                                             const double* box, double rcut, int* d_counts, void* stream) {
-    if (natoms < 0 || natoms > kNoAllocMaxAtoms) return NNAP_ERR_CAPACITY;
-    if (!box || !(rcut > 0.0) || box_kind < 0 || box_kind > 2) return NNAP_ERR_ARG;
+    // every check that needs no device comes first
+    if (natoms < 0) return NNAP_ERR_ARG;
+    if (natoms > kNoAllocMaxAtoms) return NNAP_ERR_CAPACITY;
     if (natoms > 0 && (!d_x || !d_type || !d_counts)) return NNAP_ERR_ARG;
+    StructDev s;
+    const int geo = struct_geometry(box_kind, box, rcut, natoms, s, nullptr);
+    if (geo != NNAP_OK) return geo;
+    const long long ncells = (long long)s.nc[0] * s.nc[1] * s.nc[2];
+    if (ncells > kNoAllocMaxCells) return NNAP_ERR_CAPACITY;
+
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
         cudaGetLastError();
@@ -99,42 +91,6 @@ extern "C" int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const
         g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
     }
     unsigned char* base = g_scratch_ptr[dev];
-
-    // structure descriptor (same geometry rules as the handle-based path)
-    StructDev s;
-    std::memset(&s, 0, sizeof s);
-    s.kind = box_kind;
-    for (int d = 0; d < 3; ++d) { s.a[d] = box[d]; s.b[d] = box[3 + d]; s.c[d] = box[6 + d]; }
-    if (box_kind == 0) s.a[1] = s.a[2] = s.b[0] = s.b[2] = s.c[0] = s.c[1] = 0.0;
-    else if (box_kind == 1) s.a[1] = s.a[2] = s.b[2] = 0.0;
-    cross3(s.b, s.c, s.bc);
-    cross3(s.c, s.a, s.ca);
-    cross3(s.a, s.b, s.ab);
-    s.vol = (s.a[1] * s.b[2] - s.b[1] * s.a[2]) * s.c[0] + (s.a[2] * s.b[0] - s.b[2] * s.a[0]) * s.c[1] +
-            (s.a[0] * s.b[1] - s.b[0] * s.a[1]) * s.c[2];
-    if (!(s.vol > 0.0)) return NNAP_ERR_ARG;
-    auto nrm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
-    const double h[3] = {s.vol / nrm(s.bc), s.vol / nrm(s.ca), s.vol / nrm(s.ab)};
-    double ext = 0.0;
-    long long ncells = 1;
-    for (int d = 0; d < 3; ++d) {
-        s.nc[d] = std::max(1, (int)std::floor(h[d] / rcut));
-        s.nc[d] = std::min(s.nc[d], 1024);
-        s.R[d] = (int)std::floor(rcut * s.nc[d] / h[d] + 1e-6) + 1;
-        if (s.R[d] > 64) return NNAP_ERR_ARG;
-        ncells *= s.nc[d];
-        ext += std::fabs(s.a[d]) + std::fabs(s.b[d]) + std::fabs(s.c[d]);
-    }
-    if (ncells > kNoAllocMaxCells) return NNAP_ERR_CAPACITY;
-    for (int d = 0; d < 3; ++d) { s.fa[d] = (float)s.a[d]; s.fb[d] = (float)s.b[d]; s.fc[d] = (float)s.c[d]; }
-    s.rc2 = rcut * rcut;
-    const int Rm = std::max(s.R[0], std::max(s.R[1], s.R[2]));
-    const double eps = 16.0 * (ext * (2 + Rm)) * std::ldexp(1.0, -24);
-    const double margin = 2.0 * std::sqrt(3.0) * rcut * eps + 3.0 * eps * eps + 16.0 * rcut * rcut * std::ldexp(1.0, -24);
-    s.rc2_hi = (float)(rcut * rcut + margin) * (1.0f + 1e-6f);
-    s.a0 = 0;
-    s.n = natoms;
-    s.c0 = 0;
 
     const Carve k = carve(natoms, (size_t)ncells);
     cudaStream_t st = (cudaStream_t)stream;

@@ -18,6 +18,7 @@ Boxes are 3x3 row matrices ``[a; b; c]``.  ``box_kind`` 0 is orthogonal (diagona
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
@@ -53,40 +54,135 @@ def _lmp_box(L: float, tilt: float) -> np.ndarray:
     return np.array([[L, 0.0, 0.0], [tilt * L, L, 0.0], [tilt * L, tilt * L, L]])
 
 
-_RSA = None
+def _cross(u, v):
+    return (u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0])
 
 
-def _rsa_lib():
-    """The C generator (jse_gb300/csrc/rsa.c), compiled on first use."""
-    global _RSA
-    if _RSA is None:
-        import ctypes as C
-        import os
-        import subprocess
-        here = os.path.dirname(os.path.abspath(__file__))
-        src = os.path.join(here, "csrc", "rsa.c")
-        lib = os.path.join(here, "librsa.so")
-        if not os.path.exists(lib) or os.path.getmtime(lib) < os.path.getmtime(src):
-            subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", src, "-o", lib, "-lm"], check=True)
-        L = C.CDLL(lib)
-        L.rsa_generate.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_double, C.c_uint64, C.c_int,
-                                   C.POINTER(C.c_double)]
-        L.rsa_generate.restype = C.c_int
-        _RSA = L
-    return _RSA
+def _norm(u):
+    return math.sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2])
+
+
+def _rsa_grid(box, rmin: float):
+    """Cell grid for random sequential addition: cells whose longest diagonal is below
+    rmin (so a cell holds at most one accepted point) and the cell offsets along a, b, c
+    that reach every point within rmin.  Scalar Python arithmetic (no BLAS), so the grid
+    is the same on every machine."""
+    A, B, C = [[float(v) for v in row] for row in box]
+    bc, ca, ab = _cross(B, C), _cross(C, A), _cross(A, B)
+    vol = abs(A[0] * bc[0] + A[1] * bc[1] + A[2] * bc[2])
+    h = [vol / _norm(bc), vol / _norm(ca), vol / _norm(ab)]
+    nc = [max(1, int(math.floor(_norm(r) * math.sqrt(3.0) * 1.15 / rmin))) for r in (A, B, C)]
+    while True:
+        worst = 0.0
+        for sa, sb, sc in ((1, 1, 1), (1, 1, -1), (1, -1, 1), (-1, 1, 1)):
+            v = [sa * A[d] / nc[0] + sb * B[d] / nc[1] + sc * C[d] / nc[2] for d in range(3)]
+            worst = max(worst, _norm(v))
+        if worst < rmin * 0.999:
+            break
+        nc = [k + 1 for k in nc]
+    R = [int(math.ceil(rmin * nc[d] / h[d])) for d in range(3)]
+    return np.array(nc, dtype=np.int64), np.array(R, dtype=np.int64), vol
+
+
+def _to_cart(f, box):
+    """Direct coordinates [m, 3] to Cartesian, elementwise (no BLAS, so no machine-dependent
+    fused multiply-adds)."""
+    return np.stack([f[:, 0] * box[0, d] + f[:, 1] * box[1, d] + f[:, 2] * box[2, d] for d in range(3)], axis=1)
 
 
 def _rsa(n: int, box: np.ndarray, rmin: float, seed: int) -> np.ndarray:
-    """Random sequential addition of ``n`` points with pair distance >= rmin under PBC."""
-    import ctypes as C
-    L = _rsa_lib()
-    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
-    out = np.zeros((max(n, 1), 3))
-    got = L.rsa_generate(n, b.ctypes.data_as(C.POINTER(C.c_double)), float(rmin), int(seed) & ((1 << 64) - 1),
-                         100000, out.ctypes.data_as(C.POINTER(C.c_double)))
-    if got != n:
-        raise RuntimeError("random sequential addition stalled at %d of %d points" % (got, n))
-    return out[:n]
+    """Uniform random points with every pair distance >= rmin under periodic boundaries
+    (all images), by random sequential addition in batches.
+
+    Candidates are drawn uniformly in direct coordinates from numpy's PCG64 stream of
+    ``seed`` and are accepted in draw order.  A candidate is rejected when an accepted
+    point lies within rmin, or when an earlier candidate of its batch that passed that
+    test lies within rmin (earlier candidates that are themselves rejected still count, so
+    a batch can reject a little more than one-at-a-time addition would).  Batches are
+    sized from the last batch's acceptance rate so that they accept about one point per
+    16 exclusion volumes of the box, which keeps such in-batch conflicts rare.  Pure
+    numpy, so structures are identical on every machine."""
+    box = np.asarray(box, dtype=np.float64).reshape(3, 3)
+    if n <= 0:
+        return np.zeros((0, 3))
+    rng = np.random.default_rng(int(seed) & ((1 << 63) - 1))
+    nc, R, vol = _rsa_grid(box, rmin)
+    ncell = int(nc.prod())
+    occ = np.full(ncell, -1, dtype=np.int32)   # accepted point of each cell
+    tmp = np.full(ncell, -1, dtype=np.int32)   # first passing candidate of each cell, per batch
+    frac = np.zeros((n, 3))
+    # stencil per axis; offsets whose cells are certainly farther apart than rmin still
+    # take part (the distance test rejects nothing there), which keeps the index simple
+    ax = [np.arange(-R[d], R[d] + 1) for d in range(3)]
+    r2 = rmin * rmin
+    target = max(4.0, vol / (4.0 / 3.0 * math.pi * rmin ** 3) / 16.0)
+    placed, stalled, rate = 0, 0, 1.0
+
+    def stencil(c):
+        """Flat cell index [m, sa, sb, sc] of each stencil cell and the image shift along
+        each axis ([m, sa], [m, sb], [m, sc])."""
+        q = [c[:, d, None] + ax[d][None, :] for d in range(3)]
+        img = [np.floor_divide(q[d], nc[d]) for d in range(3)]
+        w = [(q[d] - img[d] * nc[d]).astype(np.int32) for d in range(3)]
+        fl = w[0][:, :, None, None] + np.int32(nc[0]) * (w[1][:, None, :, None] + np.int32(nc[1]) * w[2][:, None, None, :])
+        return fl, img
+
+    def too_close(ci, ia, ib, ic, img, other_frac, mine):
+        df = other_frac - mine
+        df[:, 0] += img[0][ci, ia]
+        df[:, 1] += img[1][ci, ib]
+        df[:, 2] += img[2][ci, ic]
+        v = _to_cart(df, box)
+        return v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2] < r2
+
+    while placed < n:
+        nb = int(min(max(16.0, target / rate), 65536))
+        s = rng.random((nb, 3))
+        c = np.minimum((s * nc).astype(np.int64), nc - 1)
+        fl, img = stencil(c)
+        ok = np.ones(nb, dtype=bool)
+        # the 27 nearest cells first: they reject most candidates; then the rest of the
+        # stencil for the candidates still standing
+        o = occ[fl[:, R[0] - 1:R[0] + 2, R[1] - 1:R[1] + 2, R[2] - 1:R[2] + 2]]
+        ci, ia, ib, ic = np.nonzero(o >= 0)
+        if len(ci):
+            bad = too_close(ci, ia + R[0] - 1, ib + R[1] - 1, ic + R[2] - 1, img, frac[o[ci, ia, ib, ic]], s[ci])
+            ok[ci[bad]] = False
+        live = np.nonzero(ok)[0]
+        o = occ[fl[live]]
+        o[:, R[0] - 1:R[0] + 2, R[1] - 1:R[1] + 2, R[2] - 1:R[2] + 2] = -1
+        ci, ia, ib, ic = np.nonzero(o >= 0)
+        if len(ci):
+            bad = too_close(live[ci], ia, ib, ic, img, frac[o[ci, ia, ib, ic]], s[live[ci]])
+            ok[live[ci[bad]]] = False
+        # conflicts with earlier passing candidates of the same batch
+        cand = np.nonzero(ok)[0]
+        if len(cand) > 1:
+            fc = fl[cand, R[0], R[1], R[2]]
+            # the first candidate of each cell claims it (assignments in reverse order leave
+            # the earliest); later ones in that cell are too close
+            tmp[fc[::-1]] = cand[::-1].astype(np.int32)
+            reject = tmp[fc] != cand
+            o2 = tmp[fl[cand]]
+            m = (o2 >= 0) & (o2 < cand[:, None, None, None])
+            ci, ia, ib, ic = np.nonzero(m)
+            if len(ci):
+                bad = too_close(ci, ia, ib, ic, [g[cand] for g in img], s[o2[ci, ia, ib, ic]], s[cand[ci]])
+                reject[ci[bad]] = True
+            tmp[fc] = -1
+            ok[cand[reject]] = False
+        acc = np.nonzero(ok)[0][: n - placed]
+        rate = max(len(acc), 0.5) / nb
+        if len(acc) == 0:
+            stalled += nb
+            if stalled > 100000:
+                raise RuntimeError("random sequential addition stalled at %d of %d points" % (placed, n))
+            continue
+        stalled = 0
+        frac[placed:placed + len(acc)] = s[acc]
+        occ[fl[acc, R[0], R[1], R[2]]] = np.arange(placed, placed + len(acc))
+        placed += len(acc)
+    return _to_cart(frac, box)
 
 
 def random_liquid(n: int, density: float, fractions: Sequence[float], rmin: float, seed: int,
@@ -163,6 +259,35 @@ C2_BASIS = {"type": "spherical_chebyshev", "nmax": 8, "lmax": 6, "rcut": 6.0, "w
 C3_BASIS = {"type": "spherical_chebyshev", "nmax": 8, "lmax": 4, "rcut": 5.5, "wtype": "default"}
 
 
+_CACHE_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), ".cache", "workloads")
+_GEN_VERSION = 3  # bump when the generator's output changes
+
+
+def _cached(key: str, make):
+    """Structures made by ``make()``, kept as an .npz under the repository's .cache folder
+    (not committed) so that the benchmark's arms and the tests generate each large
+    workload once per machine."""
+    path = os.path.join(_CACHE_DIR, "%s_v%d.npz" % (key, _GEN_VERSION))
+    try:
+        z = np.load(path)
+        k = int(z["count"])
+        return [Structure(z["x%d" % i], z["t%d" % i], z["b%d" % i], int(z["k%d" % i])) for i in range(k)]
+    except (OSError, KeyError, ValueError):
+        pass
+    out = make()
+    try:
+        os.makedirs(_CACHE_DIR, exist_ok=True)
+        arrs = {"count": np.array(len(out))}
+        for i, st in enumerate(out):
+            arrs["x%d" % i], arrs["t%d" % i], arrs["b%d" % i], arrs["k%d" % i] = st.x, st.types, st.box, np.array(st.box_kind)
+        tmp = path + ".%d.tmp.npz" % os.getpid()
+        np.savez(tmp, **arrs)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+    return out
+
+
 def c1_structure(seed: int = 1) -> Structure:
     """FCC a=3.61 A, 10x10x10 cells (4000 atoms), sigma=0.05 A."""
     return fcc(3.61, 10, 0.05, seed)
@@ -170,17 +295,21 @@ def c1_structure(seed: int = 1) -> Structure:
 
 def c2_structure(n: int = 32000, seed: int = 2) -> Structure:
     """Ternary liquid, density 0.060 /A^3, fractions 0.46/0.46/0.08, min separation 2.0 A."""
-    return random_liquid(n, 0.060, [0.46, 0.46, 0.08], 2.0, seed)
+    return _cached("c2_%d_%d" % (n, seed), lambda: [random_liquid(n, 0.060, [0.46, 0.46, 0.08], 2.0, seed)])[0]
 
 
 def c3_structure(n: int = 1048576, seed: int = 3) -> Structure:
     """Binary glass, density 0.058 /A^3, fractions 0.64/0.36, min separation 2.1 A, tilt 0.1."""
-    return random_liquid(n, 0.058, [0.64, 0.36], 2.1, seed, tilt=0.1)
+    return _cached("c3_%d_%d" % (n, seed), lambda: [random_liquid(n, 0.058, [0.64, 0.36], 2.1, seed, tilt=0.1)])[0]
 
 
 def c4_structures(count: int = 1024, seed: int = 4) -> List[Structure]:
     """Mixed batch: n ~ log-uniform[32, 2048], half orthogonal / half triclinic (tilt 0.1),
     density ~ U[0.055, 0.065], ternary species as the liquid workload, min separation 2.0 A."""
+    return _cached("c4_%d_%d" % (count, seed), lambda: _c4_make(count, seed))
+
+
+def _c4_make(count: int, seed: int) -> List[Structure]:
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
@@ -207,6 +336,10 @@ def c5_pool(count: int = 512, seed: int = 5, sigma: float = 1.0) -> List[Structu
     clipped to [50, 20000]; ternary liquids as the 32000-atom workload (cubic box,
     density 0.060 /A^3, fractions 0.46/0.46/0.08, min separation 2.0 A).  Requests draw
     their starting structure from this pool."""
+    return _cached("c5_%d_%d_%g" % (count, seed, sigma), lambda: _c5_make(count, seed, sigma))
+
+
+def _c5_make(count: int, seed: int, sigma: float) -> List[Structure]:
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):

@@ -2,10 +2,11 @@
 list of the handle-based entry point (nnap_neighbor_list).
 
 Callers that cannot allocate device memory when they need the answer use this entry
-point: a program capturing a CUDA graph in global mode, or an engine that reserves all
-device memory up front.  Its scratch is a fixed array inside the library, shared by all
-calls, so the test calls it twice in a row: leftovers of the first call must not leak
-into the second.  Counts are integers and must match exactly.
+point: an engine that reserves all device memory for its own pool up front, or a loop
+where cudaMalloc would synchronise the device.  Its scratch is a fixed array inside the
+library, shared by all calls, so the GPU tests call it twice in a row: leftovers of the
+first call must not leak into the second.  Counts are integers and must match exactly.
+The size and argument checks run before any device work, so they are tested on the CPU.
 """
 import ctypes as C
 
@@ -14,7 +15,7 @@ import pytest
 
 from jse_gb300 import workloads as W
 
-pytestmark = pytest.mark.gpu
+NNAP_ERR_CAPACITY, NNAP_ERR_ARG = 3, 6
 
 
 def _lib():
@@ -40,6 +41,17 @@ def _noalloc_counts(L, s, rcut):
     return out.cpu().numpy()
 
 
+def _thin_triclinic(seed):
+    """About 90 atoms in a LAMMPS triclinic box whose c planes are 4.8 A apart, below the
+    6 A cutoff: the cell list searches two cell layers along c and rows hold images."""
+    box = np.array([[18.0, 0.0, 0.0], [3.0, 18.0, 0.0], [2.0, 1.5, 4.8]])
+    n = int(0.058 * 18.0 * 18.0 * 4.8)
+    x = W._rsa(n, box, 2.0, seed)
+    types = (np.arange(n) % 3 + 1).astype(np.int32)
+    return W.Structure(x, types, box, W.BOX_LMP)
+
+
+@pytest.mark.gpu
 def test_noalloc_counts_match_neighbor_list_twice():
     from jse_gb300.nnap import NNAP
     L = _lib()
@@ -56,8 +68,48 @@ def test_noalloc_counts_match_neighbor_list_twice():
     assert np.array_equal(b, ref2)
 
 
-def test_noalloc_rejects_sizes_beyond_its_scratch():
+@pytest.mark.gpu
+def test_noalloc_thin_triclinic_box_twice():
+    from jse_gb300.nnap import NNAP
+    L = _lib()
+    s = _thin_triclinic(73)
+    with NNAP(W.model_for("c2")) as p:
+        ref = np.diff(p.neighborList(s)[0])
+        rcut = p.rcutMax()
+    assert ref.max() > 0
+    for _ in range(2):
+        assert np.array_equal(_noalloc_counts(L, s, rcut), ref)
+
+
+def test_noalloc_rejects_too_many_atoms():
     L = _lib()
     box = np.diag([200.0, 200.0, 200.0]).reshape(9)
     bp = box.ctypes.data_as(C.POINTER(C.c_double))
-    assert L.nnap_neighbor_counts_noalloc(16385, None, None, 0, bp, 6.0, None, None) == 3  # NNAP_ERR_CAPACITY
+    assert L.nnap_neighbor_counts_noalloc(16385, None, None, 0, bp, 6.0, None, None) == NNAP_ERR_CAPACITY
+
+
+def test_noalloc_rejects_too_many_cells():
+    """A 200 A box with a 6 A cutoff needs 33^3 > 16384 cells: refused before any device work."""
+    L = _lib()
+    box = np.diag([200.0, 200.0, 200.0]).reshape(9)
+    bp = box.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.nnap_neighbor_counts_noalloc(100, 8, 8, 0, bp, 6.0, 8, None) == NNAP_ERR_CAPACITY
+
+
+@pytest.mark.parametrize("rcut", [float("inf"), float("nan"), 0.0, -1.0])
+def test_noalloc_rejects_bad_cutoff(rcut):
+    L = _lib()
+    box = np.diag([20.0, 20.0, 20.0]).reshape(9)
+    bp = box.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.nnap_neighbor_counts_noalloc(10, 8, 8, 0, bp, rcut, 8, None) == NNAP_ERR_ARG
+
+
+@pytest.mark.parametrize("box", [np.diag([np.inf, 20.0, 20.0]), np.diag([20.0, -20.0, 20.0]),
+                                 np.diag([20.0, 20.0, 1e-9]),
+                                 np.array([[20.0, 0, 0], [0, 20.0, 0], [20.0, 20.0, 0.0]])])
+def test_noalloc_rejects_bad_box(box):
+    """Non-finite, left-handed, far too thin and flat boxes fail the shared geometry checks."""
+    L = _lib()
+    b = np.ascontiguousarray(box, dtype=np.float64).reshape(9)
+    assert L.nnap_neighbor_counts_noalloc(10, 8, 8, 2, b.ctypes.data_as(C.POINTER(C.c_double)), 6.0, 8,
+                                          None) == NNAP_ERR_ARG
