@@ -913,7 +913,7 @@ def main():
     plain["tuned_value_over_plain"] = value / plain["value"]
     mean_nei = mean_neighbours(pot, structures)
     roof = roofline(model, mean_nei, run["stages"], natoms_step, args.workload, sm_count)
-    config["launch_shapes"] = pot.tuning(max(s.natoms for s in structures))
+    config["launch_shapes"] = pot.tuning(natoms_step)
 
     extras = rank == 0 and not args.no_extras
     liquid = None

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libnnap_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["nnap_api.cu", "nnap_server.cu", "nnap_lammps.cu", "k_struct.cu", "k_resident.cu", "k_lammps.cu",
-           "k_desc.cu", "k_net.cu", "k_zbl.cu", "k_net_tc.cu", "nnap_noalloc.cu", "k_train.cu", "nnap_train.cu",
+           "k_desc.cu", "k_desc_gen.cu", "k_net.cu", "k_zbl.cu", "k_net_tc.cu", "nnap_noalloc.cu", "k_train.cu", "nnap_train.cu",
            "model.cpp", "nep_model.cpp", "invariants.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

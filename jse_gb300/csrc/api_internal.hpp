@@ -144,7 +144,7 @@ struct Run {
 
 struct NetDev {
     int D, nlayer;
-    int H[4];
+    int H[kNetMaxLayers];
     DevBuf<float> w32;
     double mu_e, sigma_e;
     NetTC tc;  // tensor-core parameters (mixed precision)
@@ -169,6 +169,7 @@ struct nnap_handle {
     nnapgb::Model model;
     int precision = NNAP_PREC_FP32;
     bool net_tc = false;  // networks on the tensor cores (mixed precision, SiLU networks)
+    std::string net_notes;  // species whose network runs the FP32 kernel on a mixed handle, and why
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;

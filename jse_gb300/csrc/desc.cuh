@@ -101,12 +101,22 @@ cudaError_t upload_sh_constants();
 // Compact rows of the entries within rc (k_subrows): sdx / spos [n][P.M], scount [n].
 cudaError_t launch_subrows(const PairBufs& P, int n, float rc, float4* sdx, int* spos, int* scount,
                            cudaStream_t st);
-// basis: kRbNNAP or kRbNEP (the radial functions of the sub-basis)
+// basis: kRbNNAP or kRbNEP (the radial functions of the sub-basis).
+// desc_compiled: a shape-specialised instance exists (NNAP_*_SHAPES / NEP_*_SHAPES);
+// desc_supported: that, or the any-shape kernels of k_desc_gen.cu fit in shared memory.
+bool desc_compiled(int kind, int basis, int lmax, int np, int n1);
 bool desc_supported(int kind, int basis, int lmax, int np, int n1);
+// Specialised instance when there is one, else the any-shape kernels.
 cudaError_t launch_descriptor(int kind, int basis, int lmax, int np, int n1, const DescArgs& a, bool fwd,
                               cudaStream_t st);
+// The any-shape kernels (k_desc_gen.cu): runtime NP and N1 <= 21, L <= 12.
+bool desc_generic_fits(int kind, int lmax, int np, int n1);
+cudaError_t launch_descriptor_generic(int kind, int basis, int lmax, int np, int n1, const DescArgs& a, bool fwd,
+                                      cudaStream_t st);
+cudaError_t upload_sh_constants_gen();
 
 // Network over the slots of one species.
+constexpr int kNetMaxLayers = 16;  // hidden layers of a network
 struct NetArgs {
     const int* perm;
     const int* range;       // device: first slot of each species, [ntypes + 1]
@@ -115,7 +125,7 @@ struct NetArgs {
     const float* fp;        // descriptors by slot
     int fp_stride;
     int D, nlayer;
-    int H[4];
+    int H[kNetMaxLayers];
     const float* w;         // packed FP32 parameters of the species (see net_pack_layout)
     double mu_e, sigma_e;
     double* e_atom;         // energy per atom (by atom index)
@@ -125,5 +135,7 @@ struct NetArgs {
 
 // FP32 SIMT network (plain precision).
 cudaError_t launch_net_fp32(const NetArgs& a, cudaStream_t st);
+// Whether the FP32 network of this shape fits in shared memory (at least one warp per CTA).
+bool net_fp32_fits(int D, int nlayer, const int* H);
 
 }  // namespace nnapgb

@@ -1100,6 +1100,10 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
 
 
 bool desc_supported(int kind, int basis, int lmax, int np, int n1) {
+    return desc_compiled(kind, basis, lmax, np, n1) || desc_generic_fits(kind, lmax, np, n1);
+}
+
+bool desc_compiled(int kind, int basis, int lmax, int np, int n1) {
 #define R_CASE(P_, N_) if (kind == 0 && np == P_ && n1 == N_) return true;
 #define S_CASE(L_, P_, N_) if (kind == 1 && lmax == L_ && np == P_ && n1 == N_) return true;
     if (basis == kRbNNAP) {
@@ -1130,7 +1134,7 @@ cudaError_t launch_descriptor(int kind, int basis, int lmax, int np, int n1, con
     }
 #undef R_CASE
 #undef S_CASE
-    return cudaErrorInvalidValue;
+    return launch_descriptor_generic(kind, basis, lmax, np, n1, a, fwd, st);
 }
 
 }  // namespace nnapgb

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
     extern __shared__ float smem[];
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s0 = a.range[a.t], s1 = a.range[a.t + 1];
-    const int slot0 = s0 + (blockIdx.x * kNetWarps + wl) * kNetAtoms;
+    const int slot0 = s0 + (blockIdx.x * (blockDim.x >> 5) + wl) * kNetAtoms;
     if (slot0 >= s1) return;
     const int na = min(kNetAtoms, s1 - slot0);
     int Hmax = a.D;
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
             buf0[i * kNetAtoms + q] = q < na ? (a.fp[(size_t)(slot0 + q) * a.fp_stride + i] - mu[i]) * isig[i] : 0.f;
     __syncwarp();
     const float* p = isig + a.D;
-    const float* layerW[4];
+    const float* layerW[kNetMaxLayers];
     int in = a.D;
     float* cur = buf0;
     float* nxt = buf1;
@@ -152,21 +152,35 @@ __global__ void __launch_bounds__(32 * kNetWarps) k_net_fp32(NetArgs a, int warp
 
 }  // namespace
 
+namespace {
+int net_warp_floats(int D, int nlayer, const int* H) {
+    int Hmax = D;
+    for (int l = 0; l < nlayer; ++l) Hmax = Hmax > H[l] ? Hmax : H[l];
+    return (2 + nlayer) * Hmax * kNetAtoms;
+}
+constexpr size_t kNetSmemMax = 227 * 1024;
+}  // namespace
+
+bool net_fp32_fits(int D, int nlayer, const int* H) {
+    return nlayer >= 1 && nlayer <= kNetMaxLayers && sizeof(float) * (size_t)net_warp_floats(D, nlayer, H) <= kNetSmemMax;
+}
+
 cudaError_t launch_net_fp32(const NetArgs& a, cudaStream_t st) {
     const int n = a.nmax;
     if (n <= 0) return cudaSuccess;
-    int Hmax = a.D;
-    for (int l = 0; l < a.nlayer; ++l) Hmax = Hmax > a.H[l] ? Hmax : a.H[l];
-    const int warp_floats = (2 + a.nlayer) * Hmax * kNetAtoms;
-    const size_t sm = sizeof(float) * (size_t)warp_floats * kNetWarps;
+    if (!net_fp32_fits(a.D, a.nlayer, a.H)) return cudaErrorInvalidValue;
+    const int warp_floats = net_warp_floats(a.D, a.nlayer, a.H);
+    int wpc = kNetWarps;  // fewer warps per CTA for wide networks
+    while (wpc > 1 && sizeof(float) * (size_t)warp_floats * wpc > kNetSmemMax) wpc >>= 1;
+    const size_t sm = sizeof(float) * (size_t)warp_floats * wpc;
     static int limit = 0;
     if ((int)sm > limit) {
         const cudaError_t e = cudaFuncSetAttribute(k_net_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
         limit = (int)sm;
     }
-    const int per_block = kNetAtoms * kNetWarps;
-    return launch_pdl(&k_net_fp32, dim3((n + per_block - 1) / per_block), dim3(32 * kNetWarps), sm, st, a, warp_floats);
+    const int per_block = kNetAtoms * wpc;
+    return launch_pdl(&k_net_fp32, dim3((n + per_block - 1) / per_block), dim3(32 * wpc), sm, st, a, warp_floats);
 }
 
 }  // namespace nnapgb

@@ -1,31 +1,36 @@
 // Tensor-core evaluation of the per-species network and its input gradient (the
 // mixed-precision path), on the 5th-generation tensor cores (tcgen05, TMEM accumulators).
 //
-// Mathematics: normedNnForward / normedNnBackward (nnap_main.hpp:267-323) with two SiLU
-// hidden layers (nn_FeedForward.hpp:8-261):
-//   X  = (fp - mu)/sigma                      [128 x Dp]   Dp = D rounded up to 16
-//   Z1 = X W1^T + b1, A1 = silu(Z1)           [128 x H1]   GEMM 1 (N = H1, K = Dp)
-//   Z2 = A1 W2^T + b2, A2 = silu(Z2)          [128 x H2]   GEMM 2 (N = H2, K = H1)
-//   E  = (w_o . A2 + b_o) sigma_E + mu_E      (FP32 on the CUDA cores, FP64 output)
-//   dZ2 = sigma_E w_o * silu'(Z2)
-//   dA1 = dZ2 W2                              [128 x H1]   GEMM 3 (N = H1, K = H2)
-//   dZ1 = dA1 * silu'(Z1)
-//   dX  = dZ1 W1                              [128 x Dp]   GEMM 4 (N = Dp, K = H1)
-//   dE/dfp = dX / sigma
-// Operands are BF16 and every product is split as hi*hi + lo*hi + hi*lo with
-// x = hi + lo (both BF16), accumulated in FP32 in TMEM: three kind::f16 MMAs per
-// 16-wide K step keep the network error near FP32 level (about 1e-6 eV per atom)
-// while the arithmetic stays on the BF16 tensor pipe.
+// Mathematics: normedNnForward / normedNnBackward (nnap_main.hpp:267-323) with L >= 1
+// SiLU hidden layers (nn_FeedForward.hpp:8-261), widths padded to multiples of 16:
+//   X   = (fp - mu)/sigma                       [128 x Dp]
+//   Z_l = A_{l-1} W_l^T + b_l, A_l = silu(Z_l)   [128 x Hp_l]  GEMM (N = Hp_l, K = K_l), A_0 = X
+//   E   = (w_o . A_L + b_o) sigma_E + mu_E       (FP32 on the CUDA cores, FP64 output)
+//   dZ_L = sigma_E w_o * silu'(Z_L)
+//   dA_{l-1} = dZ_l W_l                          [128 x K_l]   GEMM (N = K_l, K = Hp_l)
+//   dZ_{l-1} = dA_{l-1} * silu'(Z_{l-1})
+//   dE/dfp = dA_0 / sigma
+// Padded units have zero weights and biases, so they stay zero through every layer.
+// Operands are BF16 and every product is split as hi*hi + lo*hi + hi*lo with x = hi + lo
+// (both BF16), accumulated in FP32 in TMEM: three kind::f16 MMAs per 16-wide K step keep
+// the network error near FP32 level (about 1e-6 eV per atom) while the arithmetic stays
+// on the BF16 tensor pipe.
 //
-// One CTA of 128 threads owns a 128-atom tile; thread t owns row t (one atom) in every
-// epilogue, so TMEM lane t is read by thread t with tcgen05.ld 32x32b.  One thread
-// issues the MMAs; completion is signalled through an mbarrier (tcgen05.commit) whose
-// waits are bounded in time and raise ERRBIT_TIMEOUT instead of hanging.
+// One CTA of 128 x SPLIT threads owns a 128-atom tile; the SPLIT threads of row t read
+// TMEM lane t with tcgen05.ld 32x32b, each a share of the columns.  One thread issues the
+// MMAs; completion is signalled through an mbarrier (tcgen05.commit) whose waits are
+// bounded in time and raise ERRBIT_TIMEOUT instead of hanging.  Z_l of every layer stays
+// in TMEM for the backward pass; dA and dX share one column range.  One shared-memory
+// operand buffer holds the activation of the current GEMM and is overwritten by the next
+// layer's once that GEMM has completed.  The weight images of a species are staged in
+// shared memory once per species when they fit, otherwise the B operand of each GEMM is
+// copied in before it (the images are small and stay in L2).
 // Shared-memory operands use the no-swizzle K-major canonical layout: 8x8 core
 // matrices of 128 bytes, adjacent in K at LBO = 128 bytes and in M/N at
 // SBO = (K/8)*128 bytes.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -36,50 +41,91 @@
 
 namespace nnapgb {
 
+bool TCLayout::same(const TCLayout& o) const {
+    if (nl != o.nl || Dp != o.Dp) return false;
+    for (int l = 0; l < nl; ++l)
+        if (Hp[l] != o.Hp[l]) return false;
+    return true;
+}
+
 namespace {
 
 using namespace ::nnapgb::tc;
 
-// SPLIT threads per tile row in the epilogues (a launch parameter: 2 or 4); warp w
-// reads TMEM lanes 32 * (w % 4) .. 32 * (w % 4) + 31.
-
-struct TCLayout {
-    int Dp, H1, H2;
-    // byte offsets inside the weight image (all multiples of 1024)
-    int w1, w2, w2t, w1t, fvec, bytes;  // each operand image holds hi then lo
-    int fmu, fisig, fb1, fb2, fwo;      // float offsets inside the FP32 vector block
-    int ncols;                          // TMEM columns allocated
-    int z1, z2, da1, dx;                // TMEM column offsets
-};
+constexpr int kTcSmemMax = 220 * 1024;  // dynamic shared memory; the static part (mbarrier, energies) comes on top
+constexpr int kTcWidthMax = 256;       // widest padded layer (one MMA N, one operand buffer)
+constexpr int kTcOperandMax = 96 * 1024;  // largest single weight operand image (hi + lo)
+constexpr int kOutCols = 64;           // columns of dE/dfp staged per pass
 
 __host__ __device__ inline int align1k(int b) { return (b + 1023) & ~1023; }
+inline int r16(int v) { return (v + 15) & ~15; }
 
-TCLayout make_layout(int D, int H1, int H2) {
-    TCLayout L;
-    L.Dp = (D + 15) & ~15;
-    L.H1 = H1;
-    L.H2 = H2;
-    int off = 0;
-    L.w1 = off; off = align1k(off + 2 * 2 * H1 * L.Dp);
-    L.w2 = off; off = align1k(off + 2 * 2 * H2 * H1);
-    L.w2t = off; off = align1k(off + 2 * 2 * H1 * H2);
-    L.w1t = off; off = align1k(off + 2 * 2 * L.Dp * H1);
+// Layout of a network with descriptor length D and hidden widths H[0..nl-1]; false with a
+// reason when the kernel cannot take it.
+bool make_layout(int D, const std::vector<int>& H, TCLayout& L, std::string& why) {
+    const int nl = (int)H.size();
+    if (nl < 1 || nl > kTcMaxLayers) {
+        why = "the tensor-core network takes 1 to 8 hidden layers";
+        return false;
+    }
+    L.nl = nl;
+    L.Dp = r16(D);
+    L.Wmax = L.Dp;
+    int in = L.Dp, off = 0, wimg = 0;
+    for (int l = 0; l < nl; ++l) {
+        L.K[l] = in;
+        L.Hp[l] = r16(H[l]);
+        L.Wmax = std::max(L.Wmax, L.Hp[l]);
+        const int img = 4 * L.Hp[l] * in;  // hi + lo BF16
+        wimg = std::max(wimg, img);
+        L.wf[l] = off; off = align1k(off + img);
+        L.wb[l] = off; off = align1k(off + img);
+        in = L.Hp[l];
+    }
+    if (L.Wmax > kTcWidthMax) {
+        why = "the tensor-core network takes descriptors and hidden layers of at most 256 (padded) columns";
+        return false;
+    }
+    if (wimg > kTcOperandMax) {
+        why = "a tensor-core weight operand would exceed 96 KiB";
+        return false;
+    }
     L.fvec = off;
     L.fmu = 0;
     L.fisig = L.Dp;
-    L.fb1 = 2 * L.Dp;
-    L.fb2 = L.fb1 + H1;
-    L.fwo = L.fb2 + H2;
-    off = align1k(off + 4 * (L.fwo + H2 + 4));
+    int f = 2 * L.Dp;
+    for (int l = 0; l < nl; ++l) { L.fb[l] = f; f += L.Hp[l]; }
+    L.fwo = f;
+    f += L.Hp[nl - 1];
+    L.nvec = (f + 3) & ~3;
+    off = align1k(off + 4 * L.nvec);
     L.bytes = off;
-    L.z1 = 0;
-    L.z2 = H1;
-    L.da1 = H1 + H2;
-    L.dx = 2 * H1 + H2;
-    const int need = L.dx + L.Dp;
+    L.wimg = align1k(wimg);
+    // TMEM: Z of every layer, then one range for dA / dX
+    int cols = 0, dmax = 0;
+    for (int l = 0; l < nl; ++l) { L.z[l] = cols; cols += L.Hp[l]; dmax = std::max(dmax, L.K[l]); }
+    L.dacc = cols;
+    cols += dmax;
+    if (cols > 512) {
+        why = "the tensor-core network's accumulators would exceed the 512 TMEM columns";
+        return false;
+    }
     L.ncols = 32;
-    while (L.ncols < need) L.ncols *= 2;
-    return L;
+    while (L.ncols < cols) L.ncols *= 2;
+    L.act = align1k(std::max(4 * 128 * L.Wmax, 4 * 128 * (kOutCols + 4)));
+    const int staged = L.bytes + L.act;
+    const int streamed = align1k(4 * L.nvec) + L.wimg + L.act;
+    if (staged <= kTcSmemMax) {
+        L.staged = 1;
+        L.smem = staged;
+    } else if (streamed <= kTcSmemMax) {
+        L.staged = 0;
+        L.smem = streamed;
+    } else {
+        why = "the tensor-core network's operands exceed shared memory";
+        return false;
+    }
+    return true;
 }
 
 // Element (r, k) of an R x K K-major operand in the no-swizzle core-matrix layout.
@@ -98,7 +144,7 @@ float bf16_val(uint16_t u) {
     return f;
 }
 
-// Write the hi and lo images of an R x K matrix M(r, k) (zero outside rows/cols given).
+// Write the hi and lo images of an R x K matrix M(r, k).
 template <class F>
 void put_operand(std::vector<uint8_t>& img, int byte_off, int R, int K, F&& M) {
     uint16_t* hi = reinterpret_cast<uint16_t*>(img.data() + byte_off);
@@ -115,9 +161,9 @@ void put_operand(std::vector<uint8_t>& img, int byte_off, int R, int K, F&& M) {
 
 __device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + expf(-z)); }
 
-// Species t0 .. t0+nt-1 of one launch; all share one layout (D, H1, H2).  Tiles are
-// numbered species by species; a CTA stages a species' weights when its next tile
-// belongs to another species than the last one.
+// Species t0 .. t0+nt-1 of one launch; all share one layout.  Tiles are numbered species
+// by species; a CTA stages a species' image (or its FP32 vectors, in streamed mode) when
+// its next tile belongs to another species than the last one.
 struct TcParams {
     const int* perm;
     const int* range;     // device: first slot of each species
@@ -132,6 +178,13 @@ struct TcParams {
     int* err;
 };
 
+// Copy n bytes (a multiple of 16) from global to shared memory with every thread.
+__device__ __forceinline__ void copy16(uint8_t* dst, const uint8_t* src, int n, int tid, int nthr) {
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int q = tid; q < n / 16; q += nthr) d[q] = s[q];
+}
+
 template <int SPLIT>
 __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout L) {
     pdl_enter();
@@ -139,23 +192,24 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base;
     __shared__ int s_tstart[kMaxTypes + 1];
+    __shared__ float s_e[SPLIT][128];
+    constexpr int NT = 128 * SPLIT;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int part = tid >> 7;  // column share of this thread in the epilogues
-    __shared__ float s_e[SPLIT][128];
-    const int Dp = L.Dp, H1 = L.H1, H2 = L.H2;
-    uint8_t* sw = smem;                                       // weight image
-    uint8_t* sx = smem + L.bytes;                             // X / dZ1 operand (hi, lo)
-    const int xbytes = align1k(2 * 2 * 128 * (Dp > H1 ? Dp : H1));
-    uint8_t* sa = sx + xbytes;                                // A1 / dZ2 operand (hi, lo)
-    const int ab = 2 * 128 * (H1 > H2 ? H1 : H2);             // bytes of one (hi or lo) activation image
-    const float* fv = reinterpret_cast<const float*>(sw + L.fvec);
+    const int row = tid & 127;
+    const int nl = L.nl, Dp = L.Dp;
+    // shared memory: staged [image | act]; streamed [FP32 vectors | one operand | act]
+    uint8_t* sw = smem;
+    uint8_t* swb = smem + (L.staged ? 0 : align1k(4 * L.nvec));  // per-GEMM operand (streamed)
+    uint8_t* sact = smem + (L.staged ? L.bytes : align1k(4 * L.nvec) + L.wimg);
+    const float* fv = reinterpret_cast<const float*>(L.staged ? sw + L.fvec : sw);
+    const int half = 2 * 128 * L.Wmax;  // bytes of the hi (or lo) activation image
+    uint8_t* sact_lo = sact + half;
 
     if (tid == 0) {
         s_tstart[0] = 0;
         for (int t = 0; t < p.nt; ++t)
             s_tstart[t + 1] = s_tstart[t] + (p.range[p.t0 + t + 1] - p.range[p.t0 + t] + 127) / 128;
-    }
-    if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -174,15 +228,30 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
     const uint32_t mb = smem_u32(&mbar);
     uint32_t phase = 0;
     bool ok = true;
+    const uint32_t ah = smem_u32(sact), al = ah + half;
 
-    const uint32_t w1h = smem_u32(sw + L.w1), w1l = w1h + 2 * H1 * Dp;
-    const uint32_t w2h = smem_u32(sw + L.w2), w2l = w2h + 2 * H2 * H1;
-    const uint32_t w2th = smem_u32(sw + L.w2t), w2tl = w2th + 2 * H1 * H2;
-    const uint32_t w1th = smem_u32(sw + L.w1t), w1tl = w1th + 2 * Dp * H1;
-    const uint32_t xh = smem_u32(sx), xl = xh + 2 * 128 * (Dp > H1 ? Dp : H1);
-    const uint32_t ah = smem_u32(sa), al = ah + ab;
-    uint8_t* sx_lo = sx + 2 * 128 * (Dp > H1 ? Dp : H1);
-    uint8_t* sa_lo = sa + ab;
+    // one GEMM: D (TMEM column dcol) = act [128 x K] * B [N x K]^T, B the image at byte
+    // offset boff of the species image (staged) or copied from global first (streamed)
+    auto gemm = [&](int ts, int boff, int N, int K, int dcol) -> bool {
+        uint32_t bh;
+        if (L.staged) {
+            bh = smem_u32(sw + boff);
+        } else {
+            copy16(swb, p.img[ts] + boff, 4 * N * K, tid, NT);
+            bh = smem_u32(swb);
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            fence_after();
+            issue_gemm(tbase + dcol, ah, al, bh, bh + 2 * N * K, K, N);
+            mma_commit(mb);
+        }
+        const bool done = __syncthreads_and(mbar_wait(mb, phase));
+        phase ^= 1;
+        if (done) fence_after();
+        return done;
+    };
 
     const int total = s_tstart[p.nt];
     int staged = -1;
@@ -190,17 +259,15 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
         int ts = 0;
         while (gt >= s_tstart[ts + 1]) ++ts;
         const int tile = gt - s_tstart[ts];
-        if (ts != staged) {  // stage this species' weight image (no MMA is in flight here)
+        if (ts != staged) {  // stage this species' image or FP32 vectors (no MMA is in flight here)
             __syncthreads();
-            const uint4* src = reinterpret_cast<const uint4*>(p.img[ts]);
-            uint4* dst = reinterpret_cast<uint4*>(sw);
-            for (int q = tid; q < L.bytes / 16; q += (128 * SPLIT)) dst[q] = src[q];
+            if (L.staged) copy16(sw, p.img[ts], L.bytes, tid, NT);
+            else copy16(sw, p.img[ts] + L.fvec, 4 * L.nvec, tid, NT);
             fence_async_smem();
             __syncthreads();
             staged = ts;
         }
         const int s0 = p.range[p.t0 + ts], s1 = p.range[p.t0 + ts + 1];
-        const int row = tid & 127;
         const int slot = s0 + tile * 128 + row;
         const bool valid = slot < s1;
         // ---- X = (fp - mu) / sigma, split into hi / lo.  Warp-cooperative: the lanes of a
@@ -234,137 +301,114 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
                         v[q] = k < p.D ? (v[q] - fv[L.fmu + k]) * fv[L.fisig + k] : 0.f;
                     }
                 }
-                store_split8(sx, sx_lo, r, k0, Dp, v);
+                store_split8(sact, sact_lo, r, k0, Dp, v);
             }
         }
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            issue_gemm(tbase + L.z1, xh, xl, w1h, w1l, Dp, H1);
-            mma_commit(mb);
-        }
-        ok = __syncthreads_and(mbar_wait(mb, phase));
-        phase ^= 1;
-        if (!ok) break;
-        fence_after();
-        // ---- A1 = silu(Z1 + b1)
-        for (int c0 = 16 * part; c0 < H1; c0 += 16 * SPLIT) {
-            float z[16];
-            tmem_ld16(tlane + L.z1 + c0, z);
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const float zz = z[q] + fv[L.fb1 + c0 + q];
-                z[q] = zz * sigmoidf_(zz);
-            }
-            store_split8(sa, sa_lo, row, c0, H1, z);
-            store_split8(sa, sa_lo, row, c0 + 8, H1, z + 8);
-        }
-        fence_before();
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            issue_gemm(tbase + L.z2, ah, al, w2h, w2l, H1, H2);
-            mma_commit(mb);
-        }
-        ok = __syncthreads_and(mbar_wait(mb, phase));
-        phase ^= 1;
-        if (!ok) break;
-        fence_after();
-        // ---- energy and dZ2 = sigma_E w_o silu'(Z2 + b2)
+        // ---- forward through the hidden layers
         const float se = (float)p.sigma_e[ts];
         float e = 0.f;
-        for (int c0 = 16 * part; c0 < H2; c0 += 16 * SPLIT) {
-            float z[16];
-            tmem_ld16(tlane + L.z2 + c0, z);
+        for (int l = 0; l < nl && ok; ++l) {
+            const int H = L.Hp[l];
+            ok = gemm(ts, L.wf[l], H, L.K[l], L.z[l]);
+            if (!ok) break;
+            const float* b = fv + L.fb[l];
+            const bool last = l == nl - 1;
+            for (int c0 = 16 * part; c0 < H; c0 += 16 * SPLIT) {
+                float z[16];
+                tmem_ld16(tlane + L.z[l] + c0, z);
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const float zz = z[q] + fv[L.fb2 + c0 + q];
-                const float s = sigmoidf_(zz);
-                const float wo = fv[L.fwo + c0 + q];
-                e += wo * (zz * s);
-                z[q] = se * wo * (s * (1.f + zz * (1.f - s)));
-            }
-            store_split8(sa, sa_lo, row, c0, H2, z);
-            store_split8(sa, sa_lo, row, c0 + 8, H2, z + 8);
-        }
-        s_e[part][row] = e;
-        fence_before();
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            issue_gemm(tbase + L.da1, ah, al, w2th, w2tl, H2, H1);
-            mma_commit(mb);
-        }
-        ok = __syncthreads_and(mbar_wait(mb, phase));
-        phase ^= 1;
-        if (!ok) break;
-        fence_after();
-        if (part == 0 && valid) {  // energy: the four column shares added in a fixed order
-            float e = s_e[0][row];
-#pragma unroll
-            for (int q = 1; q < SPLIT; ++q) e += s_e[q][row];
-            p.e_atom[p.perm[slot]] = ((double)e + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
-        }
-        // ---- dZ1 = dA1 * silu'(Z1 + b1)
-        for (int c0 = 16 * part; c0 < H1; c0 += 16 * SPLIT) {
-            float g[16], z[16];
-            tmem_ld16(tlane + L.da1 + c0, g);
-            tmem_ld16(tlane + L.z1 + c0, z);
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const float zz = z[q] + fv[L.fb1 + c0 + q];
-                const float s = sigmoidf_(zz);
-                g[q] *= s * (1.f + zz * (1.f - s));
-            }
-            store_split8(sx, sx_lo, row, c0, H1, g);
-            store_split8(sx, sx_lo, row, c0 + 8, H1, g + 8);
-        }
-        fence_before();
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            fence_after();
-            issue_gemm(tbase + L.dx, xh, xl, w1th, w1tl, H1, Dp);
-            mma_commit(mb);
-        }
-        ok = __syncthreads_and(mbar_wait(mb, phase));
-        phase ^= 1;
-        if (!ok) break;
-        fence_after();
-        // ---- dE/dfp = dX / sigma.  Staged in shared memory over the X and A operand areas
-        // (free once GEMM 4 has completed; rows padded to Dp + 4 floats against bank
-        // conflicts), then written row by row with coalesced float4 stores
-        {
-            const int Dps = Dp + 4;
-            float* sg = reinterpret_cast<float*>(sx);  // [128][Dps]
-            for (int c0 = 16 * part; c0 < Dp; c0 += 16 * SPLIT) {
-                float g[16];
-                tmem_ld16(tlane + L.dx + c0, g);
-                float4* o = reinterpret_cast<float4*>(sg + (size_t)row * Dps + c0);
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    o[q] = make_float4(g[4 * q] * fv[L.fisig + c0 + 4 * q], g[4 * q + 1] * fv[L.fisig + c0 + 4 * q + 1],
-                                       g[4 * q + 2] * fv[L.fisig + c0 + 4 * q + 2],
-                                       g[4 * q + 3] * fv[L.fisig + c0 + 4 * q + 3]);
-            }
-            __syncthreads();
-            for (int r = warp; r < 128; r += 4 * SPLIT) {
-                const int sl = s0 + tile * 128 + r;
-                if (sl >= s1) continue;  // uniform across the warp
-                float* gr = p.gfp + (size_t)sl * p.fp_stride;
-                const float* src = sg + (size_t)r * Dps;
-                for (int k = 4 * lane; k < p.D; k += 128) {
-                    const float4 v = *reinterpret_cast<const float4*>(src + k);
-                    if (k + 4 <= p.D) {
-                        *reinterpret_cast<float4*>(gr + k) = v;
+                for (int q = 0; q < 16; ++q) {
+                    const float zz = z[q] + b[c0 + q];
+                    const float s = sigmoidf_(zz);
+                    if (last) {  // energy share and dZ_L = sigma_E w_o silu'(Z_L)
+                        const float wo = fv[L.fwo + c0 + q];
+                        e += wo * (zz * s);
+                        z[q] = se * wo * (s * (1.f + zz * (1.f - s)));
                     } else {
-                        const float w[4] = {v.x, v.y, v.z, v.w};
-                        for (int q = 0; k + q < p.D; ++q) gr[k + q] = w[q];
+                        z[q] = zz * s;
                     }
                 }
+                store_split8(sact, sact_lo, row, c0, H, z);
+                store_split8(sact, sact_lo, row, c0 + 8, H, z + 8);
+            }
+            fence_before();
+        }
+        if (!ok) break;
+        s_e[part][row] = e;
+        // ---- backward: dA_{l-1} = dZ_l W_l; dZ_{l-1} = dA_{l-1} silu'(Z_{l-1})
+        for (int l = nl - 1; l >= 1 && ok; --l) {
+            ok = gemm(ts, L.wb[l], L.K[l], L.Hp[l], L.dacc);
+            if (!ok) break;
+            if (l == nl - 1 && part == 0 && valid) {  // energy: the column shares added in a fixed order
+                float et = s_e[0][row];
+#pragma unroll
+                for (int q = 1; q < SPLIT; ++q) et += s_e[q][row];
+                p.e_atom[p.perm[slot]] = ((double)et + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
+            }
+            const int H = L.Hp[l - 1];
+            const float* b = fv + L.fb[l - 1];
+            for (int c0 = 16 * part; c0 < H; c0 += 16 * SPLIT) {
+                float g[16], z[16];
+                tmem_ld16(tlane + L.dacc + c0, g);
+                tmem_ld16(tlane + L.z[l - 1] + c0, z);
+#pragma unroll
+                for (int q = 0; q < 16; ++q) {
+                    const float zz = z[q] + b[c0 + q];
+                    const float s = sigmoidf_(zz);
+                    g[q] *= s * (1.f + zz * (1.f - s));
+                }
+                store_split8(sact, sact_lo, row, c0, H, g);
+                store_split8(sact, sact_lo, row, c0 + 8, H, g + 8);
+            }
+            fence_before();
+        }
+        if (!ok) break;
+        // ---- dX = dZ_1 W_1
+        ok = gemm(ts, L.wb[0], Dp, L.Hp[0], L.dacc);
+        if (!ok) break;
+        if (nl == 1 && part == 0 && valid) {
+            float et = s_e[0][row];
+#pragma unroll
+            for (int q = 1; q < SPLIT; ++q) et += s_e[q][row];
+            p.e_atom[p.perm[slot]] = ((double)et + (double)p.bo[ts]) * p.sigma_e[ts] + p.mu_e[ts];
+        }
+        // ---- dE/dfp = dX / sigma, staged through the (now free) operand buffer kOutCols
+        // columns at a time (rows padded by 4 floats against bank conflicts) and written
+        // row by row with coalesced stores
+        {
+            constexpr int CS = kOutCols + 4;
+            float* sg = reinterpret_cast<float*>(sact);  // [128][CS]
+            for (int cb = 0; cb < Dp; cb += kOutCols) {
+                const int cw = Dp - cb < kOutCols ? Dp - cb : kOutCols;
+                for (int c0 = 16 * part; c0 < cw; c0 += 16 * SPLIT) {
+                    float g[16];
+                    tmem_ld16(tlane + L.dacc + cb + c0, g);
+                    float4* o = reinterpret_cast<float4*>(sg + (size_t)row * CS + c0);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        o[q] = make_float4(g[4 * q] * fv[L.fisig + cb + c0 + 4 * q],
+                                           g[4 * q + 1] * fv[L.fisig + cb + c0 + 4 * q + 1],
+                                           g[4 * q + 2] * fv[L.fisig + cb + c0 + 4 * q + 2],
+                                           g[4 * q + 3] * fv[L.fisig + cb + c0 + 4 * q + 3]);
+                }
+                __syncthreads();
+                const int lim = p.D - cb < cw ? p.D - cb : cw;  // columns of this pass that exist
+                for (int r = warp; r < 128; r += 4 * SPLIT) {
+                    const int sl = s0 + tile * 128 + r;
+                    if (sl >= s1 || lim <= 0) continue;  // uniform across the warp
+                    float* gr = p.gfp + (size_t)sl * p.fp_stride + cb;
+                    const float* src = sg + (size_t)r * CS;
+                    for (int k = 4 * lane; k < lim; k += 128) {
+                        const float4 v = *reinterpret_cast<const float4*>(src + k);
+                        if (k + 4 <= lim) {
+                            *reinterpret_cast<float4*>(gr + k) = v;
+                        } else {
+                            const float w[4] = {v.x, v.y, v.z, v.w};
+                            for (int q = 0; k + q < lim; ++q) gr[k + q] = w[q];
+                        }
+                    }
+                }
+                __syncthreads();
             }
         }
         fence_before();
@@ -382,45 +426,40 @@ __global__ void __launch_bounds__(128 * SPLIT, 1) k_net_tc(TcParams p, TCLayout 
 
 bool net_tc_prepare(const Species& sp, NetTC& tc, std::string& why) {
     tc.ready = false;
-    if (sp.hidden.size() != 2) {
-        why = "the tensor-core network needs exactly two hidden layers";
-        return false;
-    }
-    const int D = sp.D, H1 = sp.hidden[0], H2 = sp.hidden[1];
-    if (D > 128 || H1 % 16 || H2 % 16 || H1 > 128 || H2 > 128 || H1 < 16 || H2 < 16) {
-        why = "the tensor-core network needs D <= 128 and hidden widths that are multiples of 16 up to 128";
-        return false;
-    }
-    const TCLayout L = make_layout(D, H1, H2);
+    const int D = sp.D;
+    TCLayout L;
+    if (!make_layout(D, sp.hidden, L, why)) return false;
     std::vector<uint8_t> img(L.bytes, 0);
-    const int Dp = L.Dp;
-    auto W1 = [&](int o, int i) { return i < D ? sp.Wh[0][(size_t)o * D + i] : 0.0; };
-    auto W2 = [&](int o, int i) { return sp.Wh[1][(size_t)o * H1 + i]; };
-    put_operand(img, L.w1, H1, Dp, [&](int r, int k) { return W1(r, k); });         // GEMM1 B: [H1][Dp]
-    put_operand(img, L.w2, H2, H1, [&](int r, int k) { return W2(r, k); });         // GEMM2 B: [H2][H1]
-    put_operand(img, L.w2t, H1, H2, [&](int r, int k) { return W2(k, r); });        // GEMM3 B: [H1][H2]
-    put_operand(img, L.w1t, Dp, H1, [&](int r, int k) { return W1(k, r); });        // GEMM4 B: [Dp][H1]
+    int in = D;
+    for (int l = 0; l < L.nl; ++l) {
+        const int H = sp.hidden[l], Hp = L.Hp[l], K = L.K[l];
+        const std::vector<double>& W = sp.Wh[l];  // [H][in]
+        auto Wf = [&](int o, int i) { return o < H && i < in ? W[(size_t)o * in + i] : 0.0; };
+        put_operand(img, L.wf[l], Hp, K, [&](int r, int k) { return Wf(r, k); });  // [Hp][K]
+        put_operand(img, L.wb[l], K, Hp, [&](int r, int k) { return Wf(k, r); });  // [K][Hp]
+        in = H;
+    }
     float* fv = reinterpret_cast<float*>(img.data() + L.fvec);
-    for (int k = 0; k < Dp; ++k) {
+    for (int k = 0; k < L.Dp; ++k) {
         fv[L.fmu + k] = k < D ? (float)sp.mu[k] : 0.f;
         fv[L.fisig + k] = k < D ? (float)(1.0 / sp.sigma[k]) : 0.f;
     }
-    for (int o = 0; o < H1; ++o) fv[L.fb1 + o] = (float)sp.bh[0][o];
-    for (int o = 0; o < H2; ++o) fv[L.fb2 + o] = (float)sp.bh[1][o];
-    for (int o = 0; o < H2; ++o) fv[L.fwo + o] = (float)sp.wo[o];
+    for (int l = 0; l < L.nl; ++l)
+        for (int o = 0; o < sp.hidden[l]; ++o) fv[L.fb[l] + o] = (float)sp.bh[l][o];
+    for (int o = 0; o < sp.hidden.back(); ++o) fv[L.fwo + o] = (float)sp.wo[o];
     if (cudaMalloc(&tc.blob, img.size()) != cudaSuccess) {
+        cudaGetLastError();
         why = "device allocation failed";
         return false;
     }
     if (cudaMemcpy(tc.blob, img.data(), img.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
         why = "copy of the network image failed";
         return false;
     }
     tc.blob_bytes = img.size();
     tc.D = D;
-    tc.Dp = Dp;
-    tc.H1 = H1;
-    tc.H2 = H2;
+    tc.L = L;
     tc.bo = (float)sp.bo;
     tc.ready = true;
     return true;
@@ -437,23 +476,21 @@ cudaError_t launch_net_tc(const NetArgs* a, const NetTC* const* tc, int nt, int*
     if (nt < 1 || nt > kMaxTypes) return cudaErrorInvalidValue;
     for (int k = 0; k < nt; ++k) {
         if (!tc[k]->ready) return cudaErrorNotSupported;
-        if (tc[k]->D != tc[0]->D || tc[k]->H1 != tc[0]->H1 || tc[k]->H2 != tc[0]->H2) return cudaErrorInvalidValue;
+        if (tc[k]->D != tc[0]->D || !tc[k]->L.same(tc[0]->L)) return cudaErrorInvalidValue;
     }
     const int n = a[0].nmax;
     if (n <= 0) return cudaSuccess;
-    const TCLayout L = make_layout(tc[0]->D, tc[0]->H1, tc[0]->H2);
-    const int xbytes = align1k(2 * 2 * 128 * (L.Dp > L.H1 ? L.Dp : L.H1));
-    const int abytes = align1k(2 * 2 * 128 * (L.H1 > L.H2 ? L.H1 : L.H2));
-    const size_t sm = (size_t)L.bytes + xbytes + abytes;
+    const TCLayout& L = tc[0]->L;
+    const size_t sm = (size_t)L.smem;
     if (split != 2 && split != 4) return cudaErrorInvalidValue;
     static int limit2 = 0, limit4 = 0;  // raised once per instantiation, before any graph capture
     int& limit = split == 2 ? limit2 : limit4;
     if ((int)sm > limit) {
         const cudaError_t e =
-            split == 2 ? cudaFuncSetAttribute(k_net_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)
-                       : cudaFuncSetAttribute(k_net_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            split == 2 ? cudaFuncSetAttribute(k_net_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax)
+                       : cudaFuncSetAttribute(k_net_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmemMax);
         if (e != cudaSuccess) return e;
-        limit = (int)sm;
+        limit = kTcSmemMax;
     }
     TcParams p;
     std::memset(&p, 0, sizeof p);

@@ -68,7 +68,7 @@ void upload_model(nnap_handle* h) {
             const SubShape& s = r.subs[k];
             if (!desc_supported(s.kind, s.basis, s.lmax, s.np, s.n1)) {
                 char buf[160];
-                std::snprintf(buf, sizeof buf, "no compiled descriptor kernel for %s kind=%d lmax=%d np=%d nmax=%d",
+                std::snprintf(buf, sizeof buf, "descriptor shape beyond shared memory: %s kind=%d lmax=%d np=%d nmax=%d",
                               s.basis == kRbNEP ? "NEP" : "NNAP", s.kind, s.lmax, s.np, s.n1 - 1);
                 throw ApiFail(NNAP_ERR_UNSUPPORTED, buf);
             }
@@ -195,13 +195,13 @@ void upload_model(nnap_handle* h) {
     for (int t = 0; t < T; ++t) {
         const Species& sp = m.sp[t];
         NetDev& nd = h->nets[t];
-        if (sp.hidden.size() > 4) throw ApiFail(NNAP_ERR_UNSUPPORTED, "more than 4 hidden layers");
+        if (sp.hidden.size() > (size_t)kNetMaxLayers) throw ApiFail(NNAP_ERR_UNSUPPORTED, "more than 16 hidden layers");
         nd.D = sp.D;
         nd.nlayer = (int)sp.hidden.size();
-        for (int l = 0; l < nd.nlayer; ++l) {
-            nd.H[l] = sp.hidden[l];
-            if (sp.hidden[l] > 256) throw ApiFail(NNAP_ERR_UNSUPPORTED, "hidden width above 256");
-        }
+        for (int l = 0; l < nd.nlayer; ++l) nd.H[l] = sp.hidden[l];
+        if (!net_fp32_fits(nd.D, nd.nlayer, nd.H))
+            throw ApiFail(NNAP_ERR_UNSUPPORTED, "network too wide for shared memory ((2 + layers) x widest layer "
+                                                "above 7264)");
         nd.mu_e = sp.mu_e;
         nd.sigma_e = sp.sigma_e;
         nd.act = m.act ? kActTanh : kActSiLU;
@@ -222,8 +222,13 @@ void upload_model(nnap_handle* h) {
         nd.w32.ensure(w.size());
         CK(cudaMemcpy(nd.w32.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
         if (h->net_tc) {
+            // a network outside the tensor-core kernel's limits (widths above 256, more than
+            // 8 layers, operands beyond shared memory or TMEM) runs the FP32 kernel
             std::string why;
-            if (!net_tc_prepare(sp, nd.tc, why)) throw ApiFail(NNAP_ERR_UNSUPPORTED, why);
+            if (!net_tc_prepare(sp, nd.tc, why)) {
+                net_tc_release(nd.tc);
+                h->net_notes += sp.symbol + ": " + why + "; ";
+            }
         }
     }
 }
@@ -664,24 +669,25 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
             a.fp_stride = h->fp_stride;
             a.D = nd.D;
             a.nlayer = nd.nlayer;
-            for (int l = 0; l < 4; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;
+            for (int l = 0; l < kNetMaxLayers; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;
             a.w = nd.w32.p;
             a.mu_e = nd.mu_e;
             a.sigma_e = nd.sigma_e;
             a.e_atom = h->e_atom.p;
             a.gfp = h->gfp.p;
             a.act = nd.act;
-            if (!h->net_tc) {
+            if (!(h->net_tc && nd.tc.ready)) {
                 CK(launch_net_fp32(a, st));
                 ++h->launches;
             }
         }
         if (h->net_tc) {
-            // one launch per run of consecutive species with the same network shape
+            // one launch per run of consecutive tensor-core species with the same network layout
             for (int t = 0; t < T;) {
-                int u = t + 1;
                 const NetTC& a0 = h->nets[t].tc;
-                while (u < T && h->nets[u].tc.D == a0.D && h->nets[u].tc.H1 == a0.H1 && h->nets[u].tc.H2 == a0.H2) ++u;
+                if (!a0.ready) { ++t; continue; }
+                int u = t + 1;
+                while (u < T && h->nets[u].tc.ready && h->nets[u].tc.D == a0.D && h->nets[u].tc.L.same(a0.L)) ++u;
                 const NetTC* tcs[kMaxTypes];
                 for (int k = t; k < u; ++k) tcs[k - t] = &h->nets[k].tc;
                 CK(launch_net_tc(&args[t], tcs, u - t, h->status.p, h->sm_count, h->tune.net_split, st));
@@ -975,6 +981,7 @@ static int create_handle(Model&& model, int precision, int device, nnap_handle**
         CK(cudaMallocHost(&h->h_status, sizeof(int) * (3 + kMaxTypes)));
         CK(upload_sh_constants());
         CK(upload_sh_constants_train());
+        CK(upload_sh_constants_gen());
         upload_model(h.get());
     } catch (const ApiFail& e) {
         std::fprintf(stderr, "nnap_create: %s\n", e.what());

@@ -226,7 +226,7 @@ void train_enqueue(nnap_handle* h, const Batch& B, const double* bE, const doubl
         a.fp_stride = h->fp_stride;
         a.D = nd.D;
         a.nlayer = nd.nlayer;
-        for (int l = 0; l < 4; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;
+        for (int l = 0; l < 4; ++l) a.H[l] = l < nd.nlayer ? nd.H[l] : 0;  // at most 4 (checked at entry)
         a.w = nd.w32.p;
         a.sigma_e = (float)nd.sigma_e;
         a.bE = dbE;
@@ -417,6 +417,13 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         if (!grad_nn) throw ApiFail(NNAP_ERR_ARG, "grad_nn is NULL");
         const Model& m = h->model;
         if (m.radial_fn || m.act) throw ApiFail(NNAP_ERR_UNSUPPORTED, "training gradients are computed for NNAP models only");
+        for (auto& r : h->runs)
+            for (auto& sh : r.subs)
+                if (!desc_compiled(sh.kind, sh.basis, sh.lmax, sh.np, sh.n1))
+                    throw ApiFail(NNAP_ERR_UNSUPPORTED, "training gradients are compiled for the shapes of "
+                                                        "NNAP_RADIAL_SHAPES / NNAP_SPH_SHAPES only");
+        for (auto& sp : m.sp)
+            if (sp.hidden.size() > 4) throw ApiFail(NNAP_ERR_UNSUPPORTED, "training gradients take at most 4 hidden layers");
         const int T = m.ntypes();
         const bool want_w = grad_fp && any_fused(m);
         h->launches = 0;

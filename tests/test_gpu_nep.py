@@ -121,16 +121,6 @@ def test_nep_training_is_rejected():
             p.backwardEnergyForceBatch([s], np.ones(s.natoms), np.zeros((s.natoms, 3)), np.zeros((1, 9)))
 
 
-def test_nep_uncompiled_shape_is_unsupported():
-    from jse_gb300.nep import NEP
-    from jse_gb300.nnap import NNAP_ERR_UNSUPPORTED, NNAPError
-    from oracle import nep_model as NM
-    text = NM.write(["A"], n_max=(3, 3), basis=(5, 5), neurons=4, seed=1)
-    with pytest.raises(NNAPError) as e:
-        NEP(text)
-    assert e.value.status == NNAP_ERR_UNSUPPORTED
-
-
 def test_reference_cuda_nep_matches():
     """The reference's own CUDA NEP (nep_interface_cuda.cu, oracle/nep_ref_cuda.py) on the
     LAMMPS form of a fixture structure: it and this build's LAMMPS boundary both agree with

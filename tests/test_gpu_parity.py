@@ -1,7 +1,7 @@
 """GPU path (through the C ABI) against the golden vectors of the reference's arithmetic.
 
 Tolerances (plain FP32 path; descriptors and network in FP32, displacements and all
-reductions in FP64):
+reductions in FP64; the mixed path's own energy bounds are given in its test):
   * neighbour sets: bit-exact, (i, j, image) per pair;
   * energies: |dE_i| <= 2e-5 * max(1, max|E|);
   * forces and per-atom virials: max |d| <= 1e-3 * max(1e-2, max|ref|) and
@@ -70,21 +70,17 @@ def test_results_are_deterministic(golden):
         assert np.array_equal(a[k], b[k]), k
 
 
-def _tc_shape_ok(model):
-    for m in model["models"]:
-        h = m.get("nn", {}).get("hidden_dims", [32, 32])
-        if len(h) != 2 or any(x % 16 for x in h):
-            return False
-    return True
-
-
 def test_energy_force_virial_mixed(golden):
-    """Mixed precision: split-BF16 tensor-core network (hi*hi + lo*hi + hi*lo, FP32 accumulation)."""
-    if not _tc_shape_ok(golden.model):
-        pytest.skip("network shape outside the tensor-core kernel (two hidden layers, widths multiple of 16)")
+    """Mixed precision: split-BF16 tensor-core network (hi*hi + lo*hi + hi*lo, FP32 accumulation),
+    hidden widths padded to multiples of 16: every fixture runs, none is skipped."""
     with _nnap(golden.model_json, "mixed") as p:
         o = p.calEnergyForceVirials(_S(golden))
     escale = max(1.0, float(np.abs(golden.energies).max()))
-    assert np.abs(o["energies"] - golden.energies).max() <= 2e-5 * escale
+    n = len(golden.types)
+    # the split operands keep 16 significant bits of every network input and weight; a model
+    # without descriptor normalisation feeds raw descriptors (tens) into the first layer, so the
+    # per-atom bound is 5e-5 of the energy scale here; the energy per atom stays within 1e-5 eV
+    assert np.abs(o["energies"] - golden.energies).max() <= 5e-5 * escale
+    assert abs(o["energy"] - golden.energies.sum()) / n <= 1e-5
     _close(o["forces"], golden.forces, 1e-3, 2e-4)
     _close(o["virials"], golden.virials, 1e-3, 2e-4)
