@@ -2,7 +2,7 @@
  * nnap_gb300.h -- C ABI of the GB300-native NNAP energy/force/virial evaluator.
  *
  * The library replaces the per-structure evaluation path of jse's NNAP potential
- * (jsex.nnap.NNAP).  It reads the same JSON model files and returns the same
+ * (jsex.nnap.NNAP).  It reads the same JSON and YAML model files and returns the same
  * energies, forces and virials, computed on one GPU.  Plain pointers and sizes only;
  * every call returns an nnap_status (0 = success) and never throws.
  *
@@ -46,7 +46,7 @@ typedef enum {
     NNAP_ERR_BAD_TYPE = 2,     /* species outside 1..ntypes (NNAP.java:507)           */
     NNAP_ERR_CAPACITY = 3,     /* internal capacity exceeded and could not grow       */
     NNAP_ERR_CUDA = 4,         /* a CUDA runtime call failed; see nnap_last_error     */
-    NNAP_ERR_UNSUPPORTED = 5,  /* model shape without a compiled kernel               */
+    NNAP_ERR_UNSUPPORTED = 5,  /* model shape beyond the kernels' shared memory       */
     NNAP_ERR_ARG = 6,          /* invalid argument (null pointer, bad size, bad box)  */
     NNAP_ERR_TIMEOUT = 7,      /* a bounded device-side wait gave up                  */
     NNAP_ERR_DEAD = 8,         /* handle already destroyed                            */
@@ -70,12 +70,21 @@ enum {
     NNAP_WANT_VIRIALS = 16    /* per-atom virials (9n doubles)              */
 };
 
-/* Create a handle from model JSON text (the format read by NNAP(Map) /
- * NNAP(String path), NNAP.java:402-426; YAML is not accepted).  device is the CUDA
- * ordinal.  Replaces the NNAP constructor + JIT compile (NNAP.java:129-401, 446-470). */
+/* Create a handle from model text in the format read by NNAP(Map) / NNAP(String path)
+ * (NNAP.java:402-426): JSON, or YAML (the form IO.yaml2map reads for .yaml / .yml files,
+ * NNAP.java:407-411) for text that does not start with '{'.  device is the CUDA ordinal.
+ * Replaces the NNAP constructor + JIT compile (NNAP.java:129-401, 446-470).  Every shape
+ * the format allows is evaluated (nmax <= 20, lmax <= 12, any weight type, any hidden
+ * widths); NNAP_ERR_UNSUPPORTED only for shapes beyond shared memory. */
 int nnap_create(const char* model_json, size_t len, int precision, int device, nnap_handle** out);
-/* Same, reading the JSON text from a file (NNAP(String), NNAP.java:407-411). */
+/* Same, reading the JSON or YAML text from a file (NNAP(String), NNAP.java:407-411). */
 int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out);
+/* Parse and validate model text (JSON or YAML) without a GPU, as nnap_create does before
+ * any device work: NNAP_OK with the species count and a 64-bit digest of every value the
+ * kernels consume (equal digests: equal models), or NNAP_ERR_BAD_MODEL with the reason in
+ * err (errlen bytes, may be NULL).  No counterpart in the reference, whose loader runs
+ * inside the NNAP constructor (NNAP.java:129-307). */
+int nnap_model_check(const char* model_text, size_t len, int* ntypes, uint64_t* digest, char* err, size_t errlen);
 /* Create a handle from NEP potential text (nep.txt, the file read by NEP(String),
  * NEP.java:98-100 and 786-1010): potential models nep3, nep4 and nep5, with or without
  * ZBL (nepV_zbl, fixed or flexible) and with or without type-wise cutoffs; other

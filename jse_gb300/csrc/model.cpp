@@ -17,6 +17,7 @@
 #include <stdexcept>
 
 #include "json.hpp"
+#include "yaml.hpp"
 
 namespace nnapgb {
 namespace {
@@ -367,11 +368,30 @@ void load_network(Species& sp, const JValue* nnv) {
     if (const JValue* ob = m.get("output_bias")) sp.bo = ob->as_num();
 }
 
+// JSON text starts with '{' (a model file is an object); anything else is read as YAML
+// (NNAP.java:407-411 reads .yaml / .yml files with IO.yaml2map, IO.java:853).
+JValue parse_model_text(const char* text, size_t len) {
+    size_t k = 0;
+    while (k < len && (text[k] == ' ' || text[k] == '\t' || text[k] == '\n' || text[k] == '\r')) ++k;
+    if (k < len && text[k] == '{') {
+        try {
+            return JParser(text, len).parse();
+        } catch (const std::runtime_error& json_error) {
+            try {  // a YAML flow mapping (unquoted keys, comments) is not JSON
+                return YParser(text, len).parse();
+            } catch (const std::runtime_error&) {
+                throw json_error;
+            }
+        }
+    }
+    return YParser(text, len).parse();
+}
+
 }  // namespace
 
 Model load_model(const char* text, size_t len) {
-    JValue root = JParser(text, len).parse();
-    if (root.kind != JValue::OBJ) bad("model must be a JSON object");
+    JValue root = parse_model_text(text, len);
+    if (root.kind != JValue::OBJ) bad("model must be a JSON or YAML mapping");
     if (const JValue* v = root.get("version"))
         if (v->as_int() > 6) bad("unsupported model version");
     const JValue* models = root.get("models");
@@ -501,6 +521,40 @@ Model load_model(const char* text, size_t len) {
         }
     }
     return M;
+}
+
+// 64-bit FNV-1a over every value the kernels consume (basis shapes and matrices, network
+// weights, normalisation, cutoffs), in a fixed order: equal digests mean equal models.
+uint64_t model_digest(const Model& M) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void* p, size_t n) {
+        const unsigned char* c = static_cast<const unsigned char*>(p);
+        for (size_t k = 0; k < n; ++k) { h ^= c[k]; h *= 1099511628211ull; }
+    };
+    auto num = [&mix](double v) { mix(&v, sizeof v); };
+    auto vec = [&](const std::vector<double>& v) { num((double)v.size()); for (double x : v) num(x); };
+    num((double)M.ntypes());
+    num(M.rcut_max);
+    for (const Species& sp : M.sp) {
+        mix(sp.symbol.data(), sp.symbol.size());
+        num((double)sp.D);
+        for (const SubBasis& b : sp.subs) {
+            for (int v : {b.kind, b.nmax, b.lmax, b.np, b.nl2, b.l3max, b.l4max, b.fp_off, b.size}) num((double)v);
+            num(b.rcut);
+            vec(b.W);
+            vec(b.pair_rc);
+        }
+        for (int H : sp.hidden) num((double)H);
+        for (auto& w : sp.Wh) vec(w);
+        for (auto& b : sp.bh) vec(b);
+        vec(sp.wo);
+        num(sp.bo);
+        vec(sp.mu);
+        vec(sp.sigma);
+        num(sp.mu_e);
+        num(sp.sigma_e);
+    }
+    return h;
 }
 
 }  // namespace nnapgb

@@ -2,6 +2,7 @@
 // into the per-species blocks the GPU kernels consume.
 #pragma once
 
+#include <cstdint>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -66,8 +67,11 @@ struct Model {
     int ntypes() const { return (int)sp.size(); }
 };
 
-// Parse and pack; throws std::runtime_error with a message on invalid input.
+// Parse (JSON, or YAML for text that does not start with '{') and pack; throws
+// std::runtime_error with a message on invalid input.
 Model load_model(const char* text, size_t len);
+// FNV-1a digest of everything the kernels consume from a model.
+uint64_t model_digest(const Model& M);
 
 // A valid NEP file of a variant the GPU path does not evaluate (dipole, polarizability).
 struct NepUnsupported : std::runtime_error {

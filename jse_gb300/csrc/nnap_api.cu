@@ -1021,6 +1021,23 @@ int nnap_create(const char* model_json, size_t len, int precision, int device, n
     return create_handle(std::move(m), precision, device, out);
 }
 
+int nnap_model_check(const char* model_text, size_t len, int* ntypes, uint64_t* digest, char* err, size_t errlen) {
+    if (!model_text) return NNAP_ERR_ARG;
+    if (err && errlen) err[0] = 0;
+    try {
+        const Model m = load_model(model_text, len);
+        if (ntypes) *ntypes = m.ntypes();
+        if (digest) *digest = model_digest(m);
+        return NNAP_OK;
+    } catch (const std::exception& e) {
+        if (err && errlen) {
+            std::strncpy(err, e.what(), errlen - 1);
+            err[errlen - 1] = 0;
+        }
+        return NNAP_ERR_BAD_MODEL;
+    }
+}
+
 int nnap_create_from_file(const char* path, int precision, int device, nnap_handle** out) {
     std::string s;
     if (!path || !out || !read_file(path, s)) return NNAP_ERR_ARG;

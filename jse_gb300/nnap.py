@@ -70,6 +70,7 @@ def load_library(path: str = LIB_PATH):
     dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
     L.nnap_create.argtypes = [C.c_char_p, S, I, I, C.POINTER(P)]
     L.nnap_create_from_file.argtypes = [C.c_char_p, I, I, C.POINTER(P)]
+    L.nnap_model_check.argtypes = [C.c_char_p, S, ip, C.POINTER(C.c_uint64), C.c_char_p, S]
     L.nnap_destroy.argtypes = [P]
     L.nnap_ntypes.argtypes = [P, ip]
     L.nnap_rcut_max.argtypes = [P, dp]
@@ -124,6 +125,26 @@ def _unpack(data):
     return x, t, box, int(getattr(data, "box_kind", 0))
 
 
+def model_check(model) -> dict:
+    """Parse and validate model text (JSON or YAML), a dict or a model file without a GPU
+    (nnap_model_check): {"ntypes", "digest"}; raises NNAPError for an invalid model."""
+    L = load_library()
+    if isinstance(model, dict):
+        model = json.dumps(model)
+    if isinstance(model, str) and os.path.isfile(model):
+        with open(model, "rb") as f:
+            b = f.read()
+    else:
+        b = model.encode() if isinstance(model, str) else bytes(model)
+    nt = C.c_int()
+    dig = C.c_uint64()
+    err = C.create_string_buffer(512)
+    rc = L.nnap_model_check(b, len(b), C.byref(nt), C.byref(dig), err, 512)
+    if rc != NNAP_OK:
+        raise NNAPError(rc, err.value.decode(errors="replace"))
+    return {"ntypes": nt.value, "digest": dig.value}
+
+
 class NNAP:
     """GB300 NNAP potential.  ``model`` is a path to a JSON model file, JSON text or a dict."""
 
@@ -134,7 +155,7 @@ class NNAP:
         h = C.c_void_p()
         if isinstance(model, dict):
             model = json.dumps(model)
-        if isinstance(model, str) and not model.lstrip().startswith("{"):
+        if isinstance(model, str) and not model.lstrip().startswith("{") and os.path.isfile(model):
             rc = L.nnap_create_from_file(model.encode(), PREC[precision], device, C.byref(h))
         else:
             b = model.encode() if isinstance(model, str) else bytes(model)

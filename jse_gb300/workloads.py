@@ -111,27 +111,40 @@ def _rsa(n: int, box: np.ndarray, rmin: float, seed: int) -> np.ndarray:
     occ = np.full(ncell, -1, dtype=np.int32)   # accepted point of each cell
     tmp = np.full(ncell, -1, dtype=np.int32)   # first passing candidate of each cell, per batch
     frac = np.zeros((n, 3))
-    # stencil per axis; offsets whose cells are certainly farther apart than rmin still
-    # take part (the distance test rejects nothing there), which keeps the index simple
-    ax = [np.arange(-R[d], R[d] + 1) for d in range(3)]
+    # stencil: cell offsets whose cells can hold a point within rmin, the 27 nearest first.
+    # Points of cells o apart differ by at least max(|o_d| - 1, 0) / nc_d in direct
+    # coordinate d, and |x| >= s_min |f| for the box's smallest singular value s_min; an
+    # offset is left out only with a 1 % margin on that bound
+    s_min = math.sqrt(max(0.0, float(np.linalg.eigvalsh(box @ box.T)[0])))
+    g = np.stack(np.meshgrid(*[np.arange(-R[d], R[d] + 1) for d in range(3)], indexing="ij"), -1).reshape(-1, 3)
+    gap = np.maximum(np.abs(g) - 1, 0) / nc
+    keep = s_min * np.sqrt((gap * gap).sum(1)) < 1.01 * rmin
+    inner = np.abs(g).max(1) <= 1
+    offs = np.concatenate([g[inner], g[keep & ~inner]])
+    n_in = int(inner.sum())
+    centre = int(np.nonzero((offs == 0).all(1))[0][0])
     r2 = rmin * rmin
     target = max(4.0, vol / (4.0 / 3.0 * math.pi * rmin ** 3) / 16.0)
     placed, stalled, rate = 0, 0, 1.0
 
-    def stencil(c):
-        """Flat cell index [m, sa, sb, sc] of each stencil cell and the image shift along
-        each axis ([m, sa], [m, sb], [m, sc])."""
-        q = [c[:, d, None] + ax[d][None, :] for d in range(3)]
-        img = [np.floor_divide(q[d], nc[d]) for d in range(3)]
-        w = [(q[d] - img[d] * nc[d]).astype(np.int32) for d in range(3)]
-        fl = w[0][:, :, None, None] + np.int32(nc[0]) * (w[1][:, None, :, None] + np.int32(nc[1]) * w[2][:, None, None, :])
-        return fl, img
+    # per axis: the flat-index contribution of cell (c_d + o_d) mod nc_d, [nc_d][2 R_d + 1]
+    tab, stride = [], 1
+    for d in range(3):
+        q = np.arange(nc[d])[:, None] + np.arange(-R[d], R[d] + 1)[None, :]
+        tab.append(((q - np.floor_divide(q, nc[d]) * nc[d]) * stride).astype(np.int32))
+        stride *= int(nc[d])
+    oidx = offs + R  # column of each offset in the tables
 
-    def too_close(ci, ia, ib, ic, img, other_frac, mine):
-        df = other_frac - mine
-        df[:, 0] += img[0][ci, ia]
-        df[:, 1] += img[1][ci, ib]
-        df[:, 2] += img[2][ci, ic]
+    def stencil(c, o_rows):
+        """Flat cell index [m, len(o_rows)] of the stencil cells (rows of offs) of each
+        candidate cell."""
+        return (tab[0][c[:, 0, None], oidx[None, o_rows, 0]] + tab[1][c[:, 1, None], oidx[None, o_rows, 1]] +
+                tab[2][c[:, 2, None], oidx[None, o_rows, 2]])
+
+    def too_close(cc, oo, other_frac, mine):
+        """Distances of the point pairs (candidate cell cc, stencil offset oo) below rmin."""
+        q = cc + oo
+        df = other_frac - mine + np.floor_divide(q, nc)
         v = _to_cart(df, box)
         return v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2] < r2
 
@@ -139,35 +152,32 @@ def _rsa(n: int, box: np.ndarray, rmin: float, seed: int) -> np.ndarray:
         nb = int(min(max(16.0, target / rate), 65536))
         s = rng.random((nb, 3))
         c = np.minimum((s * nc).astype(np.int64), nc - 1)
-        fl, img = stencil(c)
         ok = np.ones(nb, dtype=bool)
         # the 27 nearest cells first: they reject most candidates; then the rest of the
         # stencil for the candidates still standing
-        o = occ[fl[:, R[0] - 1:R[0] + 2, R[1] - 1:R[1] + 2, R[2] - 1:R[2] + 2]]
-        ci, ia, ib, ic = np.nonzero(o >= 0)
-        if len(ci):
-            bad = too_close(ci, ia + R[0] - 1, ib + R[1] - 1, ic + R[2] - 1, img, frac[o[ci, ia, ib, ic]], s[ci])
-            ok[ci[bad]] = False
-        live = np.nonzero(ok)[0]
-        o = occ[fl[live]]
-        o[:, R[0] - 1:R[0] + 2, R[1] - 1:R[1] + 2, R[2] - 1:R[2] + 2] = -1
-        ci, ia, ib, ic = np.nonzero(o >= 0)
-        if len(ci):
-            bad = too_close(live[ci], ia, ib, ic, img, frac[o[ci, ia, ib, ic]], s[live[ci]])
-            ok[live[ci[bad]]] = False
+        for lo, hi in ((0, n_in), (n_in, len(offs))):
+            live = np.nonzero(ok)[0]
+            if hi == lo or len(live) == 0:
+                continue
+            o = occ[stencil(c[live], np.arange(lo, hi))]
+            ci, oi = np.nonzero(o >= 0)
+            if len(ci):
+                bad = too_close(c[live[ci]], offs[lo + oi], frac[o[ci, oi]], s[live[ci]])
+                ok[live[ci[bad]]] = False
         # conflicts with earlier passing candidates of the same batch
         cand = np.nonzero(ok)[0]
         if len(cand) > 1:
-            fc = fl[cand, R[0], R[1], R[2]]
+            fl = stencil(c[cand], np.arange(len(offs)))
+            fc = fl[:, centre]
             # the first candidate of each cell claims it (assignments in reverse order leave
             # the earliest); later ones in that cell are too close
             tmp[fc[::-1]] = cand[::-1].astype(np.int32)
             reject = tmp[fc] != cand
-            o2 = tmp[fl[cand]]
-            m = (o2 >= 0) & (o2 < cand[:, None, None, None])
-            ci, ia, ib, ic = np.nonzero(m)
+            o2 = tmp[fl]
+            m = (o2 >= 0) & (o2 < cand[:, None])
+            ci, oi = np.nonzero(m)
             if len(ci):
-                bad = too_close(ci, ia, ib, ic, [g[cand] for g in img], s[o2[ci, ia, ib, ic]], s[cand[ci]])
+                bad = too_close(c[cand[ci]], offs[oi], s[o2[ci, oi]], s[cand[ci]])
                 reject[ci[bad]] = True
             tmp[fc] = -1
             ok[cand[reject]] = False
@@ -180,7 +190,7 @@ def _rsa(n: int, box: np.ndarray, rmin: float, seed: int) -> np.ndarray:
             continue
         stalled = 0
         frac[placed:placed + len(acc)] = s[acc]
-        occ[fl[acc, R[0], R[1], R[2]]] = np.arange(placed, placed + len(acc))
+        occ[stencil(c[acc], np.array([centre]))[:, 0]] = np.arange(placed, placed + len(acc))
         placed += len(acc)
     return _to_cart(frac, box)
 

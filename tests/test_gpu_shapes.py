@@ -106,3 +106,17 @@ def test_nep_shapes(path):
     assert np.max(np.abs(df)) <= 1e-3
     assert np.sqrt(np.mean(df ** 2)) <= 1e-4
     assert np.max(np.abs(out["virials"] - z["virials"])) <= 2e-3
+
+
+def test_yaml_model_evaluates_like_json(tmp_path):
+    """A model file written as YAML (NNAP.java:407-411) gives the JSON model's results bitwise."""
+    from jse_gb300.nnap import NNAP
+    from tests.yaml_emit import dump
+    c = ShapeCase([p for p in NNAP_SHAPES if p.endswith("default_model_t2.npz")][0])
+    path = tmp_path / "model.yml"
+    path.write_text(dump(c.model))
+    for precision in ("fp32", "mixed"):
+        with NNAP(c.model_json, precision=precision) as a, NNAP(str(path), precision=precision) as b:
+            ra, rb = a.calEnergyForceVirials(_S(c)), b.calEnergyForceVirials(_S(c))
+        for k in ("energies", "forces", "virials"):
+            assert np.array_equal(ra[k], rb[k]), (precision, k)
