@@ -187,7 +187,7 @@ struct nnap_handle {
     nnapgb::DevBuf<uint16_t> pgrp;
     nnapgb::DevBuf<nnapgb::StructDev> sdev;
     nnapgb::DevBuf<uint64_t> pkey;
-    nnapgb::DevBuf<float4> pdx, pg;
+    nnapgb::DevBuf<float4> pdx, pg, pdxlo;  // pdxlo: low parts of the displacements (ZBL models)
     nnapgb::DevBuf<int> prev, pcount;
     nnapgb::DevBuf<float> fp, gfp, A, Gx;  // Gx: invariant-column part of dE/dA (when present)
     nnapgb::DevBuf<double> zbl_z, zbl_zp, zbl_para, zbl_rc;  // NEP ZBL: per species Z, Z^0.23; flexible parameters

@@ -53,6 +53,7 @@ struct PairBufs {
     int M;                 // neighbour capacity per atom (row stride)
     uint64_t* key;         // [n*M] (j << 32) | packed image
     float4* dx;            // [n*M] (dx, dy, dz, bits of type_j)
+    float4* dxlo;          // [n*M] low parts: dx = hi + lo to ~48 bits (NEP ZBL reads them), or NULL
     int* rev;              // [n*M] flat index of the mirrored entry
     float4* g;             // [n*M] pair gradient -dE_i/d(x_j - x_i)
     uint16_t* grp;         // [n*M] cell-offset group of the entry (rows are sorted by group, then j)

@@ -65,6 +65,9 @@ __global__ void k_lmp_rows(int inum, int nall, const int* __restrict__ ilist, co
                 const size_t q = (size_t)ii * M + pos;
                 P.key[q] = pair_key(j, pack_img(0, 0, 0));
                 P.dx[q] = make_float4((float)dx, (float)dy, (float)dz, __int_as_float(type[j]));
+                if (P.dxlo)
+                    P.dxlo[q] = make_float4((float)(dx - (double)(float)dx), (float)(dy - (double)(float)dy),
+                                            (float)(dz - (double)(float)dz), 0.f);
                 P.grp[q] = 0;
             }
         }

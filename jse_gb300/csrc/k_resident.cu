@@ -115,7 +115,7 @@ k_filter(const StructDev* __restrict__ S, const SlotDev* __restrict__ slots, con
         const int k = k0 + lane;
         bool acc = false;
         int jb = 0, na = 0, nb = 0, nc = 0;
-        float ox = 0.f, oy = 0.f, oz = 0.f;
+        float ox = 0.f, oy = 0.f, oz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
         uint16_t g = 0;
         if (k < cv) {
             const uint64_t key = vrow[k];
@@ -179,9 +179,9 @@ k_filter(const StructDev* __restrict__ S, const SlotDev* __restrict__ slots, con
                         const double dzv = ds(da(xw[3 * jb + 2], sh[2]), zi);
                         acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
                     }
-                    ox = dh[0] + dl[0];
-                    oy = dh[1] + dl[1];
-                    oz = dh[2] + dl[2];
+                    two_sum(dh[0], dl[0], ox, lx);
+                    two_sum(dh[1], dl[1], oy, ly);
+                    two_sum(dh[2], dl[2], oz, lz);
                 }
             }
         }
@@ -192,6 +192,7 @@ k_filter(const StructDev* __restrict__ S, const SlotDev* __restrict__ slots, con
                 const size_t e = (size_t)a * M + pos;
                 P.key[e] = pair_key(jb, pack_img(na, nb, nc));
                 P.dx[e] = make_float4(ox, oy, oz, xf[jb].w);
+                if (P.dxlo) P.dxlo[e] = make_float4(lx, ly, lz, 0.f);
                 P.grp[e] = g;
             }
         }

@@ -239,7 +239,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         auto exact_batch = [&](int k) {  // the first k queued candidates
             bool acc = false;
             int j = 0, slot = 0;
-            float ox = 0.f, oy = 0.f, oz = 0.f;
+            float ox = 0.f, oy = 0.f, oz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
             if (lane < k) {
                 j = s_qj[w][lane];
                 slot = s_qs[w][lane];
@@ -272,9 +272,9 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     const double dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
                     acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
                 }
-                ox = dh[0] + dl[0];
-                oy = dh[1] + dl[1];
-                oz = dh[2] + dl[2];
+                two_sum(dh[0], dl[0], ox, lx);
+                two_sum(dh[1], dl[1], oy, ly);
+                two_sum(dh[2], dl[2], oz, lz);
             }
             const unsigned m = __ballot_sync(0xffffffffu, acc);
             if (acc) {
@@ -283,6 +283,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     const size_t e = (size_t)i * M + pos;
                     P.key[e] = pair_key(j, s_img[w][slot]);
                     P.dx[e] = make_float4(ox, oy, oz, xf[j].w);
+                    if (P.dxlo) P.dxlo[e] = make_float4(lx, ly, lz, 0.f);
                     P.grp[e] = (uint16_t)(o0 + slot);
                 }
                 if (keep_groups) atomicAdd(&s_acc[w][slot], 1);

@@ -9,8 +9,10 @@
 // atom i takes f/2 of its energy and the entry's pair gradient gets -dx f'(r) / (2 r): the
 // full rows hold each pair in both directions, as the reference's neighbour lists do.
 // One warp per atom row; the row's energy is summed in a fixed order and added once.
-// The pair terms are evaluated in FP64 from the FP32 displacement: an atom's ZBL energy
-// reaches tens of eV at short range, where FP32 arithmetic alone would cost 1e-5 eV.
+// The pair terms are evaluated in FP64 from the displacement carried to ~48 bits (its FP32
+// value and the low part the row builders store for ZBL models): an atom's ZBL energy
+// reaches tens of eV at short range, where an FP32 displacement alone would cost up to
+// 1e-5 eV per atom.
 #include "common.cuh"
 #include "pdl.cuh"
 #include "zbl.cuh"
@@ -41,7 +43,15 @@ __global__ void __launch_bounds__(256) k_nep_zbl(PairBufs P, int n, const int* _
         const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
         if (r2 >= kZblMaxR * kZblMaxR) continue;
         const int tj = __float_as_int(d.w) - 1;
-        const double r = sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z), rinv = 1.0 / r;
+        // the displacement to ~48 bits: FP32 value plus its stored low part
+        double dx = d.x, dy = d.y, dz = d.z;
+        if (P.dxlo) {
+            const float4 lo = P.dxlo[e];
+            dx += lo.x;
+            dy += lo.y;
+            dz += lo.z;
+        }
+        const double r = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / r;
         const double a_inv = (z.zp[ti] + z.zp[tj]) * 2.134563;
         const double zizj = 14.399645 * z.z[ti] * z.z[tj];
         const double x = r * a_inv;
@@ -77,9 +87,9 @@ __global__ void __launch_bounds__(256) k_nep_zbl(PairBufs P, int n, const int* _
         }
         fp = fp * fc + f * fcp;
         f *= fc;
-        const float s = (float)(0.5 * fp * rinv);
+        const double s = 0.5 * fp * rinv;
         const float4 g = P.g[e];
-        P.g[e] = make_float4(g.x - s * d.x, g.y - s * d.y, g.z - s * d.z, g.w);
+        P.g[e] = make_float4(g.x - (float)(s * dx), g.y - (float)(s * dy), g.z - (float)(s * dz), g.w);
         esum += 0.5 * f;
     }
 #pragma unroll

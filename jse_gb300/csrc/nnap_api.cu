@@ -401,6 +401,7 @@ void grow_pairs(nnap_handle* h, int n, int M) {
     h->pg.ensure(np);
     h->prev.ensure(np);
     h->pgrp.ensure(np);
+    if (h->model.zbl.on) h->pdxlo.ensure(np);
     if (h->sub_rc > 0.0) {
         h->sdx.ensure(np);
         h->spos.ensure(np);
@@ -413,6 +414,7 @@ PairBufs pair_bufs(nnap_handle* h) {
     P.M = h->M;
     P.key = h->pkey.p;
     P.dx = h->pdx.p;
+    P.dxlo = h->model.zbl.on ? h->pdxlo.p : nullptr;
     P.rev = h->prev.p;
     P.g = h->pg.p;
     P.grp = h->pgrp.p;

@@ -6,11 +6,10 @@ virials of the reference's compiled NEP arithmetic on the same structures
 (tests/golden/make_golden_nep.py).  The GPU path evaluates them through nnap_create_nep
 with FP32 descriptors and network.
 
-Tolerances: |dE_i| <= 1e-5 eV per atom (the path's energy target), max |dF| <= 1e-3 eV/A
-and force RMSE <= 1e-4 eV/A, per-atom virials within 2e-3 eV.  The path holds the pair
-displacements in FP32; where close ZBL contacts make the per-atom energy more sensitive
-than that to the rounding (hundreds of eV/A at 1.3 A), |dE_i| may reach twice the error
-that rounding alone causes in the FP64 oracle.  The energy per atom stays within 1e-5 eV.
+Tolerances: |dE_i| <= 1e-5 eV per atom (the path's energy target) on every fixture, close
+ZBL contacts included (the ZBL pair terms run in FP64 on displacements carried to ~48
+bits), max |dF| <= 1e-3 eV/A and force RMSE <= 1e-4 eV/A, per-atom virials within 2e-3 eV.
+The energy per atom stays within 1e-5 eV.
 """
 import glob
 import os
@@ -28,16 +27,6 @@ BINARY = os.path.join(GOLDEN_DIR, "nep_nep4_binary.npz")   # two species, 4- and
 E_TOL, F_MAX, F_RMS, V_TOL = 1e-5, 1e-3, 1e-4, 2e-3
 
 
-def _dx_rounding_error(text, z):
-    """max_i |dE_i| of the FP64 oracle when its displacements are first rounded to FP32."""
-    from oracle import native as ON, nep_model as NM, nep_oracle as NO
-    m = NM.load(text)
-    nl = ON.neighbors(ON.wrap(z["x"], int(z["box_kind"]), z["box"]), int(z["box_kind"]), z["box"],
-                      max(m.rc_radial, m.rc_angular))
-    nl.dx = np.asarray(nl.dx, dtype=np.float32).astype(np.float64)
-    return float(np.max(np.abs(NO.energies(m, z["types"] - 1, nl) - z["energies"])))
-
-
 def _case(path):
     z = np.load(path)
     s = W.Structure(z["x"], z["types"], z["box"].reshape(3, 3), int(z["box_kind"]))
@@ -51,7 +40,9 @@ def test_nep_matches_reference(path):
     with NEP(text) as p:
         out = p.calEnergyForceVirials(s)
     de = np.max(np.abs(out["energies"] - z["energies"]))
-    assert de <= E_TOL or ("_zbl" in text.split("\n", 1)[0] and de <= 2.0 * _dx_rounding_error(text, z))
+    print("%s: max |dE_i| %.2e eV, max |dF| %.2e eV/A" % (os.path.basename(path)[:-4], de,
+                                                          np.max(np.abs(out["forces"] - z["forces"]))))
+    assert de <= E_TOL
     df = out["forces"] - z["forces"]
     assert np.max(np.abs(df)) <= F_MAX
     assert np.sqrt(np.mean(df ** 2)) <= F_RMS
