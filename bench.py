@@ -264,39 +264,46 @@ def cpu_reference(structures, model: dict, budget_s: float = 12.0, threads: int 
 
 
 # ----------------------------------------------------------------------------- serving
-def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2)) -> dict:
+def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2), steady: int = 256) -> dict:
     """Continuous-batching serving of ``nreq`` requests of 20 evaluations each.
 
     Requests start from structures of a 256-structure pool (n ~ log-normal, median 500,
     log-sd 1.0, clipped to [50, 20000]; ternary liquids at 0.060 /A^3) and move every
     coordinate by N(0, 0.01^2) A between evaluations.  The server keeps neighbour rows at
-    rcut + 0.5 A, admits by a 120 GB budget and at most 1024 resident structures.  The
-    capacity is the request rate of a saturated run (every request queued at once); the
-    Poisson runs offer fractions of it.  Latencies are wall-clock, host buffers, and
-    include queueing."""
+    rcut + 0.5 A and admits by a 120 GB budget.  The capacity is the request rate
+    sustained at a steady ``steady`` resident requests (every request queued at once, at
+    most ``steady`` slots: one is admitted as soon as one finishes); the Poisson runs offer
+    fractions of it with up to 1024 resident requests.  ``saturated`` is the same
+    all-at-once run with 1024 slots.  Latencies are wall-clock, host buffers, and include
+    queueing."""
     from jse_gb300.nnap import NNAP
     from jse_gb300.serve import GaussianMoves, NNAPServer, RequestLoop, poisson_requests
     pool = W.c5_pool(256)
     model = bench_model("c5")
     moves = GaussianMoves(sigma=0.01, seed=7)
     out = {"requests": nreq, "evaluations_per_request": 20, "skin_A": 0.5, "memory_budget_GB": 120,
-           "max_resident": 1024, "pool": "256 structures, n ~ lognormal(median 500, sd 1.0) in [50, 20000]",
-           "mean_atoms": float(np.mean([p.natoms for p in pool]))}
+           "max_resident": 1024, "steady_resident_for_capacity": steady,
+           "pool": "256 structures, n ~ lognormal(median 500, sd 1.0) in [50, 20000]",
+           "mean_atoms": float(np.mean([p.natoms for p in pool])),
+           "loop": "submit a step, move the continuing requests and admit arrivals while it runs, collect"}
     with NNAP(model, precision="mixed", device=device) as p:
-        def run(rate):
-            with NNAPServer(p, skin=0.5, memory_budget=120e9, max_structs=1024) as srv:
+        def run(rate, slots=1024):
+            with NNAPServer(p, skin=0.5, memory_budget=120e9, max_structs=slots) as srv:
                 reqs = poisson_requests(pool, nreq, rate, nsteps=20, seed=11)
                 st = RequestLoop(srv, reqs, moves=moves).run()
                 ss = srv.stats()
                 st["rebuilds_per_request"] = ss["rebuilds"] / max(1, nreq)
                 return st
-        # warm the pool allocator and kernels, then saturate
+        # warm the pool allocator and kernels
         with NNAPServer(p, skin=0.5, memory_budget=120e9, max_structs=1024) as srv:
             RequestLoop(srv, poisson_requests(pool, 64, float("inf"), nsteps=3, seed=1), moves=moves).run()
         sat = run(float("inf"))
-        cap = sat["req_per_s"]
+        out["saturated"] = {"req_s": sat["req_per_s"], "atom_evals_s": sat["atom_evals_per_s"],
+                            "eval_p50_ms": sat["eval_p50_ms"], "max_active": sat["max_active"]}
+        stdy = run(float("inf"), slots=steady)
+        cap = stdy["req_per_s"]
         out["capacity_req_s"] = cap
-        out["capacity_atom_evals_s"] = sat["atom_evals_per_s"]
+        out["capacity_atom_evals_s"] = stdy["atom_evals_per_s"]
         runs = []
         for f in loads:
             st = run(f * cap)

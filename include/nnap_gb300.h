@@ -290,6 +290,16 @@ int nnap_server_release(nnap_server* s, int slot);
  * order (energy[q], virial[9*q] per listed slot).  Host buffers, synchronous. */
 int nnap_server_step(nnap_server* s, int nslots, const int* slots, const double* x, int flags, double* energy,
                      double* energies, double* forces, double* virial, double* virials);
+/* The same step in two halves, so the caller's host work overlaps the device: submit
+ * stages the positions (xs[q]: the 3 n_q positions of slots[q]; the arrays may change as
+ * soon as it returns) and queues the whole evaluation without waiting; collect waits for
+ * it and writes the outputs selected by the submitted flags, in the order of `slots`
+ * (layout of nnap_server_step).  One step at a time: a second submit, a step call or a
+ * neighbour-list query before the collect returns NNAP_ERR_BUSY, the release of a slot of
+ * the step in flight NNAP_ERR_ARG; admissions are allowed meanwhile. */
+int nnap_server_submit(nnap_server* s, int nslots, const int* slots, const double* const* xs, int flags);
+int nnap_server_collect(nnap_server* s, double* energy, double* energies, double* forces, double* virial,
+                        double* virials);
 /* Neighbour list that the last step used for `slot` (layout of nnap_neighbor_list;
  * neighbour indices local to the slot). */
 int nnap_server_neighbor_list(nnap_server* s, int slot, int* counts, long long cap, int* j, int* img,

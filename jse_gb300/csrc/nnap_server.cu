@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "api_internal.hpp"
@@ -49,6 +50,8 @@ struct ServerSlot {
     int kind = 0;
     double box[9];
     StructDev grid;              // rebuild grid at rc + skin (cell counts, search reach)
+    StructDev evs;               // the box at rc with the rebuild grid's cells (a0 set per step)
+    long long gen = 0;           // bumped whenever the slot's device arrays are (re)allocated
     std::vector<int> type;       // host copy of the species
     std::vector<double> xb;      // positions at the last rebuild (caller's frame)
     bool need_build = true;
@@ -84,6 +87,17 @@ struct nnap_server {
     Pinned stage_in, stage_out;
     // last step: structures in batch order (for neighbour-list queries)
     int last_natoms = 0;
+    long long gens = 0;  // generation counter of slot allocations
+    // the step in flight between nnap_server_submit and nnap_server_collect
+    struct Pending {
+        bool active = false;
+        int nslots = 0, N = 0, nbs = 0, flags = 0;
+        std::vector<int> ids, order, a0, n;  // caller's slots; batch position -> caller index; per batch position
+        std::vector<long long> gen;           // slot generations at submission
+        std::vector<size_t> in_off;           // caller-order atom offsets
+        double* hx = nullptr;                 // staged positions, batch order (pinned)
+        double *oe = nullptr, *ov = nullptr, *oea = nullptr, *of = nullptr, *ova = nullptr;  // pinned outputs
+    } pend;
 };
 
 namespace {
@@ -153,6 +167,7 @@ void slot_alloc(nnap_server* s, ServerSlot& sl) {
     sl.dev.a0 = 0;
     CK(cudaMemcpyAsync(t, sl.type.data(), sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
     sl.need_build = true;
+    sl.gen = ++s->gens;
     s->resident_bytes += sl.bytes;
 }
 
@@ -183,9 +198,29 @@ T* carve(char*& c, size_t count) {
     return p;
 }
 
-// One step over the listed slots.  x holds their positions concatenated in the order
-// of ids; outputs use the same order.
-void step_impl(nnap_server* s, int nslots, const int* ids, const double* x, int flags, const Outputs& o) {
+// Run f(lo, hi) over [0, n) on up to 8 host threads (one when n is small).
+template <class F>
+void host_parallel(size_t n, size_t grain, F&& f) {
+    const size_t nt = std::min<size_t>(8, std::max<size_t>(1, n / std::max<size_t>(grain, 1)));
+    if (nt <= 1) {
+        f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t per = (n + nt - 1) / nt;
+    for (size_t k = 1; k < nt; ++k) {
+        const size_t lo = k * per, hi = std::min(n, lo + per);
+        if (lo < hi) th.emplace_back([&f, lo, hi]() { f(lo, hi); });
+    }
+    f(0, std::min(n, per));
+    for (auto& t : th) t.join();
+}
+
+// Queue one step over the listed slots (positions xs[q] of slot ids[q]) without waiting:
+// inputs are staged (the caller's arrays may change once this returns), every kernel and
+// the copies of the outputs into pinned staging are on the handle's stream.
+// rebuild_all: every listed slot is rebuilt (the retry after a capacity overflow).
+void submit_impl(nnap_server* s, int nslots, const int* ids, const double* const* xs, int flags, bool rebuild_all) {
     nnap_handle* h = s->h;
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
@@ -195,6 +230,7 @@ void step_impl(nnap_server* s, int nslots, const int* ids, const double* x, int 
         const int id = ids[q];
         if (id < 0 || id >= (int)s->slots.size() || !s->slots[id].used) throw ApiFail(NNAP_ERR_ARG, "slot is not admitted");
         if (s->slots[id].last_stamp == stamp) throw ApiFail(NNAP_ERR_ARG, "slot listed twice in one step");
+        if (!xs[q]) throw ApiFail(NNAP_ERR_ARG, "positions of a slot are NULL");
         s->slots[id].last_stamp = stamp;
         in_off[q + 1] = in_off[q] + (size_t)s->slots[id].n;
     }
@@ -202,209 +238,259 @@ void step_impl(nnap_server* s, int nslots, const int* ids, const double* x, int 
     // which slots are rebuilt: new ones, and those with an atom displaced by more than skin/2
     const double lim = 0.5 * s->skin * (1.0 - 1e-9);
     const double lim2 = lim * lim;
-    std::vector<char> rb(nslots, 0);
-    for (int q = 0; q < nslots; ++q) {
-        ServerSlot& sl = s->slots[ids[q]];
-        bool need = sl.need_build;
-        const double* xq = x + 3 * in_off[q];
-        for (int i = 0; !need && i < sl.n; ++i) {
-            const double dx = xq[3 * i] - sl.xb[3 * i], dy = xq[3 * i + 1] - sl.xb[3 * i + 1],
-                         dz = xq[3 * i + 2] - sl.xb[3 * i + 2];
-            need = !(dx * dx + dy * dy + dz * dz <= lim2);
+    std::vector<char> rb(nslots, rebuild_all ? 1 : 0);
+    if (!rebuild_all)
+        host_parallel((size_t)nslots, 64, [&](size_t lo, size_t hi) {
+            for (size_t q = lo; q < hi; ++q) {
+                const ServerSlot& sl = s->slots[ids[q]];
+                bool need = sl.need_build;
+                const double* xq = xs[q];
+                for (int i = 0; !need && i < sl.n; ++i) {
+                    const double dx = xq[3 * i] - sl.xb[3 * i], dy = xq[3 * i + 1] - sl.xb[3 * i + 1],
+                                 dz = xq[3 * i + 2] - sl.xb[3 * i + 2];
+                    need = !(dx * dx + dy * dy + dz * dz <= lim2);
+                }
+                rb[q] = need;
+            }
+        });
+    // batch order: rebuilt slots first, so the rebuild works on a prefix of the atoms
+    std::vector<int> order;
+    for (int q = 0; q < nslots; ++q)
+        if (rb[q]) order.push_back(q);
+    const int nbs = (int)order.size();
+    for (int q = 0; q < nslots; ++q)
+        if (!rb[q]) order.push_back(q);
+    Batch B;
+    B.nstruct = nslots;
+    B.natoms = N;
+    B.sc.push_back(0);
+    std::vector<StructDev> gsd;
+    std::vector<SlotDev> sdv;
+    int a0 = 0, c0 = 0, nb_atoms = 0;
+    for (int t = 0; t < nslots; ++t) {
+        ServerSlot& sl = s->slots[ids[order[t]]];
+        StructDev d = sl.evs;
+        d.a0 = a0;
+        B.sd.push_back(d);
+        if (t < nbs) {
+            StructDev g = sl.grid;
+            g.a0 = a0;
+            g.n = sl.n;
+            g.c0 = c0;
+            c0 += g.nc[0] * g.nc[1] * g.nc[2];
+            gsd.push_back(g);
+            nb_atoms += sl.n;
         }
-        rb[q] = need;
+        SlotDev sv = sl.dev;
+        sv.a0 = a0;
+        sv.n = sl.n;
+        sdv.push_back(sv);
+        for (int b = 0; b < sl.n; b += kRedChunk) {
+            B.cb.push_back(a0 + b);
+            B.ce.push_back(a0 + std::min(sl.n, b + kRedChunk));
+        }
+        B.sc.push_back((int)B.cb.size());
+        a0 += sl.n;
     }
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        // batch order: rebuilt slots first, so the rebuild works on a prefix of the atoms
-        std::vector<int> order;
-        for (int q = 0; q < nslots; ++q)
-            if (rb[q]) order.push_back(q);
-        const int nbs = (int)order.size();
-        for (int q = 0; q < nslots; ++q)
-            if (!rb[q]) order.push_back(q);
-        Batch B;
-        B.nstruct = nslots;
-        B.natoms = N;
-        B.sc.push_back(0);
-        std::vector<StructDev> gsd;
-        std::vector<SlotDev> sdv;
-        int a0 = 0, c0 = 0, nb_atoms = 0;
-        for (int t = 0; t < nslots; ++t) {
-            ServerSlot& sl = s->slots[ids[order[t]]];
-            StructDev d = make_struct(sl.kind, sl.box, s->rc, a0, sl.n, 0);
-            int Rm = 0;
-            for (int k = 0; k < 3; ++k) {
-                d.nc[k] = sl.grid.nc[k];
-                d.R[k] = sl.grid.R[k];
-                Rm = std::max(Rm, d.R[k]);
-            }
-            d.rc2_hi = screen_bound(d, s->rc, Rm + 1);
-            B.sd.push_back(d);
-            if (t < nbs) {
-                StructDev g = sl.grid;
-                g.a0 = a0;
-                g.n = sl.n;
-                g.c0 = c0;
-                c0 += g.nc[0] * g.nc[1] * g.nc[2];
-                gsd.push_back(g);
-                nb_atoms += sl.n;
-            }
-            SlotDev sv = sl.dev;
-            sv.a0 = a0;
-            sv.n = sl.n;
-            sdv.push_back(sv);
-            for (int b = 0; b < sl.n; b += kRedChunk) {
-                B.cb.push_back(a0 + b);
-                B.ce.push_back(a0 + std::min(sl.n, b + kRedChunk));
-            }
-            B.sc.push_back((int)B.cb.size());
-            a0 += sl.n;
-        }
-        B.ncells = std::max(c0, 1);
-        const int nchunks = (int)B.cb.size();
-        // buffers: the handle's work arrays at row capacity Mv, then the server's own
-        h->M = s->Mv;
-        h->GS = 0;  // filtered rows keep no group starts: the mirror search bisects
-        ensure_work(h, N, nslots, B.ncells, nchunks);
-        drop_graph(h);
-        h->layout_ok = false;
-        s->kw.ensure(std::max(N, 1));
-        s->type_b.ensure(std::max(N, 1));
-        s->x.ensure(3 * (size_t)std::max(N, 1));
-        s->dslots.ensure(nslots);
-        s->sdev_build.ensure(std::max(nbs, 1));
-        // pinned staging of everything uploaded, in batch order
-        const size_t in_bytes = align256(sizeof(double) * 3 * (size_t)N) + align256(sizeof(StructDev) * nslots) +
-                                align256(sizeof(StructDev) * std::max(nbs, 1)) + align256(sizeof(SlotDev) * nslots) +
-                                3 * align256(sizeof(int) * (size_t)(nchunks + nslots + 1));
-        char* c = static_cast<char*>(s->stage_in.ensure(in_bytes));
-        double* hx = carve<double>(c, 3 * (size_t)N);
-        StructDev* hsd = carve<StructDev>(c, nslots);
-        StructDev* hgd = carve<StructDev>(c, std::max(nbs, 1));
-        SlotDev* hsl = carve<SlotDev>(c, nslots);
-        int* hcb = carve<int>(c, nchunks + nslots + 1);
-        int* hce = carve<int>(c, nchunks + nslots + 1);
-        int* hsc = carve<int>(c, nchunks + nslots + 1);
-        for (int t = 0; t < nslots; ++t) {
+    B.ncells = std::max(c0, 1);
+    const int nchunks = (int)B.cb.size();
+    // buffers: the handle's work arrays at row capacity Mv, then the server's own
+    h->M = s->Mv;
+    h->GS = 0;  // filtered rows keep no group starts: the mirror search bisects
+    ensure_work(h, N, nslots, B.ncells, nchunks);
+    drop_graph(h);
+    h->layout_ok = false;
+    s->kw.ensure(std::max(N, 1));
+    s->type_b.ensure(std::max(N, 1));
+    s->x.ensure(3 * (size_t)std::max(N, 1));
+    s->dslots.ensure(nslots);
+    s->sdev_build.ensure(std::max(nbs, 1));
+    // pinned staging of everything uploaded, in batch order
+    const size_t in_bytes = align256(sizeof(double) * 3 * (size_t)N) + align256(sizeof(StructDev) * nslots) +
+                            align256(sizeof(StructDev) * std::max(nbs, 1)) + align256(sizeof(SlotDev) * nslots) +
+                            3 * align256(sizeof(int) * (size_t)(nchunks + nslots + 1));
+    char* c = static_cast<char*>(s->stage_in.ensure(in_bytes));
+    double* hx = carve<double>(c, 3 * (size_t)N);
+    StructDev* hsd = carve<StructDev>(c, nslots);
+    StructDev* hgd = carve<StructDev>(c, std::max(nbs, 1));
+    SlotDev* hsl = carve<SlotDev>(c, nslots);
+    int* hcb = carve<int>(c, nchunks + nslots + 1);
+    int* hce = carve<int>(c, nchunks + nslots + 1);
+    int* hsc = carve<int>(c, nchunks + nslots + 1);
+    host_parallel((size_t)nslots, 64, [&](size_t lo, size_t hi) {
+        for (size_t t = lo; t < hi; ++t) {
             const int q = order[t];
-            std::memcpy(hx + 3 * (size_t)B.sd[t].a0, x + 3 * in_off[q], sizeof(double) * 3 * (in_off[q + 1] - in_off[q]));
+            std::memcpy(hx + 3 * (size_t)B.sd[t].a0, xs[q], sizeof(double) * 3 * (in_off[q + 1] - in_off[q]));
         }
-        std::memcpy(hsd, B.sd.data(), sizeof(StructDev) * nslots);
-        if (nbs) std::memcpy(hgd, gsd.data(), sizeof(StructDev) * nbs);
-        std::memcpy(hsl, sdv.data(), sizeof(SlotDev) * nslots);
-        if (nchunks) {
-            std::memcpy(hcb, B.cb.data(), sizeof(int) * nchunks);
-            std::memcpy(hce, B.ce.data(), sizeof(int) * nchunks);
-        }
-        std::memcpy(hsc, B.sc.data(), sizeof(int) * (nslots + 1));
-        if (N) CK(cudaMemcpyAsync(s->x.p, hx, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(h->sdev.p, hsd, sizeof(StructDev) * nslots, cudaMemcpyHostToDevice, st));
-        if (nbs) CK(cudaMemcpyAsync(s->sdev_build.p, hgd, sizeof(StructDev) * nbs, cudaMemcpyHostToDevice, st));
-        CK(cudaMemcpyAsync(s->dslots.p, hsl, sizeof(SlotDev) * nslots, cudaMemcpyHostToDevice, st));
-        if (nchunks) {
-            CK(cudaMemcpyAsync(h->chunk_b.p, hcb, sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
-            CK(cudaMemcpyAsync(h->chunk_e.p, hce, sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
-        }
-        CK(cudaMemcpyAsync(h->struct_chunks.p, hsc, sizeof(int) * (nslots + 1), cudaMemcpyHostToDevice, st));
-        CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
-        // launches
-        h->launches = 0;
-        h->mark(0);
-        int* sid = h->sid.p;
-        int* tb = s->type_b.p;
-        k_tick_atoms<<<nslots, 256, 0, st>>>(s->dslots.p, sid, tb);
+    });
+    std::memcpy(hsd, B.sd.data(), sizeof(StructDev) * nslots);
+    if (nbs) std::memcpy(hgd, gsd.data(), sizeof(StructDev) * nbs);
+    std::memcpy(hsl, sdv.data(), sizeof(SlotDev) * nslots);
+    if (nchunks) {
+        std::memcpy(hcb, B.cb.data(), sizeof(int) * nchunks);
+        std::memcpy(hce, B.ce.data(), sizeof(int) * nchunks);
+    }
+    std::memcpy(hsc, B.sc.data(), sizeof(int) * (nslots + 1));
+    if (N) CK(cudaMemcpyAsync(s->x.p, hx, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->sdev.p, hsd, sizeof(StructDev) * nslots, cudaMemcpyHostToDevice, st));
+    if (nbs) CK(cudaMemcpyAsync(s->sdev_build.p, hgd, sizeof(StructDev) * nbs, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->dslots.p, hsl, sizeof(SlotDev) * nslots, cudaMemcpyHostToDevice, st));
+    if (nchunks) {
+        CK(cudaMemcpyAsync(h->chunk_b.p, hcb, sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(h->chunk_e.p, hce, sizeof(int) * nchunks, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemcpyAsync(h->struct_chunks.p, hsc, sizeof(int) * (nslots + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
+    // launches
+    h->launches = 0;
+    h->mark(0);
+    int* sid = h->sid.p;
+    int* tb = s->type_b.p;
+    k_tick_atoms<<<nslots, 256, 0, st>>>(s->dslots.p, sid, tb);
+    ++h->launches;
+    if (N > 0) {
+        k_wrap_resident<<<(N + 255) / 256, 256, 0, st>>>(h->sdev.p, sid, s->x.p, tb, N, T, h->xw.p, h->xf.p,
+                                                         h->xlo.p, s->kw.p, h->status.p);
         ++h->launches;
-        if (N > 0) {
-            k_wrap_resident<<<(N + 255) / 256, 256, 0, st>>>(h->sdev.p, sid, s->x.p, tb, N, T, h->xw.p, h->xf.p,
-                                                             h->xlo.p, s->kw.p, h->status.p);
-            ++h->launches;
+    }
+    if (nb_atoms > 0) {  // rebuild the Verlet rows of the prefix at rc + skin
+        CK(cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * B.ncells, st));
+        CK(cudaMemsetAsync(h->cell_fill.p, 0, sizeof(int) * B.ncells, st));
+        k_wrap_bin<<<(nb_atoms + 255) / 256, 256, 0, st>>>(s->sdev_build.p, sid, s->x.p, tb, nb_atoms, T, h->xw.p,
+                                                           h->xf.p, h->xlo.p, h->cell_of.p, h->cell_count.p,
+                                                           h->status.p);
+        k_scan_excl<<<1, 1024, 0, st>>>(h->cell_count.p, B.ncells, h->cell_start.p);
+        k_fill_cells<<<(nb_atoms + 255) / 256, 256, 0, st>>>(h->cell_of.p, nb_atoms, h->cell_start.p,
+                                                             h->cell_fill.p, h->cell_atoms.p);
+        k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
+        const int nw = h->tune.nb_warps;
+        k_neighbors<<<(nb_atoms + nw - 1) / nw, 32 * nw, 0, st>>>(
+            s->sdev_build.p, sid, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p,
+            nb_atoms, pair_bufs(h), h->status.p, h->status.p + 1);
+        k_verlet_store<<<(unsigned)(((size_t)nb_atoms * 32 + 127) / 128), 128, 0, st>>>(s->dslots.p, sid,
+                                                                                       pair_bufs(h), nb_atoms,
+                                                                                       s->kw.p);
+        h->launches += 6;
+    }
+    if (N > 0) {
+        k_filter<<<(N + kFilterWarps - 1) / kFilterWarps, 32 * kFilterWarps, 0, st>>>(
+            h->sdev.p, s->dslots.p, sid, h->xw.p, h->xf.p, h->xlo.p, s->kw.p, N, s->Mv, pair_bufs(h), h->status.p,
+            h->status.p + 1);
+        ++h->launches;
+    }
+    enqueue_species_mirror(h, B, tb);
+    h->mark(1);
+    enqueue_eval(h, B, tb, false, true);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
+    // outputs in batch order into pinned staging
+    const size_t out_bytes = align256(sizeof(double) * nslots) + align256(sizeof(double) * 9 * nslots) +
+                             align256(sizeof(double) * (size_t)N) + align256(sizeof(double) * 3 * (size_t)N) +
+                             align256(sizeof(double) * 9 * (size_t)N);
+    char* oc = static_cast<char*>(s->stage_out.ensure(out_bytes));
+    auto& P = s->pend;
+    P.oe = carve<double>(oc, nslots);
+    P.ov = carve<double>(oc, 9 * (size_t)nslots);
+    P.oea = carve<double>(oc, N);
+    P.of = carve<double>(oc, 3 * (size_t)N);
+    P.ova = carve<double>(oc, 9 * (size_t)N);
+    if (flags & NNAP_WANT_ENERGY)
+        CK(cudaMemcpyAsync(P.oe, h->energy.p, sizeof(double) * nslots, cudaMemcpyDeviceToHost, st));
+    if (flags & NNAP_WANT_VIRIAL)
+        CK(cudaMemcpyAsync(P.ov, h->virial.p, sizeof(double) * 9 * nslots, cudaMemcpyDeviceToHost, st));
+    if ((flags & NNAP_WANT_ENERGIES) && N)
+        CK(cudaMemcpyAsync(P.oea, h->e_atom.p, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    if ((flags & NNAP_WANT_FORCES) && N)
+        CK(cudaMemcpyAsync(P.of, h->forces.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
+    if ((flags & NNAP_WANT_VIRIALS) && N)
+        CK(cudaMemcpyAsync(P.ova, h->virials.p, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, st));
+    P.active = true;
+    P.nslots = nslots;
+    P.N = N;
+    P.nbs = nbs;
+    P.flags = flags;
+    P.ids.assign(ids, ids + nslots);
+    P.order = order;
+    P.in_off = in_off;
+    P.hx = hx;
+    P.a0.resize(nslots);
+    P.n.resize(nslots);
+    P.gen.resize(nslots);
+    for (int t = 0; t < nslots; ++t) {
+        P.a0[t] = B.sd[t].a0;
+        P.n[t] = B.sd[t].n;
+        P.gen[t] = s->slots[ids[order[t]]].gen;
+    }
+}
+
+// Wait for the step in flight and copy its outputs (caller order).  A Verlet row that
+// overflowed the shared capacity grows it and reruns the step with every slot rebuilt,
+// from the staged positions.
+void collect_impl(nnap_server* s, const Outputs& o) {
+    nnap_handle* h = s->h;
+    auto& P = s->pend;
+    if (!P.active) throw ApiFail(NNAP_ERR_ARG, "no step in flight");
+    for (int attempt = 0;; ++attempt) {
+        const cudaError_t se = cudaStreamSynchronize(h->stream);
+        if (se != cudaSuccess) {
+            P.active = false;
+            throw CudaFail(se, "cudaStreamSynchronize");
         }
-        if (nb_atoms > 0) {  // rebuild the Verlet rows of the prefix at rc + skin
-            CK(cudaMemsetAsync(h->cell_count.p, 0, sizeof(int) * B.ncells, st));
-            CK(cudaMemsetAsync(h->cell_fill.p, 0, sizeof(int) * B.ncells, st));
-            k_wrap_bin<<<(nb_atoms + 255) / 256, 256, 0, st>>>(s->sdev_build.p, sid, s->x.p, tb, nb_atoms, T, h->xw.p,
-                                                               h->xf.p, h->xlo.p, h->cell_of.p, h->cell_count.p,
-                                                               h->status.p);
-            k_scan_excl<<<1, 1024, 0, st>>>(h->cell_count.p, B.ncells, h->cell_start.p);
-            k_fill_cells<<<(nb_atoms + 255) / 256, 256, 0, st>>>(h->cell_of.p, nb_atoms, h->cell_start.p,
-                                                                 h->cell_fill.p, h->cell_atoms.p);
-            k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
-            const int nw = h->tune.nb_warps;
-            k_neighbors<<<(nb_atoms + nw - 1) / nw, 32 * nw, 0, st>>>(
-                s->sdev_build.p, sid, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p,
-                nb_atoms, pair_bufs(h), h->status.p, h->status.p + 1);
-            k_verlet_store<<<(unsigned)(((size_t)nb_atoms * 32 + 127) / 128), 128, 0, st>>>(s->dslots.p, sid,
-                                                                                           pair_bufs(h), nb_atoms,
-                                                                                           s->kw.p);
-            h->launches += 6;
-        }
-        if (N > 0) {
-            k_filter<<<(N + kFilterWarps - 1) / kFilterWarps, 32 * kFilterWarps, 0, st>>>(
-                h->sdev.p, s->dslots.p, sid, h->xw.p, h->xf.p, h->xlo.p, s->kw.p, N, s->Mv, pair_bufs(h), h->status.p,
-                h->status.p + 1);
-            ++h->launches;
-        }
-        enqueue_species_mirror(h, B, tb);
-        h->mark(1);
-        enqueue_eval(h, B, tb, false, true);
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
-        // outputs in batch order into pinned staging
-        const size_t out_bytes = align256(sizeof(double) * nslots) + align256(sizeof(double) * 9 * nslots) +
-                                 align256(sizeof(double) * (size_t)N) + align256(sizeof(double) * 3 * (size_t)N) +
-                                 align256(sizeof(double) * 9 * (size_t)N);
-        char* oc = static_cast<char*>(s->stage_out.ensure(out_bytes));
-        double* oe = carve<double>(oc, nslots);
-        double* ov = carve<double>(oc, 9 * (size_t)nslots);
-        double* oea = carve<double>(oc, N);
-        double* of = carve<double>(oc, 3 * (size_t)N);
-        double* ova = carve<double>(oc, 9 * (size_t)N);
-        if (flags & NNAP_WANT_ENERGY)
-            CK(cudaMemcpyAsync(oe, h->energy.p, sizeof(double) * nslots, cudaMemcpyDeviceToHost, st));
-        if (flags & NNAP_WANT_VIRIAL)
-            CK(cudaMemcpyAsync(ov, h->virial.p, sizeof(double) * 9 * nslots, cudaMemcpyDeviceToHost, st));
-        if ((flags & NNAP_WANT_ENERGIES) && N)
-            CK(cudaMemcpyAsync(oea, h->e_atom.p, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
-        if ((flags & NNAP_WANT_FORCES) && N)
-            CK(cudaMemcpyAsync(of, h->forces.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st));
-        if ((flags & NNAP_WANT_VIRIALS) && N)
-            CK(cudaMemcpyAsync(ova, h->virials.p, sizeof(double) * 9 * N, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
         const int bits = h->h_status[0];
         const int maxc = h->h_status[1];
-        if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
-        if (bits & ERRBIT_TIMEOUT) throw ApiFail(NNAP_ERR_TIMEOUT, "a bounded tensor-core wait gave up");
-        if (bits & ERRBIT_CELLS) throw ApiFail(NNAP_ERR_ARG, "an atom moved too many boxes since its rebuild");
+        if (bits & (ERRBIT_BAD_TYPE | ERRBIT_TIMEOUT | ERRBIT_CELLS | ERRBIT_NO_MIRROR)) {
+            P.active = false;
+            if (bits & ERRBIT_BAD_TYPE) throw ApiFail(NNAP_ERR_BAD_TYPE, "species outside 1..ntypes");
+            if (bits & ERRBIT_TIMEOUT) throw ApiFail(NNAP_ERR_TIMEOUT, "a bounded tensor-core wait gave up");
+            if (bits & ERRBIT_CELLS) throw ApiFail(NNAP_ERR_ARG, "an atom moved too many boxes since its rebuild");
+            throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
+        }
         if ((bits & ERRBIT_CAPACITY) || maxc > s->Mv) {
-            // a rebuilt row overflowed: grow the capacity; every listed slot is rebuilt
+            if (attempt >= 2) {
+                P.active = false;
+                throw ApiFail(NNAP_ERR_CAPACITY, "Verlet capacity could not be established");
+            }
+            // positions in caller order from the staged copy, then the step again
+            std::vector<double> xc(3 * (size_t)P.N);
+            std::vector<const double*> xs(P.nslots);
+            for (int t = 0; t < P.nslots; ++t) {
+                const int q = P.order[t];
+                std::memcpy(xc.data() + 3 * P.in_off[q], P.hx + 3 * (size_t)P.a0[t], sizeof(double) * 3 * P.n[t]);
+            }
+            for (int q = 0; q < P.nslots; ++q) xs[q] = xc.data() + 3 * P.in_off[q];
             set_capacity(s, ((int)std::ceil(maxc * 1.15) + 8 + 7) & ~7);
-            std::fill(rb.begin(), rb.end(), 1);
+            const std::vector<int> ids = P.ids;
+            P.active = false;
+            submit_impl(s, (int)ids.size(), ids.data(), xs.data(), P.flags, true);
             continue;
         }
-        if (bits & ERRBIT_NO_MIRROR) throw ApiFail(NNAP_ERR_CAPACITY, "neighbour list is not symmetric");
-        for (int t = 0; t < nslots; ++t) {
-            const int q = order[t];
-            ServerSlot& sl = s->slots[ids[q]];
-            sl.last_a0 = B.sd[t].a0;
+        break;
+    }
+    const int flags = P.flags;
+    for (int t = 0; t < P.nslots; ++t) {
+        const int q = P.order[t];
+        ServerSlot& sl = s->slots[P.ids[q]];
+        const bool same = sl.used && sl.gen == P.gen[t];  // not reallocated since submission
+        if (same) {
+            sl.last_a0 = P.a0[t];
             sl.last_step = s->steps;
-            if (t < nbs) {
-                sl.xb.assign(x + 3 * in_off[q], x + 3 * in_off[q + 1]);
+            if (t < P.nbs) {
+                sl.xb.assign(P.hx + 3 * (size_t)P.a0[t], P.hx + 3 * ((size_t)P.a0[t] + sl.n));
                 sl.need_build = false;
                 ++s->builds;
             }
-            const size_t n = sl.n, a = B.sd[t].a0, off = in_off[q];
-            if ((flags & NNAP_WANT_ENERGY) && o.energy) o.energy[q] = oe[t];
-            if ((flags & NNAP_WANT_VIRIAL) && o.virial) std::memcpy(o.virial + 9 * q, ov + 9 * t, sizeof(double) * 9);
-            if ((flags & NNAP_WANT_ENERGIES) && o.energies) std::memcpy(o.energies + off, oea + a, sizeof(double) * n);
-            if ((flags & NNAP_WANT_FORCES) && o.forces) std::memcpy(o.forces + 3 * off, of + 3 * a, sizeof(double) * 3 * n);
-            if ((flags & NNAP_WANT_VIRIALS) && o.virials)
-                std::memcpy(o.virials + 9 * off, ova + 9 * a, sizeof(double) * 9 * n);
         }
-        s->last_natoms = N;
-        ++s->steps;
-        return;
+        const size_t n = P.n[t], a = P.a0[t], off = P.in_off[q];
+        if ((flags & NNAP_WANT_ENERGY) && o.energy) o.energy[q] = P.oe[t];
+        if ((flags & NNAP_WANT_VIRIAL) && o.virial) std::memcpy(o.virial + 9 * q, P.ov + 9 * t, sizeof(double) * 9);
+        if ((flags & NNAP_WANT_ENERGIES) && o.energies) std::memcpy(o.energies + off, P.oea + a, sizeof(double) * n);
+        if ((flags & NNAP_WANT_FORCES) && o.forces) std::memcpy(o.forces + 3 * off, P.of + 3 * a, sizeof(double) * 3 * n);
+        if ((flags & NNAP_WANT_VIRIALS) && o.virials)
+            std::memcpy(o.virials + 9 * off, P.ova + 9 * a, sizeof(double) * 9 * n);
     }
-    throw ApiFail(NNAP_ERR_CAPACITY, "Verlet capacity could not be established");
+    s->last_natoms = P.N;
+    ++s->steps;
+    P.active = false;
 }
 
 }  // namespace
@@ -498,6 +584,17 @@ int nnap_server_admit(nnap_server* s, int natoms, const int* type, int box_kind,
         sl.kind = box_kind;
         std::memcpy(sl.box, box, sizeof sl.box);
         sl.grid = grid;
+        {  // the box at rc, searched with the rebuild grid's cells (one per slot, reused every step)
+            StructDev d = make_struct(box_kind, box, s->rc, 0, natoms, 0);
+            int Rm = 0;
+            for (int k = 0; k < 3; ++k) {
+                d.nc[k] = grid.nc[k];
+                d.R[k] = grid.R[k];
+                Rm = std::max(Rm, d.R[k]);
+            }
+            d.rc2_hi = screen_bound(d, s->rc, Rm + 1);
+            sl.evs = d;
+        }
         sl.type.assign(type, type + natoms);
         try {
             slot_alloc(s, sl);
@@ -518,6 +615,8 @@ int nnap_server_release(nnap_server* s, int slot) {
     return guarded(s->h, [&]() -> int {
         if (slot < 0 || slot >= (int)s->slots.size() || !s->slots[slot].used)
             throw ApiFail(NNAP_ERR_ARG, "slot is not admitted");
+        if (s->pend.active && std::find(s->pend.ids.begin(), s->pend.ids.end(), slot) != s->pend.ids.end())
+            throw ApiFail(NNAP_ERR_ARG, "slot is part of the step in flight; collect it first");
         ServerSlot& sl = s->slots[slot];
         slot_free(s, sl);
         s->resident_atoms -= sl.n;
@@ -533,9 +632,43 @@ int nnap_server_step(nnap_server* s, int nslots, const int* slots, const double*
     if (!s) return NNAP_ERR_ARG;
     return guarded(s->h, [&]() -> int {
         if (nslots < 1 || !slots || !x) throw ApiFail(NNAP_ERR_ARG, "a step needs slots and positions");
+        if (s->pend.active) throw ApiFail(NNAP_ERR_BUSY, "a submitted step is in flight; collect it first");
         Outputs o{energy, energies, forces, virial, virials};
         check_outputs(flags, o);
-        step_impl(s, nslots, slots, x, flags, o);
+        std::vector<const double*> xs(nslots);
+        size_t off = 0;
+        for (int q = 0; q < nslots; ++q) {
+            if (slots[q] < 0 || slots[q] >= (int)s->slots.size() || !s->slots[slots[q]].used)
+                throw ApiFail(NNAP_ERR_ARG, "slot is not admitted");
+            xs[q] = x + 3 * off;
+            off += (size_t)s->slots[slots[q]].n;
+        }
+        submit_impl(s, nslots, slots, xs.data(), flags, false);
+        collect_impl(s, o);
+        return NNAP_OK;
+    });
+}
+
+int nnap_server_submit(nnap_server* s, int nslots, const int* slots, const double* const* xs, int flags) {
+    if (!s) return NNAP_ERR_ARG;
+    return guarded(s->h, [&]() -> int {
+        if (nslots < 1 || !slots || !xs) throw ApiFail(NNAP_ERR_ARG, "a step needs slots and positions");
+        if (s->pend.active) throw ApiFail(NNAP_ERR_BUSY, "a submitted step is in flight; collect it first");
+        const int known = NNAP_WANT_ENERGY | NNAP_WANT_ENERGIES | NNAP_WANT_FORCES | NNAP_WANT_VIRIAL | NNAP_WANT_VIRIALS;
+        if (flags & ~known) throw ApiFail(NNAP_ERR_ARG, "unknown output flags");
+        submit_impl(s, nslots, slots, xs, flags, false);
+        return NNAP_OK;
+    });
+}
+
+int nnap_server_collect(nnap_server* s, double* energy, double* energies, double* forces, double* virial,
+                        double* virials) {
+    if (!s) return NNAP_ERR_ARG;
+    return guarded(s->h, [&]() -> int {
+        if (!s->pend.active) throw ApiFail(NNAP_ERR_ARG, "no step in flight");
+        Outputs o{energy, energies, forces, virial, virials};
+        check_outputs(s->pend.flags, o);
+        collect_impl(s, o);
         return NNAP_OK;
     });
 }
@@ -546,6 +679,7 @@ int nnap_server_neighbor_list(nnap_server* s, int slot, int* counts, long long c
     nnap_handle* h = s->h;
     return guarded(h, [&]() -> int {
         if (!counts || !total) throw ApiFail(NNAP_ERR_ARG, "NULL argument");
+        if (s->pend.active) throw ApiFail(NNAP_ERR_BUSY, "a submitted step is in flight; collect it first");
         if (slot < 0 || slot >= (int)s->slots.size() || !s->slots[slot].used)
             throw ApiFail(NNAP_ERR_ARG, "slot is not admitted");
         const ServerSlot& sl = s->slots[slot];

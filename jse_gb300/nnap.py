@@ -42,7 +42,8 @@ EXPORTS = ["nnap_create", "nnap_create_from_file", "nnap_destroy", "nnap_ntypes"
            "nnap_server_create", "nnap_server_destroy", "nnap_server_admit", "nnap_server_release",
            "nnap_server_step", "nnap_server_neighbor_list", "nnap_server_stats", "nnap_set_autotune",
            "nnap_get_tuning", "nnap_set_tuning", "nnap_compute_lammps", "nnap_param_sizes", "nnap_train_grad_batch",
-           "nnap_create_nep", "nnap_create_nep_from_file", "nnap_compute_lammps_nl"]
+           "nnap_create_nep", "nnap_create_nep_from_file", "nnap_compute_lammps_nl", "nnap_model_check",
+           "nnap_server_submit", "nnap_server_collect"]
 
 
 class IllegalStateError(RuntimeError):
@@ -98,6 +99,8 @@ def load_library(path: str = LIB_PATH):
     L.nnap_server_admit.argtypes = [P, I, ip, I, dp, ip]
     L.nnap_server_release.argtypes = [P, I]
     L.nnap_server_step.argtypes = [P, I, ip, dp, I, dp, dp, dp, dp, dp]
+    L.nnap_server_submit.argtypes = [P, I, ip, C.POINTER(dp), I]
+    L.nnap_server_collect.argtypes = [P, dp, dp, dp, dp, dp]
     L.nnap_server_neighbor_list.argtypes = [P, I, ip, C.c_longlong, ip, ip, C.POINTER(C.c_longlong)]
     L.nnap_server_stats.argtypes = [P, C.POINTER(C.c_longlong)]
     L.nnap_param_sizes.argtypes = [P, I, ip, ip]

@@ -41,6 +41,7 @@ class NNAPServer:
         self._s = s
         self.skin = skin
         self._n = {}
+        self._pending = None
 
     def close(self):
         if self._s is not None:
@@ -117,6 +118,46 @@ class NNAPServer:
             out["virials"] = va
         return out
 
+    def submit(self, slots: Sequence[int], xs: Sequence[np.ndarray], energies: bool = False, forces: bool = True,
+               per_atom_virial: bool = False):
+        """Queue a step over ``slots`` at positions ``xs`` (one C-contiguous float64 (n, 3)
+        array per slot) and return at once: the positions are staged, so the arrays may be
+        changed while the step runs.  :meth:`collect` returns its outputs."""
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        ptrs = (C.POINTER(C.c_double) * len(sl))()
+        N = 0
+        for q, (s, x) in enumerate(zip(sl, xs)):
+            n = self._n[int(s)]
+            if x.dtype != np.float64 or not x.flags.c_contiguous or x.size != 3 * n:
+                raise ValueError("positions of slot %d must be a contiguous float64 (%d, 3) array" % (s, n))
+            ptrs[q] = _dptr(x)
+            N += n
+        flags = WANT_ENERGY | WANT_VIRIAL
+        flags |= WANT_FORCES if forces else 0
+        flags |= WANT_ENERGIES if energies else 0
+        flags |= WANT_VIRIALS if per_atom_virial else 0
+        self._nnap._check(self._L.nnap_server_submit(self._srv(), len(sl), _iptr(sl), ptrs, flags))
+        self._pending = (len(sl), N, flags)
+
+    def collect(self) -> dict:
+        """Wait for the submitted step; outputs as :meth:`step`."""
+        S, N, flags = self._pending
+        self._pending = None
+        e, v = np.zeros(S), np.zeros((S, 9))
+        f = np.zeros((N, 3)) if flags & WANT_FORCES else None
+        ea = np.zeros(N) if flags & WANT_ENERGIES else None
+        va = np.zeros((N, 9)) if flags & WANT_VIRIALS else None
+        self._nnap._check(self._L.nnap_server_collect(self._srv(), _dptr(e), _dptr(ea), _dptr(f), _dptr(v),
+                                                      _dptr(va)))
+        out = {"energy": e, "virial": v}
+        if f is not None:
+            out["forces"] = f
+        if ea is not None:
+            out["energies"] = ea
+        if va is not None:
+            out["virials"] = va
+        return out
+
     def neighborList(self, slot: int):
         """Neighbour list the last step used for ``slot``: (offsets[n+1], j, image[n_pairs x 3])."""
         n = self._n[slot]
@@ -151,11 +192,17 @@ class GaussianMoves:
         self.sigma = sigma
         self.pool = np.random.default_rng(seed).standard_normal(pool) * sigma
 
-    def __call__(self, rid: int, k: int, x: np.ndarray) -> np.ndarray:
-        m = x.size
+    def window(self, rid: int, k: int, m: int) -> np.ndarray:
         span = self.pool.size - m
         off = ((rid * 1000003 + k * 7919) * 2654435761) % max(span, 1)
-        return x + self.pool[off:off + m].reshape(x.shape)
+        return self.pool[off:off + m]
+
+    def __call__(self, rid: int, k: int, x: np.ndarray) -> np.ndarray:
+        return x + self.window(rid, k, x.size).reshape(x.shape)
+
+    def apply(self, rid: int, k: int, x: np.ndarray) -> None:
+        """The same move, in place (no new array)."""
+        x.reshape(-1).__iadd__(self.window(rid, k, x.size))
 
 
 @dataclass
@@ -179,9 +226,11 @@ class Request:
 class RequestLoop:
     """Continuous batching over an :class:`NNAPServer`.
 
-    Every loop turn admits the queued requests that fit (FIFO), then runs one step over
-    all admitted requests, then retires the requests that finished.  With nothing
-    admitted, the loop sleeps until the next arrival."""
+    Every loop turn admits the queued requests that fit (FIFO), submits one step over all
+    admitted requests and, while the GPU runs it, moves the positions of the requests
+    that continue and admits new arrivals (they join the next step); then it collects the
+    step and retires the requests that finished.  With nothing admitted, the loop sleeps
+    until the next arrival."""
 
     def __init__(self, server: NNAPServer, requests: Sequence[Request], moves=None, keep_results: bool = False):
         self.server = server
@@ -200,10 +249,11 @@ class RequestLoop:
         steps = 0
         max_active = 0
         step_atoms = []
-        while pending or queue or active:
-            now = clock() - t0
+
+        def admit(now):
             while pending and pending[0].t_arrival <= now:
                 queue.append(pending.popleft())
+            joined = []
             while queue:
                 r = queue[0]
                 slot = srv.admit(r.structure)
@@ -211,18 +261,30 @@ class RequestLoop:
                     break
                 queue.popleft()
                 r.slot, r.t_admit, r.t_ready = slot, now, now
-                r.x = np.ascontiguousarray(r.structure.x, dtype=np.float64)
-                active.append(r)
+                r.x = np.array(r.structure.x, dtype=np.float64, order="C", copy=True)
+                joined.append(r)
+            return joined
+
+        joining: List[Request] = []
+        while pending or queue or active or joining:
+            active += joining
+            joining = []
+            active += admit(clock() - t0)
             if not active:
                 if queue:
                     raise RuntimeError("a queued request cannot be admitted into an empty server")
                 if pending:
                     time.sleep(max(0.0, pending[0].t_arrival - (clock() - t0)))
                 continue
-            for r in active:
-                if r.done > 0 and self.moves is not None:
-                    r.x = self.moves(r.rid, r.done, r.x)
-            out = srv.step([r.slot for r in active], [r.x for r in active], forces=self.keep)
+            srv.submit([r.slot for r in active], [r.x for r in active], forces=self.keep)
+            # while the step runs: the next positions of the requests that continue, and
+            # admissions of the requests that arrived meanwhile
+            if self.moves is not None:
+                for r in active:
+                    if r.done + 1 < r.nsteps:
+                        self.moves.apply(r.rid, r.done + 1, r.x)
+            joining = admit(clock() - t0)
+            out = srv.collect()
             t = clock() - t0
             steps += 1
             max_active = max(max_active, len(active))
@@ -244,6 +306,8 @@ class RequestLoop:
                     srv.release(r.slot)
                 else:
                     still.append(r)
+            for r in joining:  # joined during the step: their wait for the next one starts now
+                r.t_ready = r.t_admit
             atom_evals += n_now
             step_atoms.append(n_now)
             active = still

@@ -108,16 +108,17 @@ def test_admission_stops_at_the_budget(model):
     from jse_gb300.serve import NNAPServer
     s = W.random_liquid(2000, 0.060, [0.46, 0.46, 0.08], 2.0, 83)
     with NNAP(model, precision="mixed") as p:
-        with NNAPServer(p, skin=0.5, memory_budget=80e6) as srv:
+        with NNAPServer(p, skin=0.5, memory_budget=80e6, max_structs=64) as srv:
             slots = []
             while True:
                 k = srv.admit(s)
                 if k is None:
                     break
                 slots.append(k)
-                assert len(slots) < 100
+                assert len(slots) < 64
+            # the budget, not the 64-slot cap, refused the next admission
             st = srv.stats()
-            assert len(slots) >= 1 and st["resident_bytes"] + st["work_bytes"] <= 80e6
+            assert 1 <= len(slots) < 64 and st["resident_bytes"] + st["work_bytes"] <= 80e6
             srv.step(slots, [s.x] * len(slots))
             srv.release(slots[0])
             assert srv.admit(s) is not None
@@ -125,3 +126,37 @@ def test_admission_stops_at_the_budget(model):
             with pytest.raises(NNAPError) as e:
                 srv.admit(s)
             assert e.value.status == NNAP_ERR_CAPACITY
+
+
+def test_submit_collect_equals_step(model):
+    """The two-phase step gives the one-call step's results bitwise; the positions are staged
+    (changing them after submit changes nothing); one step is in flight at a time, a slot of
+    it cannot be released before the collect, and admissions may happen meanwhile."""
+    from jse_gb300.nnap import NNAP, NNAPError, NNAP_ERR_ARG, NNAP_ERR_BUSY
+    from jse_gb300.serve import NNAPServer
+    structs = [W.random_liquid(n, 0.060, [0.46, 0.46, 0.08], 2.0, 84 + n, tilt=0.1) for n in (300, 800, 1500)]
+    rng = np.random.default_rng(7)
+    with NNAP(model, precision="mixed") as p, NNAPServer(p, skin=0.5, memory_budget=8e9) as a, \
+            NNAP(model, precision="mixed") as q, NNAPServer(q, skin=0.5, memory_budget=8e9) as b:
+        sa = [a.admit(s) for s in structs]
+        sb = [b.admit(s) for s in structs]
+        xs = [np.array(s.x, copy=True) for s in structs]
+        for k in range(4):
+            if k:
+                xs = [x + rng.normal(0.0, 0.02, size=x.shape) for x in xs]
+            ref = a.step(sa, xs, energies=True, per_atom_virial=True)
+            work = [np.array(x, copy=True) for x in xs]
+            b.submit(sb, work, energies=True, per_atom_virial=True)
+            for w in work:
+                w += 5.0  # staged: no effect on the step in flight
+            with pytest.raises(NNAPError) as e:
+                b.submit(sb, work)
+            assert e.value.status == NNAP_ERR_BUSY
+            with pytest.raises(NNAPError) as e:
+                b.release(sb[0])
+            assert e.value.status == NNAP_ERR_ARG
+            extra = b.admit(structs[0])  # admission while the step runs
+            got = b.collect()
+            b.release(extra)
+            for key in ("energy", "virial", "forces", "energies", "virials"):
+                assert np.array_equal(ref[key], got[key]), (k, key)

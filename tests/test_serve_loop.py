@@ -35,6 +35,15 @@ class FakeServer:
         x = np.concatenate(xs)
         return {"energy": np.array([float(np.sum(v)) for v in xs]), "forces": x.copy()}
 
+    def submit(self, slots, xs, forces=False):
+        # positions are staged: the loop moves them in place while the step runs
+        assert getattr(self, "_out", None) is None, "one step in flight at a time"
+        self._out = self.step(slots, [np.array(v, copy=True) for v in xs], forces)
+
+    def collect(self):
+        out, self._out = self._out, None
+        return out
+
 
 def _pool():
     rng = np.random.default_rng(0)
