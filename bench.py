@@ -166,8 +166,11 @@ def load_traffic():
     """DRAM bytes per atom of a stage's dominant kernel, from one ncu capture
     (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided by its atoms):
     liquid32k / descriptors_bwd is k_sph_bwd_n<6,18,9> on the 32000-atom liquid, 159.2 MB
-    read + 16.9 MB written (profiles/k_sph_liquid32k.md)."""
-    return {"liquid32k/descriptors_bwd": (159.2e6 + 16.9e6) / 32000}
+    read + 16.9 MB written (profiles/k_sph_liquid32k.md); batch1024 / descriptors_bwd is the
+    same kernel over the 1024-structure batch, 2627.3 MB read + 442.8 MB written for 526124
+    atoms (profiles/batch1024_launches_and_k_sph_bwd_n.md)."""
+    return {"liquid32k/descriptors_bwd": (159.2e6 + 16.9e6) / 32000,
+            "batch1024/descriptors_bwd": (2627.281e6 + 442.828e6) / 526124}
 
 
 # ----------------------------------------------------------------------------- reference arm
@@ -264,25 +267,27 @@ def cpu_reference(structures, model: dict, budget_s: float = 12.0, threads: int 
 
 
 # ----------------------------------------------------------------------------- serving
-def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2), steady: int = 256) -> dict:
+def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2), steady: int = 64,
+                      curve=(64, 256)) -> dict:
     """Continuous-batching serving of ``nreq`` requests of 20 evaluations each.
 
     Requests start from structures of a 256-structure pool (n ~ log-normal, median 500,
     log-sd 1.0, clipped to [50, 20000]; ternary liquids at 0.060 /A^3) and move every
     coordinate by N(0, 0.01^2) A between evaluations.  The server keeps neighbour rows at
-    rcut + 0.5 A and admits by a 120 GB budget.  The capacity is the request rate
-    sustained at a steady ``steady`` resident requests (every request queued at once, at
-    most ``steady`` slots: one is admitted as soon as one finishes); the Poisson runs offer
-    fractions of it with up to 1024 resident requests.  ``saturated`` is the same
-    all-at-once run with 1024 slots.  Latencies are wall-clock, host buffers, and include
-    queueing."""
+    rcut + 0.5 A and admits by a 120 GB budget.  ``steady`` lists the request rate
+    sustained at a steady resident count R (every request queued at once, at most R slots:
+    one is admitted as soon as one finishes); ``saturated`` is that run with 1024 slots.
+    The capacity is the rate at ``steady`` resident requests, an operating point of
+    millisecond steps; the Poisson runs offer fractions of it with up to 1024 resident
+    requests, so a burst is absorbed by larger, more efficient steps.  Latencies are
+    wall-clock, host buffers, and include queueing."""
     from jse_gb300.nnap import NNAP
     from jse_gb300.serve import GaussianMoves, NNAPServer, RequestLoop, poisson_requests
     pool = W.c5_pool(256)
     model = bench_model("c5")
     moves = GaussianMoves(sigma=0.01, seed=7)
     out = {"requests": nreq, "evaluations_per_request": 20, "skin_A": 0.5, "memory_budget_GB": 120,
-           "max_resident": 1024, "steady_resident_for_capacity": steady,
+           "max_resident": 1024, "capacity_at_resident": steady,
            "pool": "256 structures, n ~ lognormal(median 500, sd 1.0) in [50, 20000]",
            "mean_atoms": float(np.mean([p.natoms for p in pool])),
            "loop": "submit a step, move the continuing requests and admit arrivals while it runs, collect"}
@@ -300,10 +305,15 @@ def serve_measurement(device: int, nreq: int = 5000, loads=(0.5, 0.8, 1.0, 1.2),
         sat = run(float("inf"))
         out["saturated"] = {"req_s": sat["req_per_s"], "atom_evals_s": sat["atom_evals_per_s"],
                             "eval_p50_ms": sat["eval_p50_ms"], "max_active": sat["max_active"]}
-        stdy = run(float("inf"), slots=steady)
-        cap = stdy["req_per_s"]
-        out["capacity_req_s"] = cap
-        out["capacity_atom_evals_s"] = stdy["atom_evals_per_s"]
+        out["steady"] = []
+        for R in sorted(set(curve) | {steady}):
+            st = run(float("inf"), slots=R)
+            out["steady"].append({"resident": R, "req_s": st["req_per_s"], "atom_evals_s": st["atom_evals_per_s"],
+                                  "eval_p50_ms": st["eval_p50_ms"]})
+            if R == steady:
+                cap = st["req_per_s"]
+                out["capacity_req_s"] = cap
+                out["capacity_atom_evals_s"] = st["atom_evals_per_s"]
         runs = []
         for f in loads:
             st = run(f * cap)
