@@ -27,8 +27,9 @@ __global__ void k_wrap_bin(const StructDev*, const int*, const double*, const in
 __global__ void k_scan_excl(const int*, int, int*);
 __global__ void k_fill_cells(const int*, int, const int*, int*, int*);
 __global__ void k_sort_cells(const int*, int, int*);
-__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const int*,
-                            const int*, const int*, int, PairBufs, int*, int*);
+__global__ void k_cell_order(const int*, int, const float4*, const float4*, float4*, float4*);
+__global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const float4*,
+                            const float4*, const int*, const int*, const int*, int, PairBufs, int*, int*);
 __global__ void k_mirror(const StructDev*, const int*, PairBufs, int, int*);
 __global__ void k_type_hist(const int*, int, int, int*);
 __global__ void k_type_offsets(int*, int, int, int*);
@@ -183,7 +184,7 @@ struct nnap_handle {
     nnapgb::DevBuf<int> type, sid, cell_of, cell_count, cell_fill, cell_start, cell_atoms, perm, block_counts,
         type_start;
     nnapgb::DevBuf<int> chunk_b, chunk_e, struct_chunks, status;
-    nnapgb::DevBuf<float4> xf, xlo;
+    nnapgb::DevBuf<float4> xf, xlo, xfc, xloc;  // positions as float + low parts; copies in cell order
     nnapgb::DevBuf<uint16_t> pgrp;
     nnapgb::DevBuf<nnapgb::StructDev> sdev;
     nnapgb::DevBuf<uint64_t> pkey;

@@ -138,21 +138,38 @@ __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int
 // of 32 cells the candidates are spread over the lanes, screened in FP32 against
 // rc^2 plus a rounding margin, and confirmed with the exact FP64 test.  Accepted
 // pairs are compacted in candidate order with a ballot, so rows are deterministic.
+// Candidate positions are read from the cell-ordered copies xfc / xloc (k_cell_order), so
+// a lane's atom index and position loads are independent and a cell's candidates are
+// contiguous in memory.
 constexpr int kNbMaxWarps = 8;  // warps per CTA are a launch parameter (2, 4 or 8)
+
+// xfc[k] = xf[cell_atoms[k]], xloc[k] = xlo[cell_atoms[k]] for the n binned atoms.
+__global__ void __launch_bounds__(256) k_cell_order(const int* __restrict__ cell_atoms, int n,
+                                                    const float4* __restrict__ xf, const float4* __restrict__ xlo,
+                                                    float4* __restrict__ xfc, float4* __restrict__ xloc) {
+    pdl_enter();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int a = cell_atoms[k];
+    xfc[k] = xf[a];
+    xloc[k] = xlo[a];
+}
 
 __global__ void __launch_bounds__(32 * kNbMaxWarps)
 k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ xw,
-            const float4* __restrict__ xf, const float4* __restrict__ xlo, const int* __restrict__ cell_of,
-            const int* __restrict__ cell_start, const int* __restrict__ cell_atoms, int n, PairBufs P,
-            int* __restrict__ err, int* __restrict__ max_count) {
+            const float4* __restrict__ xf, const float4* __restrict__ xlo, const float4* __restrict__ xfc,
+            const float4* __restrict__ xloc, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
+            const int* __restrict__ cell_atoms, int n, PairBufs P, int* __restrict__ err,
+            int* __restrict__ max_count) {
     pdl_enter();
     __shared__ int s_incl[kNbMaxWarps][32], s_start[kNbMaxWarps][32];
     __shared__ uint32_t s_img[kNbMaxWarps][32];
     __shared__ double s_sh[kNbMaxWarps][32][3];
     __shared__ float s_fsh[kNbMaxWarps][32][3], s_flo[kNbMaxWarps][32][3];
     __shared__ int s_acc[kNbMaxWarps][32];  // accepted entries per cell-offset group of the batch
-    __shared__ int s_qj[kNbMaxWarps][64];   // candidates passing the FP32 screen: atom, cell slot
-    __shared__ int s_qs[kNbMaxWarps][64];
+    __shared__ int s_qj[kNbMaxWarps][64];   // candidates passing the FP32 screen: atom, cell slot,
+    __shared__ int s_qs[kNbMaxWarps][64];   // position in cell order
+    __shared__ int s_qk[kNbMaxWarps][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + w;
     if (i >= n) return;
@@ -239,12 +256,14 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         auto exact_batch = [&](int k) {  // the first k queued candidates
             bool acc = false;
             int j = 0, slot = 0;
+            float4 fj = make_float4(0.f, 0.f, 0.f, 0.f);
             float ox = 0.f, oy = 0.f, oz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
             if (lane < k) {
                 j = s_qj[w][lane];
                 slot = s_qs[w][lane];
-                const float4 fj = xf[j];
-                const float4 lj = xlo[j];
+                const int kp = s_qk[w][lane];
+                fj = xfc[kp];
+                const float4 lj = xloc[kp];
                 // (x_j + shift) - x_i in float-float, then d^2 in float-float
                 float dh[3], dl[3];
                 const float ajh[3] = {fj.x, fj.y, fj.z}, ajl[3] = {lj.x, lj.y, lj.z};
@@ -282,7 +301,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 if (pos < M) {
                     const size_t e = (size_t)i * M + pos;
                     P.key[e] = pair_key(j, s_img[w][slot]);
-                    P.dx[e] = make_float4(ox, oy, oz, xf[j].w);
+                    P.dx[e] = make_float4(ox, oy, oz, fj.w);
                     if (P.dxlo) P.dxlo[e] = make_float4(lx, ly, lz, 0.f);
                     P.grp[e] = (uint16_t)(o0 + slot);
                 }
@@ -293,7 +312,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         for (int cb = 0; cb < total; cb += 32) {
             const int cidx = cb + lane;
             bool pass = false;
-            int j = 0, slot = 0;
+            int j = 0, slot = 0, kp = 0;
             if (cidx < total) {
                 int lo = 0, hi = 31;  // first slot with incl > cidx
                 while (lo < hi) {
@@ -302,9 +321,10 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 }
                 slot = lo;
                 const int before = slot ? s_incl[w][slot - 1] : 0;
-                j = cell_atoms[s_start[w][slot] + (cidx - before)];
+                kp = s_start[w][slot] + (cidx - before);
+                j = cell_atoms[kp];
+                const float4 fj = xfc[kp];  // independent of the load of j
                 if (!(j == i && s_img[w][slot] == pack_img(0, 0, 0))) {
-                    const float4 fj = xf[j];
                     const float fx = (fj.x + s_fsh[w][slot][0]) - fi.x;
                     const float fy = (fj.y + s_fsh[w][slot][1]) - fi.y;
                     const float fz = (fj.z + s_fsh[w][slot][2]) - fi.z;
@@ -316,21 +336,24 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 const int q = qn + __popc(m & ((1u << lane) - 1u));
                 s_qj[w][q] = j;
                 s_qs[w][q] = slot;
+                s_qk[w][q] = kp;
             }
             qn += __popc(m);
             __syncwarp();
             if (qn >= 32) {
                 exact_batch(32);
                 // move the overflow (at most 31 entries) to the front of the queue
-                int rj = 0, rs = 0;
+                int rj = 0, rs = 0, rk = 0;
                 if (lane < qn - 32) {
                     rj = s_qj[w][32 + lane];
                     rs = s_qs[w][32 + lane];
+                    rk = s_qk[w][32 + lane];
                 }
                 __syncwarp();
                 if (lane < qn - 32) {
                     s_qj[w][lane] = rj;
                     s_qs[w][lane] = rs;
+                    s_qk[w][lane] = rk;
                 }
                 qn -= 32;
                 __syncwarp();

@@ -451,6 +451,8 @@ void ensure_work(nnap_handle* h, int n, int nstruct, int ncells, int nchunks) {
     h->xw.ensure(3 * (size_t)n1);
     h->xf.ensure(n1);
     h->xlo.ensure(n1);
+    h->xfc.ensure(n1);
+    h->xloc.ensure(n1);
     h->cell_of.ensure(n1);
     h->cell_count.ensure(std::max(ncells, 1));
     h->cell_fill.ensure(std::max(ncells, 1));
@@ -532,11 +534,13 @@ void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const 
     if (n > 0) {
         CK(launch_pdl(k_fill_cells, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p));
         CK(launch_pdl(k_sort_cells, dim3((B.ncells * 32 + 255) / 256), dim3(256), 0, st, h->cell_start.p, B.ncells, h->cell_atoms.p));
+        CK(launch_pdl(k_cell_order, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_atoms.p, n, h->xf.p, h->xlo.p,
+                      h->xfc.p, h->xloc.p));
         const int nw = h->tune.nb_warps;
-        CK(launch_pdl(k_neighbors, dim3((n + nw - 1) / nw), dim3(32 * nw), 0, st, 
-            h->sdev.p, h->sid.p, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
-            pair_bufs(h), h->status.p, h->status.p + 1));
-        h->launches += 3;
+        CK(launch_pdl(k_neighbors, dim3((n + nw - 1) / nw), dim3(32 * nw), 0, st, h->sdev.p, h->sid.p, h->xw.p,
+                      h->xf.p, h->xlo.p, h->xfc.p, h->xloc.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
+                      pair_bufs(h), h->status.p, h->status.p + 1));
+        h->launches += 4;
     }
 }
 

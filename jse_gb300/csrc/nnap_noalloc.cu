@@ -39,7 +39,7 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Byte offsets of the scratch regions for n atoms and c cells.
 struct Carve {
-    size_t sdev, status, sid, xw, xf, xlo, cell_of, cell_count, cell_fill, cell_start, cell_atoms, end;
+    size_t sdev, status, sid, xw, xf, xlo, xfc, xloc, cell_of, cell_count, cell_fill, cell_start, cell_atoms, end;
 };
 constexpr Carve carve(size_t n, size_t c) {
     Carve k{};
@@ -50,6 +50,8 @@ constexpr Carve carve(size_t n, size_t c) {
     k.xw = o;         o = align256(o + 3 * n * sizeof(double));
     k.xf = o;         o = align256(o + n * sizeof(float4));
     k.xlo = o;        o = align256(o + n * sizeof(float4));
+    k.xfc = o;        o = align256(o + n * sizeof(float4));
+    k.xloc = o;       o = align256(o + n * sizeof(float4));
     k.cell_of = o;    o = align256(o + n * sizeof(int));
     k.cell_count = o; o = align256(o + c * sizeof(int));
     k.cell_fill = o;  o = align256(o + c * sizeof(int));
@@ -100,6 +102,8 @@ extern "C" int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const
     double* xw = reinterpret_cast<double*>(base + k.xw);
     float4* xf = reinterpret_cast<float4*>(base + k.xf);
     float4* xlo = reinterpret_cast<float4*>(base + k.xlo);
+    float4* xfc = reinterpret_cast<float4*>(base + k.xfc);
+    float4* xloc = reinterpret_cast<float4*>(base + k.xloc);
     int* cell_of = reinterpret_cast<int*>(base + k.cell_of);
     int* cell_count = reinterpret_cast<int*>(base + k.cell_count);
     int* cell_fill = reinterpret_cast<int*>(base + k.cell_fill);
@@ -128,8 +132,9 @@ extern "C" int nnap_neighbor_counts_noalloc(int natoms, const double* d_x, const
         std::memset(&P, 0, sizeof P);
         P.M = 0;  // count only: no pair rows are written
         P.count = d_counts;
-        k_neighbors<<<(natoms + 3) / 4, 128, 0, st>>>(sdev, sid, xw, xf, xlo, cell_of, cell_start, cell_atoms, natoms,
-                                                    P, status, status + 1);
+        k_cell_order<<<(natoms + 255) / 256, 256, 0, st>>>(cell_atoms, natoms, xf, xlo, xfc, xloc);
+        k_neighbors<<<(natoms + 3) / 4, 128, 0, st>>>(sdev, sid, xw, xf, xlo, xfc, xloc, cell_of, cell_start, cell_atoms,
+                                                    natoms, P, status, status + 1);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return NNAP_ERR_CUDA;

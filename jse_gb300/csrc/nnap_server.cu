@@ -363,14 +363,16 @@ void submit_impl(nnap_server* s, int nslots, const int* ids, const double* const
         k_fill_cells<<<(nb_atoms + 255) / 256, 256, 0, st>>>(h->cell_of.p, nb_atoms, h->cell_start.p,
                                                              h->cell_fill.p, h->cell_atoms.p);
         k_sort_cells<<<(B.ncells * 32 + 255) / 256, 256, 0, st>>>(h->cell_start.p, B.ncells, h->cell_atoms.p);
+        k_cell_order<<<(nb_atoms + 255) / 256, 256, 0, st>>>(h->cell_atoms.p, nb_atoms, h->xf.p, h->xlo.p, h->xfc.p,
+                                                             h->xloc.p);
         const int nw = h->tune.nb_warps;
         k_neighbors<<<(nb_atoms + nw - 1) / nw, 32 * nw, 0, st>>>(
-            s->sdev_build.p, sid, h->xw.p, h->xf.p, h->xlo.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p,
-            nb_atoms, pair_bufs(h), h->status.p, h->status.p + 1);
+            s->sdev_build.p, sid, h->xw.p, h->xf.p, h->xlo.p, h->xfc.p, h->xloc.p, h->cell_of.p, h->cell_start.p,
+            h->cell_atoms.p, nb_atoms, pair_bufs(h), h->status.p, h->status.p + 1);
         k_verlet_store<<<(unsigned)(((size_t)nb_atoms * 32 + 127) / 128), 128, 0, st>>>(s->dslots.p, sid,
                                                                                        pair_bufs(h), nb_atoms,
                                                                                        s->kw.p);
-        h->launches += 6;
+        h->launches += 7;
     }
     if (N > 0) {
         k_filter<<<(N + kFilterWarps - 1) / kFilterWarps, 32 * kFilterWarps, 0, st>>>(
