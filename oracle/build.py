@@ -5,7 +5,7 @@ TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).
 * ``build_oracle()``  compiles ``nnap_oracle.cpp`` (FP64, no fast-math, no FMA contraction)
   into ``oracle/liboracle.so``.
 * ``expand_ref(model)`` expands the reference's headers for one model shape from a
-  reference checkout (``$JSE_REFERENCE`` or ``/root/reference``) into
+  reference checkout (``$JSE_REFERENCE``, else a ``reference`` folder beside the repository) into
   ``oracle/_ref/<shape>/src`` with :mod:`oracle.nnapgen`.  This needs the checkout and
   therefore only runs where it exists; the expanded sources travel with the tree.
 * ``build_ref(shape)`` compiles an expanded shape with ``ref_driver.cpp`` into
@@ -27,8 +27,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 
 
+def reference_root() -> str:
+    """The reference checkout: ``$JSE_REFERENCE``, else a ``reference`` folder beside this
+    repository."""
+    return os.environ.get("JSE_REFERENCE",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
+
+
 def reference_src_dir() -> str:
-    root = os.environ.get("JSE_REFERENCE", "/root/reference")
+    root = reference_root()
     return os.path.join(root, "src", "nnap", "resources", "assets", "nnap", "src")
 
 

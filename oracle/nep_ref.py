@@ -19,15 +19,14 @@ from typing import Optional
 import numpy as np
 
 from . import nepgen
-from .build import REF_OUT
+from .build import REF_OUT, reference_root
 from .nep_model import NEPModel
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def nep_src_dir() -> str:
-    root = os.environ.get("JSE_REFERENCE", "/root/reference")
-    return os.path.join(root, "src", "nep", "resources", "assets", "nep", "src")
+    return os.path.join(reference_root(), "src", "nep", "resources", "assets", "nep", "src")
 
 
 def shape_key(m: NEPModel) -> str:

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the reference's own arithmetic.
 
 Run from the repository root, where a reference checkout is available
-(``$JSE_REFERENCE`` or ``/root/reference``):
+(``$JSE_REFERENCE``, else a ``reference`` folder beside the repository):
 
     python -m tests.golden.make_golden
 

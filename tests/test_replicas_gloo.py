@@ -55,3 +55,47 @@ def test_single_process_needs_no_group():
     assert shard([1, 2, 3], 0, 1) == [1, 2, 3]
     with pytest.raises(ValueError):
         shard([1], 2, 2)
+
+
+def _shard_worker(rank, world, port, out):
+    """Each rank evaluates its shard of a batch of independent structures (FP64 oracle) and
+    the shards' energies and forces are gathered on every rank."""
+    import numpy as np
+    from jse_gb300 import workloads as W
+    from oracle import model as OM, native as ON
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        structs = W.c4_structures(count=10, seed=13)
+        pm = OM.load(W.model_for("c4"))
+        ids = shard(list(range(len(structs))), rank, world)
+        mine = {k: ON.compute(pm, structs[k].x, structs[k].types, structs[k].box_kind, structs[k].box)
+                for k in ids}
+        mine = {k: (v["energy"], np.asarray(v["forces"])) for k, v in mine.items()}
+        gathered = [None] * world
+        dist.all_gather_object(gathered, mine)
+        if rank == 0:
+            out["all"] = {k: v for part in gathered for k, v in part.items()}
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_ranks_shard_a_batch_like_one_rank():
+    """Sharding a batch of independent structures over two ranks evaluates every structure
+    once and gives exactly the single-process results (no data collective is involved)."""
+    import numpy as np
+    from jse_gb300 import workloads as W
+    from oracle import model as OM, native as ON
+    world = 2
+    mgr = mp.get_context("spawn").Manager()
+    out = mgr.dict()
+    mp.start_processes(_shard_worker, args=(world, _free_port(), out), nprocs=world, start_method="spawn", join=True)
+    got = dict(out["all"])
+    structs = W.c4_structures(count=10, seed=13)
+    pm = OM.load(W.model_for("c4"))
+    assert sorted(got) == list(range(len(structs)))
+    for k, s in enumerate(structs):
+        r = ON.compute(pm, s.x, s.types, s.box_kind, s.box)
+        assert got[k][0] == r["energy"]
+        assert np.array_equal(got[k][1], r["forces"])
