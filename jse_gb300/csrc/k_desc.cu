@@ -589,18 +589,55 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
         sNp[q] = a.nz_p[q];
         sNw[q] = a.nz_w[q];
     }
+    // fuse rows with their one nonzero in column p mod N1: alpha[tc][tn][p] in shared memory
+    const bool diag = a.fwd_alpha != nullptr && T <= kFwdTypes;
+    const int nal = diag ? T * kFwdTypes * NP : 0;
+    float* sAl = smem + ((2 * ntab + 3) & ~3);
+    for (int q = threadIdx.x; q < nal; q += blockDim.x) sAl[q] = a.fwd_alpha[q];
     __syncthreads();
     const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * (blockDim.x >> 5) + wl;
     const int s0 = a.range[a.t0], s1 = a.range[a.t1];
     if (s0 + w >= s1) return;
-    float* sGh = smem + ((2 * ntab + 3) & ~3) + (size_t)wl * (T * S::K * S::N1P + S::SCR);  // [T][K][N1P]
+    float* sGh = sAl + ((nal + 3) & ~3) + (size_t)wl * (T * S::K * S::N1P + S::SCR);  // [T][K][N1P]
     float* scr = sGh + T * S::K * S::N1P;   // G [NP][K], then the Legendre columns [NT][32]
     const int at = a.perm[s0 + w];
     const int tc = a.type[at] - 1;
     const int M = a.P.M, cnt = min(a.P.count[at], M);
     const float rc = a.rcut, irc = 1.f / a.rcut;
-    {
+    if (diag) {
+        // Gh[tn][lm][n] = sum over p = n mod N1 of alpha[tc][tn][p] G[p][lm], with
+        // G[p][lm] = 2 * 4pi/(2l+1) * dE/dfp[p][l] * A[p][lm] held in registers: lanes over lm
+        const float* Ain = a.A + (size_t)w * NP * S::K;
+        const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
+        const float* al = sAl + (size_t)tc * kFwdTypes * NP;
+        for (int lm = lane; lm < S::K; lm += 32) {
+            int l = 0;
+            while ((l + 1) * (l + 1) <= lm) ++l;
+            const float coef = l < a.nl2 ? 2.f * kPi4 / (float)(2 * l + 1) : 0.f;
+            const int lc = l < a.nl2 ? l : 0;
+            float g[NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                g[p] = coef * gf[p * a.sl + lc] * Ain[p * S::K + lm];
+                if (a.Gx) g[p] += a.Gx[(size_t)w * NP * S::K + p * S::K + lm];
+            }
+            for (int tn = 0; tn < T; ++tn) {
+                float v[S::N1P];
+#pragma unroll
+                for (int n = 0; n < S::N1P; ++n) {
+                    v[n] = 0.f;
+#pragma unroll
+                    for (int p = n; p < NP; p += N1)
+                        if (n < N1) v[n] += al[tn * NP + p] * g[p];
+                }
+                float4* out = reinterpret_cast<float4*>(sGh + (size_t)(tn * S::K + lm) * S::N1P);
+#pragma unroll
+                for (int q = 0; q < S::N1P / 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+        }
+        __syncwarp();
+    } else {
         // G[p][lm] = 2 * 4pi/(2l+1) * dE/dfp[p][l] * A[p][lm], transposed into scr
         const float* Ain = a.A + (size_t)w * NP * S::K;
         const float* gf = a.gfp + (size_t)(s0 + w) * a.fp_stride + a.fp_off;
@@ -712,7 +749,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
         };
         const float cp = an.cp, sp = an.sp;
         float gth = 0.f, gph = 0.f;
-#pragma unroll 1
+#pragma unroll
         for (int l = 0; l <= L; ++l) {
             const int c0 = l * l + l, tl = l * (l + 1) / 2;
             const float p0 = sP[tl * 32 + lane];
@@ -721,7 +758,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
             gth += row(c0, p0) * (0.5f * (c_dup[tl] + c_ddn[tl]) * p1);
             float cmm = 1.f, cmv = cp, smm = 0.f, smv = sp;
             float pmm = p0, pmv = p1;
-#pragma unroll 1
+#pragma unroll
             for (int m = 1; m <= l; ++m) {
                 const int t = tl + m;
                 const float pmp = m + 1 <= l ? sP[(t + 1) * 32 + lane] : 0.f;
@@ -1038,7 +1075,8 @@ cudaError_t launch_sph_bwd_n(const DescArgs& a, cudaStream_t st) {
     using S = SphNShape<L, NP, N1>;
     const int wpc = a.warps;
     const int grid = (a.nmax + wpc - 1) / wpc;
-    const size_t sm = sizeof(float) * (((size_t)2 * a.T * a.T * N1 * kNz + 3) / 4 * 4 +
+    const size_t nal = (a.fwd_alpha && a.T <= kFwdTypes) ? (size_t)a.T * kFwdTypes * NP : 0;
+    const size_t sm = sizeof(float) * (((size_t)2 * a.T * a.T * N1 * kNz + 3) / 4 * 4 + (nal + 3) / 4 * 4 +
                                        (size_t)wpc * S::warp_floats(a.T));
     if (sm > 227 * 1024) return cudaErrorInvalidValue;
     static int lim = 0;
