@@ -132,6 +132,9 @@ struct Run {
     // per sub: alpha[tc][tn][p] of the radial-space forward ([T][kFwdTypes][NP]), empty
     // unless every row p of W has its only nonzero in column p mod N1, N1 < NP, T <= kFwdTypes
     std::vector<DevBuf<float>> falpha;
+    // per sub: the forward may run on the tensor cores (falpha present, every |alpha| at
+    // most kTcAlphaMax); used in mixed precision
+    std::vector<char> tc_fwd;
     // per sub: invariant-column terms (indices into A, -1 past the order; coefficients)
     // and each column's first term, [ninv + 1]
     std::vector<DevBuf<int4>> inv_idx;
@@ -169,6 +172,9 @@ struct Outputs {
 struct nnap_handle {
     nnapgb::Model model;
     int precision = NNAP_PREC_FP32;
+    // descriptors on the FP32 pipe even in mixed precision (set while training gradients,
+    // which are FP32 whatever the handle's precision)
+    bool fp32_desc = false;
     bool net_tc = false;  // networks on the tensor cores (mixed precision, SiLU networks)
     std::string net_notes;  // species whose network runs the FP32 kernel on a mixed handle, and why
     int device = 0;

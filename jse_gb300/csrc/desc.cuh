@@ -45,6 +45,11 @@ struct DescArgs {
     // NEP type-wise cutoffs: (rc, 1/rc) of each species pair, [T][T] centre species major,
     // or NULL: every pair uses rcut
     const float2* pair_rc = nullptr;
+    // spherical forward on the tensor cores: the device's SM count when the evaluation may
+    // use them (mixed precision), else 0; err receives ERRBIT_TIMEOUT if one of the
+    // kernel's bounded waits gives up
+    int tc_sms = 0;
+    int* err = nullptr;
 };
 
 // Invariant (l3max / l4max) columns of one spherical sub-basis over a run of species:
@@ -79,6 +84,7 @@ cudaError_t launch_invariants_wgrad(const InvArgs& a, cudaStream_t st);
 
 constexpr int kNz = 4;        // nonzero rows per column (or columns per row) of a fuse matrix in sparse form
 constexpr int kFwdTypes = 3;  // most species for the radial-space forward (per-species accumulators)
+constexpr float kTcAlphaMax = 1024.f;  // largest |alpha| the tensor-core forward takes (FP16 operand range)
 
 // Compiled shapes.  Radial: (NP, N1).  Spherical: (L, NP, N1).
 #define NNAP_RADIAL_SHAPES(X) X(11, 11) X(12, 6) X(4, 4) X(8, 4) X(12, 4) X(18, 9)

@@ -19,13 +19,15 @@
 // forward lanes first evaluate one neighbour each into a shared-memory tile, then own
 // columns lm of the P x K accumulator A; backward lanes own one neighbour each and
 // stream G = dE/dA from shared memory.  The radial-fuse matrices of the basis live in
-// shared memory for the whole block.
+// shared memory for the whole block.  In mixed precision the spherical forward of the
+// one-nonzero-per-row fuse matrices runs on the tensor cores (k_sph_tc.cuh).
 #include <math_constants.h>
 
 #include "common.cuh"
 #include "pdl.cuh"
 #include "desc.cuh"
 #include "sph_math.cuh"
+#include "k_sph_tc.cuh"
 
 namespace nnapgb {
 
@@ -1113,7 +1115,11 @@ cudaError_t launch_sph(const DescArgs& a, bool fwd, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     if constexpr (RB == kRbNNAP) {   // the radial-space kernels are written for the NNAP radial functions
         if (!fwd && a.nz_p && a.nz_w && N1 < NP) return launch_sph_bwd_n<L, NP, N1>(a, st);
-        if (fwd && a.fwd_alpha && N1 < NP && a.T <= kFwdTypes) return launch_sph_fwd_n<L, NP, N1>(a, st);
+        if (fwd && a.fwd_alpha && N1 < NP && a.T <= kFwdTypes) {
+            if constexpr (SphTcShape<L, NP>::fits)
+                if (a.tc_sms > 0) return launch_sph_fwd_tc<L, NP, N1>(a, st);
+            return launch_sph_fwd_n<L, NP, N1>(a, st);
+        }
     }
     const int wpc = a.warps;
     const int grid = (n + wpc - 1) / wpc;

@@ -64,7 +64,9 @@ __global__ void k_lmp_rows(int inum, int nall, const int* __restrict__ ilist, co
             if (pos < M) {
                 const size_t q = (size_t)ii * M + pos;
                 P.key[q] = pair_key(j, pack_img(0, 0, 0));
-                P.dx[q] = make_float4((float)dx, (float)dy, (float)dz, __int_as_float(type[j]));
+                const int tj = type[j];
+                if (tj < 1 || tj > ntypes) atomicOr(err, ERRBIT_BAD_TYPE);
+                P.dx[q] = make_float4((float)dx, (float)dy, (float)dz, __int_as_float(min(max(tj, 1), ntypes)));
                 if (P.dxlo)
                     P.dxlo[q] = make_float4((float)(dx - (double)(float)dx), (float)(dy - (double)(float)dy),
                                             (float)(dz - (double)(float)dz), 0.f);

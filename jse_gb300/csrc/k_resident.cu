@@ -51,7 +51,7 @@ __global__ void k_wrap_resident(const StructDev* __restrict__ S, const int* __re
     to_cartesian(st, p);
     xw[3 * i] = p[0]; xw[3 * i + 1] = p[1]; xw[3 * i + 2] = p[2];
     const float hx = (float)p[0], hy = (float)p[1], hz = (float)p[2];
-    xf[i] = make_float4(hx, hy, hz, __int_as_float(t));
+    xf[i] = make_float4(hx, hy, hz, __int_as_float(min(max(t, 1), ntypes)));  // clamped as in k_wrap_bin
     xlo[i] = make_float4((float)ds(p[0], (double)hx), (float)ds(p[1], (double)hy), (float)ds(p[2], (double)hz), 0.f);
     kw[i] = make_int4(k[0], k[1], k[2], 0);
 }

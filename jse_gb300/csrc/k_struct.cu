@@ -43,7 +43,9 @@ __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restric
     to_cartesian(st, p);
     xw[3 * i] = p[0]; xw[3 * i + 1] = p[1]; xw[3 * i + 2] = p[2];
     const float hx = (float)p[0], hy = (float)p[1], hz = (float)p[2];
-    xf[i] = make_float4(hx, hy, hz, __int_as_float(t));
+    // the species the pair rows carry, clamped into 1..ntypes: a bad species fails the call
+    // (ERRBIT_BAD_TYPE) and indexes nothing out of range meanwhile
+    xf[i] = make_float4(hx, hy, hz, __int_as_float(min(max(t, 1), ntypes)));
     // x = hi + lo exactly to 48 bits: the float-float form used by the neighbour test
     xlo[i] = make_float4((float)ds(p[0], (double)hx), (float)ds(p[1], (double)hy), (float)ds(p[2], (double)hz), 0.f);
     double f[3] = {p[0], p[1], p[2]};

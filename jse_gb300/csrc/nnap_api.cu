@@ -133,10 +133,13 @@ void upload_model(nnap_handle* h) {
                                 else if (v != 0.f) { diag = false; break; }
                             }
                 r.falpha.emplace_back();
+                bool tc = diag;
                 if (diag) {
                     r.falpha.back().ensure(al.size());
                     CK(cudaMemcpy(r.falpha.back().p, al.data(), al.size() * sizeof(float), cudaMemcpyHostToDevice));
+                    for (float v : al) tc = tc && std::fabs(v) <= kTcAlphaMax;
                 }
+                r.tc_fwd.push_back(tc);
             }
             // a spherical sub-basis after the first, on the channel-space kernels, with a cutoff
             // well inside the neighbour cutoff scans compact rows (one such cutoff per model)
@@ -605,6 +608,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
                 a.nz_p = r.nzp[k].p;
                 a.nz_w = r.nzw[k].p;
                 a.fwd_alpha = r.falpha[k].p;
+                a.tc_sms = (fwd && h->precision == NNAP_PREC_MIXED && !h->fp32_desc && r.tc_fwd[k]) ? h->sm_count : 0;
+                a.err = h->status.p;
                 a.nl2 = s.nl2;
                 a.sl = s.nl2 + s.ninv;
                 a.sub_dx = nullptr;
@@ -761,7 +766,7 @@ std::vector<long long> layout_key(nnap_handle* h, const Batch& B, const double* 
     std::vector<long long> k = {B.nstruct, B.natoms, B.ncells, h->M, (long long)(intptr_t)d_x,
                                 (long long)(intptr_t)d_type, fp_only ? 1 : 0, h->profiling ? 1 : 0,
                                 h->tune.desc_fwd_warps, h->tune.desc_bwd_warps, h->tune.nb_warps,
-                                h->tune.gather_block, h->tune.net_split};
+                                h->tune.gather_block, h->tune.net_split, h->fp32_desc ? 1 : 0};
     for (auto& s : B.sd) {
         k.push_back(s.n);
         k.push_back(s.kind);

@@ -430,6 +430,11 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, B.natoms, x, type);
+        struct Fp32Desc {  // FP32 descriptors for the gradients, restored on every exit
+            nnap_handle* h;
+            ~Fp32Desc() { h->fp32_desc = false; }
+        } fp32_guard{h};
+        h->fp32_desc = true;
         evaluate(h, B, h->x.p, h->type.p, true);
         train_enqueue(h, B, bgrad_energies, bgrad_forces, bgrad_virial, want_w);
         int Ptot = 0;

@@ -62,6 +62,21 @@ def test_descriptors_fp32(golden):
     assert (np.abs(fp[:, :D] - golden.fp) / scale).max() <= 1e-4
 
 
+def test_descriptors_mixed(golden):
+    """Mixed precision: spherical descriptors of fuse matrices with one nonzero per row come
+    from the tensor cores (FP16 hi + lo operands, three products, FP32 accumulation); they
+    keep the FP32 bound against the reference and agree with the FP32 kernels to 1e-5 of
+    each column's scale."""
+    with _nnap(golden.model_json, "mixed") as p:
+        fp = p.calFp(_S(golden))
+    with _nnap(golden.model_json) as p:
+        fp32 = p.calFp(_S(golden))
+    D = golden.fp.shape[1]
+    scale = np.maximum(np.abs(golden.fp).max(0), 1e-6)
+    assert (np.abs(fp[:, :D] - golden.fp) / scale).max() <= 1e-4
+    assert (np.abs(fp[:, :D] - fp32[:, :D]) / scale).max() <= 1e-5
+
+
 def test_results_are_deterministic(golden):
     with _nnap(golden.model_json) as p:
         a = p.calEnergyForceVirials(_S(golden))
