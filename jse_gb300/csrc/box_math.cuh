@@ -64,6 +64,25 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
 }
+// The image shift (na*a + nb*b) + nc*c as a float-float pair hi + lo, from the box rows
+// in float-float form (a = fa + la to about 48 bits): exact products of the float parts
+// (FMA residuals), their sum by two-sums, and the low parts added in FP32.  hi + lo is
+// within about 2^-45 of the shift's magnitude, on the FP32 pipe; zero for the zero image.
+__device__ __forceinline__ void image_shift_ff(const StructDev& S, int na, int nb, int nc, float hi[3], float lo[3]) {
+    const float xa = (float)na, xb = (float)nb, xc = (float)nc;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float p1 = xa * S.fa[d], e1 = fmaf(xa, S.fa[d], -p1);
+        const float p2 = xb * S.fb[d], e2 = fmaf(xb, S.fb[d], -p2);
+        const float p3 = xc * S.fc[d], e3 = fmaf(xc, S.fc[d], -p3);
+        float s1, t1, s2, t2;
+        two_sum(p1, p2, s1, t1);
+        two_sum(s1, p3, s2, t2);
+        const float l = ((t1 + t2) + ((e1 + e2) + e3)) + ((xa * S.la[d] + xb * S.lb[d]) + xc * S.lc[d]);
+        two_sum(s2, l, hi[d], lo[d]);
+    }
+}
+
 // hi + lo += v
 __device__ __forceinline__ void ff_acc(float& hi, float& lo, float v) {
     float s, e;

@@ -157,16 +157,16 @@ __global__ void __launch_bounds__(256) k_cell_order(const int* __restrict__ cell
     xloc[k] = xlo[a];
 }
 
-__global__ void __launch_bounds__(32 * kNbMaxWarps)
+__global__ void __launch_bounds__(32 * kNbMaxWarps, 4)
 k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ xw,
             const float4* __restrict__ xf, const float4* __restrict__ xlo, const float4* __restrict__ xfc,
             const float4* __restrict__ xloc, const int* __restrict__ cell_of, const int* __restrict__ cell_start,
             const int* __restrict__ cell_atoms, int n, PairBufs P, int* __restrict__ err,
             int* __restrict__ max_count) {
     pdl_enter();
-    __shared__ int s_incl[kNbMaxWarps][32], s_start[kNbMaxWarps][32];
+    __shared__ int s_base[kNbMaxWarps][32];     // per cell slot: cell-order start minus candidate start
+    __shared__ int s_slot_at[kNbMaxWarps][32];  // cell slot starting at each position of a window
     __shared__ uint32_t s_img[kNbMaxWarps][32];
-    __shared__ double s_sh[kNbMaxWarps][32][3];
     __shared__ float s_fsh[kNbMaxWarps][32][3], s_flo[kNbMaxWarps][32][3];
     __shared__ int s_acc[kNbMaxWarps][32];  // accepted entries per cell-offset group of the batch
     __shared__ int s_qj[kNbMaxWarps][64];   // candidates passing the FP32 screen: atom, cell slot,
@@ -181,7 +181,6 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     const int ci0 = cl % st.nc[0], ci1 = (cl / st.nc[0]) % st.nc[1], ci2 = cl / (st.nc[0] * st.nc[1]);
     const int wa = 2 * st.R[0] + 1, wb = 2 * st.R[1] + 1;
     const int noff = wa * wb * (2 * st.R[2] + 1);
-    const double xi = xw[3 * i], yi = xw[3 * i + 1], zi = xw[3 * i + 2];
     const float4 fi = xf[i];
     const float4 li = xlo[i];
 
@@ -193,7 +192,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         const int o = o0 + lane;
         const int cnt0 = cnt;
         s_acc[w][lane] = 0;
-        int ccount = 0;
+        int ccount = 0, cs = 0;
         if (o < noff) {
             const int oa = o % wa - st.R[0], ob = (o / wa) % wb - st.R[1], oc = o / (wa * wb) - st.R[2];
             const int q0 = ci0 + oa, q1 = ci1 + ob, q2 = ci2 + oc;
@@ -202,7 +201,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             const int nc = (q2 >= 0) ? q2 / st.nc[2] : -((-q2 + st.nc[2] - 1) / st.nc[2]);
             const int c0 = q0 - na * st.nc[0], c1 = q1 - nb * st.nc[1], c2 = q2 - nc * st.nc[2];
             const int cid = st.c0 + c0 + st.nc[0] * (c1 + st.nc[1] * c2);
-            const int cs = cell_start[cid];
+            cs = cell_start[cid];
             ccount = cell_start[cid + 1] - cs;
             if (st.kind == 0) {
                 // orthogonal box: a lower bound of the distance from atom i to the target
@@ -230,16 +229,15 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 }
                 if (st.smin2 * g2 > st.rc2_hi) ccount = 0;
             }
-            s_start[w][lane] = cs;
             s_img[w][lane] = pack_img(na, nb, nc);
-            double sh[3] = {0.0, 0.0, 0.0};  // the zero image has an exactly zero shift
-            if (na | nb | nc) image_shift(st, na, nb, nc, sh);
+            // the image shift as float-float on the FP32 pipe (the exact test forms the FP64
+            // shift itself); the zero image has an exactly zero shift
+            float hi[3], lo[3];
+            image_shift_ff(st, na, nb, nc, hi, lo);
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                const float h = (float)sh[d];
-                s_sh[w][lane][d] = sh[d];
-                s_fsh[w][lane][d] = h;
-                s_flo[w][lane][d] = (na | nb | nc) ? (float)ds(sh[d], (double)h) : 0.f;
+                s_fsh[w][lane][d] = hi[d];
+                s_flo[w][lane][d] = lo[d];
             }
         }
         int incl = ccount;
@@ -248,8 +246,9 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             int u = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += u;
         }
-        s_incl[w][lane] = incl;
         const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const int before = incl - ccount;  // candidates of the earlier cell slots
+        s_base[w][lane] = cs - before;
         __syncwarp();
         // Candidates are screened 32 at a time in FP32; the ones that pass (about one in four
         // or five) queue in candidate order in shared memory and take the exact test 32 at a
@@ -288,9 +287,13 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 if (fabsf(diff) > tol) {
                     acc = diff < 0.f;
                 } else {  // within 1e-10 of the cutoff: the exact FP64 test
-                    const double dxv = ds(da(xw[3 * j], s_sh[w][slot][0]), xi);
-                    const double dyv = ds(da(xw[3 * j + 1], s_sh[w][slot][1]), yi);
-                    const double dzv = ds(da(xw[3 * j + 2], s_sh[w][slot][2]), zi);
+                    int na, nb, nc;
+                    unpack_img(s_img[w][slot], na, nb, nc);
+                    double sh[3] = {0.0, 0.0, 0.0};
+                    if (na | nb | nc) image_shift(st, na, nb, nc, sh);
+                    const double dxv = ds(da(xw[3 * j], sh[0]), xw[3 * i]);
+                    const double dyv = ds(da(xw[3 * j + 1], sh[1]), xw[3 * i + 1]);
+                    const double dzv = ds(da(xw[3 * j + 2], sh[2]), xw[3 * i + 2]);
                     acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
                 }
                 two_sum(dh[0], dl[0], ox, lx);
@@ -311,19 +314,24 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             }
             cnt += __popc(m);
         };
+        // The cell slot of candidate cidx: the last nonempty slot starting at or before it.
+        // Per window of 32 candidates the starting positions form a bit mask (one OR
+        // reduction); a lane takes the highest start at or below its position, or the slot
+        // that ran into the window from the one before.
+        int carry = 0;
         for (int cb = 0; cb < total; cb += 32) {
             const int cidx = cb + lane;
+            const bool starts = ccount > 0 && before >= cb && before < cb + 32;
+            const unsigned smask = __reduce_or_sync(0xffffffffu, starts ? 1u << (before - cb) : 0u);
+            if (starts) s_slot_at[w][before - cb] = lane;
+            __syncwarp();
+            const unsigned mine = smask & (0xffffffffu >> (31 - lane));
+            const int slot = mine ? s_slot_at[w][31 - __clz(mine)] : carry;
+            carry = __shfl_sync(0xffffffffu, slot, 31);
             bool pass = false;
-            int j = 0, slot = 0, kp = 0;
+            int j = 0, kp = 0;
             if (cidx < total) {
-                int lo = 0, hi = 31;  // first slot with incl > cidx
-                while (lo < hi) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_incl[w][mid] > cidx) hi = mid; else lo = mid + 1;
-                }
-                slot = lo;
-                const int before = slot ? s_incl[w][slot - 1] : 0;
-                kp = s_start[w][slot] + (cidx - before);
+                kp = s_base[w][slot] + cidx;
                 j = cell_atoms[kp];
                 const float4 fj = xfc[kp];  // independent of the load of j
                 if (!(j == i && s_img[w][slot] == pack_img(0, 0, 0))) {
