@@ -567,7 +567,9 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd(DescArgs a) {
 //   v_n   = sum_p W[p][n] dc_p = sum_lm Gh[tn][lm][n] Y_lm,
 // so the per-neighbour products run over N1 instead of NP channels, and c, dc are never
 // formed.  Y and dY/dtheta are formed row by row from the lane's Legendre column in
-// shared memory with cos/sin(m phi) recurrences, instead of being stored.
+// shared memory with cos/sin(m phi) recurrences, instead of being stored.  The Gh rows of
+// m != 0 are stored times sqrt2 (the factor of those Y_lm) and the Chebyshev values times
+// fc, so the per-neighbour loop multiplies by neither.
 template <int L, int NP, int N1>
 struct SphNShape {
     static constexpr int K = (L + 1) * (L + 1);
@@ -633,9 +635,11 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
                     for (int p = n; p < NP; p += N1)
                         if (n < N1) v[n] += al[tn * NP + p] * g[p];
                 }
+                const float rs = lm != l * l + l ? kSqrt2 : 1.f;  // rows m != 0 carry sqrt2
                 float4* out = reinterpret_cast<float4*>(sGh + (size_t)(tn * S::K + lm) * S::N1P);
 #pragma unroll
-                for (int q = 0; q < S::N1P / 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                for (int q = 0; q < S::N1P / 4; ++q)
+                    out[q] = make_float4(rs * v[4 * q], rs * v[4 * q + 1], rs * v[4 * q + 2], rs * v[4 * q + 3]);
             }
         }
         __syncwarp();
@@ -674,14 +678,17 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
                     }
                 }
             }
+            int l = 0;
+            while ((l + 1) * (l + 1) <= lm) ++l;
+            const float rs = lm != l * l + l ? kSqrt2 : 1.f;  // rows m != 0 carry sqrt2
             float4* out = reinterpret_cast<float4*>(sGh + (size_t)idx * S::N1P);
 #pragma unroll
-            for (int q = 0; q < S::N1P / 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            for (int q = 0; q < S::N1P / 4; ++q)
+                out[q] = make_float4(rs * v[4 * q], rs * v[4 * q + 1], rs * v[4 * q + 2], rs * v[4 * q + 3]);
         }
         __syncwarp();
     }
     float* sP = scr;  // [NT][32], one Legendre column per lane
-    const float r2 = 1.41421356237309515f;
     constexpr int H2 = S::N1P / 2;
     for (int base = 0; base < cnt; base += 32) {
         const int k = base + lane;
@@ -711,7 +718,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
         float2 T2[H2], v2[H2];
 #pragma unroll
         for (int h = 0; h < H2; ++h) {
-            T2[h] = make_float2(Tn[2 * h], Tn[2 * h + 1]);
+            T2[h] = make_float2(fc * Tn[2 * h], fc * Tn[2 * h + 1]);
             v2[h] = make_float2(0.f, 0.f);
         }
         const float* gh = sGh + (size_t)tn * S::K * S::N1P;
@@ -747,7 +754,7 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
                     v2[n >> 1].x = fmaf(g, y, v2[n >> 1].x);
                 }
             }
-            return fc * ((da.x + db.x) + (da.y + db.y));
+            return (da.x + db.x) + (da.y + db.y);
         };
         const float cp = an.cp, sp = an.sp;
         float gth = 0.f, gph = 0.f;
@@ -765,10 +772,10 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
                 const int t = tl + m;
                 const float pmp = m + 1 <= l ? sP[(t + 1) * 32 + lane] : 0.f;
                 const float dpt = 0.5f * (c_dup[t] * pmp - c_ddn[t] * pmm);
-                const float yp = r2 * pmv * cmv, ym = r2 * pmv * smv;
+                const float yp = pmv * cmv, ym = pmv * smv;  // Y / sqrt2 (the Gh rows carry sqrt2)
                 const float dYp = row(c0 + m, yp);
                 const float dYm = row(c0 - m, ym);
-                gth += r2 * dpt * (dYp * cmv + dYm * smv);
+                gth += dpt * (dYp * cmv + dYm * smv);
                 gph += (float)m * (dYm * yp - dYp * ym);
                 const float cn = 2.f * cp * cmv - cmm, sn = 2.f * cp * smv - smm;
                 cmm = cmv; cmv = cn; smm = smv; smv = sn;
@@ -781,13 +788,14 @@ __global__ void __launch_bounds__(32 * kDescMaxWarps, 2) k_sph_bwd_n(DescArgs a)
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (valid) {
                 const float fcg = 8.f * fc1 * fc2 * irc * irc;
-                float TG[N1];
+                float TG[N1], Tr[N1];  // T_n formed again: fc T_n went into the row products
                 cheby_grad_f<N1>(x, 2.f / (r * rc), TG);
+                cheby_f<N1>(x, Tr);
                 float dfc = 0.f, drn = 0.f;
 #pragma unroll
                 for (int n = 0; n < N1; ++n) {
                     const float vn = (n & 1) ? v2[n >> 1].y : v2[n >> 1].x;
-                    dfc += vn * Tn[n];
+                    dfc += vn * Tr[n];
                     drn += vn * TG[n];
                 }
                 const float gr = dfc * fcg + fc * drn;

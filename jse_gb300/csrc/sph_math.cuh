@@ -44,6 +44,7 @@ cudaError_t upload_sh_tables() {
 }
 
 constexpr float kPi4 = 12.566370614359172f;
+constexpr float kSqrt2 = 1.41421356237309515f;
 
 __host__ __device__ constexpr int tri(int l, int m) { return l * (l + 1) / 2 + m; }
 
