@@ -167,10 +167,10 @@ def load_traffic():
     (dram__bytes_read.sum + dram__bytes_write.sum of one launch divided by its atoms):
     liquid32k / descriptors_bwd is k_sph_bwd_n<6,18,9> on the 32000-atom liquid, 159.2 MB
     read + 16.9 MB written (profiles/k_sph_liquid32k.md); batch1024 / descriptors_bwd is the
-    same kernel over the 1024-structure batch, 2627.3 MB read + 442.8 MB written for 526124
-    atoms (profiles/batch1024_launches_and_k_sph_bwd_n.md)."""
+    same kernel over the 1024-structure batch, 2626.6 MB read + 443.2 MB written for 526124
+    atoms (profiles/batch1024_launches_and_top_kernels.md)."""
     return {"liquid32k/descriptors_bwd": (159.2e6 + 16.9e6) / 32000,
-            "batch1024/descriptors_bwd": (2627.281e6 + 442.828e6) / 526124}
+            "batch1024/descriptors_bwd": (2626.569e6 + 443.240e6) / 526124}
 
 
 # ----------------------------------------------------------------------------- reference arm

@@ -53,7 +53,10 @@ struct SphTcShape {
     static constexpr int OPS = kFwdTcWarps * WARP_BYTES > A2_BYTES ? kFwdTcWarps * WARP_BYTES : A2_BYTES;
     // at least 46 KB, so that at most four CTAs (4 x 128 TMEM columns) share an SM
     static constexpr int SMEM = AL_BYTES + OPS > 47104 ? AL_BYTES + OPS : 47104;
-    static constexpr bool fits = KM <= 64 && NPN <= 32;
+    // lmax 6 or 7: the tile's 64 rows are mostly in use.  Below that the FP32-pipe kernel,
+    // whose work scales with (L+1)^2, is faster (lmax 4, 131k-atom glass: 0.34 against
+    // 0.41 ms; lmax 6, 1024-structure batch: 2.41 against 2.08 ms on the tensor cores)
+    static constexpr bool fits = KM >= 49 && KM <= 64 && NPN <= 32;
 };
 
 __device__ __forceinline__ uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
