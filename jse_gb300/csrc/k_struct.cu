@@ -145,6 +145,16 @@ __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int
 // contiguous in memory.
 constexpr int kNbMaxWarps = 8;  // warps per CTA are a launch parameter (2, 4 or 8)
 
+// floor(a / b) for b >= 1 and |a| < 2^22, from a float reciprocal of b and one correction
+// step (the float quotient is within one of the true one).
+__device__ __forceinline__ int floor_div(int a, int b, float inv_b) {
+    int q = __float2int_rd((float)a * inv_b);
+    const int r = a - q * b;
+    if (r < 0) --q;
+    else if (r >= b) ++q;
+    return q;
+}
+
 // xfc[k] = xf[cell_atoms[k]], xloc[k] = xlo[cell_atoms[k]] for the n binned atoms.
 __global__ void __launch_bounds__(256) k_cell_order(const int* __restrict__ cell_atoms, int n,
                                                     const float4* __restrict__ xf, const float4* __restrict__ xlo,
@@ -194,11 +204,15 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         s_acc[w][lane] = 0;
         int ccount = 0, cs = 0;
         if (o < noff) {
-            const int oa = o % wa - st.R[0], ob = (o / wa) % wb - st.R[1], oc = o / (wa * wb) - st.R[2];
+            const float inv_wa = __frcp_rn((float)wa), inv_wb = __frcp_rn((float)wb);
+            const float inv_nc0 = __frcp_rn((float)st.nc[0]), inv_nc1 = __frcp_rn((float)st.nc[1]),
+                        inv_nc2 = __frcp_rn((float)st.nc[2]);
+            const int oab = floor_div(o, wa, inv_wa), ocr = floor_div(oab, wb, inv_wb);
+            const int oa = o - oab * wa - st.R[0], ob = oab - ocr * wb - st.R[1], oc = ocr - st.R[2];
             const int q0 = ci0 + oa, q1 = ci1 + ob, q2 = ci2 + oc;
-            const int na = (q0 >= 0) ? q0 / st.nc[0] : -((-q0 + st.nc[0] - 1) / st.nc[0]);
-            const int nb = (q1 >= 0) ? q1 / st.nc[1] : -((-q1 + st.nc[1] - 1) / st.nc[1]);
-            const int nc = (q2 >= 0) ? q2 / st.nc[2] : -((-q2 + st.nc[2] - 1) / st.nc[2]);
+            const int na = floor_div(q0, st.nc[0], inv_nc0);
+            const int nb = floor_div(q1, st.nc[1], inv_nc1);
+            const int nc = floor_div(q2, st.nc[2], inv_nc2);
             const int c0 = q0 - na * st.nc[0], c1 = q1 - nb * st.nc[1], c2 = q2 - nc * st.nc[2];
             const int cid = st.c0 + c0 + st.nc[0] * (c1 + st.nc[1] * c2);
             cs = cell_start[cid];
