@@ -139,6 +139,22 @@ class NNAPServer:
         self._nnap._check(self._L.nnap_server_submit(self._srv(), len(sl), _iptr(sl), ptrs, flags))
         self._pending = (len(sl), N, flags)
 
+    def submit_prepared(self, slots: np.ndarray, ptrs: np.ndarray, natoms: int, energies: bool = False,
+                        forces: bool = True, per_atom_virial: bool = False):
+        """:meth:`submit` for a caller that checked its position arrays once (at admission):
+        ``slots`` int32, ``ptrs`` the arrays' addresses (uintp), ``natoms`` their total
+        atom count.  Skips the per-array checks, which cost more than the launch for
+        hundreds of small structures."""
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        pa = np.ascontiguousarray(ptrs, dtype=np.uintp)
+        flags = WANT_ENERGY | WANT_VIRIAL
+        flags |= WANT_FORCES if forces else 0
+        flags |= WANT_ENERGIES if energies else 0
+        flags |= WANT_VIRIALS if per_atom_virial else 0
+        self._nnap._check(self._L.nnap_server_submit(self._srv(), len(sl), _iptr(sl),
+                                                     pa.ctypes.data_as(C.POINTER(C.POINTER(C.c_double))), flags))
+        self._pending = (len(sl), int(natoms), flags)
+
     def collect(self) -> dict:
         """Wait for the submitted step; outputs as :meth:`step`."""
         S, N, flags = self._pending
@@ -218,6 +234,8 @@ class Request:
     t_admit: float = float("nan")
     t_done: float = float("nan")
     t_ready: float = float("nan")
+    xptr: int = 0                         # address of x (set at admission; x is updated in place)
+    natoms: int = 0
     step_latency: List[float] = field(default_factory=list)
     energies: List[float] = field(default_factory=list)
     forces: List[np.ndarray] = field(default_factory=list)
@@ -226,11 +244,13 @@ class Request:
 class RequestLoop:
     """Continuous batching over an :class:`NNAPServer`.
 
-    Every loop turn admits the queued requests that fit (FIFO), submits one step over all
-    admitted requests and, while the GPU runs it, moves the positions of the requests
-    that continue and admits new arrivals (they join the next step); then it collects the
-    step and retires the requests that finished.  With nothing admitted, the loop sleeps
-    until the next arrival."""
+    Every loop turn has one step on the GPU.  While it runs, the loop moves the positions
+    of the requests that continue and admits new arrivals (FIFO, they join the next step).
+    When it completes, the finished requests release their slots, the next step (the
+    continuing and the newly admitted requests) is submitted at once, and only then does
+    the loop do the accounting of the step it collected, so the GPU does not wait for the
+    host's per-request work.  With nothing admitted, the loop sleeps until the next
+    arrival."""
 
     def __init__(self, server: NNAPServer, requests: Sequence[Request], moves=None, keep_results: bool = False):
         self.server = server
@@ -262,37 +282,63 @@ class RequestLoop:
                 queue.popleft()
                 r.slot, r.t_admit, r.t_ready = slot, now, now
                 r.x = np.array(r.structure.x, dtype=np.float64, order="C", copy=True)
+                r.xptr = r.x.ctypes.data
+                r.natoms = len(r.structure.types)
                 joined.append(r)
             return joined
 
-        joining: List[Request] = []
-        while pending or queue or active or joining:
-            active += joining
-            joining = []
-            active += admit(clock() - t0)
+        prepared = hasattr(srv, "submit_prepared")
+
+        def submit(batch):
+            if prepared:
+                srv.submit_prepared(np.fromiter((r.slot for r in batch), dtype=np.int32, count=len(batch)),
+                                    np.fromiter((r.xptr for r in batch), dtype=np.uintp, count=len(batch)),
+                                    sum(r.natoms for r in batch), forces=self.keep)
+            else:
+                srv.submit([r.slot for r in batch], [r.x for r in batch], forces=self.keep)
+
+        active: List[Request] = []   # the step in flight
+        joining: List[Request] = []  # admitted while it runs: they join the next step
+        while True:
             if not active:
-                if queue:
-                    raise RuntimeError("a queued request cannot be admitted into an empty server")
-                if pending:
+                active = joining + admit(clock() - t0)
+                joining = []
+                if not active:
+                    if queue:
+                        raise RuntimeError("a queued request cannot be admitted into an empty server")
+                    if not pending:
+                        break
                     time.sleep(max(0.0, pending[0].t_arrival - (clock() - t0)))
-                continue
-            srv.submit([r.slot for r in active], [r.x for r in active], forces=self.keep)
+                    continue
+                submit(active)
             # while the step runs: the next positions of the requests that continue, and
             # admissions of the requests that arrived meanwhile
             if self.moves is not None:
                 for r in active:
                     if r.done + 1 < r.nsteps:
                         self.moves.apply(r.rid, r.done + 1, r.x)
-            joining = admit(clock() - t0)
+            joining += admit(clock() - t0)
             out = srv.collect()
             t = clock() - t0
             steps += 1
             max_active = max(max_active, len(active))
+            # the next step goes to the GPU before this one's accounting: the finished
+            # requests release their slots, arrivals are admitted, and the rest continue
+            nxt = []
+            for r in active:
+                if r.done + 1 < r.nsteps:
+                    nxt.append(r)
+                else:
+                    srv.release(r.slot)
+            nxt += joining
+            nxt += admit(clock() - t0)
+            joining = []
+            if nxt:
+                submit(nxt)
             n_now = 0
             a0 = 0
-            still = []
             for q, r in enumerate(active):
-                n = len(r.structure.types)
+                n = r.natoms
                 n_now += n
                 r.step_latency.append(t - r.t_ready)
                 r.t_ready = t
@@ -303,14 +349,9 @@ class RequestLoop:
                 r.done += 1
                 if r.done >= r.nsteps:
                     r.t_done = t
-                    srv.release(r.slot)
-                else:
-                    still.append(r)
-            for r in joining:  # joined during the step: their wait for the next one starts now
-                r.t_ready = r.t_admit
             atom_evals += n_now
             step_atoms.append(n_now)
-            active = still
+            active = nxt
         wall = clock() - t0
         lat = np.array([r.t_done - r.t_arrival for r in self.requests]) * 1e3
         ev = np.concatenate([np.asarray(r.step_latency) for r in self.requests]) * 1e3
