@@ -176,8 +176,10 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     pdl_enter();
     __shared__ int s_base[kNbMaxWarps][32];     // per cell slot: cell-order start minus candidate start
     __shared__ int s_slot_at[kNbMaxWarps][32];  // cell slot starting at each position of a window
-    __shared__ uint32_t s_img[kNbMaxWarps][32];
-    __shared__ float s_fsh[kNbMaxWarps][32][3], s_flo[kNbMaxWarps][32][3];
+    // per cell slot: the image shift's high parts and the packed image (one 16-byte load in
+    // the candidate loop), and the shift's low parts (the float-float test)
+    __shared__ float4 s_sh4[kNbMaxWarps][32];
+    __shared__ float s_flo[kNbMaxWarps][32][3];
     __shared__ int s_acc[kNbMaxWarps][32];  // accepted entries per cell-offset group of the batch
     __shared__ int s_qj[kNbMaxWarps][64];   // candidates passing the FP32 screen: atom, cell slot,
     __shared__ int s_qs[kNbMaxWarps][64];   // position in cell order
@@ -195,6 +197,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     const float4 li = xlo[i];
 
     const float rc2h = (float)st.rc2, rc2l = (float)(st.rc2 - (double)(float)st.rc2);
+    const float rc2_hi = st.rc2_hi;
     const float tol = 1e-10f * rc2h;  // float-float d^2 is accurate to ~1e-12 relative
     int cnt = 0;
     const bool keep_groups = P.GS > noff;
@@ -226,7 +229,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 const float gx = fmaxf(0.f, fmaxf((float)q0 * wx - fi.x, fi.x - (float)(q0 + 1) * wx));
                 const float gy = fmaxf(0.f, fmaxf((float)q1 * wy - fi.y, fi.y - (float)(q1 + 1) * wy));
                 const float gz = fmaxf(0.f, fmaxf((float)q2 * wz - fi.z, fi.z - (float)(q2 + 1) * wz));
-                if (gx * gx + gy * gy + gz * gz > st.rc2_hi) ccount = 0;
+                if (gx * gx + gy * gy + gz * gz > rc2_hi) ccount = 0;
             } else if (st.smin2 > 0.f) {
                 // skewed box: the gap in direct coordinates times the box's smallest
                 // singular value bounds the Cartesian distance from below (the atom's
@@ -241,18 +244,16 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     const float g = fmaxf(0.f, fmaxf((float)q[d] * inv_n - ui, ui - (float)(q[d] + 1) * inv_n));
                     g2 += g * g;
                 }
-                if (st.smin2 * g2 > st.rc2_hi) ccount = 0;
+                if (st.smin2 * g2 > rc2_hi) ccount = 0;
             }
-            s_img[w][lane] = pack_img(na, nb, nc);
+
             // the image shift as float-float on the FP32 pipe (the exact test forms the FP64
             // shift itself); the zero image has an exactly zero shift
             float hi[3], lo[3];
             image_shift_ff(st, na, nb, nc, hi, lo);
+            s_sh4[w][lane] = make_float4(hi[0], hi[1], hi[2], __uint_as_float(pack_img(na, nb, nc)));
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                s_fsh[w][lane][d] = hi[d];
-                s_flo[w][lane][d] = lo[d];
-            }
+            for (int d = 0; d < 3; ++d) s_flo[w][lane][d] = lo[d];
         }
         int incl = ccount;
 #pragma unroll
@@ -271,12 +272,16 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
         auto exact_batch = [&](int k) {  // the first k queued candidates
             bool acc = false;
             int j = 0, slot = 0;
+            uint32_t img = 0;
             float4 fj = make_float4(0.f, 0.f, 0.f, 0.f);
             float ox = 0.f, oy = 0.f, oz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
             if (lane < k) {
                 j = s_qj[w][lane];
                 slot = s_qs[w][lane];
                 const int kp = s_qk[w][lane];
+                const float4 s4 = s_sh4[w][slot];
+                const float sh[3] = {s4.x, s4.y, s4.z};
+                img = __float_as_uint(s4.w);
                 fj = xfc[kp];
                 const float4 lj = xloc[kp];
                 // (x_j + shift) - x_i in float-float, then d^2 in float-float
@@ -286,7 +291,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     float s1, e1, s2, e2;
-                    two_sum(ajh[d], s_fsh[w][slot][d], s1, e1);
+                    two_sum(ajh[d], sh[d], s1, e1);
                     two_sum(s1, -aih[d], s2, e2);
                     const float lo = ((ajl[d] + s_flo[w][slot][d]) - ail[d]) + (e1 + e2);
                     two_sum(s2, lo, dh[d], dl[d]);
@@ -302,7 +307,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     acc = diff < 0.f;
                 } else {  // within 1e-10 of the cutoff: the exact FP64 test
                     int na, nb, nc;
-                    unpack_img(s_img[w][slot], na, nb, nc);
+                    unpack_img(img, na, nb, nc);
                     double sh[3] = {0.0, 0.0, 0.0};
                     if (na | nb | nc) image_shift(st, na, nb, nc, sh);
                     const double dxv = ds(da(xw[3 * j], sh[0]), xw[3 * i]);
@@ -319,7 +324,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 const int pos = cnt + __popc(m & ((1u << lane) - 1u));
                 if (pos < M) {
                     const size_t e = (size_t)i * M + pos;
-                    P.key[e] = pair_key(j, s_img[w][slot]);
+                    P.key[e] = pair_key(j, img);
                     P.dx[e] = make_float4(ox, oy, oz, fj.w);
                     if (P.dxlo) P.dxlo[e] = make_float4(lx, ly, lz, 0.f);
                     P.grp[e] = (uint16_t)(o0 + slot);
@@ -348,11 +353,12 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                 kp = s_base[w][slot] + cidx;
                 j = cell_atoms[kp];
                 const float4 fj = xfc[kp];  // independent of the load of j
-                if (!(j == i && s_img[w][slot] == pack_img(0, 0, 0))) {
-                    const float fx = (fj.x + s_fsh[w][slot][0]) - fi.x;
-                    const float fy = (fj.y + s_fsh[w][slot][1]) - fi.y;
-                    const float fz = (fj.z + s_fsh[w][slot][2]) - fi.z;
-                    pass = fx * fx + fy * fy + fz * fz < st.rc2_hi;
+                const float4 sh = s_sh4[w][slot];
+                if (!(j == i && __float_as_uint(sh.w) == pack_img(0, 0, 0))) {
+                    const float fx = (fj.x + sh.x) - fi.x;
+                    const float fy = (fj.y + sh.y) - fi.y;
+                    const float fz = (fj.z + sh.z) - fi.z;
+                    pass = fx * fx + fy * fy + fz * fz < rc2_hi;
                 }
             }
             const unsigned m = __ballot_sync(0xffffffffu, pass);
