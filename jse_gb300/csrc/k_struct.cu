@@ -181,9 +181,8 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
     __shared__ float4 s_sh4[kNbMaxWarps][32];
     __shared__ float s_flo[kNbMaxWarps][32][3];
     __shared__ int s_acc[kNbMaxWarps][32];  // accepted entries per cell-offset group of the batch
-    __shared__ int s_qj[kNbMaxWarps][64];   // candidates passing the FP32 screen: atom, cell slot,
-    __shared__ int s_qs[kNbMaxWarps][64];   // position in cell order
-    __shared__ int s_qk[kNbMaxWarps][64];
+    __shared__ int s_qs[kNbMaxWarps][64];   // candidates passing the FP32 screen: cell slot,
+    __shared__ int s_qk[kNbMaxWarps][64];   // position in cell order
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + w;
     if (i >= n) return;
@@ -276,9 +275,9 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             float4 fj = make_float4(0.f, 0.f, 0.f, 0.f);
             float ox = 0.f, oy = 0.f, oz = 0.f, lx = 0.f, ly = 0.f, lz = 0.f;
             if (lane < k) {
-                j = s_qj[w][lane];
                 slot = s_qs[w][lane];
                 const int kp = s_qk[w][lane];
+                j = cell_atoms[kp];
                 const float4 s4 = s_sh4[w][slot];
                 const float sh[3] = {s4.x, s4.y, s4.z};
                 img = __float_as_uint(s4.w);
@@ -315,6 +314,7 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
                     const double dzv = ds(da(xw[3 * j + 2], sh[2]), xw[3 * i + 2]);
                     acc = da(da(dm(dxv, dxv), dm(dyv, dyv)), dm(dzv, dzv)) < st.rc2;
                 }
+                if (j == i && img == pack_img(0, 0, 0)) acc = false;  // the atom itself
                 two_sum(dh[0], dl[0], ox, lx);
                 two_sum(dh[1], dl[1], oy, ly);
                 two_sum(dh[2], dl[2], oz, lz);
@@ -347,24 +347,22 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             const unsigned mine = smask & (0xffffffffu >> (31 - lane));
             const int slot = mine ? s_slot_at[w][31 - __clz(mine)] : carry;
             carry = __shfl_sync(0xffffffffu, slot, 31);
+            // the screen reads only the candidate's cell-order position; its atom index is
+            // loaded by the exact test, which also drops the atom itself (zero image)
             bool pass = false;
-            int j = 0, kp = 0;
+            int kp = 0;
             if (cidx < total) {
                 kp = s_base[w][slot] + cidx;
-                j = cell_atoms[kp];
-                const float4 fj = xfc[kp];  // independent of the load of j
+                const float4 fj = xfc[kp];
                 const float4 sh = s_sh4[w][slot];
-                if (!(j == i && __float_as_uint(sh.w) == pack_img(0, 0, 0))) {
-                    const float fx = (fj.x + sh.x) - fi.x;
-                    const float fy = (fj.y + sh.y) - fi.y;
-                    const float fz = (fj.z + sh.z) - fi.z;
-                    pass = fx * fx + fy * fy + fz * fz < rc2_hi;
-                }
+                const float fx = (fj.x + sh.x) - fi.x;
+                const float fy = (fj.y + sh.y) - fi.y;
+                const float fz = (fj.z + sh.z) - fi.z;
+                pass = fx * fx + fy * fy + fz * fz < rc2_hi;
             }
             const unsigned m = __ballot_sync(0xffffffffu, pass);
             if (pass) {
                 const int q = qn + __popc(m & ((1u << lane) - 1u));
-                s_qj[w][q] = j;
                 s_qs[w][q] = slot;
                 s_qk[w][q] = kp;
             }
@@ -373,15 +371,13 @@ k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const 
             if (qn >= 32) {
                 exact_batch(32);
                 // move the overflow (at most 31 entries) to the front of the queue
-                int rj = 0, rs = 0, rk = 0;
+                int rs = 0, rk = 0;
                 if (lane < qn - 32) {
-                    rj = s_qj[w][32 + lane];
                     rs = s_qs[w][32 + lane];
                     rk = s_qk[w][32 + lane];
                 }
                 __syncwarp();
                 if (lane < qn - 32) {
-                    s_qj[w][lane] = rj;
                     s_qs[w][lane] = rs;
                     s_qk[w][lane] = rk;
                 }
