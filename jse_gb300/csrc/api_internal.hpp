@@ -175,6 +175,11 @@ struct nnap_handle {
     // descriptors on the FP32 pipe even in mixed precision (set while training gradients,
     // which are FP32 whatever the handle's precision)
     bool fp32_desc = false;
+    // the last batch layout and the counts, kinds and boxes it was planned from
+    nnapgb::Batch plan;
+    std::vector<int> plan_nat, plan_kind;
+    std::vector<double> plan_box;
+    bool plan_valid = false;
     bool net_tc = false;  // networks on the tensor cores (mixed precision, SiLU networks)
     std::string net_notes;  // species whose network runs the FP32 kernel on a mixed handle, and why
     int device = 0;
@@ -302,7 +307,7 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
 // capacity and repeating as needed; returns after the stream has drained.
 void evaluate(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool fp_only);
 // Plan a batch: structure descriptors, cell grids and reduction chunks.
-Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes);
+const Batch& plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes);
 // Copy host positions and species into the handle's device buffers.
 void upload_inputs(nnap_handle* h, int n, const double* x, const int* type);
 // Bytes of the spherical expansion-coefficient arena for n atom slots.

@@ -245,34 +245,29 @@ void cross3(const double* u, const double* v, double* r) {
 
 // Smallest eigenvalue of G = H H^T for the box matrix H (rows a, b, c): the squared
 // smallest singular value, so |u H| >= sqrt of it times |u| for any direct-coordinate
-// vector u.  Cyclic Jacobi rotations on the symmetric 3 x 3 matrix.
+// vector u.  The closed form of a symmetric 3 x 3 matrix's eigenvalues (trace, the
+// deviatoric part's norm and determinant, one arccosine), less a margin of 1e-12 of the
+// largest eigenvalue for its rounding: the result stays a lower bound, which is all the
+// cell pruning needs.
 double smallest_sq_singular(const StructDev& s) {
     const double* r[3] = {s.a, s.b, s.c};
     double G[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) G[i][j] = r[i][0] * r[j][0] + r[i][1] * r[j][1] + r[i][2] * r[j][2];
-    for (int sweep = 0; sweep < 50; ++sweep) {
-        const double off = G[0][1] * G[0][1] + G[0][2] * G[0][2] + G[1][2] * G[1][2];
-        const double diag = G[0][0] * G[0][0] + G[1][1] * G[1][1] + G[2][2] * G[2][2];
-        if (off <= 1e-30 * diag) break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q) {
-                if (G[p][q] == 0.0) continue;
-                const double th = 0.5 * std::atan2(2.0 * G[p][q], G[q][q] - G[p][p]);
-                const double c = std::cos(th), sn = std::sin(th);
-                for (int k = 0; k < 3; ++k) {  // columns p, q
-                    const double gp = G[k][p], gq = G[k][q];
-                    G[k][p] = c * gp - sn * gq;
-                    G[k][q] = sn * gp + c * gq;
-                }
-                for (int k = 0; k < 3; ++k) {  // rows p, q
-                    const double gp = G[p][k], gq = G[q][k];
-                    G[p][k] = c * gp - sn * gq;
-                    G[q][k] = sn * gp + c * gq;
-                }
-            }
-    }
-    return std::max(0.0, std::min(G[0][0], std::min(G[1][1], G[2][2])));
+    const double off = G[0][1] * G[0][1] + G[0][2] * G[0][2] + G[1][2] * G[1][2];
+    if (off == 0.0) return std::max(0.0, std::min(G[0][0], std::min(G[1][1], G[2][2])));
+    const double q = (G[0][0] + G[1][1] + G[2][2]) / 3.0;
+    const double d0 = G[0][0] - q, d1 = G[1][1] - q, d2 = G[2][2] - q;
+    const double p = std::sqrt((d0 * d0 + d1 * d1 + d2 * d2 + 2.0 * off) / 6.0);
+    if (!(p > 0.0)) return std::max(0.0, q);
+    // B = (G - q I) / p; r = det(B) / 2 in [-1, 1]
+    const double b00 = d0 / p, b11 = d1 / p, b22 = d2 / p, b01 = G[0][1] / p, b02 = G[0][2] / p, b12 = G[1][2] / p;
+    const double det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
+    const double rr = std::min(1.0, std::max(-1.0, 0.5 * det));
+    const double phi = std::acos(rr) / 3.0;
+    const double lmax = q + 2.0 * p * std::cos(phi);
+    const double lmin = q + 2.0 * p * std::cos(phi + 2.0943951023931957);  // + 2 pi / 3
+    return std::max(0.0, lmin - 1e-12 * std::fabs(lmax));
 }
 
 // Float bound for the candidate screen: rc^2 plus the worst rounding of the FP32
@@ -373,7 +368,16 @@ StructDev make_struct(int kind, const double* box, double rc, int a0, int n, int
 }
 
 // ------------------------------------------------------------------ pipeline
-Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes) {
+// The batch layout of a call.  The last one is kept with the counts, kinds and boxes it was
+// made from, and returned again while they are unchanged (repeated evaluations of the same
+// structures skip the per-structure geometry).
+const Batch& plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kinds, const double* boxes) {
+    if (h->plan_valid && h->plan.nstruct == nstruct && nstruct > 0 &&
+        std::memcmp(h->plan_nat.data(), natoms, sizeof(int) * nstruct) == 0 &&
+        std::memcmp(h->plan_kind.data(), kinds, sizeof(int) * nstruct) == 0 &&
+        std::memcmp(h->plan_box.data(), boxes, sizeof(double) * 9 * nstruct) == 0)
+        return h->plan;
+    h->plan_valid = false;
     Batch B;
     B.nstruct = nstruct;
     const double rc = h->model.rcut_max;
@@ -393,7 +397,12 @@ Batch plan_batch(nnap_handle* h, int nstruct, const int* natoms, const int* kind
     }
     B.natoms = a0;
     B.ncells = c0;
-    return B;
+    h->plan = std::move(B);
+    h->plan_nat.assign(natoms, natoms + nstruct);
+    h->plan_kind.assign(kinds, kinds + nstruct);
+    h->plan_box.assign(boxes, boxes + 9 * (size_t)nstruct);
+    h->plan_valid = true;
+    return h->plan;
 }
 
 void grow_pairs(nnap_handle* h, int n, int M) {
@@ -1194,7 +1203,7 @@ int nnap_compute_batch(nnap_handle* h, int nstruct, const int* natoms, const dou
         Outputs o{energy, energies, forces, virial, virials};
         check_outputs(flags, o);
         h->launches = 0;
-        Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
+        const Batch& B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, B.natoms, x, type);
         evaluate(h, B, h->x.p, h->type.p, false);
@@ -1211,7 +1220,7 @@ int nnap_compute_device(nnap_handle* h, int natoms, const double* d_x, const int
         if (!box) throw ApiFail(NNAP_ERR_ARG, "box is NULL");
         Outputs o{d_energy, d_energies, d_forces, d_virial, d_virials};
         check_outputs(flags, o);
-        Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
+        const Batch& B = plan_batch(h, 1, &natoms, &box_kind, box);
         if (natoms && (!d_x || !d_type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         // NULL is CUDA's default stream; the handle's stream is ordered after the caller's
         // work and the caller's stream waits for the results.
@@ -1235,7 +1244,7 @@ int nnap_compute_batch_device(nnap_handle* h, int nstruct, const int* natoms, co
         if (nstruct < 1 || !natoms || !box_kind || !boxes) throw ApiFail(NNAP_ERR_ARG, "invalid batch description");
         Outputs o{d_energy, d_energies, d_forces, d_virial, d_virials};
         check_outputs(flags, o);
-        Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
+        const Batch& B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!d_x || !d_type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         cudaStream_t user = (cudaStream_t)stream;
         if (!h->order_ev) CK(cudaEventCreateWithFlags(&h->order_ev, cudaEventDisableTiming));
@@ -1304,7 +1313,7 @@ int nnap_compute_fp(nnap_handle* h, int natoms, const double* x, const int* type
         for (auto& sp : h->model.sp) dmax = std::max(dmax, sp.D);
         if (stride < dmax) throw ApiFail(NNAP_ERR_ARG, "stride smaller than the descriptor size");
         h->launches = 0;
-        Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
+        const Batch& B = plan_batch(h, 1, &natoms, &box_kind, box);
         if (natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, natoms, x, type);
         evaluate(h, B, h->x.p, h->type.p, true);
@@ -1329,7 +1338,7 @@ int nnap_neighbor_list(nnap_handle* h, int natoms, const double* x, const int* t
     return guarded(h, [&]() -> int {
         if (!box || !counts || !total) throw ApiFail(NNAP_ERR_ARG, "NULL argument");
         h->launches = 0;
-        Batch B = plan_batch(h, 1, &natoms, &box_kind, box);
+        const Batch& B = plan_batch(h, 1, &natoms, &box_kind, box);
         if (natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, natoms, x, type);
         evaluate(h, B, h->x.p, h->type.p, true);

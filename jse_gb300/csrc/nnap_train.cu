@@ -427,7 +427,7 @@ int nnap_train_grad_batch(nnap_handle* h, int nstruct, const int* natoms, const 
         const int T = m.ntypes();
         const bool want_w = grad_fp && any_fused(m);
         h->launches = 0;
-        Batch B = plan_batch(h, nstruct, natoms, box_kind, boxes);
+        const Batch& B = plan_batch(h, nstruct, natoms, box_kind, boxes);
         if (B.natoms && (!x || !type)) throw ApiFail(NNAP_ERR_ARG, "positions or types are NULL");
         upload_inputs(h, B.natoms, x, type);
         struct Fp32Desc {  // FP32 descriptors for the gradients, restored on every exit
