@@ -109,11 +109,16 @@ __global__ void k_fill_cells(const int* __restrict__ cell_of, int n, const int* 
 }
 
 // Order each cell's atoms by index so that every neighbour row is deterministic.
-// One warp per cell: up to 32 atoms are placed by rank; larger cells are sorted by lane 0.
+// One warp per cell (8 per CTA of 256 threads): up to 32 atoms are placed by rank from
+// registers; up to kSortCellMax atoms by rank from a copy of the cell in shared memory (the
+// small boxes of a batch have cells of a hundred atoms); larger cells are sorted by lane 0.
+constexpr int kSortCellMax = 1024;
+
 __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int* __restrict__ cell_atoms) {
     pdl_enter();
+    __shared__ int s_cell[8][kSortCellMax];
     const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) & 7;
     if (c >= ncells) return;
     const int b = cell_start[c], e = cell_start[c + 1], m = e - b;
     if (m <= 32) {
@@ -125,6 +130,15 @@ __global__ void k_sort_cells(const int* __restrict__ cell_start, int ncells, int
         }
         __syncwarp();
         if (lane < m) cell_atoms[b + rank] = v;
+    } else if (m <= kSortCellMax) {
+        for (int t = lane; t < m; t += 32) s_cell[w][t] = cell_atoms[b + t];
+        __syncwarp();
+        for (int t = lane; t < m; t += 32) {
+            const int v = s_cell[w][t];
+            int rank = 0;
+            for (int q = 0; q < m; ++q) rank += s_cell[w][q] < v ? 1 : 0;
+            cell_atoms[b + rank] = v;
+        }
     } else if (lane == 0) {
         for (int k = b + 1; k < e; ++k) {
             const int v = cell_atoms[k];
