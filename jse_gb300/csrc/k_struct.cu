@@ -587,23 +587,36 @@ __global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double*
 #pragma unroll
     for (int d = 0; d < 9; ++d) { vh[d] = 0.f; vl[d] = 0.f; }
     const size_t row = (size_t)a * M;
-    for (int k = sub; k < cnt; k += kGatherLanes) {
-        const float4 go = P.g[row + k];
-        const float4 dn = P.dx[row + k];
-        const float4 gr = P.g[P.rev[row + k]];
-        const float dx = -dn.x, dy = -dn.y, dz = -dn.z;
-        ff_acc(fh[0], fl[0], gr.x); ff_acc(fh[0], fl[0], -go.x);
-        ff_acc(fh[1], fl[1], gr.y); ff_acc(fh[1], fl[1], -go.y);
-        ff_acc(fh[2], fl[2], gr.z); ff_acc(fh[2], fl[2], -go.z);
-        ff_acc_prod(vh[0], vl[0], dx, gr.x);
-        ff_acc_prod(vh[1], vl[1], dy, gr.y);
-        ff_acc_prod(vh[2], vl[2], dz, gr.z);
-        ff_acc_prod(vh[3], vl[3], dx, gr.y);
-        ff_acc_prod(vh[4], vl[4], dx, gr.z);
-        ff_acc_prod(vh[5], vl[5], dy, gr.z);
-        ff_acc_prod(vh[6], vl[6], dy, gr.x);
-        ff_acc_prod(vh[7], vl[7], dz, gr.x);
-        ff_acc_prod(vh[8], vl[8], dz, gr.y);
+    // two entries per step: both mirrored-gradient loads (an index load, then a gather) are
+    // in flight before either is used; the second entry's terms are added after the first's,
+    // so the summation order is that of one entry per step
+    for (int k0 = sub; k0 < cnt; k0 += 2 * kGatherLanes) {
+        const int k1 = k0 + kGatherLanes;
+        const bool two = k1 < cnt;
+        const int r0 = P.rev[row + k0], r1 = two ? P.rev[row + k1] : r0;
+        const float4 gr0 = P.g[r0], gr1 = P.g[r1];
+        const float4 go0 = P.g[row + k0], go1 = two ? P.g[row + k1] : go0;
+        const float4 dn0 = P.dx[row + k0], dn1 = two ? P.dx[row + k1] : dn0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (h == 1 && !two) break;
+            const float4 go = h ? go1 : go0;
+            const float4 dn = h ? dn1 : dn0;
+            const float4 gr = h ? gr1 : gr0;
+            const float dx = -dn.x, dy = -dn.y, dz = -dn.z;
+            ff_acc(fh[0], fl[0], gr.x); ff_acc(fh[0], fl[0], -go.x);
+            ff_acc(fh[1], fl[1], gr.y); ff_acc(fh[1], fl[1], -go.y);
+            ff_acc(fh[2], fl[2], gr.z); ff_acc(fh[2], fl[2], -go.z);
+            ff_acc_prod(vh[0], vl[0], dx, gr.x);
+            ff_acc_prod(vh[1], vl[1], dy, gr.y);
+            ff_acc_prod(vh[2], vl[2], dz, gr.z);
+            ff_acc_prod(vh[3], vl[3], dx, gr.y);
+            ff_acc_prod(vh[4], vl[4], dx, gr.z);
+            ff_acc_prod(vh[5], vl[5], dy, gr.z);
+            ff_acc_prod(vh[6], vl[6], dy, gr.x);
+            ff_acc_prod(vh[7], vl[7], dz, gr.x);
+            ff_acc_prod(vh[8], vl[8], dz, gr.y);
+        }
     }
 #pragma unroll
     for (int off = kGatherLanes / 2; off > 0; off >>= 1) {
