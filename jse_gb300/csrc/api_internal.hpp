@@ -28,13 +28,16 @@ __global__ void k_scan_excl(const int*, int, int*);
 __global__ void k_fill_cells(const int*, int, const int*, int*, int*);
 __global__ void k_sort_cells(const int*, int, int*);
 __global__ void k_cell_order(const int*, int, const float4*, const float4*, float4*, float4*);
+__global__ void k_renumber(int*, int, const float4*, const float4*, const double*, const int*, const int*, float4*,
+                           float4*, double*, int*, int*, int*);
+__global__ void k_unpermute(const double*, const int*, int, double*);
 __global__ void k_neighbors(const StructDev*, const int*, const double*, const float4*, const float4*, const float4*,
                             const float4*, const int*, const int*, const int*, int, PairBufs, int*, int*);
 __global__ void k_mirror(const StructDev*, const int*, PairBufs, int, int*);
 __global__ void k_type_hist(const int*, int, int, int*);
 __global__ void k_type_offsets(int*, int, int, int*);
 __global__ void k_type_scatter(const int*, int, int, const int*, int*);
-__global__ void k_gather(PairBufs, int, double*, double*);
+__global__ void k_gather(PairBufs, int, const int*, double*, double*);
 __global__ void k_reduce_chunks(const int*, const int*, const double*, const double*, double*);
 __global__ void k_reduce_structs(const int*, int, const double*, double*, double*);
 
@@ -196,6 +199,11 @@ struct nnap_handle {
         type_start;
     nnapgb::DevBuf<int> chunk_b, chunk_e, struct_chunks, status;
     nnapgb::DevBuf<float4> xf, xlo, xfc, xloc;  // positions as float + low parts; copies in cell order
+    // the evaluation in cell order (k_renumber): wrapped positions, cell and species of each
+    // cell-order position, the atom at each, and per-atom energies back in atom order
+    nnapgb::DevBuf<double> xw2, e_out;
+    nnapgb::DevBuf<int> cell_of2, type2, orig;
+    bool renumbered = false;  // the last enqueue ran in cell order
     nnapgb::DevBuf<uint16_t> pgrp;
     nnapgb::DevBuf<nnapgb::StructDev> sdev;
     nnapgb::DevBuf<uint64_t> pkey;
@@ -301,7 +309,10 @@ void enqueue_species(nnap_handle* h, int n, const int* d_type);
 void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type);
 // Queue descriptors, networks and descriptor gradients; with gather, also the
 // force / virial gather over mirrored rows and the per-structure reductions.
-void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather);
+// orig: the atom of each row when the rows are in cell order (forces and virials are
+// written at it), or NULL when rows are atoms.
+void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather,
+                  const int* orig = nullptr);
 // Run the whole launch sequence of a batch (neighbours, species order, descriptors and,
 // unless fp_only, networks, pair gradients and reductions), growing the neighbour
 // capacity and repeating as needed; returns after the stream has drained.

@@ -181,6 +181,40 @@ __global__ void __launch_bounds__(256) k_cell_order(const int* __restrict__ cell
     xloc[k] = xlo[a];
 }
 
+// Renumber the atoms of an evaluation in cell order: position k of the sorted cell lists
+// takes the float positions and low parts (xfc / xloc), the FP64 wrapped position, the cell
+// and the species of the atom there, and orig[k] records that atom; the cell lists become
+// the identity.  Rows, pair keys and per-atom work arrays then use cell-order numbers, so
+// the rows of atoms close in space are close in memory (the mirror search and the gather
+// read the rows of each atom's neighbours).  A structure's atoms keep their index range.
+__global__ void __launch_bounds__(256) k_renumber(int* __restrict__ cell_atoms, int n, const float4* __restrict__ xf,
+                                                  const float4* __restrict__ xlo, const double* __restrict__ xw,
+                                                  const int* __restrict__ cell_of, const int* __restrict__ type,
+                                                  float4* __restrict__ xfc, float4* __restrict__ xloc,
+                                                  double* __restrict__ xw2, int* __restrict__ cell_of2,
+                                                  int* __restrict__ type2, int* __restrict__ orig) {
+    pdl_enter();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int a = cell_atoms[k];
+    xfc[k] = xf[a];
+    xloc[k] = xlo[a];
+    xw2[3 * (size_t)k] = xw[3 * (size_t)a];
+    xw2[3 * (size_t)k + 1] = xw[3 * (size_t)a + 1];
+    xw2[3 * (size_t)k + 2] = xw[3 * (size_t)a + 2];
+    cell_of2[k] = cell_of[a];
+    type2[k] = type[a];
+    orig[k] = a;
+    cell_atoms[k] = k;
+}
+
+// out[orig[k]] = in[k]: a per-atom array of a cell-ordered evaluation back in atom order.
+__global__ void k_unpermute(const double* __restrict__ in, const int* __restrict__ orig, int n,
+                            double* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[orig[k]] = in[k];
+}
+
 __global__ void __launch_bounds__(32 * kNbMaxWarps, 4)
 k_neighbors(const StructDev* __restrict__ S, const int* __restrict__ sid, const double* __restrict__ xw,
             const float4* __restrict__ xf, const float4* __restrict__ xlo, const float4* __restrict__ xfc,
@@ -574,7 +608,9 @@ __device__ __forceinline__ void ff_merge(float& h, float& l, unsigned mask, int 
     l = (l + ol) + e;
 }
 
-__global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double* __restrict__ virials) {
+// orig: the atom of each row (rows in cell order), or NULL (rows are atoms).
+__global__ void k_gather(PairBufs P, int n, const int* __restrict__ orig, double* __restrict__ forces,
+                         double* __restrict__ virials) {
     pdl_enter();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int a = t / kGatherLanes, sub = t & (kGatherLanes - 1);
@@ -626,10 +662,11 @@ __global__ void k_gather(PairBufs P, int n, double* __restrict__ forces, double*
         for (int d = 0; d < 9; ++d) ff_merge(vh[d], vl[d], mask, off);
     }
     if (sub == 0) {
+        const size_t o = orig ? (size_t)orig[a] : (size_t)a;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) forces[3 * (size_t)a + d] = (double)fh[d] + (double)fl[d];
+        for (int d = 0; d < 3; ++d) forces[3 * o + d] = (double)fh[d] + (double)fl[d];
 #pragma unroll
-        for (int d = 0; d < 9; ++d) virials[9 * (size_t)a + d] = (double)vh[d] + (double)vl[d];
+        for (int d = 0; d < 9; ++d) virials[9 * o + d] = (double)vh[d] + (double)vl[d];
     }
 }
 

@@ -465,6 +465,11 @@ void ensure_work(nnap_handle* h, int n, int nstruct, int ncells, int nchunks) {
     h->xlo.ensure(n1);
     h->xfc.ensure(n1);
     h->xloc.ensure(n1);
+    h->xw2.ensure(3 * (size_t)n1);
+    h->e_out.ensure(n1);
+    h->cell_of2.ensure(n1);
+    h->type2.ensure(n1);
+    h->orig.ensure(n1);
     h->cell_of.ensure(n1);
     h->cell_count.ensure(std::max(ncells, 1));
     h->cell_fill.ensure(std::max(ncells, 1));
@@ -530,7 +535,7 @@ void prepare_layout(nnap_handle* h, const Batch& B) {
 
 // Cell list and neighbour rows of every atom of the batch (cutoff and cell grid from
 // the structure descriptors already on the device).
-void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type) {
+void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const int* d_type, bool renumber) {
     const int n = B.natoms;
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
@@ -546,12 +551,21 @@ void enqueue_neighbors(nnap_handle* h, const Batch& B, const double* d_x, const 
     if (n > 0) {
         CK(launch_pdl(k_fill_cells, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_of.p, n, h->cell_start.p, h->cell_fill.p, h->cell_atoms.p));
         CK(launch_pdl(k_sort_cells, dim3((B.ncells * 32 + 255) / 256), dim3(256), 0, st, h->cell_start.p, B.ncells, h->cell_atoms.p));
-        CK(launch_pdl(k_cell_order, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_atoms.p, n, h->xf.p, h->xlo.p,
-                      h->xfc.p, h->xloc.p));
         const int nw = h->tune.nb_warps;
-        CK(launch_pdl(k_neighbors, dim3((n + nw - 1) / nw), dim3(32 * nw), 0, st, h->sdev.p, h->sid.p, h->xw.p,
-                      h->xf.p, h->xlo.p, h->xfc.p, h->xloc.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
-                      pair_bufs(h), h->status.p, h->status.p + 1));
+        if (renumber) {  // the rest of the evaluation numbers atoms in cell order
+            CK(launch_pdl(k_renumber, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_atoms.p, n, h->xf.p, h->xlo.p,
+                          h->xw.p, h->cell_of.p, d_type, h->xfc.p, h->xloc.p, h->xw2.p, h->cell_of2.p, h->type2.p,
+                          h->orig.p));
+            CK(launch_pdl(k_neighbors, dim3((n + nw - 1) / nw), dim3(32 * nw), 0, st, h->sdev.p, h->sid.p, h->xw2.p,
+                          h->xfc.p, h->xloc.p, h->xfc.p, h->xloc.p, h->cell_of2.p, h->cell_start.p, h->cell_atoms.p,
+                          n, pair_bufs(h), h->status.p, h->status.p + 1));
+        } else {
+            CK(launch_pdl(k_cell_order, dim3((n + 255) / 256), dim3(256), 0, st, h->cell_atoms.p, n, h->xf.p, h->xlo.p,
+                          h->xfc.p, h->xloc.p));
+            CK(launch_pdl(k_neighbors, dim3((n + nw - 1) / nw), dim3(32 * nw), 0, st, h->sdev.p, h->sid.p, h->xw.p,
+                          h->xf.p, h->xlo.p, h->xfc.p, h->xloc.p, h->cell_of.p, h->cell_start.p, h->cell_atoms.p, n,
+                          pair_bufs(h), h->status.p, h->status.p + 1));
+        }
         h->launches += 4;
     }
 }
@@ -576,7 +590,7 @@ void enqueue_species_mirror(nnap_handle* h, const Batch& B, const int* d_type) {
     ++h->launches;
 }
 
-void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather) {
+void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_only, bool gather, const int* orig) {
     const int n = B.natoms;
     const int T = h->model.ntypes();
     cudaStream_t st = h->stream;
@@ -736,8 +750,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     if (!fp_only && gather) {
         if (n > 0) {
             const int gb = h->tune.gather_block;  // threads per CTA, eight per atom
-            CK(launch_pdl(k_gather, dim3((unsigned)(((size_t)n * 8 + gb - 1) / gb)), dim3(gb), 0, st, pair_bufs(h), n, h->forces.p,
-                                                                               h->virials.p));
+            CK(launch_pdl(k_gather, dim3((unsigned)(((size_t)n * 8 + gb - 1) / gb)), dim3(gb), 0, st, pair_bufs(h), n,
+                          orig, h->forces.p, h->virials.p));
             ++h->launches;
         }
         const int nchunks = (int)B.cb.size();
@@ -762,10 +776,15 @@ void enqueue(nnap_handle* h, const Batch& B, const double* d_x, const int* d_typ
     h->mark(0);
     CK(cudaMemcpyAsync(h->sdev.p, h->h_sdev, sizeof(StructDev) * B.nstruct, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(h->status.p, 0, sizeof(int) * 2, st));
-    enqueue_neighbors(h, B, d_x, d_type);
-    enqueue_species_mirror(h, B, d_type);
+    // energy / force evaluations run in cell order (descriptor-only calls, which return
+    // per-slot rows or neighbour rows, keep atom order)
+    const bool renumber = !fp_only && B.natoms > 0;
+    h->renumbered = renumber;
+    enqueue_neighbors(h, B, d_x, d_type, renumber);
+    const int* dt = renumber ? h->type2.p : d_type;
+    enqueue_species_mirror(h, B, dt);
     h->mark(1);
-    enqueue_eval(h, B, d_type, fp_only, true);
+    enqueue_eval(h, B, dt, fp_only, true, renumber ? h->orig.p : nullptr);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_status, h->status.p, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
 }
@@ -955,8 +974,15 @@ void copy_out(nnap_handle* h, const Batch& B, int flags, const Outputs& o, cudaM
     const size_t n = B.natoms;
     if ((flags & NNAP_WANT_ENERGY) && o.energy)
         CK(cudaMemcpyAsync(o.energy, h->energy.p, sizeof(double) * B.nstruct, kind, st));
-    if ((flags & NNAP_WANT_ENERGIES) && o.energies && n)
-        CK(cudaMemcpyAsync(o.energies, h->e_atom.p, sizeof(double) * n, kind, st));
+    if ((flags & NNAP_WANT_ENERGIES) && o.energies && n) {
+        const double* e = h->e_atom.p;
+        if (h->renumbered) {  // per-atom energies of a cell-ordered evaluation, back in atom order
+            k_unpermute<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->e_atom.p, h->orig.p, (int)n, h->e_out.p);
+            CK(cudaGetLastError());
+            e = h->e_out.p;
+        }
+        CK(cudaMemcpyAsync(o.energies, e, sizeof(double) * n, kind, st));
+    }
     if ((flags & NNAP_WANT_FORCES) && o.forces && n)
         CK(cudaMemcpyAsync(o.forces, h->forces.p, sizeof(double) * 3 * n, kind, st));
     if ((flags & NNAP_WANT_VIRIAL) && o.virial)
