@@ -40,6 +40,10 @@ __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restric
 #pragma unroll
     for (int d = 0; d < 3; ++d)
         if (p[d] < 0.0 || p[d] >= 1.0) p[d] = ds(p[d], floor(p[d]));
+    // the cell comes from these wrapped direct coordinates: every atom is binned by the same
+    // rule, and the stencil's slack (R cells cover at least rc plus 1e-6 of a cell) dwarfs
+    // their rounding, so no second conversion of the wrapped position is needed
+    const double f[3] = {p[0], p[1], p[2]};
     to_cartesian(st, p);
     xw[3 * i] = p[0]; xw[3 * i + 1] = p[1]; xw[3 * i + 2] = p[2];
     const float hx = (float)p[0], hy = (float)p[1], hz = (float)p[2];
@@ -48,8 +52,6 @@ __global__ void k_wrap_bin(const StructDev* __restrict__ S, const int* __restric
     xf[i] = make_float4(hx, hy, hz, __int_as_float(min(max(t, 1), ntypes)));
     // x = hi + lo exactly to 48 bits: the float-float form used by the neighbour test
     xlo[i] = make_float4((float)ds(p[0], (double)hx), (float)ds(p[1], (double)hy), (float)ds(p[2], (double)hz), 0.f);
-    double f[3] = {p[0], p[1], p[2]};
-    to_direct(st, f);
     int c[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
