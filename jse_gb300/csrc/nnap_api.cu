@@ -3,12 +3,13 @@
 //
 // Pipeline of one evaluation over a batch of structures (a single structure is a
 // batch of one):
-//   k_wrap_bin -> k_scan_excl -> k_fill_cells -> k_sort_cells -> k_neighbors
-//   -> species sort (k_type_hist, k_type_offsets, k_type_scatter)
-//   -> [one host synchronisation: neighbour capacity, species ranges, error bits]
-//   -> k_mirror -> descriptor forward (per run of species sharing a basis shape, per
-//   sub-basis) -> network per species -> descriptor backward -> k_gather
-//   -> k_reduce_chunks -> k_reduce_structs.
+//   k_wrap_bin -> k_scan_excl -> k_fill_cells -> k_sort_cells
+//   -> k_renumber (energy/force evaluations: atoms in cell order from here on; descriptor-
+//      only calls take k_cell_order and keep atom order) -> k_neighbors
+//   -> species sort (k_type_hist, k_type_offsets, k_type_scatter) -> k_mirror
+//   -> descriptor forward (per run of species sharing a basis shape, per sub-basis)
+//   -> network per species -> descriptor backward -> k_gather -> k_reduce_chunks
+//   -> k_reduce_structs, then one host synchronisation (neighbour capacity, error bits).
 #include <cuda_runtime.h>
 
 #include <algorithm>
