@@ -12,7 +12,7 @@ The expected values come from the reference's own per-atom arithmetic (its NNAP 
 expanded and compiled without fast-math into oracle/_ref, run on all host threads over
 the oracle's neighbour list), or from the FP64 oracle where that build is absent.
 
-Targets (the benchmark spec's): bit-exact neighbour sets (every (i, j, image) triple); force
+Targets of the mixed-precision path: bit-exact neighbour sets (every (i, j, image) triple); force
 RMSE <= 1e-3 eV/A; |E - E_ref| / N <= 1e-5 eV/atom (per structure for the batch); max
 |dE_i| <= 1e-4 eV; virials within 1e-3 relative.
 """
