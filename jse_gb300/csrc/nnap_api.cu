@@ -750,8 +750,8 @@ void enqueue_eval(nnap_handle* h, const Batch& B, const int* d_type, bool fp_onl
     h->mark(4);
     if (!fp_only && gather) {
         if (n > 0) {
-            const int gb = h->tune.gather_block;  // threads per CTA, eight per atom
-            CK(launch_pdl(k_gather, dim3((unsigned)(((size_t)n * 8 + gb - 1) / gb)), dim3(gb), 0, st, pair_bufs(h), n,
+            const int gb = h->tune.gather_block;  // threads per CTA, four per atom
+            CK(launch_pdl(k_gather, dim3((unsigned)(((size_t)n * 4 + gb - 1) / gb)), dim3(gb), 0, st, pair_bufs(h), n,
                           orig, h->forces.p, h->virials.p));
             ++h->launches;
         }
